@@ -1,0 +1,331 @@
+/*
+ * kiyosi-gb300 C ABI: GB300 (sm_103a) Monte Carlo and least-squares Monte Carlo
+ * pricing engines for kiyosi, behind plain pointers, sizes and status codes.
+ *
+ * The host side that replaces the reference's Rust engines builds a *plan* for each
+ * contract -- the same per-step transitions, cash events and thresholds that the
+ * reference's engines build before their sampling loops -- and hands the plans to
+ * this library.  The library owns all device memory; every output buffer is
+ * caller-owned host memory.  No C++ exception and no torch type crosses this ABI.
+ *
+ * Reference interfaces replaced (paths inside the kiyosi crate):
+ *   PricingEngine::{price, price_with_seed, price_with_statistics}
+ *       crates/kiyosi/src/risk/analytics.rs:771,782,796
+ *   MonteCarloVanillaEngine (European)       engines/monte_carlo.rs:1093-1141,1254-1330
+ *   MonteCarloAutocallableEngine::{price, price_many}
+ *                                             engines/monte_carlo/autocallable.rs:119-152,293-430
+ *   MonteCarloAccumulatorEngine               engines/monte_carlo/accumulator.rs:91-218
+ *   MonteCarloDigitalEngine                   engines/monte_carlo/digital.rs:55-130
+ *   MonteCarloVanillaEngine (American, LSMC)  engines/monte_carlo/american.rs:955-1455
+ *   MonteCarloEstimate / status               engines/monte_carlo.rs:858-1001
+ *   Error variants                            crates/kiyosi/src/error.rs:19-48
+ */
+#ifndef KIYOSI_GB300_KGPU_H
+#define KIYOSI_GB300_KGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KGPU_ABI_VERSION 1
+
+/* Status codes map one-to-one onto kiyosi's Error variants (error.rs:19-48), plus a
+ * device error.  KGPU_INTERRUPTED is Error::Io(Interrupted) from cancellation. */
+typedef enum kgpu_status {
+    KGPU_OK = 0,
+    KGPU_INVALID_INPUT = 1,
+    KGPU_MISSING_HISTORY = 2,
+    KGPU_UNSUPPORTED_OPERATION = 3,
+    KGPU_GREEK_UNAVAILABLE = 4,
+    KGPU_COMPUTATION_FAILURE = 5,
+    KGPU_ROOT_NOT_BRACKETED = 6,
+    KGPU_INTERRUPTED = 7,
+    KGPU_DEVICE_ERROR = 8
+} kgpu_status;
+
+/* MonteCarloSampling (monte_carlo.rs:71-80). */
+enum { KGPU_SAMPLING_PSEUDO_RANDOM = 0, KGPU_SAMPLING_SOBOL = 1 };
+
+/* Arithmetic of the path kernels.  FP64 follows the reference's arithmetic step for step;
+ * FP32 steps paths in single precision with compensated per-thread payoff sums and
+ * FP64 cross-block reductions. */
+enum { KGPU_PRECISION_FP64 = 0, KGPU_PRECISION_FP32 = 1 };
+
+/* Launch schedule.  PLAIN: one contract per launch, one thread per sample, the
+ * reference's 256-sample blocks as CUDA blocks, sequential scaled-Welford moments per
+ * block merged in block order.  PERSISTENT: one launch for the whole book; warps pull
+ * (contract, tile) work items from a device queue and refill finished lanes with the
+ * next path of the tile. */
+enum { KGPU_SCHEDULE_PLAIN = 0, KGPU_SCHEDULE_PERSISTENT = 1 };
+
+/* MonteCarloSettings (monte_carlo.rs:86-105) plus the GPU controls. */
+typedef struct kgpu_settings {
+    int32_t path_count;   /* default path count; kgpu_contract.path_count > 0 overrides */
+    int32_t sampling;     /* KGPU_SAMPLING_* */
+    int32_t antithetic;   /* pairs Z and -Z */
+    int32_t precision;    /* KGPU_PRECISION_* */
+    int32_t schedule;     /* KGPU_SCHEDULE_* */
+    int32_t tile_paths;   /* persistent schedule: paths per work item (0 = autotuned) */
+    uint64_t seed;        /* resolved seed (the host resolves entropy seeds first) */
+} kgpu_settings;
+
+/* Models.  Rates are flat, as every reference MC engine requires (engines.rs:133-136). */
+enum { KGPU_MODEL_BSM = 0, KGPU_MODEL_HESTON = 1, KGPU_MODEL_LOCAL_VOL = 2 };
+
+typedef struct kgpu_model {
+    int32_t kind;           /* KGPU_MODEL_* */
+    int32_t lv_time_count;  /* local volatility: >= 2 time nodes */
+    int32_t lv_spot_count;  /* local volatility: >= 2 spot nodes */
+    int32_t reserved;
+    double spot;            /* spot at valuation */
+    double rate;            /* flat risk-free rate */
+    double dividend;        /* flat dividend yield */
+    double volatility;      /* BSM sigma */
+    double v0, kappa, theta, xi, rho;  /* Heston (market/heston.rs:58-227) */
+    /* Local volatility surface (market/local_volatility.rs:322-359): bilinear in (years
+     * since lv_times[0], absolute spot) with both axes clamped; values[time][spot]. */
+    const double* lv_times;
+    const double* lv_spots;
+    const double* lv_values;
+} kgpu_model;
+
+/* Payoff families. */
+enum {
+    KGPU_PAYOFF_EUROPEAN = 0,     /* exact terminal sampling, one dimension (monte_carlo.rs:1165-1252) */
+    KGPU_PAYOFF_VANILLA_PATH = 1, /* vanilla payoff of the spot after stepping every grid step */
+    KGPU_PAYOFF_ASIAN = 2,        /* arithmetic average of the spots at FIXING steps */
+    KGPU_PAYOFF_AUTOCALLABLE = 3, /* snowball / phoenix / binary / ternary (autocallable.rs:823-862) */
+    KGPU_PAYOFF_ACCUMULATOR = 4,  /* accumulator.rs:160-216 */
+    KGPU_PAYOFF_DIGITAL = 5       /* terminal digital, one dimension (digital.rs:111-130) */
+};
+
+/* One simulated grid step of a contract.  For BSM the transition is the reference's
+ * transition() (monte_carlo.rs:2123-2137) computed on the host:
+ *   drift = (r - q - sigma^2/2) dt,  diffusion = sigma sqrt(dt).
+ * For Heston and local volatility drift = dt and diffusion = sqrt(dt); the kernel
+ * forms the state-dependent transition.  `time` is the step's start in years since
+ * valuation, `discount` the discount factor exp(-r t_end) at the step's end. */
+typedef struct kgpu_step {
+    double drift;
+    double diffusion;
+    double time;
+    double discount;
+} kgpu_step;
+
+/* Per-step flags (one byte per step, same indexing as kgpu_step). */
+enum {
+    KGPU_STEP_KNOCK_IN = 1,    /* daily knock-in observation (autocallable) */
+    KGPU_STEP_EVENT = 2,       /* cash event (autocallable) or knock-out observation (accumulator) */
+    KGPU_STEP_FIXING = 4,      /* Asian fixing */
+    KGPU_STEP_ACCUMULATE = 8   /* accumulator purchase date */
+};
+
+/* Autocallable cash event (CashEvent, autocallable.rs:524-562).  Thresholds are log
+ * returns relative to the valuation spot (numerics.rs:80-92 log_ratio).  payment[k] is
+ * the discounted amount for k = coupon_due | (knocked_out << 1), i.e. the reference's
+ * discounted_payment() evaluated on the host for the four outcomes. */
+typedef struct kgpu_event {
+    double knock_out;        /* log KO threshold; ignored unless has_knock_out */
+    double coupon_barrier;   /* log coupon threshold */
+    double payment[4];
+    int32_t has_knock_out;
+    int32_t step;            /* grid step index of the event, ascending within a contract */
+} kgpu_event;
+
+/* Brownian-bridge plan (BridgePlan, autocallable.rs:451-515).  Intervals end at cash
+ * events or expiry; `daily` entries are per grid step (weight, width). */
+typedef struct kgpu_bridge_interval {
+    int32_t end;        /* grid step index ending the interval */
+    int32_t reserved;
+    double drift;
+    double diffusion;
+} kgpu_bridge_interval;
+
+typedef struct kgpu_bridge_daily {
+    double weight;      /* fraction of the remaining interval covered by this step */
+    double width;       /* sigma sqrt(dt (1 - fraction)) */
+} kgpu_bridge_daily;
+
+/* Contract flags. */
+enum {
+    KGPU_C_HAS_KNOCK_IN = 1,     /* knock_in threshold present */
+    KGPU_C_KNOCKED_IN = 2,       /* already knocked in at valuation */
+    KGPU_C_EXPIRY_KNOCK_IN = 4,  /* knock-in observed at expiry */
+    KGPU_C_DOWNSIDE = 8,         /* knocked-in redemption is the capped downside */
+    KGPU_C_BRIDGE = 16,          /* sample with the Brownian bridge plan */
+    KGPU_C_ASSET_DIGITAL = 32    /* digital pays the asset (no payout amount) */
+};
+
+/* A contract's plan.  Field groups are used by the payoff families named beside them. */
+typedef struct kgpu_contract {
+    int32_t payoff;          /* KGPU_PAYOFF_* */
+    int32_t flags;           /* KGPU_C_* */
+    int32_t path_count;      /* > 0 overrides kgpu_settings.path_count */
+    int32_t step_count;      /* simulated steps (sampling dimensions follow from the model) */
+    int64_t step_offset;     /* first kgpu_step / flag / bridge daily entry */
+    int32_t event_offset;    /* first kgpu_event */
+    int32_t event_count;
+    int32_t bridge_offset;   /* first kgpu_bridge_interval */
+    int32_t bridge_count;
+    /* vanilla / Asian / European / digital / accumulator */
+    double strike;
+    double sign;             /* +1 call, -1 put */
+    /* European and digital terminal sampling (EuropeanPayoff::new, monte_carlo.rs:1170-1222) */
+    double diffusion;
+    double half_variance;
+    double moneyness;
+    double log_scale;        /* price = mean payoff * exp(log_scale) */
+    /* autocallable */
+    double knock_in;         /* log KI threshold */
+    double initial_cash;     /* coupon fixed at valuation (Initial::coupon) */
+    double terminal_base;    /* principal + rebate at expiry */
+    double terminal_plain;   /* maturity coupon x accrual when not knocked in */
+    double terminal_fixed;   /* fixed coupon x accrual when knocked in (not downside) */
+    double downside_lower;   /* settlement strikes and the note's initial spot */
+    double downside_upper;
+    double downside_initial;
+    double final_discount;   /* discount factor at expiry */
+    /* accumulator (accumulator.rs:91-218) */
+    double knock_out;        /* log KO threshold */
+    double quantity;         /* quantity already accrued at valuation */
+    double daily_quantity;
+    double acceleration;
+    double log_strike;       /* log_ratio(strike, spot) */
+} kgpu_contract;
+
+/* A book of contracts sharing one model.  Arrays are indexed through the offsets in
+ * each kgpu_contract; bridge_daily has one entry per grid step (may be NULL when no
+ * contract uses KGPU_C_BRIDGE); events and intervals may be NULL when unused. */
+typedef struct kgpu_book {
+    int32_t contract_count;
+    int32_t reserved;
+    const kgpu_contract* contracts;
+    int64_t step_total;
+    const kgpu_step* steps;
+    const uint8_t* step_flags;
+    const kgpu_bridge_daily* bridge_daily;
+    int32_t event_total;
+    int32_t interval_total;
+    const kgpu_event* events;
+    const kgpu_bridge_interval* intervals;
+} kgpu_book;
+
+/* MonteCarloUncertaintyStatus (monte_carlo.rs:868-894). */
+enum {
+    KGPU_UNCERTAINTY_AVAILABLE = 0,
+    KGPU_UNCERTAINTY_UNSUPPORTED_SAMPLING = 1,
+    KGPU_UNCERTAINTY_INSUFFICIENT_OBSERVATIONS = 2,
+    KGPU_UNCERTAINTY_INCOMPLETE_ANTITHETIC_PAIR = 3,
+    KGPU_UNCERTAINTY_ZERO_OBSERVED_VARIANCE = 4
+};
+
+/* MonteCarloEstimate (monte_carlo.rs:858-865) per contract, plus GPU diagnostics. */
+typedef struct kgpu_estimate {
+    double price;
+    double standard_error;       /* valid when status == KGPU_UNCERTAINTY_AVAILABLE */
+    double sample_error;         /* i.i.d.-formula error, also reported for Sobol */
+    int32_t uncertainty_status;  /* KGPU_UNCERTAINTY_* */
+    int32_t reserved;
+    uint64_t seed;
+    double path_steps;           /* paths x grid steps represented by the estimate */
+    double executed_steps;       /* grid steps actually simulated (early exits excluded) */
+} kgpu_estimate;
+
+typedef struct kgpu_context kgpu_context;
+
+/* Creates a context on `device` (CUDA ordinal).  One context per thread, or serialise
+ * calls on a shared context: a context owns one stream and its scratch buffers. */
+kgpu_status kgpu_context_create(int device, kgpu_context** out);
+void kgpu_context_destroy(kgpu_context* ctx);
+
+/* The last error message recorded on `ctx` (thread-local when ctx is NULL). */
+const char* kgpu_last_error_message(const kgpu_context* ctx);
+
+/* Prices every contract of `book` under `model`.  `out` has book->contract_count
+ * entries.  `cancel_flag` (may be NULL) is polled between launches and by persistent
+ * kernels once per work item through host-mapped memory; a nonzero value ends the call
+ * with KGPU_INTERRUPTED and no partial result (cancellation.rs:33-100).
+ * Replaces PricingEngine::price_with_statistics of the MC engines and
+ * MonteCarloAutocallableEngine::price_many (autocallable.rs:119-125). */
+kgpu_status kgpu_price_book(kgpu_context* ctx, const kgpu_model* model, const kgpu_book* book,
+                            const kgpu_settings* settings, kgpu_estimate* out,
+                            const volatile int32_t* cancel_flag);
+
+/* Device-resident variant for callers that keep plans in HBM and time the kernels
+ * alone: `book` pointers are device pointers except `book->contracts` which is host;
+ * the call stages nothing from the host beyond the contract table. */
+kgpu_status kgpu_price_book_device(kgpu_context* ctx, const kgpu_model* model,
+                                   const kgpu_book* device_book,
+                                   const kgpu_settings* settings, kgpu_estimate* out);
+
+/* Raw normal stream of one reference block: the `count` normals that block `block`
+ * draws from Pcg32::new(seed, block) with Box-Muller (monte_carlo.rs:1678-1703,
+ * 1830-1894), starting at normal index `first`.  precision selects FP64 or FP32
+ * transforms.  Integer words are bit-exact; normals follow the precision. */
+kgpu_status kgpu_pcg_normals(kgpu_context* ctx, uint64_t seed, uint64_t block, uint64_t first,
+                             int64_t count, int32_t precision, double* out);
+
+/* Raw PCG32 words of stream `stream` starting at word `first` (Pcg32::next, advance). */
+kgpu_status kgpu_pcg_words(kgpu_context* ctx, uint64_t seed, uint64_t stream, uint64_t first,
+                           int64_t count, uint32_t* out);
+
+/* Scrambled Sobol integers (52-bit) for points [first, first+count) of `dimension`
+ * out of `dimensions` (sobol.rs:85-174), and their inverse-normal transforms. */
+kgpu_status kgpu_sobol_points(kgpu_context* ctx, uint64_t seed, int32_t dimensions,
+                              int32_t dimension, uint64_t first, int64_t count,
+                              uint64_t* bits_out, double* normals_out, int32_t precision);
+
+/* ---------------------------------------------------------------------------------
+ * American exercise by least-squares Monte Carlo (american.rs:955-1455).
+ * --------------------------------------------------------------------------------- */
+enum { KGPU_BASIS_QUADRATIC = 0, KGPU_BASIS_POLY3 = 1, KGPU_BASIS_MLP = 2 };
+
+typedef struct kgpu_lsmc_settings {
+    int32_t path_count;
+    int32_t exercise_dates;    /* exercise intervals (step_count of the reference) */
+    int32_t substeps;          /* Euler substeps per exercise interval (Heston) */
+    int32_t basis;             /* KGPU_BASIS_* */
+    int32_t sampling;          /* KGPU_SAMPLING_PSEUDO_RANDOM only for Heston */
+    int32_t mlp_epochs;        /* MLP basis: epochs per exercise date */
+    int32_t mlp_batch;         /* MLP basis: minibatch size */
+    int32_t mlp_hidden;        /* MLP basis: hidden width (64) */
+    double mlp_learning_rate;
+    uint64_t seed;
+    uint64_t mlp_seed;
+} kgpu_lsmc_settings;
+
+typedef struct kgpu_lsmc_result {
+    double price;              /* in-sample LSMC price, max(immediate, estimate) */
+    double standard_error;     /* of the discounted cash flows */
+    double out_of_sample;      /* lower bound on fresh paths, NaN when not requested */
+    double out_of_sample_error;
+    double wall_ms;            /* device time of the whole pricing */
+    double path_store_ms;      /* forward pass writing the path store */
+    double regression_ms;      /* backward regression / training */
+} kgpu_lsmc_result;
+
+/* Prices an American put or call (sign) with strike `strike` and expiry `expiry`
+ * (years) under `model` (BSM or Heston).  `fresh_seed` != `settings.seed` also runs the
+ * out-of-sample pass with the fitted exercise policy (american.rs:574-637). */
+kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double strike,
+                            double sign, double expiry, const kgpu_lsmc_settings* settings,
+                            uint64_t fresh_seed, kgpu_lsmc_result* out);
+
+/* Instrumentation of the last call on `ctx`: device time from the first to the last
+ * kernel of the call (CUDA events on the context's stream) and the number of kernel
+ * launches it made. */
+double kgpu_context_last_kernel_ms(const kgpu_context* ctx);
+int32_t kgpu_context_last_launches(const kgpu_context* ctx);
+
+/* Library identification. */
+int32_t kgpu_abi_version(void);
+int32_t kgpu_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KIYOSI_GB300_KGPU_H */

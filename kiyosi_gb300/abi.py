@@ -1,0 +1,189 @@
+"""ctypes mirror of include/kgpu.h (the C ABI of libkiyosi_gpu.so).
+
+Field order and types match the header exactly; `tests/test_abi.py` checks the struct
+sizes against the compiled library.
+"""
+import ctypes as C
+
+KGPU_OK = 0
+KGPU_INVALID_INPUT = 1
+KGPU_MISSING_HISTORY = 2
+KGPU_UNSUPPORTED_OPERATION = 3
+KGPU_GREEK_UNAVAILABLE = 4
+KGPU_COMPUTATION_FAILURE = 5
+KGPU_ROOT_NOT_BRACKETED = 6
+KGPU_INTERRUPTED = 7
+KGPU_DEVICE_ERROR = 8
+
+SAMPLING_PSEUDO_RANDOM = 0
+SAMPLING_SOBOL = 1
+PRECISION_FP64 = 0
+PRECISION_FP32 = 1
+SCHEDULE_PLAIN = 0
+SCHEDULE_PERSISTENT = 1
+
+MODEL_BSM = 0
+MODEL_HESTON = 1
+MODEL_LOCAL_VOL = 2
+
+PAYOFF_EUROPEAN = 0
+PAYOFF_VANILLA_PATH = 1
+PAYOFF_ASIAN = 2
+PAYOFF_AUTOCALLABLE = 3
+PAYOFF_ACCUMULATOR = 4
+PAYOFF_DIGITAL = 5
+
+STEP_KNOCK_IN = 1
+STEP_EVENT = 2
+STEP_FIXING = 4
+STEP_ACCUMULATE = 8
+
+C_HAS_KNOCK_IN = 1
+C_KNOCKED_IN = 2
+C_EXPIRY_KNOCK_IN = 4
+C_DOWNSIDE = 8
+C_BRIDGE = 16
+C_ASSET_DIGITAL = 32
+
+UNCERTAINTY_NAMES = {
+    0: "available",
+    1: "unsupported_sampling",
+    2: "insufficient_observations",
+    3: "incomplete_antithetic_pair",
+    4: "zero_observed_variance",
+}
+
+BASIS_QUADRATIC = 0
+BASIS_POLY3 = 1
+BASIS_MLP = 2
+
+_D = C.c_double
+_I = C.c_int32
+_P = C.POINTER
+
+
+class Settings(C.Structure):
+    _fields_ = [("path_count", _I), ("sampling", _I), ("antithetic", _I), ("precision", _I),
+                ("schedule", _I), ("tile_paths", _I), ("seed", C.c_uint64)]
+
+
+class Model(C.Structure):
+    _fields_ = [("kind", _I), ("lv_time_count", _I), ("lv_spot_count", _I), ("reserved", _I),
+                ("spot", _D), ("rate", _D), ("dividend", _D), ("volatility", _D),
+                ("v0", _D), ("kappa", _D), ("theta", _D), ("xi", _D), ("rho", _D),
+                ("lv_times", _P(_D)), ("lv_spots", _P(_D)), ("lv_values", _P(_D))]
+
+
+class Step(C.Structure):
+    _fields_ = [("drift", _D), ("diffusion", _D), ("time", _D), ("discount", _D)]
+
+
+class Event(C.Structure):
+    _fields_ = [("knock_out", _D), ("coupon_barrier", _D), ("payment", _D * 4),
+                ("has_knock_out", _I), ("step", _I)]
+
+
+class BridgeInterval(C.Structure):
+    _fields_ = [("end", _I), ("reserved", _I), ("drift", _D), ("diffusion", _D)]
+
+
+class BridgeDaily(C.Structure):
+    _fields_ = [("weight", _D), ("width", _D)]
+
+
+class Contract(C.Structure):
+    _fields_ = [("payoff", _I), ("flags", _I), ("path_count", _I), ("step_count", _I),
+                ("step_offset", C.c_int64), ("event_offset", _I), ("event_count", _I),
+                ("bridge_offset", _I), ("bridge_count", _I),
+                ("strike", _D), ("sign", _D),
+                ("diffusion", _D), ("half_variance", _D), ("moneyness", _D), ("log_scale", _D),
+                ("knock_in", _D), ("initial_cash", _D), ("terminal_base", _D),
+                ("terminal_plain", _D), ("terminal_fixed", _D), ("downside_lower", _D),
+                ("downside_upper", _D), ("downside_initial", _D), ("final_discount", _D),
+                ("knock_out", _D), ("quantity", _D), ("daily_quantity", _D),
+                ("acceleration", _D), ("log_strike", _D)]
+
+
+class Book(C.Structure):
+    _fields_ = [("contract_count", _I), ("reserved", _I), ("contracts", _P(Contract)),
+                ("step_total", C.c_int64), ("steps", _P(Step)), ("step_flags", _P(C.c_uint8)),
+                ("bridge_daily", _P(BridgeDaily)), ("event_total", _I), ("interval_total", _I),
+                ("events", _P(Event)), ("intervals", _P(BridgeInterval))]
+
+
+class Estimate(C.Structure):
+    _fields_ = [("price", _D), ("standard_error", _D), ("sample_error", _D),
+                ("uncertainty_status", _I), ("reserved", _I), ("seed", C.c_uint64),
+                ("path_steps", _D), ("executed_steps", _D)]
+
+
+class LsmcSettings(C.Structure):
+    _fields_ = [("path_count", _I), ("exercise_dates", _I), ("substeps", _I), ("basis", _I),
+                ("sampling", _I), ("mlp_epochs", _I), ("mlp_batch", _I), ("mlp_hidden", _I),
+                ("mlp_learning_rate", _D), ("seed", C.c_uint64), ("mlp_seed", C.c_uint64)]
+
+
+class LsmcResult(C.Structure):
+    _fields_ = [("price", _D), ("standard_error", _D), ("out_of_sample", _D),
+                ("out_of_sample_error", _D), ("wall_ms", _D), ("path_store_ms", _D),
+                ("regression_ms", _D)]
+
+
+STRUCT_SIZES = {
+    "kgpu_settings": C.sizeof(Settings),
+    "kgpu_model": C.sizeof(Model),
+    "kgpu_step": C.sizeof(Step),
+    "kgpu_event": C.sizeof(Event),
+    "kgpu_bridge_interval": C.sizeof(BridgeInterval),
+    "kgpu_bridge_daily": C.sizeof(BridgeDaily),
+    "kgpu_contract": C.sizeof(Contract),
+    "kgpu_book": C.sizeof(Book),
+    "kgpu_estimate": C.sizeof(Estimate),
+    "kgpu_lsmc_settings": C.sizeof(LsmcSettings),
+    "kgpu_lsmc_result": C.sizeof(LsmcResult),
+}
+
+# Every entry point include/kgpu.h declares.
+EXPORTED_SYMBOLS = (
+    "kgpu_context_create", "kgpu_context_destroy", "kgpu_last_error_message",
+    "kgpu_price_book", "kgpu_price_book_device", "kgpu_pcg_normals", "kgpu_pcg_words",
+    "kgpu_sobol_points", "kgpu_lsmc_price", "kgpu_context_last_kernel_ms",
+    "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count",
+)
+
+
+def declare(lib):
+    """Declares argument and result types of every kgpu_* entry point on `lib`."""
+    V = C.c_void_p
+    lib.kgpu_context_create.argtypes = [C.c_int, _P(V)]
+    lib.kgpu_context_create.restype = _I
+    lib.kgpu_context_destroy.argtypes = [V]
+    lib.kgpu_context_destroy.restype = None
+    lib.kgpu_last_error_message.argtypes = [V]
+    lib.kgpu_last_error_message.restype = C.c_char_p
+    lib.kgpu_price_book.argtypes = [V, _P(Model), _P(Book), _P(Settings), _P(Estimate),
+                                    _P(_I)]
+    lib.kgpu_price_book.restype = _I
+    lib.kgpu_price_book_device.argtypes = [V, _P(Model), _P(Book), _P(Settings), _P(Estimate)]
+    lib.kgpu_price_book_device.restype = _I
+    lib.kgpu_pcg_normals.argtypes = [V, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int64, _I,
+                                     _P(_D)]
+    lib.kgpu_pcg_normals.restype = _I
+    lib.kgpu_pcg_words.argtypes = [V, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int64,
+                                   _P(C.c_uint32)]
+    lib.kgpu_pcg_words.restype = _I
+    lib.kgpu_sobol_points.argtypes = [V, C.c_uint64, _I, _I, C.c_uint64, C.c_int64,
+                                      _P(C.c_uint64), _P(_D), _I]
+    lib.kgpu_sobol_points.restype = _I
+    lib.kgpu_lsmc_price.argtypes = [V, _P(Model), _D, _D, _D, _P(LsmcSettings), C.c_uint64,
+                                    _P(LsmcResult)]
+    lib.kgpu_lsmc_price.restype = _I
+    lib.kgpu_context_last_kernel_ms.argtypes = [V]
+    lib.kgpu_context_last_kernel_ms.restype = C.c_double
+    lib.kgpu_context_last_launches.argtypes = [V]
+    lib.kgpu_context_last_launches.restype = _I
+    lib.kgpu_abi_version.argtypes = []
+    lib.kgpu_abi_version.restype = _I
+    lib.kgpu_device_count.argtypes = []
+    lib.kgpu_device_count.restype = _I
+    return lib

@@ -1,0 +1,63 @@
+// Internal state of a kgpu_context.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/kgpu.h"
+
+namespace kgpu {
+
+// Grow-only device allocation owned by a context.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    kgpu_status ensure(size_t n);
+    void release();
+};
+
+void build_sobol(int dims, uint64_t seed, std::vector<uint64_t>& directions,
+                 std::vector<uint64_t>& shifts);
+
+}  // namespace kgpu
+
+struct kgpu_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    std::mutex mu;
+    std::string error;
+    // book staging
+    kgpu::DeviceBuffer contracts, steps, flags, events, intervals, daily, lv;
+    // plain schedule
+    kgpu::DeviceBuffer partials, merged;
+    // persistent schedule
+    kgpu::DeviceBuffer items, order, first_item, tiles, tile_out, queue;
+    // Sobol sequence cache (one sequence per (seed, dims))
+    kgpu::DeviceBuffer sobol_dirs, sobol_shifts;
+    int sobol_dims = 0;
+    uint64_t sobol_seed = 0;
+    // LSMC
+    kgpu::DeviceBuffer lsmc_store, lsmc_cash, lsmc_sums, lsmc_coef, lsmc_misc, mlp_params,
+        mlp_scratch;
+    // raw streams
+    kgpu::DeviceBuffer stream_out;
+    // cancellation word mirrored into host-mapped memory for persistent kernels
+    volatile int* cancel_host = nullptr;
+    int* cancel_dev = nullptr;
+    // instrumentation of the last call
+    double last_kernel_ms = 0.0;
+    int last_launches = 0;
+    size_t h2d_bytes = 0;
+
+    std::vector<kgpu::DeviceBuffer*> buffers() {
+        return {&contracts, &steps,     &flags,     &events,   &intervals, &daily,     &lv,
+                &partials,  &merged,    &items,     &order,    &first_item, &tiles,    &tile_out,
+                &queue,     &sobol_dirs, &sobol_shifts, &lsmc_store, &lsmc_cash, &lsmc_sums,
+                &lsmc_coef, &lsmc_misc, &mlp_params, &mlp_scratch, &stream_out};
+    }
+};

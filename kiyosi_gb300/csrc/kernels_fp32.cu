@@ -1,0 +1,4 @@
+// FP32 kernels: single-precision path arithmetic on the reference's integer streams.
+#define REAL float
+#define PRECISION fp32
+#include "kernels_impl.cuh"

@@ -1,0 +1,5 @@
+// FP64 kernels.  Compiled with --fmad=false so that every product and sum is rounded
+// separately, as in the Rust reference; fma() appears exactly where it calls mul_add.
+#define REAL double
+#define PRECISION fp64
+#include "kernels_impl.cuh"

@@ -1,0 +1,111 @@
+// Instantiation body shared by kernels_fp64.cu and kernels_fp32.cu; REAL and PRECISION
+// are defined by the including translation unit.
+#include "launch.h"
+
+namespace kgpu {
+
+template <int MODEL, bool SOBOL>
+static cudaError_t plain_one(int blocks, size_t smem, cudaStream_t s, const PlainArgs& a,
+                             const kgpu_model& m, const double* lv) {
+    auto k = plain_kernel<REAL, MODEL, SOBOL>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    k<<<blocks, kThreads, smem, s>>>(a, m, lv);
+    return cudaGetLastError();
+}
+
+template <int MODEL, bool SOBOL>
+static cudaError_t persistent_one(int blocks, size_t smem, cudaStream_t s,
+                                  const PersistentArgs& a, const kgpu_model& m, const double* lv) {
+    auto k = persistent_kernel<REAL, MODEL, SOBOL>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    k<<<blocks, kThreads, smem, s>>>(a, m, lv);
+    return cudaGetLastError();
+}
+
+template <int MODEL, bool SOBOL>
+static int occupancy_one(size_t smem) {
+    auto k = persistent_kernel<REAL, MODEL, SOBOL>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
+        return 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kThreads, smem) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
+}
+
+#define KGPU_DISPATCH(FN, ...)                                                         \
+    switch (model * 2 + int(sobol)) {                                                  \
+        case 0: return FN<KGPU_MODEL_BSM, false>(__VA_ARGS__);                         \
+        case 1: return FN<KGPU_MODEL_BSM, true>(__VA_ARGS__);                          \
+        case 2: return FN<KGPU_MODEL_HESTON, false>(__VA_ARGS__);                      \
+        case 3: return FN<KGPU_MODEL_HESTON, true>(__VA_ARGS__);                       \
+        case 4: return FN<KGPU_MODEL_LOCAL_VOL, false>(__VA_ARGS__);                   \
+        default: return FN<KGPU_MODEL_LOCAL_VOL, true>(__VA_ARGS__);                   \
+    }
+
+#define KGPU_CAT2(a, b) a##b
+#define KGPU_CAT(a, b) KGPU_CAT2(a, b)
+
+cudaError_t KGPU_CAT(launch_plain_, PRECISION)(int model, bool sobol, int blocks, size_t smem,
+                                               cudaStream_t s, const PlainArgs& a,
+                                               const kgpu_model& m, const double* lv) {
+    KGPU_DISPATCH(plain_one, blocks, smem, s, a, m, lv)
+}
+
+cudaError_t KGPU_CAT(launch_persistent_, PRECISION)(int model, bool sobol, int blocks, size_t smem,
+                                                    cudaStream_t s, const PersistentArgs& a,
+                                                    const kgpu_model& m, const double* lv) {
+    KGPU_DISPATCH(persistent_one, blocks, smem, s, a, m, lv)
+}
+
+int KGPU_CAT(persistent_occupancy_, PRECISION)(int model, bool sobol, size_t smem) {
+    KGPU_DISPATCH(occupancy_one, smem)
+}
+
+// Normals first..first+count of block `block`, one thread per Box-Muller pair.
+static __global__ void pcg_normals_kernel(uint64_t seed, uint64_t block, uint64_t first, int64_t count,
+                                   double* out) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    uint64_t index = first + uint64_t(i);
+    Pcg g = pcg_new(seed, block);
+    pcg_advance(g, (index / 2) * 4);
+    uint64_t b1 = pcg_bits52(g), b2 = pcg_bits52(g);
+    REAL c, s;
+    box_muller(b1, b2, &c, &s);
+    out[i] = double((index & 1) ? s : c);
+}
+
+static __global__ void sobol_points_kernel(SobolTables t, int dim, uint64_t first, int64_t count,
+                                    uint64_t* bits, double* normals) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    uint64_t index = first + uint64_t(i);
+    uint64_t x = t.shifts[dim];
+    uint64_t g = index ^ (index >> 1);
+    while (g) {
+        x ^= t.directions[size_t(__ffsll(g) - 1) * t.dims + dim];
+        g &= g - 1;
+    }
+    if (bits) bits[i] = x;
+    if (normals) normals[i] = double(sobol_normal(x, REAL()));
+}
+
+cudaError_t KGPU_CAT(launch_pcg_normals_, PRECISION)(uint64_t seed, uint64_t block, uint64_t first,
+                                                     int64_t count, double* out, cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    pcg_normals_kernel<<<unsigned((count + 255) / 256), 256, 0, s>>>(seed, block, first, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t KGPU_CAT(launch_sobol_points_, PRECISION)(const SobolTables& t, int dim, uint64_t first,
+                                                      int64_t count, uint64_t* bits,
+                                                      double* normals, cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    sobol_points_kernel<<<unsigned((count + 255) / 256), 256, 0, s>>>(t, dim, first, count, bits,
+                                                                      normals);
+    return cudaGetLastError();
+}
+
+}  // namespace kgpu

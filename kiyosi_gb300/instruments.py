@@ -1,0 +1,209 @@
+"""Contracts priced by the Monte Carlo engines.
+
+These mirror the reference's instruments (crates/kiyosi/src/instruments/) for the fields
+the Monte Carlo path reads.  Observation schedules are given as year fractions after the
+valuation time (Actual/365 Fixed); calendar and schedule generation are host-side
+inputs, so callers pass the resolved observation times.
+"""
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+from .errors import InvalidInputError
+
+CALL = "call"
+PUT = "put"
+
+
+def _sign(option_type: str) -> float:
+    if option_type not in (CALL, PUT):
+        raise InvalidInputError("option_type must be 'call' or 'put'")
+    return 1.0 if option_type == CALL else -1.0
+
+
+def _times(values: Sequence[float], expiry: float, name: str) -> List[float]:
+    out = [float(v) for v in values]
+    if any(not math.isfinite(v) for v in out):
+        raise InvalidInputError(f"{name} must be finite")
+    if any(b <= a for a, b in zip(out, out[1:])):
+        raise InvalidInputError(f"{name} must be strictly increasing")
+    if out and (out[0] < 0.0 or out[-1] > expiry):
+        raise InvalidInputError(f"{name} must lie within the contract's life")
+    return out
+
+
+@dataclass(frozen=True)
+class EuropeanOption:
+    option_type: str
+    strike: float
+    expiry: float  # years after valuation
+
+    def __post_init__(self):
+        _sign(self.option_type)
+        if not (self.strike > 0.0 and self.expiry >= 0.0):
+            raise InvalidInputError("strike must be positive and expiry nonnegative")
+
+    @property
+    def sign(self) -> float:
+        return _sign(self.option_type)
+
+
+@dataclass(frozen=True)
+class AmericanOption(EuropeanOption):
+    pass
+
+
+@dataclass(frozen=True)
+class DigitalOption(EuropeanOption):
+    payout: Optional[float] = None  # cash amount; None pays the asset
+
+
+@dataclass(frozen=True)
+class AsianOption:
+    """Arithmetic average-price option on the spots at `fixings` (years)."""
+    option_type: str
+    strike: float
+    expiry: float
+    fixings: Sequence[float]
+
+    def __post_init__(self):
+        _sign(self.option_type)
+        object.__setattr__(self, "fixings", tuple(_times(self.fixings, self.expiry, "fixings")))
+        if not self.fixings:
+            raise InvalidInputError("an Asian option needs at least one fixing")
+
+    @property
+    def sign(self) -> float:
+        return _sign(self.option_type)
+
+
+@dataclass(frozen=True)
+class Observation:
+    """One observation date of an autocallable: knock-out level (absolute spot, or None),
+    coupon barrier level (absolute spot, or None) and the annual coupon rate accrued on
+    knock-out (snowball)."""
+    time: float
+    knock_out_level: Optional[float] = None
+    coupon_barrier_level: Optional[float] = None
+    coupon_rate: float = 0.0
+
+
+@dataclass(frozen=True)
+class AutocallableNote:
+    """Snowball, binary/ternary snowball or Phoenix note (instruments/autocallable.rs).
+
+    knocked-in redemption is either the capped downside (`fixed_knock_in_coupon` None):
+        principal + rebate + (clamp(S, lower, upper) - upper) / initial_spot
+    or a fixed annual coupon.  Without knock-in the note pays principal + rebate +
+    maturity_coupon_rate x accrual.  Phoenix notes pay `period_coupon` at each coupon
+    observation whose barrier is met.
+    """
+    initial_spot: float
+    expiry: float
+    observations: Sequence[Observation]
+    knock_in_level: Optional[float] = None
+    knock_in_times: Optional[Sequence[float]] = None  # daily monitoring; None = expiry only
+    upper_strike: float = 0.0
+    lower_strike: float = 0.0
+    maturity_coupon_rate: float = 0.0
+    period_coupon: float = 0.0
+    fixed_knock_in_coupon: Optional[float] = None
+    principal: float = 1.0
+    rebate_rate: float = 0.0
+    annual_rebate_rate: float = 0.0
+    effective_time: float = 0.0
+    knocked_in: bool = False
+
+    def __post_init__(self):
+        obs = tuple(self.observations)
+        object.__setattr__(self, "observations", obs)
+        _times([o.time for o in obs], self.expiry, "observations")
+        if self.knock_in_times is not None:
+            object.__setattr__(self, "knock_in_times",
+                               tuple(_times(self.knock_in_times, self.expiry, "knock_in_times")))
+        if not (self.initial_spot > 0.0 and self.expiry > 0.0):
+            raise InvalidInputError("initial spot and expiry must be positive")
+        if self.upper_strike == 0.0:
+            object.__setattr__(self, "upper_strike", self.initial_spot)
+        if self.lower_strike > self.upper_strike:
+            raise InvalidInputError("lower strike must not exceed the upper strike")
+
+    def rebate_payment(self, time: float) -> float:
+        """AutocallableNote::rebate_payment (instruments/autocallable.rs:1415-1418)."""
+        return self.rebate_rate + self.annual_rebate_rate * (time - self.effective_time)
+
+    def knock_out_payment(self, obs: Observation) -> float:
+        """AutocallableNote::knock_out_payment (instruments/autocallable.rs:1419-1424)."""
+        return (self.principal + self.rebate_payment(obs.time)
+                + obs.coupon_rate * (obs.time - self.effective_time))
+
+    def terminal(self, spot: float, knocked_in: bool) -> float:
+        """AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)."""
+        base = self.principal + self.rebate_payment(self.expiry)
+        if knocked_in:
+            if self.fixed_knock_in_coupon is None:
+                clamped = min(max(spot, self.lower_strike), self.upper_strike)
+                return base + (clamped - self.upper_strike) / self.initial_spot
+            coupon = self.fixed_knock_in_coupon
+        else:
+            coupon = self.maturity_coupon_rate
+        return base + coupon * (self.expiry - self.effective_time)
+
+    def knock_in_affects_payoff(self) -> bool:
+        """instruments/autocallable.rs:1323-1332."""
+        if self.knock_in_level is None:
+            return False
+        if self.fixed_knock_in_coupon is not None:
+            return self.fixed_knock_in_coupon != self.maturity_coupon_rate
+        return self.lower_strike != self.upper_strike or self.maturity_coupon_rate != 0.0
+
+
+def SnowballOption(maturity_coupon_rate: float, initial_spot: float, knock_in_level: float,
+                   upper_strike: float, lower_strike: float, expiry: float,
+                   autocall_observations: Sequence[Observation],
+                   knock_in_times: Optional[Sequence[float]] = None, **kw) -> AutocallableNote:
+    """Basic snowball: knock-out pays principal plus the accrued annual coupon; otherwise
+    the maturity coupon if no knock-in occurred, or the capped downside after knock-in."""
+    return AutocallableNote(initial_spot=initial_spot, expiry=expiry,
+                            observations=autocall_observations, knock_in_level=knock_in_level,
+                            knock_in_times=knock_in_times, upper_strike=upper_strike,
+                            lower_strike=lower_strike, maturity_coupon_rate=maturity_coupon_rate,
+                            **kw)
+
+
+def PhoenixOption(coupon_per_period: float, initial_spot: float, knock_in_level: float,
+                  upper_strike: float, lower_strike: float, expiry: float,
+                  observations: Sequence[Observation],
+                  knock_in_times: Optional[Sequence[float]] = None, **kw) -> AutocallableNote:
+    """Phoenix: `coupon_per_period` at each observation whose coupon barrier is met."""
+    return AutocallableNote(initial_spot=initial_spot, expiry=expiry, observations=observations,
+                            knock_in_level=knock_in_level, knock_in_times=knock_in_times,
+                            upper_strike=upper_strike, lower_strike=lower_strike,
+                            period_coupon=coupon_per_period, **kw)
+
+
+@dataclass(frozen=True)
+class Accumulator:
+    """Accumulator (instruments/accumulator.rs): buys `daily_quantity` at each
+    accumulation date (times `acceleration` when the spot is beyond the strike), knocked
+    out at observation dates; settles quantity x (S - K) for calls."""
+    option_type: str
+    strike: float
+    knock_out_level: float
+    expiry: float
+    accumulation_times: Sequence[float]
+    knock_out_times: Sequence[float]
+    daily_quantity: float = 1.0
+    acceleration: float = 2.0
+    quantity: float = 0.0
+
+    def __post_init__(self):
+        _sign(self.option_type)
+        object.__setattr__(self, "accumulation_times",
+                           tuple(_times(self.accumulation_times, self.expiry, "accumulation_times")))
+        object.__setattr__(self, "knock_out_times",
+                           tuple(_times(self.knock_out_times, self.expiry, "knock_out_times")))
+
+    @property
+    def sign(self) -> float:
+        return _sign(self.option_type)

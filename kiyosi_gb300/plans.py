@@ -1,0 +1,412 @@
+"""Host-side plans: the per-step transitions, events and thresholds the reference's
+engines build before sampling, packed into the kgpu_* structs of include/kgpu.h.
+
+Each builder restates one reference planning routine:
+  european()       EuropeanPayoff::new           engines/monte_carlo.rs:1170-1222
+  digital()        MonteCarloDigitalEngine        engines/monte_carlo/digital.rs:75-110
+  path_vanilla()   path_samples over a uniform grid with transition() (monte_carlo.rs:2123)
+  asian()          arithmetic average of fixing spots on a uniform grid
+  autocallable()   prepare_sample_on_grid        engines/monte_carlo/autocallable.rs:293-430
+                   BridgePlan::new               autocallable.rs:464-515
+                   CashEvent::{new, discounted_payment} autocallable.rs:532-562
+  accumulator()    MonteCarloAccumulatorEngine   engines/monte_carlo/accumulator.rs:91-160
+A builder returns either a Known value (no sampling) or a ContractPlan; BookBuilder
+packs plans into one kgpu_book.
+"""
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import abi
+from .errors import ComputationFailureError, InvalidInputError
+from .instruments import (Accumulator, AsianOption, AutocallableNote, DigitalOption,
+                          EuropeanOption)
+from .market import (BlackScholesMertonParameters, HestonParameters, LocalVolatilitySurface,
+                     PricingContext, discounted_product, log_ratio, safe_log_returns)
+
+STEP_DTYPE = np.dtype(abi.Step)
+EVENT_DTYPE = np.dtype(abi.Event)
+INTERVAL_DTYPE = np.dtype(abi.BridgeInterval)
+DAILY_DTYPE = np.dtype(abi.BridgeDaily)
+CONTRACT_DTYPE = np.dtype(abi.Contract)
+
+
+@dataclass
+class Known:
+    """A price that needs no sampling (expiry reached, sigma = 0, settled note)."""
+    value: float
+
+
+@dataclass
+class ContractPlan:
+    contract: np.ndarray                 # one CONTRACT_DTYPE record
+    steps: np.ndarray                    # STEP_DTYPE[step_count]
+    flags: np.ndarray                    # uint8[step_count]
+    events: np.ndarray = field(default_factory=lambda: np.zeros(0, EVENT_DTYPE))
+    intervals: np.ndarray = field(default_factory=lambda: np.zeros(0, INTERVAL_DTYPE))
+    daily: Optional[np.ndarray] = None   # DAILY_DTYPE[step_count] when bridged
+
+    @property
+    def record(self):
+        return self.contract[0]
+
+
+def _unstable():
+    return ComputationFailureError("Monte Carlo produced a non-finite parameter, path or result")
+
+
+def transition(rate, dividend, sigma, time, discount_time):
+    """transition (engines/monte_carlo.rs:2123-2137)."""
+    drift = (rate - dividend - 0.5 * sigma * sigma) * time
+    diffusion = sigma * math.sqrt(time)
+    log_discount = -rate * discount_time
+    if not (math.isfinite(drift) and math.isfinite(diffusion) and math.isfinite(log_discount)):
+        raise _unstable()
+    return drift, diffusion, log_discount
+
+
+def _new_contract(payoff: int) -> np.ndarray:
+    c = np.zeros(1, CONTRACT_DTYPE)
+    c["payoff"] = payoff
+    c["sign"] = 1.0
+    return c
+
+
+def _grid_steps(ctx: PricingContext, times: List[float]):
+    """Per-step records of a grid ending at `times` (ascending, > 0)."""
+    model = ctx.model
+    n = len(times)
+    steps = np.zeros(n, STEP_DTYPE)
+    previous = 0.0
+    for i, t in enumerate(times):
+        dt = t - previous
+        if isinstance(model, BlackScholesMertonParameters):
+            drift, diffusion, log_discount = transition(model.rate, model.dividend,
+                                                        model.volatility, dt, t)
+        else:
+            drift, diffusion, log_discount = dt, math.sqrt(dt), -model.rate * t
+        steps[i] = (drift, diffusion, previous, math.exp(log_discount))
+        previous = t
+    return steps
+
+
+def _uniform_times(expiry: float, count: int) -> List[float]:
+    return [expiry * (i + 1) / count for i in range(count)]
+
+
+def european(option: EuropeanOption, ctx: PricingContext):
+    """EuropeanPayoff::new (monte_carlo.rs:1170-1222): exact terminal sampling."""
+    model = ctx.model
+    if not isinstance(model, BlackScholesMertonParameters):
+        raise InvalidInputError("the European Monte Carlo engine requires BSM parameters")
+    sign = option.sign
+    time = option.expiry
+    if time == 0.0:
+        return Known(max(sign * (ctx.spot - option.strike), 0.0))
+    rate, dividend, sigma = model.rate, model.dividend, model.volatility
+    if sigma == 0.0:
+        forward = ctx.spot * math.exp((rate - dividend) * time)
+        return Known(max(sign * (forward - option.strike), 0.0) * math.exp(-rate * time))
+    diffusion = sigma * math.sqrt(time)
+    carry = (rate - dividend) * time
+    half_variance = (0.5 * diffusion) * diffusion
+    drift = carry - half_variance
+    if not (math.isfinite(drift) and math.isfinite(diffusion)):
+        raise _unstable()
+    moneyness = (log_ratio(ctx.spot, option.strike) + carry) - half_variance
+    log_scale = (math.log(ctx.spot) - dividend * time) if sign > 0 else (
+        math.log(option.strike) - rate * time)
+    c = _new_contract(abi.PAYOFF_EUROPEAN)
+    c["strike"] = option.strike
+    c["sign"] = sign
+    c["diffusion"] = diffusion
+    c["half_variance"] = half_variance
+    c["moneyness"] = moneyness
+    c["log_scale"] = log_scale
+    c["step_count"] = 1
+    steps = np.zeros(1, STEP_DTYPE)
+    steps[0] = (drift, diffusion, 0.0, math.exp(-rate * time))
+    return ContractPlan(c, steps, np.zeros(1, np.uint8))
+
+
+def digital(option: DigitalOption, ctx: PricingContext):
+    """MonteCarloDigitalEngine::native (digital.rs:75-121): d2 standardisation, cash or
+    asset payment exp(exponent)."""
+    model = ctx.model
+    sign = option.sign
+    time = option.expiry
+    if time == 0.0:
+        hit = (ctx.spot > option.strike) if sign > 0 else (ctx.spot < option.strike)
+        return Known((option.payout if option.payout is not None else ctx.spot) if hit else 0.0)
+    rate, dividend, sigma = model.rate, model.dividend, model.volatility
+    root = math.sqrt(time)
+    width = sigma * root
+    carry = (rate - dividend) * time
+    moneyness = log_ratio(ctx.spot, option.strike) + carry
+    d2 = moneyness / width - 0.5 * width
+    asset = option.payout is None
+    amount = ctx.spot if asset else option.payout
+    drift = (-dividend - 0.5 * sigma * sigma) * time if asset else -rate * time
+    c = _new_contract(abi.PAYOFF_DIGITAL)
+    c["flags"] = abi.C_ASSET_DIGITAL if asset else 0
+    c["strike"] = amount
+    c["sign"] = sign
+    c["diffusion"] = width
+    c["moneyness"] = d2
+    c["log_scale"] = drift
+    c["step_count"] = 1
+    steps = np.zeros(1, STEP_DTYPE)
+    steps[0] = (drift, width, 0.0, math.exp(-rate * time))
+    return ContractPlan(c, steps, np.zeros(1, np.uint8))
+
+
+def path_vanilla(option: EuropeanOption, ctx: PricingContext, step_count: int):
+    """Vanilla payoff after `step_count` uniform log-Euler steps (the reference's generic
+    D-dimensional sampler path_samples, monte_carlo.rs:1498, with transition())."""
+    if step_count < 1:
+        raise InvalidInputError("step_count must be positive")
+    times = _uniform_times(option.expiry, step_count)
+    steps = _grid_steps(ctx, times)
+    c = _new_contract(abi.PAYOFF_VANILLA_PATH)
+    c["strike"] = option.strike
+    c["sign"] = option.sign
+    c["step_count"] = step_count
+    c["final_discount"] = math.exp(-ctx.rate * option.expiry)
+    return ContractPlan(c, steps, np.zeros(step_count, np.uint8))
+
+
+def asian(option: AsianOption, ctx: PricingContext, step_count: Optional[int] = None):
+    """Arithmetic average of the spots at the fixing times.  The grid is the fixing
+    times, refined to `step_count` uniform steps when given (each fixing must then lie on
+    the uniform grid)."""
+    fixings = list(option.fixings)
+    if step_count is None:
+        times = fixings
+    else:
+        times = _uniform_times(option.expiry, step_count)
+    flags = np.zeros(len(times), np.uint8)
+    index = {round(t, 12): i for i, t in enumerate(times)}
+    for f in fixings:
+        i = index.get(round(f, 12))
+        if i is None:
+            raise InvalidInputError("every fixing must lie on the simulation grid")
+        flags[i] |= abi.STEP_FIXING
+    c = _new_contract(abi.PAYOFF_ASIAN)
+    c["strike"] = option.strike
+    c["sign"] = option.sign
+    c["step_count"] = len(times)
+    c["final_discount"] = math.exp(-ctx.rate * option.expiry)
+    return ContractPlan(c, _grid_steps(ctx, times), flags)
+
+
+def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool = True):
+    """prepare_sample_on_grid (autocallable.rs:293-430) for a note valued before its first
+    observation: merged event and daily knock-in grid, log-space thresholds, discounted
+    cash events, and the Brownian-bridge plan when the reference would use one."""
+    model = ctx.model
+    spot = ctx.spot
+    rate, dividend = model.rate, model.dividend
+    bsm = isinstance(model, BlackScholesMertonParameters)
+    knocked_in = bool(note.knocked_in)
+    daily = (note.knock_in_times is not None and not knocked_in and note.knock_in_affects_payoff())
+    knock_in = log_ratio(note.knock_in_level, spot) if note.knock_in_level is not None else 0.0
+    expiry_knock_in = note.knock_in_level is not None and (
+        note.knock_in_times is None or (len(note.knock_in_times) > 0
+                                        and note.knock_in_times[-1] == note.expiry))
+    # future_event_times (instruments/autocallable/pricing.rs:70-106)
+    events = [o for o in note.observations if o.time > 0.0]
+    times = sorted(set([o.time for o in events] + (list(note.knock_in_times) if daily else [])
+                       + [note.expiry]))
+    times = [t for t in times if t > 0.0]
+    daily_set = set(note.knock_in_times) if daily else set()
+    event_at = {o.time: o for o in events}
+    steps = _grid_steps(ctx, times)
+    flags = np.zeros(len(times), np.uint8)
+    ev = np.zeros(len(events), EVENT_DTYPE)
+    excursion = 0.0
+    k = 0
+    for i, t in enumerate(times):
+        if bsm:
+            excursion += abs(steps[i]["drift"]) + 20.0 * steps[i]["diffusion"]
+        if t in daily_set:
+            flags[i] |= abi.STEP_KNOCK_IN
+        o = event_at.get(t)
+        if o is not None:
+            flags[i] |= abi.STEP_EVENT
+            # CashEvent::new (autocallable.rs:532-550)
+            has_ko = o.knock_out_level is not None
+            ko = log_ratio(o.knock_out_level, spot) if has_ko else 0.0
+            barrier = log_ratio(o.coupon_barrier_level if o.coupon_barrier_level is not None
+                                else 0.0, spot)
+            period_coupon = note.period_coupon if o.coupon_barrier_level is not None else 0.0
+            redemption = note.knock_out_payment(o) if has_ko else 0.0
+            log_discount = -rate * t
+            payments = []
+            for outcome in range(4):
+                coupon_due, knocked_out = outcome & 1, outcome >> 1
+                coupon = period_coupon if coupon_due else 0.0
+                amount = redemption + coupon if knocked_out else coupon
+                payments.append(discounted_product(1.0, amount, log_discount))
+            ev[k] = (ko, barrier, tuple(payments), int(has_ko), i)
+            k += 1
+    c = _new_contract(abi.PAYOFF_AUTOCALLABLE)
+    flag = 0
+    if note.knock_in_level is not None:
+        flag |= abi.C_HAS_KNOCK_IN
+    if knocked_in:
+        flag |= abi.C_KNOCKED_IN
+    if expiry_knock_in:
+        flag |= abi.C_EXPIRY_KNOCK_IN
+    if note.fixed_knock_in_coupon is None:
+        flag |= abi.C_DOWNSIDE
+    c["step_count"] = len(times)
+    c["event_count"] = len(events)
+    c["knock_in"] = knock_in
+    c["initial_cash"] = 0.0
+    c["terminal_base"] = note.principal + note.rebate_payment(note.expiry)
+    c["terminal_plain"] = note.terminal(0.0, False)
+    c["terminal_fixed"] = note.terminal(0.0, True) if note.fixed_knock_in_coupon is not None else 0.0
+    c["downside_lower"] = note.lower_strike
+    c["downside_upper"] = note.upper_strike
+    c["downside_initial"] = note.initial_spot
+    c["final_discount"] = math.exp(-rate * times[-1])
+    plan = ContractPlan(c, steps, flags, ev)
+    low, high = safe_log_returns(spot)
+    if (allow_bridge and bsm and daily and low <= excursion <= high and low <= -excursion <= high):
+        bridge = _bridge_plan(times, steps, flags, model)
+        if bridge is not None:
+            plan.intervals, plan.daily = bridge
+            c["flags"] = flag | abi.C_BRIDGE
+            c["bridge_count"] = len(plan.intervals)
+            return plan
+    c["flags"] = flag
+    return plan
+
+
+def _bridge_plan(times, steps, flags, model):
+    """BridgePlan::new (autocallable.rs:464-515)."""
+    rate, dividend, sigma = model.rate, model.dividend, model.volatility
+    intervals = []
+    first = 0
+    has_gap = False
+    n = len(times)
+    for end in range(n):
+        if (flags[end] & abi.STEP_EVENT) or end + 1 == n:
+            has_gap |= end - first >= 8
+            start = 0.0 if first == 0 else times[first - 1]
+            drift, diffusion, _ = transition(rate, dividend, sigma, times[end] - start, 0.0)
+            intervals.append((end, 0, drift, diffusion))
+            first = end + 1
+    if not has_gap:
+        return None
+    daily = np.zeros(n, DAILY_DTYPE)
+    first = 0
+    previous = 0.0
+    for end, _, _, _ in intervals:
+        end_time = times[end]
+        for i in range(first, end):
+            dt = times[i] - previous
+            fraction = dt / (end_time - previous)
+            if not (0.0 < fraction < 1.0):
+                return None
+            daily[i] = (fraction, sigma * math.sqrt(dt * (1.0 - fraction)))
+            previous = times[i]
+        first = end + 1
+        previous = end_time
+    return np.array(intervals, INTERVAL_DTYPE), daily
+
+
+def accumulator(option: Accumulator, ctx: PricingContext):
+    """MonteCarloAccumulatorEngine::sample (accumulator.rs:91-160) without fixed purchase
+    events: steps on the union of accumulation and knock-out dates."""
+    spot = ctx.spot
+    times = sorted(set(option.accumulation_times) | set(option.knock_out_times))
+    times = [t for t in times if t > 0.0]
+    if not times:
+        raise InvalidInputError("an accumulator needs a future observation")
+    acc = set(option.accumulation_times)
+    ko = set(option.knock_out_times)
+    flags = np.zeros(len(times), np.uint8)
+    for i, t in enumerate(times):
+        if t in ko:
+            flags[i] |= abi.STEP_EVENT
+        if t in acc:
+            flags[i] |= abi.STEP_ACCUMULATE
+    c = _new_contract(abi.PAYOFF_ACCUMULATOR)
+    c["strike"] = option.strike
+    c["sign"] = option.sign
+    c["step_count"] = len(times)
+    c["knock_out"] = log_ratio(option.knock_out_level, spot)
+    c["log_strike"] = log_ratio(option.strike, spot)
+    c["quantity"] = option.quantity
+    c["daily_quantity"] = option.daily_quantity
+    c["acceleration"] = option.acceleration
+    c["final_discount"] = math.exp(-ctx.rate * times[-1])
+    return ContractPlan(c, _grid_steps(ctx, times), flags)
+
+
+class BookBuilder:
+    """Packs contract plans into the flat arrays of one kgpu_book."""
+
+    def __init__(self):
+        self.plans: List[ContractPlan] = []
+
+    def add(self, plan: ContractPlan) -> int:
+        self.plans.append(plan)
+        return len(self.plans) - 1
+
+    def build(self, path_counts=None):
+        n = len(self.plans)
+        contracts = np.zeros(n, CONTRACT_DTYPE)
+        steps = np.concatenate([p.steps for p in self.plans]) if n else np.zeros(0, STEP_DTYPE)
+        flags = np.concatenate([p.flags for p in self.plans]) if n else np.zeros(0, np.uint8)
+        events = np.concatenate([p.events for p in self.plans]) if n else np.zeros(0, EVENT_DTYPE)
+        intervals = (np.concatenate([p.intervals for p in self.plans]) if n
+                     else np.zeros(0, INTERVAL_DTYPE))
+        any_bridge = any(p.daily is not None for p in self.plans)
+        daily = (np.concatenate([p.daily if p.daily is not None
+                                 else np.zeros(len(p.steps), DAILY_DTYPE) for p in self.plans])
+                 if any_bridge else None)
+        so = eo = io = 0
+        for i, p in enumerate(self.plans):
+            contracts[i] = p.contract[0]
+            contracts[i]["step_offset"] = so
+            contracts[i]["event_offset"] = eo
+            contracts[i]["bridge_offset"] = io
+            if path_counts is not None:
+                contracts[i]["path_count"] = int(path_counts[i])
+            so += len(p.steps)
+            eo += len(p.events)
+            io += len(p.intervals)
+        return PackedBook(contracts, steps, flags, events, intervals, daily)
+
+
+class PackedBook:
+    """Owns the numpy arrays behind a kgpu_book and exposes the struct."""
+
+    def __init__(self, contracts, steps, flags, events, intervals, daily):
+        self.contracts = np.ascontiguousarray(contracts)
+        self.steps = np.ascontiguousarray(steps)
+        self.flags = np.ascontiguousarray(flags)
+        self.events = np.ascontiguousarray(events)
+        self.intervals = np.ascontiguousarray(intervals)
+        self.daily = None if daily is None else np.ascontiguousarray(daily)
+
+    def struct(self) -> abi.Book:
+        b = abi.Book()
+        P = abi.C.POINTER
+        b.contract_count = len(self.contracts)
+        b.contracts = self.contracts.ctypes.data_as(P(abi.Contract))
+        b.step_total = len(self.steps)
+        b.steps = self.steps.ctypes.data_as(P(abi.Step))
+        b.step_flags = self.flags.ctypes.data_as(P(abi.C.c_uint8))
+        b.bridge_daily = (self.daily.ctypes.data_as(P(abi.BridgeDaily))
+                          if self.daily is not None else None)
+        b.event_total = len(self.events)
+        b.interval_total = len(self.intervals)
+        b.events = self.events.ctypes.data_as(P(abi.Event)) if len(self.events) else None
+        b.intervals = (self.intervals.ctypes.data_as(P(abi.BridgeInterval))
+                       if len(self.intervals) else None)
+        return b

@@ -1,0 +1,233 @@
+"""Monte Carlo engines with kiyosi's Python surface, pricing on the GPU.
+
+Class names, keyword arguments and MonteCarloEstimate fields mirror
+`kiyosi.pricing` (crates/kiyosi-python/src/engines/monte_carlo.rs:90-344,476-510).
+Added keywords select the GPU arithmetic (`precision`), the launch `schedule` and the
+`device`.  Pricing calls go through the C ABI of include/kgpu.h; plans are built on the
+host by kiyosi_gb300.plans.
+"""
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass, replace
+from typing import Optional, Sequence, Tuple
+
+from . import abi, plans
+from ._native import context
+from .errors import InvalidInputError, UnsupportedOperationError
+from .instruments import (Accumulator, AmericanOption, AsianOption, AutocallableNote,
+                          DigitalOption, EuropeanOption)
+from .market import PricingContext
+
+PSEUDO_RANDOM = "pseudo_random"
+SOBOL = "sobol"
+_SAMPLING = {PSEUDO_RANDOM: abi.SAMPLING_PSEUDO_RANDOM, SOBOL: abi.SAMPLING_SOBOL}
+_PRECISION = {"fp64": abi.PRECISION_FP64, "fp32": abi.PRECISION_FP32}
+_SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT}
+Z95 = 1.959963984540054
+
+
+class MonteCarloSampling:
+    PSEUDO_RANDOM = PSEUDO_RANDOM
+    SOBOL = SOBOL
+
+
+@dataclass(frozen=True)
+class MonteCarloEstimate:
+    """MonteCarloEstimate (engines/monte_carlo.rs:858-1001): price, optional standard
+    error and 95% interval, uncertainty status and replay seed; plus the GPU's i.i.d.
+    sample error (also for Sobol) and the path-step counts of the run."""
+    price: float
+    standard_error: Optional[float]
+    uncertainty_status: str
+    seed: Optional[int]
+    sample_error: float = 0.0
+    path_steps: float = 0.0
+    executed_steps: float = 0.0
+
+    @property
+    def confidence_interval(self) -> Optional[Tuple[float, float]]:
+        if self.standard_error is None:
+            return None
+        half = Z95 * self.standard_error
+        return (self.price - half, self.price + half)
+
+    @staticmethod
+    def known(value: float) -> "MonteCarloEstimate":
+        return MonteCarloEstimate(value, None, "insufficient_observations", None)
+
+    @staticmethod
+    def from_native(e: abi.Estimate) -> "MonteCarloEstimate":
+        status = abi.UNCERTAINTY_NAMES[e.uncertainty_status]
+        return MonteCarloEstimate(e.price, e.standard_error if e.uncertainty_status == 0 else None,
+                                  status, int(e.seed), e.sample_error, e.path_steps,
+                                  e.executed_steps)
+
+
+def _resolve_seed(seed):
+    if seed is not None:
+        if not (0 <= int(seed) < 2 ** 64):
+            raise InvalidInputError("seed must be an unsigned 64-bit integer")
+        return int(seed)
+    return int.from_bytes(os.urandom(8), "little")
+
+
+class _MonteCarloEngine:
+    _STATE_FIELDS = ("path_count", "seed", "max_active_workers", "sampling", "antithetic",
+                     "precision", "schedule", "device", "tile_paths")
+
+    def __init__(self, *, path_count: int = 131_072, seed: Optional[int] = None,
+                 max_active_workers: int = 0, sampling: str = PSEUDO_RANDOM,
+                 antithetic: bool = False, precision: str = "fp64", schedule: str = "plain",
+                 device: int = 0, tile_paths: int = 0):
+        if not (1 <= int(path_count) <= 2_147_483_647):
+            raise InvalidInputError("path_count must be positive")
+        if int(max_active_workers) < 0:
+            raise InvalidInputError("max_active_workers must be nonnegative")
+        if sampling not in _SAMPLING:
+            raise InvalidInputError(f"unknown sampling {sampling!r}")
+        if sampling == SOBOL and (int(path_count) & (int(path_count) - 1)) != 0:
+            raise InvalidInputError("path_count must be a power of two for Sobol sampling")
+        if precision not in _PRECISION:
+            raise InvalidInputError(f"unknown precision {precision!r}")
+        if schedule not in _SCHEDULE:
+            raise InvalidInputError(f"unknown schedule {schedule!r}")
+        self.path_count = int(path_count)
+        self.seed = None if seed is None else int(seed)
+        self.max_active_workers = int(max_active_workers)
+        self.sampling = sampling
+        self.antithetic = bool(antithetic)
+        self.precision = precision
+        self.schedule = schedule
+        self.device = int(device)
+        self.tile_paths = int(tile_paths)
+
+    def _kwargs(self):
+        return {k: getattr(self, k) for k in self._STATE_FIELDS if hasattr(self, k)}
+
+    def replace(self, **changes):
+        kw = self._kwargs()
+        kw.update(changes)
+        return type(self)(**kw)
+
+    def with_resolved_seed(self):
+        """An engine with a concrete seed (entropy when none is set), other controls kept."""
+        return self.replace(seed=_resolve_seed(self.seed))
+
+    def _settings(self, seed: int) -> abi.Settings:
+        return abi.Settings(path_count=self.path_count, sampling=_SAMPLING[self.sampling],
+                            antithetic=int(self.antithetic),
+                            precision=_PRECISION[self.precision],
+                            schedule=_SCHEDULE[self.schedule], tile_paths=self.tile_paths,
+                            seed=seed)
+
+    def _run(self, ctx: PricingContext, contract_plans, path_counts=None, cancel=None):
+        """Prices plans (Known or ContractPlan) through kgpu_price_book."""
+        seed = _resolve_seed(self.seed)
+        results = [None] * len(contract_plans)
+        builder = plans.BookBuilder()
+        index = []
+        counts = []
+        for i, p in enumerate(contract_plans):
+            if isinstance(p, plans.Known):
+                if not math.isfinite(p.value):
+                    from .errors import ComputationFailureError
+                    raise ComputationFailureError("Monte Carlo produced a non-finite result")
+                results[i] = MonteCarloEstimate(p.value, 0.0 if self.sampling == PSEUDO_RANDOM
+                                                else None,
+                                                "available" if self.sampling == PSEUDO_RANDOM
+                                                else "unsupported_sampling", None)
+            else:
+                builder.add(p)
+                index.append(i)
+                counts.append(path_counts[i] if path_counts is not None else 0)
+        if index:
+            packed = builder.build(counts)
+            native = context(self.device)
+            out = (abi.Estimate * len(index))()
+            model = ctx.kgpu_model()
+            book = packed.struct()
+            flag = None if cancel is None else C.byref(cancel)
+            native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book),
+                                                    C.byref(self._settings(seed)), out, flag))
+            for j, i in enumerate(index):
+                results[i] = MonteCarloEstimate.from_native(out[j])
+        return results
+
+    def price(self, contract, ctx: PricingContext) -> float:
+        return self.price_with_statistics(contract, ctx).price
+
+    def price_with_seed(self, contract, ctx: PricingContext):
+        e = self.price_with_statistics(contract, ctx)
+        return e.price, e.seed
+
+
+class MonteCarloVanillaEngine(_MonteCarloEngine):
+    """European (exact terminal sampling) and American (LSMC) vanilla options.
+
+    `terminal_sampling=False` steps `step_count` uniform log-Euler steps instead of the
+    exact terminal draw (the reference's generic D-dimensional sampler)."""
+    _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + ("step_count", "terminal_sampling")
+
+    def __init__(self, *, step_count: int = 50, terminal_sampling: bool = True, **kw):
+        if not (1 <= int(step_count) <= 10_000):
+            raise InvalidInputError("step_count is outside the supported Monte Carlo range")
+        super().__init__(**kw)
+        self.step_count = int(step_count)
+        self.terminal_sampling = bool(terminal_sampling)
+
+    def _plan(self, option, ctx):
+        if self.terminal_sampling:
+            return plans.european(option, ctx)
+        if option.expiry == 0.0:
+            return plans.Known(max(option.sign * (ctx.spot - option.strike), 0.0))
+        return plans.path_vanilla(option, ctx, self.step_count)
+
+    def price_with_statistics(self, option, ctx: PricingContext) -> MonteCarloEstimate:
+        if isinstance(option, AmericanOption):
+            from .lsmc import price_american
+            return price_american(self, option, ctx)
+        return self._run(ctx, [self._plan(option, ctx)])[0]
+
+    def price_strikes(self, option, ctx: PricingContext, strikes: Sequence[float]):
+        opts = [replace(option, strike=float(k)) for k in strikes]
+        return [e.price for e in self._run(ctx, [self._plan(o, ctx) for o in opts])]
+
+
+class MonteCarloAsianEngine(_MonteCarloEngine):
+    """Arithmetic average-price options on their fixing dates (optionally refined to a
+    uniform `step_count` grid)."""
+    _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + ("step_count",)
+
+    def __init__(self, *, step_count: int = 0, **kw):
+        super().__init__(**kw)
+        self.step_count = int(step_count)
+
+    def price_with_statistics(self, option: AsianOption, ctx: PricingContext):
+        return self._run(ctx, [plans.asian(option, ctx, self.step_count or None)])[0]
+
+
+class MonteCarloAutocallableEngine(_MonteCarloEngine):
+    """Snowball / Phoenix notes (autocallable.rs), singly or as a batched book."""
+
+    def price_with_statistics(self, note: AutocallableNote, ctx: PricingContext):
+        return self._run(ctx, [plans.autocallable(note, ctx)])[0]
+
+    def price_many(self, notes: Sequence[AutocallableNote], ctx: PricingContext,
+                   path_counts: Optional[Sequence[int]] = None):
+        """Prices a book of notes in input order.  Unlike the reference's price_many,
+        each note may carry its own path count."""
+        return [e.price for e in self.price_many_with_statistics(notes, ctx, path_counts)]
+
+    def price_many_with_statistics(self, notes, ctx: PricingContext, path_counts=None):
+        return self._run(ctx, [plans.autocallable(n, ctx) for n in notes], path_counts)
+
+
+class MonteCarloAccumulatorEngine(_MonteCarloEngine):
+    def price_with_statistics(self, option: Accumulator, ctx: PricingContext):
+        return self._run(ctx, [plans.accumulator(option, ctx)])[0]
+
+
+class MonteCarloDigitalEngine(_MonteCarloEngine):
+    def price_with_statistics(self, option: DigitalOption, ctx: PricingContext):
+        return self._run(ctx, [plans.digital(option, ctx)])[0]

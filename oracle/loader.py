@@ -1,0 +1,101 @@
+"""TEST INFRASTRUCTURE: ctypes loader of the FP64 CPU oracle (liboracle.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_LOCK = threading.Lock()
+
+
+def build() -> str:
+    """Compiles liboracle.so with the committed Makefile (seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return os.path.join(HERE, "liboracle.so")
+
+
+def load():
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = os.path.join(HERE, "liboracle.so")
+        sources = [os.path.join(HERE, f) for f in ("oracle.cpp", "lsmc.cpp", "oracle_core.h",
+                                                  "heston_adi.cpp")]
+        newest = max(os.path.getmtime(s) for s in sources if os.path.exists(s))
+        if not os.path.exists(path) or os.path.getmtime(path) < newest:
+            build()
+        from kiyosi_gb300 import abi
+        lib = C.CDLL(path)
+        P = C.POINTER
+        lib.kor_price_book.argtypes = [P(abi.Model), P(abi.Book), P(abi.Settings),
+                                       P(abi.Estimate), C.c_int]
+        lib.kor_price_book.restype = C.c_int
+        lib.kor_pcg_words.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int64,
+                                      P(C.c_uint32)]
+        lib.kor_pcg_normals.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int64,
+                                        P(C.c_double)]
+        lib.kor_sobol_points.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_uint64, C.c_int64,
+                                         P(C.c_uint64), P(C.c_double)]
+        lib.kor_sin_cos_turns.argtypes = [C.c_double, P(C.c_double), P(C.c_double)]
+        lib.kor_ndtri.argtypes = [C.c_double]
+        lib.kor_ndtri.restype = C.c_double
+        lib.kor_golden_european_v019.argtypes = [C.c_uint64, C.c_int64] + [C.c_double] * 6 + [
+            C.c_int, C.c_int]
+        lib.kor_golden_european_v019.restype = C.c_double
+        if hasattr(lib, "kor_lsmc_price"):
+            lib.kor_lsmc_price.argtypes = [P(abi.Model), C.c_double, C.c_double, C.c_double,
+                                           P(abi.LsmcSettings), C.c_uint64, P(abi.LsmcResult),
+                                           C.c_int]
+            lib.kor_lsmc_price.restype = C.c_int
+        if hasattr(lib, "kor_heston_adi_american"):
+            lib.kor_heston_adi_american.argtypes = [P(abi.Model), C.c_double, C.c_double,
+                                                    C.c_double, C.c_int, C.c_int, C.c_int,
+                                                    C.c_int]
+            lib.kor_heston_adi_american.restype = C.c_double
+        _LIB = lib
+        return lib
+
+
+def price_book(ctx, packed, settings, threads=0):
+    """Prices a PackedBook on the CPU oracle; returns a list of abi.Estimate."""
+    from kiyosi_gb300 import abi
+    lib = load()
+    n = len(packed.contracts)
+    out = (abi.Estimate * n)()
+    model = ctx.kgpu_model()
+    book = packed.struct()
+    status = lib.kor_price_book(C.byref(model), C.byref(book), C.byref(settings), out, threads)
+    if status != 0:
+        raise RuntimeError(f"oracle status {status}")
+    return list(out)
+
+
+def pcg_normals(seed, block, first, count):
+    lib = load()
+    out = np.zeros(count, np.float64)
+    lib.kor_pcg_normals(seed, block, first, count, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def pcg_words(seed, stream, first, count):
+    lib = load()
+    out = np.zeros(count, np.uint32)
+    lib.kor_pcg_words(seed, stream, first, count, out.ctypes.data_as(C.POINTER(C.c_uint32)))
+    return out
+
+
+def sobol_points(seed, dims, dim, first, count):
+    lib = load()
+    bits = np.zeros(count, np.uint64)
+    normals = np.zeros(count, np.float64)
+    lib.kor_sobol_points(seed, dims, dim, first, count,
+                         bits.ctypes.data_as(C.POINTER(C.c_uint64)),
+                         normals.ctypes.data_as(C.POINTER(C.c_double)))
+    return bits, normals

@@ -1,0 +1,626 @@
+// TEST INFRASTRUCTURE -- FP64 CPU oracle for kiyosi's Monte Carlo hot path.
+//
+// Restates the reference engines (kiyosi 0.23.0, paths inside crates/kiyosi/src) on the
+// plan structs of include/kgpu.h.  Used only by tests/, the smoke check and the CPU
+// baseline of bench.py; the product never links it.  Build with -ffp-contract=off.
+#include "oracle_core.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+#include "../include/kgpu.h"
+
+namespace kor {
+
+#include "../kiyosi_gb300/csrc/joe_kuo_6_21201.inc"
+
+const uint32_t* joe_kuo_table() { return kgpu_joe_kuo_table; }
+
+// --------------------------------------------------------------------------------------
+// Cephes ndtri (engines/monte_carlo/sobol.rs:253-346; Cephes by S. L. Moshier).
+// --------------------------------------------------------------------------------------
+static double poly(double value, const double* c, int n, double leading) {
+    double r = leading;
+    for (int i = 0; i < n; ++i) r = r * value + c[i];
+    return r;
+}
+
+double inverse_normal_cdf(double probability) {
+    static const double P0[] = {-59.96335010141079, 98.00107541859997, -56.67628574690703,
+                                13.931260938727968, -1.2391658386738125};
+    static const double Q0[] = {1.9544885833814176, 4.676279128988815,  86.36024213908905,
+                                -225.46268785411937, 200.26021238006066, -82.03722561683334,
+                                15.90562251262117,   -1.1833162112133};
+    static const double P1[] = {4.0554489230596245,  31.525109459989388,  57.16281922464213,
+                                44.08050738932008,   14.684956192885803,  2.1866330685079025,
+                                -0.1402560791713545, -0.03504246268278482,
+                                -0.0008574567851546854};
+    static const double Q1[] = {15.779988325646675,   45.39076351288792,   41.3172038254672,
+                                15.04253856929075,    2.504649462083094,   -0.14218292285478779,
+                                -0.03808064076915783, -0.0009332594808954574};
+    static const double P2[] = {3.2377489177694603,     6.915228890689842,
+                                3.9388102529247444,     1.3330346081580755,
+                                0.20148538954917908,    0.012371663481782003,
+                                0.00030158155350823543, 2.6580697468673755e-06,
+                                6.239745391849833e-09};
+    static const double Q2[] = {6.02427039364742,      3.6798356385616087,
+                                1.3770209948908132,    0.21623699359449663,
+                                0.013420400608854318,  0.00032801446468212774,
+                                2.8924786474538068e-06, 6.790194080099813e-09};
+    const double tail_boundary = 0.1353352832366127;
+    bool upper = probability > 1.0 - tail_boundary;
+    double tail = upper ? 1.0 - probability : probability;
+    if (tail > tail_boundary) {
+        double centered = tail - 0.5;
+        double square = centered * centered;
+        return (centered + centered * square * poly(square, P0, 5, 0.0) / poly(square, Q0, 8, 1.0)) *
+               std::sqrt(2.0 * 3.141592653589793);
+    }
+    double root = std::sqrt(-2.0 * std::log(tail));
+    double inverse = 1.0 / root;
+    double correction = inverse * (root < 8.0 ? poly(inverse, P1, 9, 0.0) / poly(inverse, Q1, 8, 1.0)
+                                              : poly(inverse, P2, 9, 0.0) / poly(inverse, Q2, 8, 1.0));
+    double quantile = root - std::log(root) / root - correction;
+    return upper ? quantile : -quantile;
+}
+
+// --------------------------------------------------------------------------------------
+// SobolSequence::new (sobol.rs:85-134)
+// --------------------------------------------------------------------------------------
+SobolSequence::SobolSequence(int dims, uint64_t seed) : dimensions(dims) {
+    directions.assign(size_t(dims) * kSobolBits, 0);
+    shifts.resize(dims);
+    const uint32_t* polynomial = kgpu_joe_kuo_table;
+    for (int dimension = 0; dimension < dims; ++dimension) {
+        uint64_t raw[kSobolBits];
+        if (dimension == 0) {
+            for (int column = 0; column < kSobolBits; ++column)
+                raw[column] = uint64_t(1) << (kSobolBits - column - 1);
+        } else {
+            int degree = int(polynomial[0]);
+            uint32_t coefficients = polynomial[1];
+            for (int column = 0; column < degree; ++column)
+                raw[column] = uint64_t(polynomial[column + 2]) << (kSobolBits - column - 1);
+            polynomial += degree + 2;
+            for (int column = degree; column < kSobolBits; ++column) {
+                uint64_t direction = raw[column - degree] ^ (raw[column - degree] >> degree);
+                for (int offset = 1; offset < degree; ++offset)
+                    if ((coefficients >> (degree - offset - 1)) & 1) direction ^= raw[column - offset];
+                raw[column] = direction;
+            }
+        }
+        Pcg32 generator(seed, uint64_t(dimension));
+        auto word = [&]() {
+            uint64_t hi = generator.next();
+            uint64_t lo = generator.next();
+            return (hi << 32) | lo;
+        };
+        shifts[dimension] = word() & kSobolMask;
+        uint64_t matrix[kSobolBits];
+        for (int row = 0; row < kSobolBits; ++row) {
+            int bit = kSobolBits - row - 1;
+            matrix[row] = (word() & (kSobolMask << (bit + 1))) | (uint64_t(1) << bit);
+        }
+        for (int column = 0; column < kSobolBits; ++column) {
+            uint64_t scrambled = 0;
+            for (int row = 0; row < kSobolBits; ++row)
+                scrambled |= uint64_t(__builtin_popcountll(raw[column] & matrix[row]) & 1)
+                             << (kSobolBits - row - 1);
+            directions[size_t(column) * dims + dimension] = scrambled;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------------------
+// Worker pool over fixed blocks, merged in block order (monte_carlo.rs:1914-1997).
+// --------------------------------------------------------------------------------------
+template <class F>
+static void run_blocks(size_t blocks, int threads, F&& simulate) {
+    if (threads <= 0) threads = int(std::max(1u, std::thread::hardware_concurrency()));
+    threads = int(std::min<size_t>(size_t(threads), blocks));
+    if (threads <= 1) {
+        for (size_t b = 0; b < blocks; ++b) simulate(b);
+        return;
+    }
+    // Contiguous chunks, one per worker, as par_chunks_mut does.
+    size_t chunk = (blocks + threads - 1) / threads;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        size_t begin = size_t(t) * chunk, end = std::min(blocks, begin + chunk);
+        if (begin >= end) break;
+        pool.emplace_back([&, begin, end]() {
+            for (size_t b = begin; b < end; ++b) simulate(b);
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
+// --------------------------------------------------------------------------------------
+// Path normals of one sample: lazy draws with skip (LazyPath / SkippingPath,
+// monte_carlo.rs:1621-1676) or the eager buffer of an antithetic pair.
+// --------------------------------------------------------------------------------------
+struct PathNormals {
+    BlockDraws* draws;
+    const double* cache;  // antithetic pair: all dimensions drawn eagerly
+    int used = 0;
+    double sign = 1.0;
+    double normal() {
+        double z = cache ? cache[used] : draws->normal();
+        ++used;
+        return sign * z;
+    }
+    void skip(int count) {
+        if (count <= 0) return;
+        if (!cache) draws->skip(uint64_t(count));
+        used += count;
+    }
+};
+
+struct Failure {
+    bool failed = false;
+};
+
+static inline double spot_at(double initial, double log_return) {
+    return discounted_product(initial, 1.0, log_return);  // scaled_value(initial, 1, lr)
+}
+
+// Local volatility lookup (market/local_volatility.rs:322-359).
+struct LocalVol {
+    int nt = 0, ns = 0;
+    const double* times = nullptr;
+    const double* spots = nullptr;
+    const double* values = nullptr;
+    std::vector<double> years;
+    static void bracket(const double* nodes, int n, double value, int* left, double* weight) {
+        int count = int(std::upper_bound(nodes, nodes + n, value) - nodes);  // partition_point(<=)
+        int l = std::min(std::max(count - 1, 0), n - 2);
+        double w = (value - nodes[l]) / (nodes[l + 1] - nodes[l]);
+        *left = l;
+        *weight = std::min(std::max(w, 0.0), 1.0);
+    }
+    static double interpolate(double low, double high, double weight) {
+        return weight <= 0.5 ? low + weight * (high - low) : high + (1.0 - weight) * (low - high);
+    }
+    double at(double time, double spot) const {
+        int row, column;
+        double tw, sw;
+        bracket(years.data(), nt, time, &row, &tw);
+        bracket(spots, ns, spot, &column, &sw);
+        const double* r0 = values + size_t(row) * ns;
+        const double* r1 = values + size_t(row + 1) * ns;
+        return interpolate(interpolate(r0[column], r0[column + 1], sw),
+                           interpolate(r1[column], r1[column + 1], sw), tw);
+    }
+};
+
+struct Model {
+    const kgpu_model* m;
+    LocalVol lv;
+    explicit Model(const kgpu_model* model) : m(model) {
+        if (m->kind == KGPU_MODEL_LOCAL_VOL) {
+            lv.nt = m->lv_time_count;
+            lv.ns = m->lv_spot_count;
+            lv.times = m->lv_times;
+            lv.spots = m->lv_spots;
+            lv.values = m->lv_values;
+            lv.years.resize(lv.nt);
+            for (int i = 0; i < lv.nt; ++i) lv.years[i] = lv.times[i] - lv.times[0];
+        }
+    }
+    int normals_per_step() const { return m->kind == KGPU_MODEL_HESTON ? 2 : 1; }
+};
+
+// One grid step of the state (log return relative to the valuation spot, variance).
+// BSM: the reference's `log_return += diffusion.mul_add(normal, drift)`.
+// Heston: full-truncation Euler in log spot; local vol: Euler in log spot with the
+// surface read at the step's start.
+struct State {
+    double lr = 0.0;
+    double v = 0.0;
+};
+
+static inline void step_state(const Model& model, const kgpu_step& st, State& s, PathNormals& n) {
+    const kgpu_model* m = model.m;
+    if (m->kind == KGPU_MODEL_BSM) {
+        s.lr += std::fma(st.diffusion, n.normal(), st.drift);
+    } else if (m->kind == KGPU_MODEL_HESTON) {
+        double z1 = n.normal();
+        double z2 = n.normal();
+        double dt = st.drift, sq = st.diffusion;
+        double vp = s.v > 0.0 ? s.v : 0.0;
+        double sv = std::sqrt(vp) * sq;
+        double zv = m->rho * z1 + std::sqrt(1.0 - m->rho * m->rho) * z2;
+        s.lr += (m->rate - m->dividend - 0.5 * vp) * dt + sv * z1;
+        s.v += m->kappa * (m->theta - vp) * dt + m->xi * sv * zv;
+    } else {
+        double spot = m->spot * std::exp(s.lr);
+        double sigma = model.lv.at(st.time, spot);
+        double dt = st.drift, sq = st.diffusion;
+        s.lr += (m->rate - m->dividend - 0.5 * sigma * sigma) * dt + sigma * sq * n.normal();
+    }
+}
+
+// --------------------------------------------------------------------------------------
+// Payoff families on one path.
+// --------------------------------------------------------------------------------------
+struct Plan {
+    const kgpu_book* book;
+    const kgpu_contract* c;
+    const kgpu_step* steps;
+    const uint8_t* flags;
+    const kgpu_event* events;
+    const kgpu_bridge_interval* intervals;
+    const kgpu_bridge_daily* daily;
+};
+
+// TerminalPayoff::at_normal (monte_carlo.rs:1238-1251)
+static double european_payoff(const kgpu_contract* c, double z, Failure& f) {
+    double distance = std::fma(c->diffusion, z, c->moneyness);
+    double payoff;
+    if (c->sign * distance <= 0.0)
+        payoff = 0.0;
+    else if (c->sign < 0.0)
+        payoff = -std::expm1(distance);
+    else
+        payoff = -std::expm1(-distance) * std::exp(std::fma(c->diffusion, z, -c->half_variance));
+    if (!std::isfinite(payoff)) f.failed = true;
+    return payoff;
+}
+
+// Digital terminal payoff (digital.rs:111-121): moneyness = d2, diffusion = width,
+// log_scale = exponent offset, strike = paid amount.
+static double digital_payoff(const kgpu_contract* c, double z) {
+    double distance = c->moneyness + z;
+    bool call = c->sign > 0.0;
+    if (!(call ? distance > 0.0 : distance < 0.0)) return 0.0;
+    double exponent = c->log_scale + ((c->flags & KGPU_C_ASSET_DIGITAL) ? c->diffusion * z : 0.0);
+    return discounted_product(c->strike, 1.0, exponent);
+}
+
+// AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
+static inline double autocallable_terminal(const kgpu_contract* c, double spot, bool knocked_in) {
+    if (knocked_in) {
+        if (c->flags & KGPU_C_DOWNSIDE) {
+            double clamped = std::min(std::max(spot, c->downside_lower), c->downside_upper);
+            return c->terminal_base + (clamped - c->downside_upper) / c->downside_initial;
+        }
+        return c->terminal_fixed;
+    }
+    return c->terminal_plain;
+}
+
+// PathPlan::payoff (autocallable.rs:823-862), one note, forward stepping.
+static double autocallable_forward(const Plan& p, const Model& model, PathNormals& n) {
+    const kgpu_contract* c = p.c;
+    bool has_ki = c->flags & KGPU_C_HAS_KNOCK_IN;
+    State s;
+    s.v = model.m->v0;
+    bool knocked_in = c->flags & KGPU_C_KNOCKED_IN;
+    double cash = c->initial_cash;
+    int ev = 0;
+    for (int i = 0; i < c->step_count; ++i) {
+        step_state(model, p.steps[i], s, n);
+        uint8_t fl = p.flags[i];
+        if (fl & KGPU_STEP_KNOCK_IN) knocked_in |= has_ki && s.lr < c->knock_in;
+        if (fl & KGPU_STEP_EVENT) {
+            const kgpu_event& e = p.events[ev++];
+            bool coupon_due = s.lr >= e.coupon_barrier;
+            bool knocked_out = e.has_knock_out && s.lr >= e.knock_out;
+            cash += e.payment[int(coupon_due) | (int(knocked_out) << 1)];
+            if (knocked_out) return cash;
+        }
+    }
+    knocked_in |= (c->flags & KGPU_C_EXPIRY_KNOCK_IN) && has_ki && s.lr < c->knock_in;
+    double spot = spot_at(model.m->spot, s.lr);
+    cash += autocallable_terminal(c, spot, knocked_in) * c->final_discount;
+    return cash;
+}
+
+// PathPlan::bridge_payoffs::<1, true> (autocallable.rs:628-736).
+static double autocallable_bridge(const Plan& p, const Model& model, PathNormals& n) {
+    const kgpu_contract* c = p.c;
+    bool has_ki = c->flags & KGPU_C_HAS_KNOCK_IN;
+    double cash = c->initial_cash;
+    bool knocked_in = c->flags & KGPU_C_KNOCKED_IN;
+    bool monitoring = !knocked_in && has_ki;
+    const double level = c->knock_in;
+    int start = 0;
+    double lr = 0.0;
+    int ev = 0;
+    for (int k = 0; k < c->bridge_count; ++k) {
+        const kgpu_bridge_interval& iv = p.intervals[k];
+        double target = lr + std::fma(iv.diffusion, n.normal(), iv.drift);
+        double minimum = std::numeric_limits<double>::infinity();
+        for (int i = start; i < iv.end; ++i) {
+            if (!monitoring || minimum < level) {
+                n.skip(iv.end - i);
+                break;
+            }
+            double z = n.normal();
+            const kgpu_bridge_daily& d = p.daily[i];
+            lr += std::fma(d.weight, target - lr, d.width * z);
+            minimum = std::min(minimum, lr);
+        }
+        lr = target;
+        start = iv.end + 1;
+        uint8_t fl = p.flags[iv.end];
+        if (monitoring && (minimum < level || ((fl & KGPU_STEP_KNOCK_IN) && lr < level))) {
+            monitoring = false;
+            knocked_in = true;
+        }
+        if (fl & KGPU_STEP_EVENT) {
+            const kgpu_event& e = p.events[ev++];
+            bool hit = e.has_knock_out && lr >= e.knock_out;
+            cash += e.payment[int(lr >= e.coupon_barrier) | (int(hit) << 1)];
+            if (hit) return cash;
+        }
+    }
+    bool hit = knocked_in || ((c->flags & KGPU_C_EXPIRY_KNOCK_IN) && has_ki && lr < level);
+    cash += autocallable_terminal(c, spot_at(model.m->spot, lr), hit) * c->final_discount;
+    return cash;
+}
+
+// Vanilla payoff after stepping every grid step, and the arithmetic average of the
+// fixing spots (Asian).
+static double path_vanilla(const Plan& p, const Model& model, PathNormals& n, bool asian) {
+    const kgpu_contract* c = p.c;
+    State s;
+    s.v = model.m->v0;
+    double sum = 0.0;
+    int fixings = 0;
+    for (int i = 0; i < c->step_count; ++i) {
+        step_state(model, p.steps[i], s, n);
+        if (asian && (p.flags[i] & KGPU_STEP_FIXING)) {
+            sum += spot_at(model.m->spot, s.lr);
+            ++fixings;
+        }
+    }
+    double underlying = asian ? sum / double(fixings) : spot_at(model.m->spot, s.lr);
+    double value = c->sign * (underlying - c->strike);
+    return (value > 0.0 ? value : 0.0) * c->final_discount;
+}
+
+// MonteCarloAccumulatorEngine path (accumulator.rs:160-216) without fixed purchase events.
+static double accumulator_path(const Plan& p, const Model& model, PathNormals& n) {
+    const kgpu_contract* c = p.c;
+    State s;
+    s.v = model.m->v0;
+    double quantity = c->quantity;
+    auto unit = [&](double lr) {
+        double distance = lr - c->log_strike;
+        if (std::fabs(distance) < 0.5) return c->sign * c->strike * std::expm1(distance);
+        double spot = spot_at(model.m->spot, lr);
+        return c->sign > 0.0 ? spot - c->strike : c->strike - spot;
+    };
+    for (int i = 0; i < c->step_count; ++i) {
+        step_state(model, p.steps[i], s, n);
+        uint8_t fl = p.flags[i];
+        if ((fl & KGPU_STEP_EVENT) && c->sign * s.lr >= c->sign * c->knock_out)
+            return quantity * unit(s.lr) * p.steps[i].discount;
+        if (fl & KGPU_STEP_ACCUMULATE)
+            quantity += c->daily_quantity *
+                        (c->sign * s.lr < c->sign * c->log_strike ? c->acceleration : 1.0);
+    }
+    return quantity * unit(s.lr) * c->final_discount;
+}
+
+static int dimensions_of(const kgpu_contract* c, const Model& model) {
+    if (c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL) return 1;
+    return c->step_count * model.normals_per_step();
+}
+
+static double evaluate(const Plan& p, const Model& model, PathNormals& n, Failure& f) {
+    const kgpu_contract* c = p.c;
+    switch (c->payoff) {
+        case KGPU_PAYOFF_EUROPEAN:
+            return european_payoff(c, n.normal(), f);
+        case KGPU_PAYOFF_DIGITAL:
+            return digital_payoff(c, n.normal());
+        case KGPU_PAYOFF_VANILLA_PATH:
+            return path_vanilla(p, model, n, false);
+        case KGPU_PAYOFF_ASIAN:
+            return path_vanilla(p, model, n, true);
+        case KGPU_PAYOFF_AUTOCALLABLE:
+            return (c->flags & KGPU_C_BRIDGE) ? autocallable_bridge(p, model, n)
+                                              : autocallable_forward(p, model, n);
+        case KGPU_PAYOFF_ACCUMULATOR:
+            return accumulator_path(p, model, n);
+    }
+    f.failed = true;
+    return 0.0;
+}
+
+struct BlockResult {
+    Moments moments, pairs;
+    Moments variance;  // i.i.d. sample moments with variance, for the sample error
+    uint64_t steps = 0;
+};
+
+// sample_paths (monte_carlo.rs:1761-1811) for one contract.
+static int price_contract(const Model& model, const Plan& p, const kgpu_settings* settings,
+                          int threads, kgpu_estimate* out) {
+    const kgpu_contract* c = p.c;
+    int64_t paths = c->path_count > 0 ? c->path_count : settings->path_count;
+    if (paths < 1) return KGPU_INVALID_INPUT;
+    bool sobol = settings->sampling == KGPU_SAMPLING_SOBOL;
+    bool antithetic = settings->antithetic != 0;
+    int dims = dimensions_of(c, model);
+    int64_t samples = antithetic ? (paths + 1) / 2 : paths;
+    size_t blocks = size_t((samples + kBlockSize - 1) / kBlockSize);
+    std::unique_ptr<SobolSequence> seq;
+    if (sobol) seq.reset(new SobolSequence(dims, settings->seed));
+    bool statistics = !sobol && (!antithetic || paths % 2 == 0);
+    bool variance = statistics && !antithetic;
+    std::vector<BlockResult> partials(blocks);
+    std::atomic<bool> failed{false};
+    run_blocks(blocks, threads, [&](size_t b) {
+        BlockResult r;
+        BlockDraws draws(settings->seed, b, seq.get());
+        std::vector<double> buffer(dims);
+        Failure f;
+        int64_t first = int64_t(b) * kBlockSize;
+        int64_t last = std::min<int64_t>(first + kBlockSize, samples);
+        for (int64_t sample = first; sample < last; ++sample) {
+            bool paired = antithetic && sample < paths / 2;
+            double positive, negative = 0.0;
+            if (paired) {
+                for (int d = 0; d < dims; ++d) buffer[d] = draws.normal();
+                PathNormals n{&draws, buffer.data()};
+                positive = evaluate(p, model, n, f);
+                PathNormals m{&draws, buffer.data()};
+                m.sign = -1.0;
+                negative = evaluate(p, model, m, f);
+                r.steps += uint64_t(std::max(n.used, m.used));
+            } else {
+                PathNormals n{&draws, nullptr};
+                positive = evaluate(p, model, n, f);
+                r.steps += uint64_t(n.used);
+                n.skip(dims - n.used);
+            }
+            if (!std::isfinite(positive) || !std::isfinite(negative)) f.failed = true;
+            r.moments.add(positive, variance);
+            r.variance.add(positive, true);
+            if (paired) {
+                r.moments.add(negative, variance);
+                r.variance.add(negative, true);
+                if (statistics) r.pairs.add(midpoint(positive, negative), true);
+            }
+            draws.next_path();
+        }
+        if (f.failed) failed = true;
+        partials[b] = r;
+    });
+    if (failed) return KGPU_COMPUTATION_FAILURE;
+    Moments total, pairs, var;
+    uint64_t executed = 0;
+    for (auto& r : partials) {
+        total.merge(r.moments, variance);
+        var.merge(r.variance, true);
+        if (statistics && antithetic) pairs.merge(r.pairs, true);
+        executed += r.steps;
+    }
+    double log_discount = (c->payoff == KGPU_PAYOFF_EUROPEAN) ? c->log_scale : 0.0;
+    double price = discounted_product(total.scale, total.mean, log_discount);
+    if (!std::isfinite(price)) return KGPU_COMPUTATION_FAILURE;
+    // sampling_standard_error (monte_carlo.rs:1435-1452) and from_sampling (939-963).
+    const Moments& u = antithetic ? pairs : total;
+    out->price = price;
+    out->seed = settings->seed;
+    out->standard_error = 0.0;
+    bool have = statistics && u.count >= 2;
+    if (have) {
+        double deviation = std::sqrt(std::max(u.m2, 0.0) / double(u.count - 1) / double(u.count));
+        double se = discounted_product(u.scale, deviation, log_discount);
+        if (se == 0.0) {
+            out->uncertainty_status = KGPU_UNCERTAINTY_ZERO_OBSERVED_VARIANCE;
+        } else {
+            out->standard_error = se;
+            out->uncertainty_status = KGPU_UNCERTAINTY_AVAILABLE;
+        }
+    } else if (sobol) {
+        out->uncertainty_status = KGPU_UNCERTAINTY_UNSUPPORTED_SAMPLING;
+    } else if (antithetic && paths % 2 != 0) {
+        out->uncertainty_status = KGPU_UNCERTAINTY_INCOMPLETE_ANTITHETIC_PAIR;
+    } else {
+        out->uncertainty_status = KGPU_UNCERTAINTY_INSUFFICIENT_OBSERVATIONS;
+    }
+    out->sample_error =
+        var.count >= 2
+            ? discounted_product(var.scale,
+                                 std::sqrt(std::max(var.m2, 0.0) / double(var.count - 1) /
+                                           double(var.count)),
+                                 log_discount)
+            : 0.0;
+    int grid = (c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL) ? 1
+                                                                                        : c->step_count;
+    out->path_steps = double(paths) * double(grid);
+    out->executed_steps = double(executed) / double(model.normals_per_step());
+    return KGPU_OK;
+}
+
+}  // namespace kor
+
+using namespace kor;
+
+extern "C" {
+
+int kor_price_book(const kgpu_model* model, const kgpu_book* book, const kgpu_settings* settings,
+                   kgpu_estimate* out, int threads) {
+    Model m(model);
+    for (int i = 0; i < book->contract_count; ++i) {
+        const kgpu_contract* c = &book->contracts[i];
+        Plan p{book,
+               c,
+               book->steps + c->step_offset,
+               book->step_flags + c->step_offset,
+               book->events ? book->events + c->event_offset : nullptr,
+               book->intervals ? book->intervals + c->bridge_offset : nullptr,
+               book->bridge_daily ? book->bridge_daily + c->step_offset : nullptr};
+        int status = price_contract(m, p, settings, threads, &out[i]);
+        if (status != KGPU_OK) return status;
+    }
+    return KGPU_OK;
+}
+
+// Raw PCG32 words of stream `stream` from word `first`.
+void kor_pcg_words(uint64_t seed, uint64_t stream, uint64_t first, int64_t count, uint32_t* out) {
+    Pcg32 g(seed, stream);
+    g.advance(first);
+    for (int64_t i = 0; i < count; ++i) out[i] = g.next();
+}
+
+// Normals `first .. first+count` of block `block` (NormalDraws with skip_normals).
+void kor_pcg_normals(uint64_t seed, uint64_t block, uint64_t first, int64_t count, double* out) {
+    BlockDraws d(seed, block, nullptr);
+    d.skip(first);
+    for (int64_t i = 0; i < count; ++i) out[i] = d.normal();
+}
+
+void kor_sobol_points(uint64_t seed, int dims, int dim, uint64_t first, int64_t count,
+                      uint64_t* bits, double* normals) {
+    SobolSequence s(dims, seed);
+    for (int64_t i = 0; i < count; ++i) {
+        uint64_t v = s.point(first + uint64_t(i), dim);
+        if (bits) bits[i] = v;
+        if (normals) normals[i] = normal_from_bits(v);
+    }
+}
+
+void kor_sin_cos_turns(double turns, double* s, double* c) { sin_cos_turns(turns, s, c); }
+double kor_ndtri(double p) { return inverse_normal_cdf(p); }
+
+// European MC price with the terminal payoff of the kiyosi 0.19.0 build that produced
+// benchmarks/quantlib/calibration/monte_carlo.json: max(sign (S_T - K), 0) with
+// S_T = S exp(fma(sigma sqrt(T), z, (r - q - sigma^2/2) T)), discounted by exp(-r T)
+// after the block-ordered Welford merge.  It uses the same normal stream and block
+// structure as the 0.23.0 engine, so the recorded per-seed prices pin that stream.
+double kor_golden_european_v019(uint64_t seed, int64_t paths, double spot, double strike,
+                                double rate, double dividend, double sigma, double time, int call,
+                                int threads) {
+    double diffusion = sigma * std::sqrt(time);
+    double drift = (rate - dividend - 0.5 * sigma * sigma) * time;
+    double sign = call ? 1.0 : -1.0;
+    size_t blocks = size_t((paths + kBlockSize - 1) / kBlockSize);
+    std::vector<Moments> partial(blocks);
+    run_blocks(blocks, threads, [&](size_t b) {
+        BlockDraws d(seed, b, nullptr);
+        Moments m;
+        int64_t first = int64_t(b) * kBlockSize, last = std::min<int64_t>(first + kBlockSize, paths);
+        for (int64_t s = first; s < last; ++s) {
+            double st = spot * std::exp(std::fma(diffusion, d.normal(), drift));
+            double v = sign * (st - strike);
+            m.add(v > 0.0 ? v : 0.0, false);
+        }
+        partial[b] = m;
+    });
+    Moments total;
+    for (auto& m : partial) total.merge(m, false);
+    return discounted_product(total.scale, total.mean, -rate * time);
+}
+
+}  // extern "C"
