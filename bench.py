@@ -1,0 +1,366 @@
+"""Throughput benchmark of the GB300 Monte Carlo engine.
+
+Workload (one "step" = one full pricing): a single snowball autocallable under BSM,
+S0=100, sigma=0.25, r=0.03, q=0, T=2y, 504 daily steps, 24 monthly knock-out
+observations at 103%, daily knock-in at 80%, 15% p.a. coupon, 2^20 Sobol paths, seed 42.
+The metric is path-steps/s = paths x grid steps / time.
+
+Arms:
+  ours (default)    FP32 persistent lane-refill kernel.  `value` times the kernels with
+                    the plan resident in HBM (kgpu_price_book_device, CUDA events on the
+                    library's stream); `e2e` times kgpu_price_book from host buffers
+                    (plan upload, kernels, estimate download) with the host clock.
+                    Also measured: the FP64 plain one-contract-per-launch path on the
+                    same random numbers, the oracle (FP64 CPU) price and a timed CPU
+                    baseline sample.
+  --impl reference  the FP64 CPU oracle (restatement of kiyosi's Rust engine, which
+                    cannot be built here) on all host cores, same workload.
+
+Prints one JSON line.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PATHS = 1 << 20
+STEPS = 504
+SEED = 42
+# Warp instructions issued per executed path-step by the FP32 persistent kernel on
+# this workload, measured with ncu (smsp__inst_executed.sum / executed path-steps,
+# profiles/persistent_kernel_snowball.txt).  Used to express the kernel's rate as a
+# fraction of the SM issue peak (4 warp-instructions per cycle per SM).
+WARP_INST_PER_EXECUTED_STEP = None
+
+
+def snowball():
+    from kiyosi_gb300.instruments import AutocallableNote, Observation
+    from kiyosi_gb300.market import BlackScholesMertonParameters, PricingContext
+    ctx = PricingContext(BlackScholesMertonParameters(0.03, 0.0, 0.25), 100.0)
+    dt = 2.0 / STEPS
+    times = [dt * (i + 1) for i in range(STEPS)]
+    obs = [Observation(times[21 * (m + 1) - 1], knock_out_level=103.0, coupon_rate=0.15)
+           for m in range(24)]
+    note = AutocallableNote(initial_spot=100.0, expiry=times[-1], observations=obs,
+                            knock_in_level=80.0, knock_in_times=times, upper_strike=100.0,
+                            lower_strike=0.0, maturity_coupon_rate=0.15)
+    return ctx, note
+
+
+def packed_plan():
+    from kiyosi_gb300 import plans
+    ctx, note = snowball()
+    b = plans.BookBuilder()
+    b.add(plans.autocallable(note, ctx))
+    return ctx, b.build()
+
+
+TUNING = {"tile_paths": 0, "ctas_per_sm": 0, "refill": 0}
+
+
+def settings(precision, schedule, paths=PATHS):
+    from kiyosi_gb300 import abi
+    return abi.Settings(path_count=paths, sampling=abi.SAMPLING_SOBOL, antithetic=0,
+                        precision=precision, schedule=schedule, seed=SEED, **TUNING)
+
+
+class Cuda:
+    """Minimal CUDA runtime access for device-resident plans and L2 flushing."""
+
+    def __init__(self):
+        for name in ("libcudart.so", "libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"):
+            try:
+                self.rt = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        self.rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        self.rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        self.rt.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+        self.rt.cudaDeviceSynchronize.argtypes = []
+        self.rt.cudaFree.argtypes = [C.c_void_p]
+        self.ptrs = []
+
+    def to_device(self, array):
+        p = C.c_void_p()
+        n = max(int(array.nbytes), 16)
+        assert self.rt.cudaMalloc(C.byref(p), n) == 0
+        if array.nbytes:
+            assert self.rt.cudaMemcpy(p, array.ctypes.data, array.nbytes, 1) == 0
+        self.ptrs.append(p)
+        return p
+
+    def flush_l2(self, nbytes=512 << 20):
+        if not hasattr(self, "scratch"):
+            self.scratch = C.c_void_p()
+            assert self.rt.cudaMalloc(C.byref(self.scratch), nbytes) == 0
+            self.scratch_bytes = nbytes
+        self.rt.cudaMemset(self.scratch, 1, self.scratch_bytes)
+        self.rt.cudaDeviceSynchronize()
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __enter__(self):
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9 or not f[1].replace(".", "").isdigit():
+                    continue
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+                for name, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_ours(args):
+    from kiyosi_gb300 import _native, abi
+    from oracle import loader
+    native = _native.context(0)
+    lib = native.lib
+    ctx, packed = packed_plan()
+    model = ctx.kgpu_model()
+    host_book = packed.struct()
+    cuda = Cuda()
+    # Device-resident plan for the kernel-only measurement.
+    dev = abi.Book()
+    dev.contract_count = 1
+    dev.contracts = host_book.contracts  # the contract table is read on the host
+    dev.step_total = host_book.step_total
+    dev.steps = C.cast(cuda.to_device(packed.steps), C.POINTER(abi.Step))
+    dev.step_flags = C.cast(cuda.to_device(packed.flags), C.POINTER(C.c_uint8))
+    dev.bridge_daily = C.cast(cuda.to_device(packed.daily), C.POINTER(abi.BridgeDaily))
+    dev.event_total = host_book.event_total
+    dev.interval_total = host_book.interval_total
+    dev.events = C.cast(cuda.to_device(packed.events), C.POINTER(abi.Event))
+    dev.intervals = C.cast(cuda.to_device(packed.intervals), C.POINTER(abi.BridgeInterval))
+    out = (abi.Estimate * 1)()
+
+    def device_call(s):
+        native.check(lib.kgpu_price_book_device(native.handle, C.byref(model), C.byref(dev),
+                                                C.byref(s), out))
+        # Copy: `out` is reused by the next call.
+        return abi.Estimate.from_buffer_copy(out[0]), native.last_kernel_ms, native.last_launches
+
+    def host_call(s):
+        native.check(lib.kgpu_price_book(native.handle, C.byref(model), C.byref(host_book),
+                                         C.byref(s), out, None))
+        return abi.Estimate.from_buffer_copy(out[0])
+
+    s32 = settings(abi.PRECISION_FP32, abi.SCHEDULE_PERSISTENT)
+    s64 = settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN)
+    for _ in range(args.warmup):
+        device_call(s32)
+    kernel_ms, launches = [], 0
+    est32 = None
+    with Clocks() as clocks:
+        for _ in range(args.steps):
+            cuda.flush_l2()
+            est32, ms, nl = device_call(s32)
+            kernel_ms.append(ms)
+            launches += nl
+    clock = clocks.summary()
+    total_ms = sum(kernel_ms)
+    path_steps = est32.path_steps
+    value = path_steps * args.steps / (total_ms / 1e3)
+    # End to end through the host-buffer C ABI call.
+    h2d = (packed.steps.nbytes + packed.flags.nbytes + packed.events.nbytes
+           + packed.intervals.nbytes + (packed.daily.nbytes if packed.daily is not None else 0)
+           + packed.contracts.nbytes)
+    d2h = C.sizeof(abi.Estimate)
+    for _ in range(max(1, args.warmup // 2)):
+        host_call(s32)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_call(s32)
+    e2e_s = time.perf_counter() - t0
+    e2e = path_steps * args.steps / e2e_s
+    # FP64 plain one-contract-per-launch path on the same random numbers.
+    device_call(s64)
+    f64_ms = []
+    for _ in range(max(1, min(args.steps, 3))):
+        cuda.flush_l2()
+        est64, ms, _ = device_call(s64)
+        f64_ms.append(ms)
+    fp64_rate = path_steps / (statistics.median(f64_ms) / 1e3)
+    # FP64 CPU oracle at full size (parity) and timed as the CPU baseline.
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ref = loader.price_book(ctx, packed, s64, threads=threads)[0]
+    cpu_s = time.perf_counter() - t0
+    se = ref.sample_error
+    executed = est32.executed_steps
+    issue = None
+    if WARP_INST_PER_EXECUTED_STEP and clock["sm_mhz"]:
+        achieved = WARP_INST_PER_EXECUTED_STEP * executed / (total_ms / args.steps / 1e3)
+        peak = 4.0 * native_sm_count(native) * clock["sm_mhz"] * 1e6
+        issue = {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9,
+                 "unit": "Gwarp-inst/s", "frac": achieved / peak, "traffic": None}
+    line = {
+        "metric": "path-steps/s (FP32 batched vs FP64 plain) at <=0.5 SE",
+        "value": value,
+        "unit": "path-steps/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded Sobol draws; benchmark contract parameters)",
+        "config": {"workload": "snowball autocallable, BSM, 2^20 Sobol paths x 504 daily "
+                               "steps, 24 monthly KO 103%, daily KI 80%, 15% p.a. coupon",
+                   "paths": PATHS, "grid_steps": STEPS, "sampling": "sobol", "seed": SEED,
+                   "precision": "fp32", "schedule": "persistent",
+                   "l2": "flushed between timed iterations (512 MiB memset)"},
+        "e2e": {"value": e2e, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "clocks": clock,
+        "roofline": issue,
+        "fp64_plain": {"value": fp64_rate, "unit": "path-steps/s",
+                       "speedup_fp32_persistent": value / fp64_rate,
+                       "price": est64.price},
+        "parity": {"fp32_price": est32.price, "oracle_fp64_price": ref.price,
+                   "sample_se": se, "fp32_error_in_se": abs(est32.price - ref.price) / se,
+                   "fp64_gpu_rel_error": abs(est64.price - ref.price) / abs(ref.price)},
+        "executed_steps_per_path": executed / PATHS,
+        "fp64_executed_steps_per_path": est64.executed_steps / PATHS,
+        "cpu_baseline": {"value": path_steps / cpu_s, "unit": "path-steps/s", "cores": threads,
+                         "kind": "port", "sample": "full workload (2^20 paths x 504 steps), "
+                                                   "one pricing, FP64 oracle"},
+    }
+    print(json.dumps(line))
+
+
+def native_sm_count(native):
+    """Multiprocessor count of device 0 (cudaDevAttrMultiProcessorCount)."""
+    rt = Cuda().rt
+    v = C.c_int(0)
+    rt.cudaDeviceGetAttribute(C.byref(v), 16, 0)
+    return v.value
+
+
+def run_kernel_only(args):
+    """Device-resident pricings of one arm only, for ncu captures of the kernels."""
+    from kiyosi_gb300 import _native, abi
+    native = _native.context(0)
+    ctx, packed = packed_plan()
+    model = ctx.kgpu_model()
+    book = packed.struct()
+    s = (settings(abi.PRECISION_FP32, abi.SCHEDULE_PERSISTENT, args.paths)
+         if args.kernel_only == "fp32" else
+         settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN, args.paths))
+    out = (abi.Estimate * 1)()
+    for _ in range(args.warmup + args.steps):
+        native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book),
+                                                C.byref(s), out, None))
+    print(json.dumps({"arm": args.kernel_only, "paths": args.paths, "price": out[0].price,
+                      "kernel_ms": native.last_kernel_ms}))
+
+
+def run_reference(args):
+    """The FP64 CPU restatement of kiyosi's engine on all host threads (the Rust reference
+    cannot be compiled here), same workload and metric."""
+    from kiyosi_gb300 import abi
+    from oracle import loader
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    ctx, packed = packed_plan()
+    threads = os.cpu_count() or 1
+    s = settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN)
+    for _ in range(args.warmup):
+        loader.price_book(ctx, packed, settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN, 1 << 14),
+                          threads=threads)
+    t0 = time.perf_counter()
+    est = None
+    for _ in range(args.steps):
+        est = loader.price_book(ctx, packed, s, threads=threads)[0]
+    elapsed = time.perf_counter() - t0
+    value = est.path_steps * args.steps / elapsed
+    line = {
+        "impl": "reference",
+        "metric": "path-steps/s (FP32 batched vs FP64 plain) at <=0.5 SE",
+        "value": value, "unit": "path-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Sobol draws; benchmark contract parameters)",
+        "config": {"workload": "snowball autocallable, BSM, 2^20 Sobol paths x 504 daily "
+                               "steps, 24 monthly KO 103%, daily KI 80%, 15% p.a. coupon",
+                   "paths": PATHS, "grid_steps": STEPS, "sampling": "sobol", "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": threads,
+                         "kind": "port", "sample": f"{args.steps} full pricings"},
+        "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "price": est.price,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--paths", type=int, default=PATHS,
+                    help="path count (profiling runs use smaller cases)")
+    ap.add_argument("--kernel-only", choices=["fp32", "fp64"],
+                    help="run only the device-resident pricing of one arm (for profilers)")
+    ap.add_argument("--tile", type=int, default=0, help="persistent tile paths (0 = default)")
+    ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")
+    ap.add_argument("--refill", type=int, default=0, help="units between lane refills (0 = 16)")
+    args = ap.parse_args()
+    TUNING.update(tile_paths=args.tile, ctas_per_sm=args.ctas_per_sm, refill=args.refill)
+    if args.kernel_only:
+        run_kernel_only(args)
+        return
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -68,7 +68,10 @@ typedef struct kgpu_settings {
     int32_t antithetic;   /* pairs Z and -Z */
     int32_t precision;    /* KGPU_PRECISION_* */
     int32_t schedule;     /* KGPU_SCHEDULE_* */
-    int32_t tile_paths;   /* persistent schedule: paths per work item (0 = autotuned) */
+    int32_t tile_paths;   /* persistent schedule: paths per work item (0 = tuned default;
+                             Sobol tiles must divide 256) */
+    int32_t ctas_per_sm;  /* persistent schedule: resident CTAs per SM (0 = occupancy limit) */
+    int32_t refill;       /* persistent schedule: path units between lane refills (0 = 16) */
     uint64_t seed;        /* resolved seed (the host resolves entropy seeds first) */
 } kgpu_settings;
 

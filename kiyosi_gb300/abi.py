@@ -64,7 +64,8 @@ _P = C.POINTER
 
 class Settings(C.Structure):
     _fields_ = [("path_count", _I), ("sampling", _I), ("antithetic", _I), ("precision", _I),
-                ("schedule", _I), ("tile_paths", _I), ("seed", C.c_uint64)]
+                ("schedule", _I), ("tile_paths", _I), ("ctas_per_sm", _I), ("refill", _I),
+                ("seed", C.c_uint64)]
 
 
 class Model(C.Structure):

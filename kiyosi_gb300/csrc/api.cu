@@ -10,6 +10,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/kgpu.h"
@@ -272,6 +273,17 @@ void estimate_from_sums(const kgpu_contract& c, const kgpu_settings& s, int64_t 
 
 bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 
+// Samples per persistent work item.  FP64 Sobol items are one reference block (they
+// share the block's high part in shared memory); FP32 Sobol items may be any divisor
+// of 256 (every lane reads its own block's row of the high table).
+int64_t persistent_tile(bool sobol, int requested, int precision) {
+    if (sobol) {
+        if (precision == KGPU_PRECISION_FP64) return 256;
+        return (requested > 0 && requested <= 256 && 256 % requested == 0) ? requested : 64;
+    }
+    return requested > 0 ? requested : 1024;
+}
+
 }  // namespace
 
 static kgpu_status ensure_sobol(kgpu_context* ctx, int dims, uint64_t seed, SobolTables* t) {
@@ -284,11 +296,32 @@ static kgpu_status ensure_sobol(kgpu_context* ctx, int dims, uint64_t seed, Sobo
         if (st != KGPU_OK) return st;
         st = upload(ctx, ctx->sobol_shifts, shifts.data(), shifts.size() * 8);
         if (st != KGPU_OK) return st;
+        if (ctx->sobol_nibbles.ensure(size_t(dims) * 32 * 8) || ctx->sobol_dirs32.ensure(size_t(dims) * 52 * 4) ||
+            ctx->sobol_shifts32.ensure(size_t(dims) * 4) || ctx->sobol_nibbles32.ensure(size_t(dims) * 32 * 4))
+            return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of Sobol tables failed");
+        sobol_nibbles_kernel<<<(dims * 32 + 255) / 256, 256, 0, ctx->stream>>>(
+            static_cast<const uint64_t*>(ctx->sobol_dirs.ptr), dims, static_cast<uint64_t*>(ctx->sobol_nibbles.ptr));
+        CUDA_TRY(ctx, cudaGetLastError());
+        auto top32 = [&](const DeviceBuffer& in, DeviceBuffer& out, int64_t n) {
+            sobol_top32_kernel<<<unsigned((n + 255) / 256), 256, 0, ctx->stream>>>(
+                static_cast<const uint64_t*>(in.ptr), n, static_cast<uint32_t*>(out.ptr));
+        };
+        top32(ctx->sobol_dirs, ctx->sobol_dirs32, int64_t(dims) * 52);
+        top32(ctx->sobol_shifts, ctx->sobol_shifts32, dims);
+        top32(ctx->sobol_nibbles, ctx->sobol_nibbles32, int64_t(dims) * 32);
+        CUDA_TRY(ctx, cudaGetLastError());
+        // `dirs` and `shifts` are host vectors freed on return.
+        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
         ctx->sobol_dims = dims;
         ctx->sobol_seed = seed;
     }
     t->directions = static_cast<const uint64_t*>(ctx->sobol_dirs.ptr);
     t->shifts = static_cast<const uint64_t*>(ctx->sobol_shifts.ptr);
+    t->nibbles = static_cast<const uint64_t*>(ctx->sobol_nibbles.ptr);
+    t->directions32 = static_cast<const uint32_t*>(ctx->sobol_dirs32.ptr);
+    t->shifts32 = static_cast<const uint32_t*>(ctx->sobol_shifts32.ptr);
+    t->nibbles32 = static_cast<const uint32_t*>(ctx->sobol_nibbles32.ptr);
+    t->high32 = static_cast<const uint32_t*>(ctx->sobol_high32.ptr);
     t->dims = dims;
     return KGPU_OK;
 }
@@ -313,6 +346,369 @@ struct CancelWatcher {
     }
 };
 
+namespace {
+
+// Everything a precision-specific runner needs about the staged call.
+struct Call {
+    kgpu_context* ctx;
+    const kgpu_model* model;
+    const kgpu_book* book;
+    kgpu_settings s;
+    kgpu_estimate* out;
+    const volatile int32_t* cancel;
+    std::vector<ContractInfo> info;
+    RawBook raw;
+    const double* lv_dev;
+    int lv_values;
+    bool sobol;
+};
+
+template <class Real>
+struct PrecisionOps;
+template <>
+struct PrecisionOps<double> {
+    static constexpr int precision = KGPU_PRECISION_FP64;
+    static cudaError_t plain(int m, bool so, int b, size_t sm, cudaStream_t st, const PlainArgs<double>& a,
+                             const kgpu_model& mo, const double* lv) {
+        return launch_plain_fp64(m, so, b, sm, st, a, mo, lv);
+    }
+    static cudaError_t persistent(int m, bool so, int b, size_t sm, cudaStream_t st,
+                                  const PersistentArgs<double>& a, const kgpu_model& mo, const double* lv) {
+        return launch_persistent_fp64(m, so, b, sm, st, a, mo, lv);
+    }
+    static int occupancy(int m, bool so, size_t sm) { return persistent_occupancy_fp64(m, so, sm); }
+    static cudaError_t contracts(const kgpu_contract* in, int n, ContractT<double>* out, cudaStream_t st) {
+        return launch_compile_contracts_fp64(in, n, out, st);
+    }
+    static cudaError_t units(const kgpu_contract* c, int n, const kgpu_bridge_interval* iv,
+                             const kgpu_bridge_daily* d, const uint8_t* f, const kgpu_event* e,
+                             UnitT<double>* out, EndT<double>* ends, cudaStream_t st) {
+        return launch_compile_units_fp64(c, n, iv, d, f, e, out, ends, st);
+    }
+};
+template <>
+struct PrecisionOps<float> {
+    static constexpr int precision = KGPU_PRECISION_FP32;
+    static cudaError_t plain(int m, bool so, int b, size_t sm, cudaStream_t st, const PlainArgs<float>& a,
+                             const kgpu_model& mo, const double* lv) {
+        return launch_plain_fp32(m, so, b, sm, st, a, mo, lv);
+    }
+    static cudaError_t persistent(int m, bool so, int b, size_t sm, cudaStream_t st,
+                                  const PersistentArgs<float>& a, const kgpu_model& mo, const double* lv) {
+        return launch_persistent_fp32(m, so, b, sm, st, a, mo, lv);
+    }
+    static int occupancy(int m, bool so, size_t sm) { return persistent_occupancy_fp32(m, so, sm); }
+    static cudaError_t contracts(const kgpu_contract* in, int n, ContractT<float>* out, cudaStream_t st) {
+        return launch_compile_contracts_fp32(in, n, out, st);
+    }
+    static cudaError_t units(const kgpu_contract* c, int n, const kgpu_bridge_interval* iv,
+                             const kgpu_bridge_daily* d, const uint8_t* f, const kgpu_event* e,
+                             UnitT<float>* out, EndT<float>* ends, cudaStream_t st) {
+        return launch_compile_units_fp32(c, n, iv, d, f, e, out, ends, st);
+    }
+};
+
+// The plan in the kernel's precision: FP64 reads the caller's arrays, FP32 converts them.
+template <class Real>
+kgpu_status compile_book(Call& k, DevBook<Real>* db);
+
+template <>
+kgpu_status compile_book<double>(Call& k, DevBook<double>* db) {
+    kgpu_context* ctx = k.ctx;
+    const int n = k.raw.contract_count;
+    if (ctx->ccontracts.ensure(size_t(n) * sizeof(ContractT<double>)))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the contract table failed");
+    CUDA_TRY(ctx, launch_compile_contracts_fp64(k.raw.contracts, n,
+                                                static_cast<ContractT<double>*>(ctx->ccontracts.ptr), ctx->stream));
+    db->contracts = static_cast<const ContractT<double>*>(ctx->ccontracts.ptr);
+    db->steps = reinterpret_cast<const StepT<double>*>(k.raw.steps);
+    db->flags = k.raw.flags;
+    db->events = reinterpret_cast<const EventT<double>*>(k.raw.events);
+    db->intervals = reinterpret_cast<const IntervalT<double>*>(k.raw.intervals);
+    db->daily = reinterpret_cast<const DailyT<double>*>(k.raw.daily);
+    db->units = nullptr;
+    db->ends = nullptr;
+    return KGPU_OK;
+}
+
+template <>
+kgpu_status compile_book<float>(Call& k, DevBook<float>* db) {
+    kgpu_context* ctx = k.ctx;
+    const RawBook& r = k.raw;
+    const int n = r.contract_count;
+    if (ctx->ccontracts.ensure(size_t(n) * sizeof(ContractT<float>)) ||
+        ctx->csteps.ensure(size_t(r.step_total) * sizeof(StepT<float>)) ||
+        ctx->cevents.ensure(size_t(r.event_total) * sizeof(EventT<float>) + 16) ||
+        ctx->cintervals.ensure(size_t(r.interval_total) * sizeof(IntervalT<float>) + 16) ||
+        ctx->cdaily.ensure((r.daily ? size_t(r.step_total) : 1) * sizeof(DailyT<float>)))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the single-precision plan failed");
+    CUDA_TRY(ctx, launch_compile_contracts_fp32(r.contracts, n,
+                                                static_cast<ContractT<float>*>(ctx->ccontracts.ptr), ctx->stream));
+    CUDA_TRY(ctx, launch_compile_arrays_fp32(r, static_cast<StepT<float>*>(ctx->csteps.ptr),
+                                             static_cast<EventT<float>*>(ctx->cevents.ptr),
+                                             static_cast<IntervalT<float>*>(ctx->cintervals.ptr),
+                                             static_cast<DailyT<float>*>(ctx->cdaily.ptr), ctx->stream));
+    db->contracts = static_cast<const ContractT<float>*>(ctx->ccontracts.ptr);
+    db->steps = static_cast<const StepT<float>*>(ctx->csteps.ptr);
+    db->flags = r.flags;
+    db->events = r.events ? static_cast<const EventT<float>*>(ctx->cevents.ptr) : nullptr;
+    db->intervals = r.intervals ? static_cast<const IntervalT<float>*>(ctx->cintervals.ptr) : nullptr;
+    db->daily = r.daily ? static_cast<const DailyT<float>*>(ctx->cdaily.ptr) : nullptr;
+    db->units = nullptr;
+    db->ends = nullptr;
+    return KGPU_OK;
+}
+
+template <class Real>
+kgpu_status run_plain(Call& k, const DevBook<Real>& db, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const kgpu_settings& s = k.s;
+    const int n = k.raw.contract_count;
+    int64_t max_blocks = 0;
+    for (int i = 0; i < n; ++i) max_blocks = std::max<int64_t>(max_blocks, (k.info[i].samples + 255) / 256);
+    if (ctx->partials.ensure(size_t(max_blocks) * sizeof(BlockPartial)) ||
+        ctx->merged.ensure(size_t(n) * sizeof(BlockPartial)))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of partials failed");
+    for (int i = 0; i < n; ++i) {
+        if (k.cancel && *k.cancel) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
+        const ContractInfo& ci = k.info[i];
+        PlainArgs<Real> a;
+        a.book = db;
+        a.contract = i;
+        a.dims = ci.dims;
+        a.paths = ci.paths;
+        a.samples = ci.samples;
+        a.seed = s.seed;
+        a.antithetic = s.antithetic;
+        a.statistics = !k.sobol && (!s.antithetic || ci.paths % 2 == 0);
+        a.variance = a.statistics && !s.antithetic;
+        a.sobol = SobolTables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+        kgpu_status st;
+        if (k.sobol && (st = ensure_sobol(ctx, ci.dims, s.seed, &a.sobol))) return st;
+        a.partials = static_cast<BlockPartial*>(ctx->partials.ptr);
+        const int blocks = int((ci.samples + 255) / 256);
+        size_t smem = plain_smem_bytes(PrecisionOps<Real>::precision, k.sobol, ci.dims, k.lv_values);
+        if (smem > 227 * 1024)
+            return fail(ctx, KGPU_INVALID_INPUT, "dimension %d exceeds the plain kernel's shared memory", ci.dims);
+        CUDA_TRY(ctx, PrecisionOps<Real>::plain(k.model->kind, k.sobol, blocks, smem, ctx->stream, a, *k.model,
+                                                k.lv_dev));
+        merge_blocks_kernel<<<1, 32, 0, ctx->stream>>>(a.partials, blocks, a.variance, a.statistics, s.antithetic,
+                                                        static_cast<BlockPartial*>(ctx->merged.ptr) + i);
+        CUDA_TRY(ctx, cudaGetLastError());
+        launches += 2;
+        if (k.cancel) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    std::vector<BlockPartial> merged(n);
+    CUDA_TRY(ctx, cudaMemcpyAsync(merged.data(), ctx->merged.ptr, sizeof(BlockPartial) * n, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n; ++i) {
+        const kgpu_contract& c = k.book->contracts[i];
+        estimate_from_moments(c, s, k.info[i].paths, merged[i], &k.out[i]);
+        int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
+        k.out[i].path_steps = double(k.info[i].paths) * grid;
+        k.out[i].executed_steps = merged[i].executed;
+        if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].standard_error))
+            return fail(ctx, KGPU_COMPUTATION_FAILURE,
+                        "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
+    }
+    return KGPU_OK;
+}
+
+template <class Real>
+kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const kgpu_settings& s = k.s;
+    const int n = k.raw.contract_count;
+    // Bridged contracts run on per-position units compiled from their bridge plans.
+    bool bridged = false;
+    for (int i = 0; i < n; ++i) bridged |= (k.book->contracts[i].flags & KGPU_C_BRIDGE) != 0;
+    if (bridged) {
+        if (ctx->cunits.ensure(size_t(k.raw.step_total) * sizeof(UnitT<Real>)) ||
+            ctx->cends.ensure(size_t(k.raw.step_total) * sizeof(EndT<Real>)))
+            return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of bridge units failed");
+        CUDA_TRY(ctx, PrecisionOps<Real>::units(k.raw.contracts, n, k.raw.intervals, k.raw.daily, k.raw.flags,
+                                                k.raw.events, static_cast<UnitT<Real>*>(ctx->cunits.ptr),
+                                                static_cast<EndT<Real>*>(ctx->cends.ptr), ctx->stream));
+        db.units = static_cast<const UnitT<Real>*>(ctx->cunits.ptr);
+        db.ends = static_cast<const EndT<Real>*>(ctx->cends.ptr);
+        launches += 1;
+    }
+    // Sobol books run one launch per sampling dimension (one sequence per launch);
+    // pseudo-random books run in a single launch.
+    std::vector<int> group_of(n, 0);
+    std::vector<int> group_dims;
+    if (k.sobol) {
+        for (int i = 0; i < n; ++i) {
+            auto it = std::find(group_dims.begin(), group_dims.end(), k.info[i].dims);
+            if (it == group_dims.end()) {
+                group_of[i] = int(group_dims.size());
+                group_dims.push_back(k.info[i].dims);
+            } else {
+                group_of[i] = int(it - group_dims.begin());
+            }
+        }
+    } else {
+        group_dims.push_back(0);
+    }
+    // Work items grouped by contract, in contract order.  Sobol tiles are one reference
+    // block (they share the block's high gray-code bits).
+    std::vector<int4> items;
+    std::vector<int64_t> value_offset(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision);
+        for (int64_t b = 0; b < k.info[i].samples; b += tile)
+            items.push_back(make_int4(i, int(b), int(std::min<int64_t>(tile, k.info[i].samples - b)), k.info[i].dims));
+        value_offset[i + 1] = value_offset[i] + k.info[i].samples;
+    }
+    // Reduction chunks of each contract's per-path values.
+    const int64_t chunk = 4096;
+    std::vector<int4> chunks;
+    std::vector<int> first_chunk(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        first_chunk[i] = int(chunks.size());
+        for (int64_t b = 0; b < k.info[i].samples; b += chunk)
+            chunks.push_back(make_int4(i, int(b), int(std::min<int64_t>(chunk, k.info[i].samples - b)), 0));
+    }
+    first_chunk[n] = int(chunks.size());
+    const int item_count = int(items.size());
+    kgpu_status st;
+    if ((st = upload(ctx, ctx->items, items.data(), items.size() * sizeof(int4))) ||
+        (st = upload(ctx, ctx->value_offset, value_offset.data(), value_offset.size() * sizeof(int64_t))) ||
+        (st = upload(ctx, ctx->chunks, chunks.data(), chunks.size() * sizeof(int4))) ||
+        (st = upload(ctx, ctx->first_item, first_chunk.data(), first_chunk.size() * sizeof(int))))
+        return st;
+    if (ctx->values.ensure(size_t(value_offset[n]) * sizeof(Real)) ||
+        ctx->tiles.ensure(chunks.size() * sizeof(TilePartial)) || ctx->tile_out.ensure(size_t(n) * sizeof(TilePartial)) ||
+        ctx->executed.ensure(size_t(n) * sizeof(unsigned long long)) || ctx->queue.ensure(sizeof(int) * 4))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of path values failed");
+    CUDA_TRY(ctx, cudaMemsetAsync(static_cast<int*>(ctx->queue.ptr) + 1, 0, sizeof(int), ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(ctx->executed.ptr, 0, size_t(n) * sizeof(unsigned long long), ctx->stream));
+    CancelWatcher watcher(k.cancel, ctx->cancel_host);
+    std::vector<int> order;
+    std::vector<int> first_item(n + 1, 0);
+    {
+        int q = 0;
+        for (int i = 0; i < n; ++i) {
+            first_item[i] = q;
+            const int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision);
+            q += int((k.info[i].samples + tile - 1) / tile);
+        }
+        first_item[n] = q;
+    }
+    for (size_t g = 0; g < group_dims.size(); ++g) {
+        order.clear();
+        std::vector<int> members;
+        for (int i = 0; i < n; ++i)
+            if (group_of[i] == int(g)) members.push_back(i);
+        // Dispatch order: most expensive contracts first.
+        std::stable_sort(members.begin(), members.end(), [&](int x, int y) {
+            return double(k.info[x].samples) * k.book->contracts[x].step_count >
+                   double(k.info[y].samples) * k.book->contracts[y].step_count;
+        });
+        for (int i : members)
+            for (int q = first_item[i]; q < first_item[i + 1]; ++q) order.push_back(q);
+        if (order.empty()) continue;
+        if (k.cancel && *k.cancel) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
+        if ((st = upload(ctx, ctx->order, order.data(), order.size() * sizeof(int)))) return st;
+        PersistentArgs<Real> a;
+        a.book = db;
+        a.items = static_cast<const int4*>(ctx->items.ptr);
+        a.order = static_cast<const int*>(ctx->order.ptr);
+        a.item_count = int(order.size());
+        a.queue = static_cast<int*>(ctx->queue.ptr);
+        a.seed = s.seed;
+        a.sobol = SobolTables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+        if (k.sobol && (st = ensure_sobol(ctx, group_dims[g], s.seed, &a.sobol))) return st;
+        if (k.sobol) {
+            // High parts of every reference block the group's contracts use.
+            int64_t blocks = 1;
+            for (int i : members) blocks = std::max<int64_t>(blocks, (k.info[i].samples + 255) / 256);
+            if (ctx->sobol_high32.ensure(size_t(blocks) * group_dims[g] * 4))
+                return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the Sobol high table failed");
+            a.sobol.high32 = static_cast<const uint32_t*>(ctx->sobol_high32.ptr);
+            const int64_t total = blocks * group_dims[g];
+            sobol_high_table_kernel<<<unsigned((total + 255) / 256), 256, 0, ctx->stream>>>(
+                a.sobol, int(blocks), static_cast<uint32_t*>(ctx->sobol_high32.ptr));
+            CUDA_TRY(ctx, cudaGetLastError());
+            launches += 1;
+        }
+        a.values = static_cast<Real*>(ctx->values.ptr);
+        a.value_offset = static_cast<const int64_t*>(ctx->value_offset.ptr);
+        a.executed = static_cast<unsigned long long*>(ctx->executed.ptr);
+        a.cancel = k.cancel ? ctx->cancel_dev : nullptr;
+        a.aborted = static_cast<int*>(ctx->queue.ptr) + 1;
+        a.refill = s.refill > 0 ? s.refill : kRefill;
+        size_t smem = persistent_smem_bytes(PrecisionOps<Real>::precision, k.sobol, k.sobol ? group_dims[g] : 0,
+                                            k.lv_values);
+        if (smem > 227 * 1024)
+            return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
+                        "Sobol dimension %d exceeds the persistent kernel's shared memory; use the plain schedule",
+                        group_dims[g]);
+        int per_sm = PrecisionOps<Real>::occupancy(k.model->kind, k.sobol, smem);
+        if (s.ctas_per_sm > 0) per_sm = std::min(per_sm, s.ctas_per_sm);
+        const int blocks = std::max(1, std::min(ctx->sm_count * per_sm, (a.item_count + kWarps - 1) / kWarps));
+        CUDA_TRY(ctx, cudaMemsetAsync(ctx->queue.ptr, 0, sizeof(int), ctx->stream));
+        CUDA_TRY(ctx, PrecisionOps<Real>::persistent(k.model->kind, k.sobol, blocks, smem, ctx->stream, a, *k.model,
+                                                     k.lv_dev));
+        launches += 1;
+        // `order` is reused by the next group: wait for this launch's upload to be consumed.
+        if (group_dims.size() > 1) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    reduce_values_kernel<Real><<<int(chunks.size()), 256, 0, ctx->stream>>>(
+        static_cast<const Real*>(ctx->values.ptr), static_cast<const int4*>(ctx->chunks.ptr),
+        static_cast<const int64_t*>(ctx->value_offset.ptr), static_cast<TilePartial*>(ctx->tiles.ptr));
+    CUDA_TRY(ctx, cudaGetLastError());
+    reduce_tiles_kernel<<<n, 256, 0, ctx->stream>>>(static_cast<const TilePartial*>(ctx->tiles.ptr),
+                                                     static_cast<const int*>(ctx->first_item.ptr),
+                                                     static_cast<TilePartial*>(ctx->tile_out.ptr));
+    CUDA_TRY(ctx, cudaGetLastError());
+    launches += 2;
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    std::vector<TilePartial> sums(n);
+    std::vector<unsigned long long> executed(n);
+    int aborted = 0;
+    CUDA_TRY(ctx, cudaMemcpyAsync(sums.data(), ctx->tile_out.ptr, sizeof(TilePartial) * n, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpyAsync(executed.data(), ctx->executed.ptr, sizeof(unsigned long long) * n,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpyAsync(&aborted, static_cast<int*>(ctx->queue.ptr) + 1, sizeof(int),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (aborted) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
+    for (int i = 0; i < n; ++i) {
+        const kgpu_contract& c = k.book->contracts[i];
+        sums[i].executed = double(executed[i]);
+        estimate_from_sums(c, s, k.info[i].paths, sums[i], &k.out[i]);
+        int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
+        k.out[i].path_steps = double(k.info[i].paths) * grid;
+        k.out[i].executed_steps = sums[i].executed;
+        if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].standard_error))
+            return fail(ctx, KGPU_COMPUTATION_FAILURE,
+                        "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
+    }
+    return KGPU_OK;
+}
+
+template <class Real>
+kgpu_status run_book(Call& k) {
+    kgpu_context* ctx = k.ctx;
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    DevBook<Real> db;
+    kgpu_status st = compile_book<Real>(k, &db);
+    if (st) return st;
+    int launches = std::is_same<Real, float>::value ? 2 : 1;
+    st = k.s.schedule == KGPU_SCHEDULE_PERSISTENT ? run_persistent<Real>(k, db, launches)
+                                                  : run_plain<Real>(k, db, launches);
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop) == cudaSuccess) ctx->last_kernel_ms = ms;
+    ctx->last_launches = launches;
+    return st;
+}
+
+}  // namespace
+
 static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, const kgpu_book* book,
                                    const kgpu_settings* settings, kgpu_estimate* out,
                                    const volatile int32_t* cancel, bool device_resident) {
@@ -327,26 +723,33 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
     const int n = book->contract_count;
     if (n < 0) return fail(ctx, KGPU_INVALID_INPUT, "negative contract count");
     if (n == 0) return KGPU_OK;
-    const kgpu_settings s = *settings;
+    Call k;
+    k.ctx = ctx;
+    k.model = model;
+    k.book = book;
+    k.s = *settings;
+    k.out = out;
+    k.cancel = cancel;
+    const kgpu_settings& s = k.s;
     if (s.precision != KGPU_PRECISION_FP64 && s.precision != KGPU_PRECISION_FP32)
         return fail(ctx, KGPU_INVALID_INPUT, "unknown precision %d", s.precision);
     if (s.sampling != KGPU_SAMPLING_PSEUDO_RANDOM && s.sampling != KGPU_SAMPLING_SOBOL)
         return fail(ctx, KGPU_INVALID_INPUT, "unknown sampling %d", s.sampling);
     if (model->kind < KGPU_MODEL_BSM || model->kind > KGPU_MODEL_LOCAL_VOL)
         return fail(ctx, KGPU_INVALID_INPUT, "unknown model %d", model->kind);
-    const bool sobol = s.sampling == KGPU_SAMPLING_SOBOL;
+    k.sobol = s.sampling == KGPU_SAMPLING_SOBOL;
     const bool persistent = s.schedule == KGPU_SCHEDULE_PERSISTENT;
     if (persistent && s.antithetic)
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
                     "the persistent schedule does not pair antithetic samples; use the plain schedule");
     // Validate contracts (MonteCarloSettings::validate, monte_carlo.rs:197-220).
-    std::vector<ContractInfo> info(n);
+    k.info.resize(n);
     for (int i = 0; i < n; ++i) {
         const kgpu_contract& c = book->contracts[i];
         int64_t paths = c.path_count > 0 ? c.path_count : s.path_count;
         if (paths < 1 || paths > 2147483647LL)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: path_count must be positive", i);
-        if (sobol && !is_pow2(paths))
+        if (k.sobol && !is_pow2(paths))
             return fail(ctx, KGPU_INVALID_INPUT, "path_count must be a power of two for Sobol sampling");
         if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_DIGITAL)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: unknown payoff %d", i, c.payoff);
@@ -354,56 +757,58 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: steps out of range", i);
         if (c.event_count < 0 || c.event_offset < 0 || c.event_offset + c.event_count > book->event_total)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: events out of range", i);
+        if (c.event_count > 0 && !book->events)
+            return fail(ctx, KGPU_INVALID_INPUT, "contract %d: events missing", i);
         if (c.flags & KGPU_C_BRIDGE) {
-            if (model->kind != KGPU_MODEL_BSM || !book->bridge_daily || c.bridge_count < 1 ||
+            if (model->kind != KGPU_MODEL_BSM || !book->bridge_daily || !book->intervals || c.bridge_count < 1 ||
                 c.bridge_offset < 0 || c.bridge_offset + c.bridge_count > book->interval_total)
                 return fail(ctx, KGPU_INVALID_INPUT, "contract %d: invalid bridge plan", i);
         }
-        if (c.payoff == KGPU_PAYOFF_AUTOCALLABLE || c.payoff == KGPU_PAYOFF_ACCUMULATOR) {
-            // Every event flag must be backed by an event record.
-            if (!device_resident) {
-                int events = 0;
-                for (int k = 0; k < c.step_count; ++k)
-                    events += (book->step_flags[c.step_offset + k] & KGPU_STEP_EVENT) != 0;
-                if (c.payoff == KGPU_PAYOFF_AUTOCALLABLE && events != c.event_count)
-                    return fail(ctx, KGPU_INVALID_INPUT, "contract %d: %d event steps but %d events",
-                                i, events, c.event_count);
-            }
+        if (!device_resident && c.payoff == KGPU_PAYOFF_AUTOCALLABLE) {
+            // Every event step must be backed by an event record.
+            int events = 0;
+            for (int q = 0; q < c.step_count; ++q) events += (book->step_flags[c.step_offset + q] & KGPU_STEP_EVENT) != 0;
+            if (events != c.event_count)
+                return fail(ctx, KGPU_INVALID_INPUT, "contract %d: %d event steps but %d events", i, events,
+                            c.event_count);
         }
-        info[i].dims = dims_of(c, model);
-        info[i].paths = paths;
-        info[i].samples = s.antithetic ? (paths + 1) / 2 : paths;
+        k.info[i].dims = dims_of(c, model);
+        k.info[i].paths = paths;
+        k.info[i].samples = s.antithetic ? (paths + 1) / 2 : paths;
     }
     kgpu_status st;
     // Stage the book.
-    DevBook db;
+    RawBook& r = k.raw;
+    r.contract_count = n;
+    r.step_total = book->step_total;
+    r.event_total = book->event_total;
+    r.interval_total = book->interval_total;
     if (!device_resident) {
         if ((st = upload(ctx, ctx->steps, book->steps, size_t(book->step_total) * sizeof(kgpu_step))) ||
             (st = upload(ctx, ctx->flags, book->step_flags, size_t(book->step_total))) ||
             (st = upload(ctx, ctx->events, book->events, size_t(book->event_total) * sizeof(kgpu_event))) ||
-            (st = upload(ctx, ctx->intervals, book->intervals,
-                         size_t(book->interval_total) * sizeof(kgpu_bridge_interval))))
+            (st = upload(ctx, ctx->intervals, book->intervals, size_t(book->interval_total) * sizeof(kgpu_bridge_interval))))
             return st;
         if (book->bridge_daily &&
             (st = upload(ctx, ctx->daily, book->bridge_daily, size_t(book->step_total) * sizeof(kgpu_bridge_daily))))
             return st;
-        db.steps = static_cast<const kgpu_step*>(ctx->steps.ptr);
-        db.flags = static_cast<const uint8_t*>(ctx->flags.ptr);
-        db.events = book->event_total ? static_cast<const kgpu_event*>(ctx->events.ptr) : nullptr;
-        db.intervals = book->interval_total ? static_cast<const kgpu_bridge_interval*>(ctx->intervals.ptr) : nullptr;
-        db.daily = book->bridge_daily ? static_cast<const kgpu_bridge_daily*>(ctx->daily.ptr) : nullptr;
+        r.steps = static_cast<const kgpu_step*>(ctx->steps.ptr);
+        r.flags = static_cast<const uint8_t*>(ctx->flags.ptr);
+        r.events = book->event_total ? static_cast<const kgpu_event*>(ctx->events.ptr) : nullptr;
+        r.intervals = book->interval_total ? static_cast<const kgpu_bridge_interval*>(ctx->intervals.ptr) : nullptr;
+        r.daily = book->bridge_daily ? static_cast<const kgpu_bridge_daily*>(ctx->daily.ptr) : nullptr;
     } else {
-        db.steps = book->steps;
-        db.flags = book->step_flags;
-        db.events = book->events;
-        db.intervals = book->intervals;
-        db.daily = book->bridge_daily;
+        r.steps = book->steps;
+        r.flags = book->step_flags;
+        r.events = book->event_total ? book->events : nullptr;
+        r.intervals = book->interval_total ? book->intervals : nullptr;
+        r.daily = book->bridge_daily;
     }
     if ((st = upload(ctx, ctx->contracts, book->contracts, size_t(n) * sizeof(kgpu_contract)))) return st;
-    db.contracts = static_cast<const kgpu_contract*>(ctx->contracts.ptr);
+    r.contracts = static_cast<const kgpu_contract*>(ctx->contracts.ptr);
     // Local volatility surface: [years since the first node][spots][values].
-    int lv_values = 0;
-    const double* lv_dev = nullptr;
+    k.lv_values = 0;
+    k.lv_dev = nullptr;
     if (model->kind == KGPU_MODEL_LOCAL_VOL) {
         const int nt = model->lv_time_count, ns = model->lv_spot_count;
         if (nt < 2 || ns < 2 || !model->lv_times || !model->lv_spots || !model->lv_values)
@@ -412,188 +817,13 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
         for (int i = 0; i < nt; ++i) lv[i] = model->lv_times[i] - model->lv_times[0];
         for (int i = 0; i < ns; ++i) lv[nt + i] = model->lv_spots[i];
         std::memcpy(&lv[nt + ns], model->lv_values, sizeof(double) * size_t(nt) * ns);
-        lv_values = int(lv.size());
+        k.lv_values = int(lv.size());
         if ((st = upload(ctx, ctx->lv, lv.data(), lv.size() * sizeof(double)))) return st;
-        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // `lv` is a stack vector
-        lv_dev = static_cast<const double*>(ctx->lv.ptr);
+        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // `lv` is a host vector
+        k.lv_dev = static_cast<const double*>(ctx->lv.ptr);
     }
     *ctx->cancel_host = 0;
-    int launches = 0;
-    bool started = false;
-    auto start_clock = [&]() -> kgpu_status {
-        if (!started) {
-            CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
-            started = true;
-        }
-        return KGPU_OK;
-    };
-    if (!persistent) {
-        // Plain schedule: one contract per launch.
-        int64_t max_blocks = 0;
-        for (int i = 0; i < n; ++i) max_blocks = std::max<int64_t>(max_blocks, (info[i].samples + 255) / 256);
-        if ((st = ctx->partials.ensure(size_t(max_blocks) * sizeof(BlockPartial)) ? KGPU_DEVICE_ERROR : KGPU_OK) ||
-            (st = ctx->merged.ensure(size_t(n) * sizeof(BlockPartial)) ? KGPU_DEVICE_ERROR : KGPU_OK))
-            return fail(ctx, st, "cudaMalloc of partials failed");
-        for (int i = 0; i < n; ++i) {
-            if (cancel && *cancel) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
-            const ContractInfo& ci = info[i];
-            PlainArgs a;
-            a.book = db;
-            a.contract = i;
-            a.dims = ci.dims;
-            a.paths = ci.paths;
-            a.samples = ci.samples;
-            a.seed = s.seed;
-            a.antithetic = s.antithetic;
-            a.statistics = !sobol && (!s.antithetic || ci.paths % 2 == 0);
-            a.variance = a.statistics && !s.antithetic;
-            a.sobol = SobolTables{nullptr, nullptr, 0};
-            if (sobol && (st = ensure_sobol(ctx, ci.dims, s.seed, &a.sobol))) return st;
-            a.partials = static_cast<BlockPartial*>(ctx->partials.ptr);
-            const int blocks = int((ci.samples + 255) / 256);
-            size_t smem = plain_smem_bytes(s.precision, sobol, ci.dims, lv_values);
-            if (smem > 227 * 1024)
-                return fail(ctx, KGPU_INVALID_INPUT, "dimension %d exceeds the plain kernel's shared memory",
-                            ci.dims);
-            if ((st = start_clock())) return st;
-            CUDA_TRY(ctx, launch_plain(s.precision, model->kind, sobol, blocks, smem, ctx->stream, a, *model, lv_dev));
-            const bool variance = a.variance;
-            merge_blocks_kernel<<<1, 32, 0, ctx->stream>>>(a.partials, blocks, variance, a.statistics,
-                                                            s.antithetic, static_cast<BlockPartial*>(ctx->merged.ptr) + i);
-            CUDA_TRY(ctx, cudaGetLastError());
-            launches += 2;
-            if (cancel) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        }
-        CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
-        std::vector<BlockPartial> merged(n);
-        CUDA_TRY(ctx, cudaMemcpyAsync(merged.data(), ctx->merged.ptr, sizeof(BlockPartial) * n,
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
-        ctx->last_kernel_ms = ms;
-        ctx->last_launches = launches;
-        for (int i = 0; i < n; ++i) {
-            const kgpu_contract& c = book->contracts[i];
-            estimate_from_moments(c, s, info[i].paths, merged[i], &out[i]);
-            int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
-            out[i].path_steps = double(info[i].paths) * grid;
-            out[i].executed_steps = merged[i].executed;
-            if (!std::isfinite(out[i].price) || !std::isfinite(out[i].standard_error))
-                return fail(ctx, KGPU_COMPUTATION_FAILURE,
-                            "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
-        }
-        return KGPU_OK;
-    }
-    // Persistent schedule: group contracts by sampling dimension for Sobol (one sequence
-    // per launch); pseudo-random books run in a single launch.
-    std::vector<int> group_of(n, 0);
-    std::vector<int> group_dims;
-    if (sobol) {
-        for (int i = 0; i < n; ++i) {
-            auto it = std::find(group_dims.begin(), group_dims.end(), info[i].dims);
-            if (it == group_dims.end()) {
-                group_of[i] = int(group_dims.size());
-                group_dims.push_back(info[i].dims);
-            } else {
-                group_of[i] = int(it - group_dims.begin());
-            }
-        }
-    } else {
-        group_dims.push_back(0);
-    }
-    // Items grouped by contract (contract order), tile size per contract.
-    std::vector<int4> items;
-    std::vector<int> first_item(n + 1, 0);
-    for (int i = 0; i < n; ++i) {
-        first_item[i] = int(items.size());
-        int64_t tile = sobol ? 256 : (s.tile_paths > 0 ? s.tile_paths : 1024);
-        for (int64_t b = 0; b < info[i].samples; b += tile)
-            items.push_back(make_int4(i, int(b), int(std::min<int64_t>(tile, info[i].samples - b)), info[i].dims));
-    }
-    first_item[n] = int(items.size());
-    const int item_count = int(items.size());
-    if ((st = upload(ctx, ctx->items, items.data(), items.size() * sizeof(int4))) ||
-        (st = upload(ctx, ctx->first_item, first_item.data(), first_item.size() * sizeof(int))))
-        return st;
-    if (ctx->tiles.ensure(size_t(item_count) * sizeof(TilePartial)) ||
-        ctx->tile_out.ensure(size_t(n) * sizeof(TilePartial)) || ctx->queue.ensure(sizeof(int) * 4))
-        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of tile partials failed");
-    CancelWatcher watcher(cancel, ctx->cancel_host);
-    std::vector<int> order;
-    for (size_t g = 0; g < group_dims.size(); ++g) {
-        // Dispatch order: most expensive contracts first.
-        order.clear();
-        std::vector<int> members;
-        for (int i = 0; i < n; ++i)
-            if (group_of[i] == int(g)) members.push_back(i);
-        std::stable_sort(members.begin(), members.end(), [&](int x, int y) {
-            return double(info[x].samples) * book->contracts[x].step_count >
-                   double(info[y].samples) * book->contracts[y].step_count;
-        });
-        int max_dims = 0;
-        for (int i : members) {
-            for (int k = first_item[i]; k < first_item[i + 1]; ++k) order.push_back(k);
-            max_dims = std::max(max_dims, info[i].dims);
-        }
-        if (order.empty()) continue;
-        if (cancel && *cancel) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
-        if ((st = upload(ctx, ctx->order, order.data(), order.size() * sizeof(int)))) return st;
-        PersistentArgs a;
-        a.book = db;
-        a.items = static_cast<const int4*>(ctx->items.ptr);
-        a.order = static_cast<const int*>(ctx->order.ptr);
-        a.item_count = int(order.size());
-        a.queue = static_cast<int*>(ctx->queue.ptr);
-        a.seed = s.seed;
-        a.sobol = SobolTables{nullptr, nullptr, 0};
-        if (sobol && (st = ensure_sobol(ctx, group_dims[g], s.seed, &a.sobol))) return st;
-        a.partials = static_cast<TilePartial*>(ctx->tiles.ptr);
-        a.cancel = cancel ? ctx->cancel_dev : nullptr;
-        a.aborted = static_cast<int*>(ctx->queue.ptr) + 1;
-        size_t smem = persistent_smem_bytes(s.precision, sobol, sobol ? group_dims[g] : 0, lv_values);
-        if (smem > 227 * 1024)
-            return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
-                        "Sobol dimension %d exceeds the persistent kernel's shared memory; use the plain schedule",
-                        group_dims[g]);
-        const int per_sm = persistent_blocks_per_sm(s.precision, model->kind, sobol, smem);
-        const int blocks = std::max(1, std::min(ctx->sm_count * per_sm, (a.item_count + kWarps - 1) / kWarps));
-        CUDA_TRY(ctx, cudaMemsetAsync(ctx->queue.ptr, 0, sizeof(int) * 2, ctx->stream));
-        if ((st = start_clock())) return st;
-        CUDA_TRY(ctx, launch_persistent(s.precision, model->kind, sobol, blocks, smem, ctx->stream, a,
-                                        *model, lv_dev));
-        launches += 1;
-        if (group_dims.size() > 1) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    }
-    reduce_tiles_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(
-        static_cast<const TilePartial*>(ctx->tiles.ptr), static_cast<const int*>(ctx->first_item.ptr), n,
-        static_cast<TilePartial*>(ctx->tile_out.ptr));
-    CUDA_TRY(ctx, cudaGetLastError());
-    launches += 1;
-    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
-    std::vector<TilePartial> sums(n);
-    int aborted = 0;
-    CUDA_TRY(ctx, cudaMemcpyAsync(sums.data(), ctx->tile_out.ptr, sizeof(TilePartial) * n,
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    CUDA_TRY(ctx, cudaMemcpyAsync(&aborted, static_cast<int*>(ctx->queue.ptr) + 1, sizeof(int),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
-    ctx->last_kernel_ms = ms;
-    ctx->last_launches = launches;
-    if (aborted) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
-    for (int i = 0; i < n; ++i) {
-        const kgpu_contract& c = book->contracts[i];
-        estimate_from_sums(c, s, info[i].paths, sums[i], &out[i]);
-        int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
-        out[i].path_steps = double(info[i].paths) * grid;
-        out[i].executed_steps = sums[i].executed;
-        if (!std::isfinite(out[i].price) || !std::isfinite(out[i].standard_error))
-            return fail(ctx, KGPU_COMPUTATION_FAILURE,
-                        "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
-    }
-    return KGPU_OK;
+    return s.precision == KGPU_PRECISION_FP64 ? run_book<double>(k) : run_book<float>(k);
 }
 
 namespace kgpu {
@@ -605,37 +835,9 @@ size_t plain_smem_bytes(int precision, bool sobol, int dims, int lv_values) {
 
 size_t persistent_smem_bytes(int precision, bool sobol, int dims, int lv_values) {
     size_t real = precision == KGPU_PRECISION_FP64 ? 8 : 4;
-    return (sobol ? size_t(dims) * 8 * (8 + kWarps) : 0) + size_t(lv_values) * real + 16;
-}
-
-cudaError_t launch_plain_fp64(int, bool, int, size_t, cudaStream_t, const PlainArgs&, const kgpu_model&, const double*);
-cudaError_t launch_plain_fp32(int, bool, int, size_t, cudaStream_t, const PlainArgs&, const kgpu_model&, const double*);
-cudaError_t launch_persistent_fp64(int, bool, int, size_t, cudaStream_t, const PersistentArgs&, const kgpu_model&, const double*);
-cudaError_t launch_persistent_fp32(int, bool, int, size_t, cudaStream_t, const PersistentArgs&, const kgpu_model&, const double*);
-int persistent_occupancy_fp64(int, bool, size_t);
-int persistent_occupancy_fp32(int, bool, size_t);
-cudaError_t launch_pcg_normals_fp64(uint64_t, uint64_t, uint64_t, int64_t, double*, cudaStream_t);
-cudaError_t launch_pcg_normals_fp32(uint64_t, uint64_t, uint64_t, int64_t, double*, cudaStream_t);
-cudaError_t launch_sobol_points_fp64(const SobolTables&, int, uint64_t, int64_t, uint64_t*, double*, cudaStream_t);
-cudaError_t launch_sobol_points_fp32(const SobolTables&, int, uint64_t, int64_t, uint64_t*, double*, cudaStream_t);
-
-cudaError_t launch_plain(int precision, int model, bool sobol, int blocks, size_t smem, cudaStream_t stream,
-                         const PlainArgs& a, const kgpu_model& m, const double* lv) {
-    return precision == KGPU_PRECISION_FP64 ? launch_plain_fp64(model, sobol, blocks, smem, stream, a, m, lv)
-                                            : launch_plain_fp32(model, sobol, blocks, smem, stream, a, m, lv);
-}
-
-cudaError_t launch_persistent(int precision, int model, bool sobol, int blocks, size_t smem,
-                              cudaStream_t stream, const PersistentArgs& a, const kgpu_model& m,
-                              const double* lv) {
-    return precision == KGPU_PRECISION_FP64
-               ? launch_persistent_fp64(model, sobol, blocks, smem, stream, a, m, lv)
-               : launch_persistent_fp32(model, sobol, blocks, smem, stream, a, m, lv);
-}
-
-int persistent_blocks_per_sm(int precision, int model, bool sobol, size_t smem) {
-    return precision == KGPU_PRECISION_FP64 ? persistent_occupancy_fp64(model, sobol, smem)
-                                            : persistent_occupancy_fp32(model, sobol, smem);
+    // FP64 Sobol keeps a per-warp shared copy of the item's high part; FP32 reads a table.
+    return (sobol && precision == KGPU_PRECISION_FP64 ? size_t(dims) * 8 * kWarps : 0) +
+           size_t(lv_values) * real + 16;
 }
 
 __global__ void pcg_words_kernel(uint64_t seed, uint64_t stream_id, uint64_t first, int64_t count,

@@ -36,9 +36,11 @@ struct kgpu_context {
     // plain schedule
     kgpu::DeviceBuffer partials, merged;
     // persistent schedule
-    kgpu::DeviceBuffer items, order, first_item, tiles, tile_out, queue;
+    kgpu::DeviceBuffer items, order, first_item, tiles, tile_out, queue, values, value_offset, chunks, executed;
+    // plan in the kernel's precision (contract table always, arrays for FP32)
+    kgpu::DeviceBuffer ccontracts, csteps, cevents, cintervals, cdaily, cunits, cends;
     // Sobol sequence cache (one sequence per (seed, dims))
-    kgpu::DeviceBuffer sobol_dirs, sobol_shifts;
+    kgpu::DeviceBuffer sobol_dirs, sobol_shifts, sobol_nibbles, sobol_dirs32, sobol_shifts32, sobol_nibbles32, sobol_high32;
     int sobol_dims = 0;
     uint64_t sobol_seed = 0;
     // LSMC
@@ -57,7 +59,8 @@ struct kgpu_context {
     std::vector<kgpu::DeviceBuffer*> buffers() {
         return {&contracts, &steps,     &flags,     &events,   &intervals, &daily,     &lv,
                 &partials,  &merged,    &items,     &order,    &first_item, &tiles,    &tile_out,
-                &queue,     &sobol_dirs, &sobol_shifts, &lsmc_store, &lsmc_cash, &lsmc_sums,
+                &queue,     &values,    &value_offset, &chunks, &executed, &sobol_dirs, &sobol_shifts, &sobol_nibbles, &sobol_dirs32, &sobol_shifts32, &sobol_nibbles32, &sobol_high32, &ccontracts, &csteps,
+                &cevents,   &cintervals, &cdaily,      &cunits,     &cends,      &lsmc_store, &lsmc_cash, &lsmc_sums,
                 &lsmc_coef, &lsmc_misc, &mlp_params, &mlp_scratch, &stream_out};
     }
 };

@@ -9,6 +9,8 @@ namespace kgpu {
 
 constexpr int kThreads = 256;  // one CUDA block = one reference block of 256 samples
 constexpr int kWarps = kThreads / 32;
+// Path units a warp runs in lockstep between lane refills (persistent kernel).
+constexpr int kRefill = 16;
 
 // Partial result of one reference block (plain schedule).
 struct BlockPartial {
@@ -23,15 +25,35 @@ struct TilePartial {
     double sum, sumsq, count, executed;
 };
 
-// Sobol tables of one sequence: directions [column * dims + dim] and shifts [dim].
+// Sobol tables of one sequence: directions [column * dims + dim], shifts [dim] and the
+// 4-bit nibble XOR tables of direction rows 0-7, [dim][32].
 struct SobolTables {
     const uint64_t* directions;
     const uint64_t* shifts;
+    const uint64_t* nibbles;
+    const uint32_t* directions32;  // top 32 of the 52 bits, same layouts
+    const uint32_t* shifts32;
+    const uint32_t* nibbles32;
+    const uint32_t* high32;  // [block][dims]: the high part of every reference block in use
     int dims;
 };
 
+// The caller's plan (kgpu_* arrays, device pointers).
+struct RawBook {
+    const kgpu_contract* contracts;
+    const kgpu_step* steps;
+    const uint8_t* flags;
+    const kgpu_event* events;
+    const kgpu_bridge_interval* intervals;
+    const kgpu_bridge_daily* daily;
+    int contract_count;
+    int64_t step_total;
+    int event_total, interval_total;
+};
+
+template <class Real>
 struct PlainArgs {
-    DevBook book;
+    DevBook<Real> book;
     int contract;
     int dims;
     int64_t paths;
@@ -44,18 +66,167 @@ struct PlainArgs {
     BlockPartial* partials;
 };
 
+template <class Real>
 struct PersistentArgs {
-    DevBook book;
+    DevBook<Real> book;
     const int4* items;  // (contract, first sample, sample count, dims), grouped by contract
     const int* order;   // dispatch order of the items (longest contracts first)
     int item_count;
     int* queue;         // work-queue head
     uint64_t seed;
     SobolTables sobol;
-    TilePartial* partials;
-    const volatile int* cancel;  // host-mapped cancellation word (may be null)
+    Real* values;                  // per-path payoffs
+    const int64_t* value_offset;   // per contract: first slot of its samples in `values`
+    unsigned long long* executed;  // per contract: grid steps simulated
+    const volatile int* cancel;    // host-mapped cancellation word (may be null)
     int* aborted;
+    int refill;                    // path units between lane refills
 };
+
+// ------------------------------------------------------------------------------------
+// Plan compilation: the caller's FP64 plan into the kernel's precision.
+// ------------------------------------------------------------------------------------
+template <class Real>
+__global__ void compile_contracts_kernel(const kgpu_contract* in, int n, ContractT<Real>* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const kgpu_contract c = in[i];
+    ContractT<Real> o;
+    o.payoff = c.payoff;
+    o.flags = c.flags;
+    o.step_count = c.step_count;
+    o.event_count = c.event_count;
+    o.bridge_count = c.bridge_count;
+    o.reserved = 0;
+    o.step_offset = c.step_offset;
+    o.event_offset = c.event_offset;
+    o.bridge_offset = c.bridge_offset;
+    o.strike = Real(c.strike);
+    o.sign = Real(c.sign);
+    o.diffusion = Real(c.diffusion);
+    o.half_variance = Real(c.half_variance);
+    o.moneyness = Real(c.moneyness);
+    o.log_scale = Real(c.log_scale);
+    o.knock_in = Real(c.knock_in);
+    o.initial_cash = Real(c.initial_cash);
+    o.terminal_base = Real(c.terminal_base);
+    o.terminal_plain = Real(c.terminal_plain);
+    o.terminal_fixed = Real(c.terminal_fixed);
+    o.downside_lower = Real(c.downside_lower);
+    o.downside_upper = Real(c.downside_upper);
+    o.downside_initial = Real(c.downside_initial);
+    o.final_discount = Real(c.final_discount);
+    o.knock_out = Real(c.knock_out);
+    o.quantity = Real(c.quantity);
+    o.daily_quantity = Real(c.daily_quantity);
+    o.acceleration = Real(c.acceleration);
+    o.log_strike = Real(c.log_strike);
+    out[i] = o;
+}
+
+// Steps, events, intervals and bridge weights to single precision (grid-stride).
+static __global__ void compile_arrays_fp32_kernel(RawBook b, StepT<float>* steps, EventT<float>* events,
+                                                  IntervalT<float>* intervals, DailyT<float>* daily) {
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    const int64_t first = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (int64_t i = first; i < b.step_total; i += stride) {
+        const kgpu_step s = b.steps[i];
+        steps[i] = StepT<float>{float(s.drift), float(s.diffusion), float(s.time), float(s.discount)};
+        if (b.daily) daily[i] = DailyT<float>{float(b.daily[i].weight), float(b.daily[i].width)};
+    }
+    for (int64_t i = first; i < b.event_total; i += stride) {
+        const kgpu_event e = b.events[i];
+        EventT<float> o;
+        o.knock_out = float(e.knock_out);
+        o.coupon_barrier = float(e.coupon_barrier);
+        for (int k = 0; k < 4; ++k) o.payment[k] = float(e.payment[k]);
+        o.has_knock_out = e.has_knock_out;
+        o.step = e.step;
+        events[i] = o;
+    }
+    for (int64_t i = first; i < b.interval_total; i += stride) {
+        const kgpu_bridge_interval v = b.intervals[i];
+        intervals[i] = IntervalT<float>{v.end, 0, float(v.drift), float(v.diffusion)};
+    }
+}
+
+// Per-position bridge units of every bridged contract: one CTA per contract walks its
+// intervals; the positions of an interval are written in parallel.
+template <class Real>
+__global__ void compile_units_kernel(const kgpu_contract* contracts, const kgpu_bridge_interval* intervals,
+                                     const kgpu_bridge_daily* daily, const uint8_t* flags,
+                                     const kgpu_event* events, UnitT<Real>* units, EndT<Real>* ends) {
+    const kgpu_contract c = contracts[blockIdx.x];
+    if (!(c.flags & KGPU_C_BRIDGE)) return;
+    int start = 0;
+    int ev = c.event_offset;
+    for (int k = 0; k < c.bridge_count; ++k) {
+        const kgpu_bridge_interval iv = intervals[c.bridge_offset + k];
+        const int fl = flags[c.step_offset + iv.end];
+        const bool event = (fl & KGPU_STEP_EVENT) != 0;
+        const kgpu_event e = event ? events[ev] : kgpu_event{};
+        for (int q = start + int(threadIdx.x); q <= iv.end; q += blockDim.x) {
+            UnitT<Real> u;
+            if (q == start) {
+                u.a = Real(iv.diffusion);
+                u.b = Real(iv.drift);
+                u.flags = kUnitBegin;
+            } else {
+                const kgpu_bridge_daily d = daily[c.step_offset + q - 1];
+                u.a = Real(d.width);
+                u.b = Real(d.weight);
+                u.flags = 0;
+            }
+            u.end = iv.end;
+            u.flags |= fl << 8;
+            if (q == iv.end) u.flags |= kUnitLast;
+            if (event && e.has_knock_out) u.flags |= kUnitKnockOut;
+            units[c.step_offset + q] = u;
+            EndT<Real> o{};
+            if (q == iv.end && event) {
+                o.knock_out = Real(e.knock_out);
+                o.coupon_barrier = Real(e.coupon_barrier);
+                for (int j = 0; j < 4; ++j) o.payment[j] = Real(e.payment[j]);
+            }
+            ends[c.step_offset + q] = o;
+        }
+        ev += event ? 1 : 0;
+        start = iv.end + 1;
+    }
+}
+
+// The 32-bit high part of every reference block: row b holds, per dimension, the shift
+// XOR the directions of the gray-code bits >= 8 of block b's points.
+static __global__ void sobol_high_table_kernel(SobolTables t, int blocks, uint32_t* out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= int64_t(blocks) * t.dims) return;
+    const int b = int(i / t.dims), d = int(i % t.dims);
+    const uint64_t first = uint64_t(b) * kBlockSize;
+    uint64_t g = (first ^ (first >> 1)) >> 8;
+    uint32_t x = t.shifts32[d];
+    for (; g; g &= g - 1) x ^= t.directions32[size_t(__ffsll(g) - 1 + 8) * t.dims + d];
+    out[i] = x;
+}
+
+// Top 32 of the 52 bits of a 64-bit Sobol table.
+static __global__ void sobol_top32_kernel(const uint64_t* in, int64_t n, uint32_t* out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = uint32_t(in[i] >> 20);
+}
+
+// Nibble tables of a Sobol sequence: for each dimension, the XOR of direction rows 0-3
+// selected by a 4-bit pattern (16 entries) then rows 4-7 (16 entries).
+static __global__ void sobol_nibbles_kernel(const uint64_t* directions, int dims, uint64_t* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dims * 32) return;
+    const int d = i / 32, e = i % 32;
+    const int base = e < 16 ? 0 : 4;
+    const int pattern = e & 15;
+    uint64_t x = 0;
+    for (int b = 0; b < 4; ++b)
+        if ((pattern >> b) & 1) x ^= directions[size_t(base + b) * dims + d];
+    out[i] = x;
+}
 
 template <class Real>
 __device__ __forceinline__ void load_model(DevModel<Real>& m, const kgpu_model& src, Real* smem_lv,
@@ -96,30 +267,70 @@ __device__ __forceinline__ void sobol_high(const SobolTables& t, uint64_t block,
     }
 }
 
+// The same from the 32-bit tables.
+__device__ __forceinline__ void sobol_high(const SobolTables& t, uint64_t block, uint32_t* high,
+                                           int lane, int width) {
+    uint64_t first = block * kBlockSize;
+    uint64_t gray = (first ^ (first >> 1)) >> 8;
+    for (int d = lane; d < t.dims; d += width) {
+        uint32_t x = t.shifts32[d];
+        uint64_t g = gray;
+        while (g) {
+            int c = __ffsll(g) - 1 + 8;
+            x ^= t.directions32[size_t(c) * t.dims + d];
+            g &= g - 1;
+        }
+        high[d] = x;
+    }
+}
+
+// The Sobol source and high-table word of each precision: FP32 kernels use the 32-bit
+// tables, FP64 kernels the full 52-bit ones.
+template <class Real>
+struct SobolKind;
+template <>
+struct SobolKind<double> {
+    using Word = uint64_t;
+    using Source = SobolSource<double>;
+    static __device__ __forceinline__ Source make(const SobolTables& t, const Word* high) {
+        return Source{high, t.nibbles, t.dims, 0, 0, 0};
+    }
+    static constexpr bool global_high = false;
+    static __device__ __forceinline__ void set_row(Source&, const SobolTables&, uint64_t) {}
+};
+template <>
+struct SobolKind<float> {
+    using Word = uint32_t;
+    using Source = SobolSource32;
+    static __device__ __forceinline__ Source make(const SobolTables& t, const Word* high) {
+        return Source{high, t.nibbles32, t.directions, t.shifts, t.dims, 0, 0, 0, 0};
+    }
+    static constexpr bool global_high = true;
+    static __device__ __forceinline__ void set_row(Source& n, const SobolTables& t, uint64_t sample) {
+        n.high32 = t.high32 + size_t(sample / kBlockSize) * t.dims;
+    }
+};
+
 template <class S, class Real>
 struct Negated {
     S& s;
     __device__ __forceinline__ Real normal() { return -s.normal(); }
+    __device__ __forceinline__ Real normal_if(bool need) { return -s.normal_if(need); }
     __device__ __forceinline__ void skip(int n) { s.skip(n); }
 };
 
 // Runs one whole path to completion.
 template <class Real, int MODEL, class Source>
-__device__ __forceinline__ Real run_path(const DevModel<Real>& m, const kgpu_contract& c,
-                                         const DevBook& b, Source& n, int& executed) {
+__device__ __forceinline__ Real run_path(const DevModel<Real>& m, const ContractT<Real>& c,
+                                         const PlanPtrs<Real>& p, Source& n, int& executed) {
     PathState<Real> s;
     path_init(s, c, m.v0);
-    const kgpu_step* steps = b.steps + c.step_offset;
-    const uint8_t* flags = b.flags + c.step_offset;
-    const kgpu_event* events = b.events ? b.events + c.event_offset : nullptr;
-    const kgpu_bridge_interval* intervals = b.intervals ? b.intervals + c.bridge_offset : nullptr;
-    const kgpu_bridge_daily* daily = b.daily ? b.daily + c.step_offset : nullptr;
     Real value = Real(0);
     // Every path ends within step_count + bridge_count units of work.
-    int guard = 2 * c.step_count + c.bridge_count + 2;
-    while (!path_step<Real, MODEL>(m, c, steps, flags, events, intervals, daily, s, n, value)) {
+    int guard = 2 * c.step_count + 2 * c.bridge_count + 2;
+    while (!path_step<Real, MODEL>(m, c, p, s, n, value)) {
         if (--guard == 0) {
-            value = Real(__int_as_float(0x7fc00000));  // NaN: reported as a computation failure
+            value = xnan(Real());  // reported as a computation failure
             break;
         }
     }
@@ -130,7 +341,7 @@ __device__ __forceinline__ Real run_path(const DevModel<Real>& m, const kgpu_con
 // Plain schedule: thread = sample, CUDA block = reference block; the block's moments are
 // accumulated sequentially in sample order as sample_paths does (monte_carlo.rs:1778-1798).
 template <class Real, int MODEL, bool SOBOL>
-__global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs a, kgpu_model model,
+__global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs<Real> a, kgpu_model model,
                                                          const double* lv_dev) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* values = reinterpret_cast<double*>(smem_raw);          // [2 * kThreads]
@@ -142,7 +353,8 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs a, kgpu_model
     const uint64_t block = blockIdx.x;
     if (SOBOL) sobol_high(a.sobol, block, high, threadIdx.x, blockDim.x);
     __syncthreads();
-    const kgpu_contract& c = a.book.contracts[a.contract];
+    const ContractT<Real> c = a.book.contracts[a.contract];
+    const PlanPtrs<Real> plan = plan_of(a.book, c);
     const int64_t sample = int64_t(block) * kBlockSize + threadIdx.x;
     double positive = 0.0, negative = 0.0;
     int executed = 0;
@@ -150,22 +362,22 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs a, kgpu_model
         const bool paired = a.antithetic && sample < a.paths / 2;
         int e1 = 0, e2 = 0;
         if (SOBOL) {
-            SobolSource<Real> n{high, a.sobol.directions, a.dims, 0, 0};
+            SobolSource<Real> n{high, a.sobol.nibbles, a.dims, 0, 0, 0};
             n.start(uint64_t(sample));
-            positive = double(run_path<Real, MODEL>(m, c, a.book, n, e1));
+            positive = double(run_path<Real, MODEL>(m, c, plan, n, e1));
             if (paired) {
                 n.start(uint64_t(sample));
                 Negated<SobolSource<Real>, Real> neg{n};
-                negative = double(run_path<Real, MODEL>(m, c, a.book, neg, e2));
+                negative = double(run_path<Real, MODEL>(m, c, plan, neg, e2));
             }
         } else {
             PcgSource<Real> n;
             n.start(a.seed, uint64_t(sample), a.dims);
-            positive = double(run_path<Real, MODEL>(m, c, a.book, n, e1));
+            positive = double(run_path<Real, MODEL>(m, c, plan, n, e1));
             if (paired) {
                 n.start(a.seed, uint64_t(sample), a.dims);
                 Negated<PcgSource<Real>, Real> neg{n};
-                negative = double(run_path<Real, MODEL>(m, c, a.book, neg, e2));
+                negative = double(run_path<Real, MODEL>(m, c, plan, neg, e2));
             }
         }
         executed = e1 > e2 ? e1 : e2;
@@ -203,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs a, kgpu_model
 
 // Merges the block partials of one contract in block order (monte_carlo.rs:1800-1809).
 static __global__ void merge_blocks_kernel(const BlockPartial* partials, int blocks, int variance,
-                                    int statistics, int antithetic, BlockPartial* out) {
+                                           int statistics, int antithetic, BlockPartial* out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     BlockPartial r;
     r.moments = Moments{0, 0, 0, 0};
@@ -225,7 +437,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Kahan-compensated single-precision running sum.
+// Kahan-compensated running sum in the kernel's precision.
 template <class Real>
 struct Compensated {
     Real sum, carry;
@@ -238,136 +450,211 @@ struct Compensated {
     __device__ __forceinline__ double value() const { return double(sum) - double(carry); }
 };
 
-// Persistent schedule: warps pull (contract, tile) items from a queue; inside an item,
-// a lane whose path has finished starts the tile's next unstarted sample, so the warp
-// stays full however unevenly its paths end (early knock-out, bridge skipping).
-// Refill order is a deterministic function of the path lengths (warp-synchronous
-// ballots), so results do not depend on scheduling.
+// Persistent schedule.  Warps pull (contract, tile) items from a device queue and keep
+// two items in flight: a lane whose path has finished starts the next unstarted sample
+// of the older item, else of the newer one, so lanes never wait for an item to drain
+// while work is queued (early knock-out and bridge skipping make path lengths very
+// uneven).  Each finished path writes its payoff to values[value_offset[contract] +
+// sample]; reduce_values_kernel then sums them in a fixed order, so results do not
+// depend on which warp ran which path.
+// Persistent schedule.  Warps pull (contract, tile) items from a device queue and hand
+// the item's samples to lanes one at a time: lanes run kRefill path units in lockstep,
+// then every lane whose path has finished takes the next unstarted sample -- of the
+// current item, or of the next queued one -- so a warp never waits for an item to drain
+// while work is queued.  Lanes may therefore hold paths of different items (and
+// contracts); each lane keeps its own contract and plan.  Sobol points read the high
+// part of their reference block from a global table (FP32) or, in FP64, from the
+// warp's shared copy (FP64 keeps one item per warp).  Each finished path writes its
+// payoff to values[value_offset[contract] + sample]; reduce_values_kernel sums them in a
+// fixed order, so results do not depend on which warp ran which path.
 template <class Real, int MODEL, bool SOBOL>
-__global__ void __launch_bounds__(kThreads) persistent_kernel(PersistentArgs a, kgpu_model model,
+__global__ void __launch_bounds__(kThreads) persistent_kernel(PersistentArgs<Real> a, kgpu_model model,
                                                               const double* lv_dev) {
+    using Kind = SobolKind<Real>;
+    using Word = typename Kind::Word;
+    constexpr bool kGlobalHigh = Kind::global_high;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t* low = reinterpret_cast<uint64_t*>(smem_raw);                  // [8 * dims]
-    uint64_t* highs = low + (SOBOL ? 8 * a.sobol.dims : 0);                 // [kWarps * dims]
-    Real* lv = reinterpret_cast<Real*>(highs + (SOBOL ? kWarps * a.sobol.dims : 0));
+    Word* highs = reinterpret_cast<Word*>(smem_raw);
+    const int dims = SOBOL ? a.sobol.dims : 0;
+    const int shared_dims = (SOBOL && !kGlobalHigh) ? dims : 0;
+    Real* lv = reinterpret_cast<Real*>(highs + kWarps * shared_dims);
     DevModel<Real> m;
     load_model(m, model, lv, lv_dev);
-    if (SOBOL) {
-        for (int i = threadIdx.x; i < 8 * a.sobol.dims; i += blockDim.x) low[i] = a.sobol.directions[i];
-    }
     __syncthreads();
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    uint64_t* high = highs + (SOBOL ? warp * a.sobol.dims : 0);
-    for (;;) {
-        int item = 0;
+    const unsigned below = lanemask_lt();
+    Word* high = highs + warp * shared_dims;
+
+    // Current item of the warp (uniform).
+    int item_contract = 0, item_dims = 0;
+    int64_t next = 0, end = 0;
+    bool have = false;
+    auto fetch = [&]() {
+        int it = -1;
         if (lane == 0) {
             int q = atomicAdd(a.queue, 1);
             if (a.cancel && *a.cancel) {
                 atomicExch(a.aborted, 1);
                 q = a.item_count;
             }
-            item = q < a.item_count ? a.order[q] : -1;
+            it = q < a.item_count ? a.order[q] : -1;
         }
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item < 0) break;
-        const int4 w = a.items[item];
-        const kgpu_contract& c = a.book.contracts[w.x];
-        const int64_t begin = w.y, end = int64_t(w.y) + w.z;
-        const int dims = w.w;
-        if (SOBOL) {
-            sobol_high(a.sobol, uint64_t(begin) / kBlockSize, high, lane, 32);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        have = it >= 0;
+        if (!have) return;
+        const int4 w = a.items[it];
+        item_contract = w.x;
+        item_dims = w.w;
+        next = w.y;
+        end = int64_t(w.y) + w.z;
+        if (SOBOL && !kGlobalHigh) {
+            __syncwarp();
+            sobol_high(a.sobol, uint64_t(w.y) / kBlockSize, high, lane, 32);
             __syncwarp();
         }
-        const kgpu_step* steps = a.book.steps + c.step_offset;
-        const uint8_t* flags = a.book.flags + c.step_offset;
-        const kgpu_event* events = a.book.events ? a.book.events + c.event_offset : nullptr;
-        const kgpu_bridge_interval* intervals =
-            a.book.intervals ? a.book.intervals + c.bridge_offset : nullptr;
-        const kgpu_bridge_daily* daily = a.book.daily ? a.book.daily + c.step_offset : nullptr;
-        Compensated<Real> sum{0, 0}, sumsq{0, 0};
-        int count = 0;
-        int executed = 0;
-        int64_t next = begin + 32;
-        int64_t sample = begin + lane;
-        bool active = sample < end;
-        PathState<Real> s;
-        PcgSource<Real> pn;
-        SobolSource<Real> sn{high, low, dims, 0, 0};
-        if (active) {
-            path_init(s, c, m.v0);
-            if (SOBOL)
-                sn.start(uint64_t(sample));
-            else
-                pn.start(a.seed, uint64_t(sample), dims);
+    };
+    fetch();
+
+    // Per-lane path.
+    bool active = false;
+    int contract = 0;
+    int64_t sample = 0;
+    int guard = 0;
+    bool bridged = false;
+    PlanPtrs<Real> plan{};
+    PathState<Real> s;
+    PcgSource<Real> pn;
+    typename Kind::Source sn = Kind::make(a.sobol, high);
+    unsigned long long exec = 0;
+    int exec_contract = -1;
+
+    for (;;) {
+        // Refill: idle lanes take unstarted samples in lane order, crossing into the next
+        // queued item when the current one runs out.  FP64 Sobol keeps one item per warp
+        // (its high part is a per-warp shared copy), so it crosses only once all lanes idle.
+        unsigned want = __ballot_sync(0xffffffffu, !active);
+        while (want && have) {
+            if (SOBOL && !kGlobalHigh && next == end) {
+                if (want != 0xffffffffu) break;
+                fetch();
+                continue;
+            }
+            const int64_t avail = end - next;
+            const int rank = __popc(want & below);
+            if (!active && rank < avail) {
+                sample = next + rank;
+                if (contract != item_contract || exec_contract < 0) {
+                    if (exec) atomicAdd(a.executed + exec_contract, exec);
+                    exec = 0;
+                }
+                contract = item_contract;
+                exec_contract = item_contract;
+                const ContractT<Real>& c = a.book.contracts[contract];
+                plan = plan_of(a.book, c);
+                bridged = MODEL == KGPU_MODEL_BSM && c.payoff == KGPU_PAYOFF_AUTOCALLABLE &&
+                          (c.flags & KGPU_C_BRIDGE) && plan.units != nullptr;
+                guard = 2 * c.step_count + 2 * c.bridge_count + 2;
+                path_init(s, c, m.v0);
+                if (SOBOL) {
+                    Kind::set_row(sn, a.sobol, uint64_t(sample));
+                    sn.start(uint64_t(sample));
+                } else {
+                    pn.start(a.seed, uint64_t(sample), item_dims);
+                }
+                active = true;
+            }
+            const int taken = __popc(want);
+            const int64_t take = taken < avail ? taken : avail;
+            next += take;
+            want = __ballot_sync(0xffffffffu, !active);
+            if (next == end && !(SOBOL && !kGlobalHigh)) fetch();
         }
-        const int guard_limit = 2 * c.step_count + c.bridge_count + 2;
-        int guard = guard_limit;
-        while (__any_sync(0xffffffffu, active)) {
+        if (!__any_sync(0xffffffffu, active)) {
+            if (!have) break;
+            continue;
+        }
+        const ContractT<Real>& c = a.book.contracts[contract];
+        Real* values = a.values + a.value_offset[contract];
+#pragma unroll 1
+        for (int r = 0; r < a.refill; ++r) {
             bool finished = false;
             Real value = Real(0);
             if (active) {
-                if (SOBOL)
-                    finished = path_step<Real, MODEL>(m, c, steps, flags, events, intervals, daily, s,
-                                                      sn, value);
-                else
-                    finished = path_step<Real, MODEL>(m, c, steps, flags, events, intervals, daily, s,
-                                                      pn, value);
+                if (bridged) {
+                    finished = SOBOL ? bridge_unit_step<Real>(c, plan, s, sn) : bridge_unit_step<Real>(c, plan, s, pn);
+                    if (finished) value = bridge_value(m, c, s);
+                } else {
+                    finished = SOBOL ? path_step<Real, MODEL>(m, c, plan, s, sn, value)
+                                     : path_step<Real, MODEL>(m, c, plan, s, pn, value);
+                }
                 if (!finished && --guard == 0) {
                     finished = true;
-                    value = Real(__int_as_float(0x7fc00000));
-                }
-                if (finished) {
-                    sum.add(value);
-                    sumsq.add(value * value);
-                    count += 1;
-                    executed += s.executed;
+                    value = xnan(Real());
                 }
             }
-            const unsigned done = __ballot_sync(0xffffffffu, finished);
-            if (done) {
-                if (finished) {
-                    int64_t mine = next + __popc(done & lanemask_lt());
-                    if (mine < end) {
-                        sample = mine;
-                        path_init(s, c, m.v0);
-                        guard = guard_limit;
-                        if (SOBOL)
-                            sn.start(uint64_t(sample));
-                        else
-                            pn.start(a.seed, uint64_t(sample), dims);
-                    } else {
-                        active = false;
-                    }
-                }
-                next += __popc(done);
+            if (finished) {
+                values[sample] = value;
+                exec += s.executed;
+                active = false;
             }
         }
-        double t0 = sum.value(), t1 = sumsq.value(), t2 = double(count), t3 = double(executed);
-        for (int off = 16; off > 0; off >>= 1) {
-            t0 += __shfl_xor_sync(0xffffffffu, t0, off);
-            t1 += __shfl_xor_sync(0xffffffffu, t1, off);
-            t2 += __shfl_xor_sync(0xffffffffu, t2, off);
-            t3 += __shfl_xor_sync(0xffffffffu, t3, off);
-        }
-        if (lane == 0) a.partials[item] = TilePartial{t0, t1, t2, t3};
-        __syncwarp();
     }
+    if (exec) atomicAdd(a.executed + exec_contract, exec);
 }
 
-// Sums each contract's tile partials in item order.
-static __global__ void reduce_tiles_kernel(const TilePartial* partials, const int* first_item,
-                                    int contracts, TilePartial* out) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= contracts) return;
-    TilePartial r{0, 0, 0, 0};
-    for (int i = first_item[c]; i < first_item[c + 1]; ++i) {
-        r.sum += partials[i].sum;
-        r.sumsq += partials[i].sumsq;
-        r.count += partials[i].count;
-        r.executed += partials[i].executed;
+// Sums per-path values in a fixed order: one CTA per chunk of a contract's values,
+// a fixed strided assignment and a fixed tree.
+template <class Real>
+__global__ void __launch_bounds__(256) reduce_values_kernel(const Real* values, const int4* chunks,
+                                                            const int64_t* value_offset, TilePartial* out) {
+    __shared__ double red[3][256];
+    const int4 ch = chunks[blockIdx.x];
+    const Real* v = values + value_offset[ch.x] + ch.y;
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int i = threadIdx.x; i < ch.z; i += blockDim.x) {
+        const double x = double(v[i]);
+        s0 += x;
+        s1 += x * x;
+        s2 += 1.0;
     }
-    out[c] = r;
+    red[0][threadIdx.x] = s0;
+    red[1][threadIdx.x] = s1;
+    red[2][threadIdx.x] = s2;
+    __syncthreads();
+    for (int half = 128; half > 0; half >>= 1) {
+        if (threadIdx.x < half)
+            for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + half];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = TilePartial{red[0][0], red[1][0], red[2][0], 0.0};
+}
+
+// Sums each contract's tile partials: one CTA per contract, a fixed strided assignment
+// and a fixed shared-memory tree, so the order of additions never changes.
+static __global__ void __launch_bounds__(256) reduce_tiles_kernel(const TilePartial* partials,
+                                                                  const int* first_item,
+                                                                  TilePartial* out) {
+    __shared__ double red[4][256];
+    const int c = blockIdx.x;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    for (int i = first_item[c] + threadIdx.x; i < first_item[c + 1]; i += blockDim.x) {
+        a0 += partials[i].sum;
+        a1 += partials[i].sumsq;
+        a2 += partials[i].count;
+        a3 += partials[i].executed;
+    }
+    red[0][threadIdx.x] = a0;
+    red[1][threadIdx.x] = a1;
+    red[2][threadIdx.x] = a2;
+    red[3][threadIdx.x] = a3;
+    __syncthreads();
+    for (int half = 128; half > 0; half >>= 1) {
+        if (threadIdx.x < half)
+            for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + half];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = TilePartial{red[0][0], red[1][0], red[2][0], red[3][0]};
 }
 
 }  // namespace kgpu

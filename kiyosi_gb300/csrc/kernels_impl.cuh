@@ -5,7 +5,7 @@
 namespace kgpu {
 
 template <int MODEL, bool SOBOL>
-static cudaError_t plain_one(int blocks, size_t smem, cudaStream_t s, const PlainArgs& a,
+static cudaError_t plain_one(int blocks, size_t smem, cudaStream_t s, const PlainArgs<REAL>& a,
                              const kgpu_model& m, const double* lv) {
     auto k = plain_kernel<REAL, MODEL, SOBOL>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -16,7 +16,7 @@ static cudaError_t plain_one(int blocks, size_t smem, cudaStream_t s, const Plai
 
 template <int MODEL, bool SOBOL>
 static cudaError_t persistent_one(int blocks, size_t smem, cudaStream_t s,
-                                  const PersistentArgs& a, const kgpu_model& m, const double* lv) {
+                                  const PersistentArgs<REAL>& a, const kgpu_model& m, const double* lv) {
     auto k = persistent_kernel<REAL, MODEL, SOBOL>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -48,19 +48,34 @@ static int occupancy_one(size_t smem) {
 #define KGPU_CAT(a, b) KGPU_CAT2(a, b)
 
 cudaError_t KGPU_CAT(launch_plain_, PRECISION)(int model, bool sobol, int blocks, size_t smem,
-                                               cudaStream_t s, const PlainArgs& a,
+                                               cudaStream_t s, const PlainArgs<REAL>& a,
                                                const kgpu_model& m, const double* lv) {
     KGPU_DISPATCH(plain_one, blocks, smem, s, a, m, lv)
 }
 
 cudaError_t KGPU_CAT(launch_persistent_, PRECISION)(int model, bool sobol, int blocks, size_t smem,
-                                                    cudaStream_t s, const PersistentArgs& a,
+                                                    cudaStream_t s, const PersistentArgs<REAL>& a,
                                                     const kgpu_model& m, const double* lv) {
     KGPU_DISPATCH(persistent_one, blocks, smem, s, a, m, lv)
 }
 
 int KGPU_CAT(persistent_occupancy_, PRECISION)(int model, bool sobol, size_t smem) {
     KGPU_DISPATCH(occupancy_one, smem)
+}
+
+cudaError_t KGPU_CAT(launch_compile_contracts_, PRECISION)(const kgpu_contract* in, int n,
+                                                           ContractT<REAL>* out, cudaStream_t s) {
+    compile_contracts_kernel<REAL><<<(n + 255) / 256, 256, 0, s>>>(in, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t KGPU_CAT(launch_compile_units_, PRECISION)(const kgpu_contract* contracts, int n,
+                                                       const kgpu_bridge_interval* intervals,
+                                                       const kgpu_bridge_daily* daily, const uint8_t* flags,
+                                                       const kgpu_event* events, UnitT<REAL>* units,
+                                                       EndT<REAL>* ends, cudaStream_t s) {
+    compile_units_kernel<REAL><<<n, 128, 0, s>>>(contracts, intervals, daily, flags, events, units, ends);
+    return cudaGetLastError();
 }
 
 // Normals first..first+count of block `block`, one thread per Box-Muller pair.
@@ -91,6 +106,15 @@ static __global__ void sobol_points_kernel(SobolTables t, int dim, uint64_t firs
     if (bits) bits[i] = x;
     if (normals) normals[i] = double(sobol_normal(x, REAL()));
 }
+
+#if KGPU_FP32_UNIT
+cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, EventT<float>* events,
+                                       IntervalT<float>* intervals, DailyT<float>* daily,
+                                       cudaStream_t s) {
+    compile_arrays_fp32_kernel<<<1024, 256, 0, s>>>(b, steps, events, intervals, daily);
+    return cudaGetLastError();
+}
+#endif
 
 cudaError_t KGPU_CAT(launch_pcg_normals_, PRECISION)(uint64_t seed, uint64_t block, uint64_t first,
                                                      int64_t count, double* out, cudaStream_t s) {

@@ -6,26 +6,48 @@
 
 namespace kgpu {
 
-// Shared-memory bytes of the plain kernel for `dims` Sobol dimensions and a surface.
+// Shared-memory bytes of the kernels for `dims` Sobol dimensions and a surface.
 size_t plain_smem_bytes(int precision, bool sobol, int dims, int lv_values);
 size_t persistent_smem_bytes(int precision, bool sobol, int dims, int lv_values);
 
-cudaError_t launch_plain(int precision, int model, bool sobol, int blocks, size_t smem,
-                         cudaStream_t stream, const PlainArgs& a, const kgpu_model& m,
-                         const double* lv_dev);
-cudaError_t launch_persistent(int precision, int model, bool sobol, int blocks, size_t smem,
-                              cudaStream_t stream, const PersistentArgs& a, const kgpu_model& m,
-                              const double* lv_dev);
-// Resident CTAs per SM of the persistent kernel at `smem` bytes.
-int persistent_blocks_per_sm(int precision, int model, bool sobol, size_t smem);
+cudaError_t launch_plain_fp64(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
+                              const PlainArgs<double>& a, const kgpu_model& m, const double* lv);
+cudaError_t launch_plain_fp32(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
+                              const PlainArgs<float>& a, const kgpu_model& m, const double* lv);
+cudaError_t launch_persistent_fp64(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
+                                   const PersistentArgs<double>& a, const kgpu_model& m,
+                                   const double* lv);
+cudaError_t launch_persistent_fp32(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
+                                   const PersistentArgs<float>& a, const kgpu_model& m,
+                                   const double* lv);
+int persistent_occupancy_fp64(int model, bool sobol, size_t smem);
+int persistent_occupancy_fp32(int model, bool sobol, size_t smem);
+cudaError_t launch_compile_contracts_fp64(const kgpu_contract* in, int n, ContractT<double>* out,
+                                          cudaStream_t s);
+cudaError_t launch_compile_contracts_fp32(const kgpu_contract* in, int n, ContractT<float>* out,
+                                          cudaStream_t s);
+cudaError_t launch_compile_units_fp64(const kgpu_contract* contracts, int n,
+                                      const kgpu_bridge_interval* intervals,
+                                      const kgpu_bridge_daily* daily, const uint8_t* flags,
+                                      const kgpu_event* events, UnitT<double>* units,
+                                      EndT<double>* ends, cudaStream_t s);
+cudaError_t launch_compile_units_fp32(const kgpu_contract* contracts, int n,
+                                      const kgpu_bridge_interval* intervals,
+                                      const kgpu_bridge_daily* daily, const uint8_t* flags,
+                                      const kgpu_event* events, UnitT<float>* units,
+                                      EndT<float>* ends, cudaStream_t s);
+cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, EventT<float>* events,
+                                       IntervalT<float>* intervals, DailyT<float>* daily,
+                                       cudaStream_t s);
 
 // Raw streams (kgpu_pcg_words, kgpu_pcg_normals, kgpu_sobol_points).
-cudaError_t launch_pcg_words(uint64_t seed, uint64_t stream_id, uint64_t first, int64_t count,
-                             uint32_t* out, cudaStream_t stream);
-cudaError_t launch_pcg_normals(int precision, uint64_t seed, uint64_t block, uint64_t first,
-                               int64_t count, double* out, cudaStream_t stream);
-cudaError_t launch_sobol_points(int precision, const SobolTables& t, int dim, uint64_t first,
-                                int64_t count, uint64_t* bits, double* normals,
-                                cudaStream_t stream);
+cudaError_t launch_pcg_normals_fp64(uint64_t seed, uint64_t block, uint64_t first, int64_t count,
+                                    double* out, cudaStream_t s);
+cudaError_t launch_pcg_normals_fp32(uint64_t seed, uint64_t block, uint64_t first, int64_t count,
+                                    double* out, cudaStream_t s);
+cudaError_t launch_sobol_points_fp64(const SobolTables& t, int dim, uint64_t first, int64_t count,
+                                     uint64_t* bits, double* normals, cudaStream_t s);
+cudaError_t launch_sobol_points_fp32(const SobolTables& t, int dim, uint64_t first, int64_t count,
+                                     uint64_t* bits, double* normals, cudaStream_t s);
 
 }  // namespace kgpu

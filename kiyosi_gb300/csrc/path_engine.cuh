@@ -13,6 +13,10 @@
 // normals [ (s % 256) * D, (s % 256 + 1) * D ) of stream Pcg32::new(seed, s / 256), or
 // Sobol point s, dimensions 0..D-1; skipped normals keep later positions unchanged
 // (LazyPath::finish / SkippingPath::skip, monte_carlo.rs:1591-1676).
+//
+// Plans are read in the kernel's own precision: FP64 kernels read the caller's kgpu_*
+// arrays directly (identical layouts), FP32 kernels read single-precision copies made
+// on the device by compile_plan_kernel, so no FP64 instruction runs per step.
 #pragma once
 #include <cstdint>
 
@@ -21,14 +25,75 @@
 
 namespace kgpu {
 
-// Device view of the book (device pointers).
+template <class Real>
+struct StepT {
+    Real drift, diffusion, time, discount;
+};
+template <class Real>
+struct EventT {
+    Real knock_out, coupon_barrier;
+    Real payment[4];
+    int32_t has_knock_out, step;
+};
+template <class Real>
+struct DailyT {
+    Real weight, width;
+};
+template <class Real>
+struct IntervalT {
+    int32_t end, reserved;
+    Real drift, diffusion;
+};
+static_assert(sizeof(StepT<double>) == sizeof(kgpu_step), "step layout");
+static_assert(sizeof(EventT<double>) == sizeof(kgpu_event), "event layout");
+static_assert(sizeof(DailyT<double>) == sizeof(kgpu_bridge_daily), "daily layout");
+static_assert(sizeof(IntervalT<double>) == sizeof(kgpu_bridge_interval), "interval layout");
+
+// One position of a bridged path (persistent kernels): position `start` of an interval
+// draws the interval end (a = diffusion, b = drift), positions start+1..end are the
+// daily bridge steps (a = width, b = weight).  Compiled on the device from the
+// reference's BridgePlan intervals and daily weights.
+template <class Real>
+struct UnitT {
+    Real a, b;
+    int32_t end;    // last position of the interval
+    int32_t flags;  // kUnitBegin | kUnitLast | kUnitKnockOut | end step flags << 8
+};
+constexpr int32_t kUnitBegin = 1;
+constexpr int32_t kUnitLast = 2;
+constexpr int32_t kUnitKnockOut = 4;  // the interval's end has a knock-out level
+
+// Cash event of an interval's end, stored at the interval's last position.
+template <class Real>
+struct EndT {
+    Real knock_out, coupon_barrier;
+    Real payment[4];
+    Real pad[2];
+};
+
+// A contract's scalars in the kernel's precision.
+template <class Real>
+struct ContractT {
+    int32_t payoff, flags, step_count, event_count, bridge_count, reserved;
+    int64_t step_offset;
+    int32_t event_offset, bridge_offset;
+    Real strike, sign, diffusion, half_variance, moneyness, log_scale;
+    Real knock_in, initial_cash, terminal_base, terminal_plain, terminal_fixed;
+    Real downside_lower, downside_upper, downside_initial, final_discount;
+    Real knock_out, quantity, daily_quantity, acceleration, log_strike;
+};
+
+// Device view of the book in the kernel's precision.
+template <class Real>
 struct DevBook {
-    const kgpu_contract* contracts;
-    const kgpu_step* steps;
+    const ContractT<Real>* contracts;
+    const StepT<Real>* steps;
     const uint8_t* flags;
-    const kgpu_event* events;
-    const kgpu_bridge_interval* intervals;
-    const kgpu_bridge_daily* daily;
+    const EventT<Real>* events;
+    const IntervalT<Real>* intervals;
+    const DailyT<Real>* daily;
+    const UnitT<Real>* units;  // per-position bridge units (persistent kernels), may be null
+    const EndT<Real>* ends;    // per-position interval-end events (persistent kernels)
 };
 
 // Device view of the model.  The local-volatility surface is staged in shared memory
@@ -81,6 +146,7 @@ struct PcgSource {
         has_spare = true;
         return c;
     }
+    __device__ __forceinline__ Real normal_if(bool need) { return need ? normal() : Real(0); }
     __device__ __forceinline__ void skip(int remaining) {
         if (remaining <= 0) return;
         if (has_spare) {
@@ -92,47 +158,94 @@ struct PcgSource {
     }
 };
 
-// Sobol point: bits of dimension d are high[d] ^ XOR_{c in low gray bits} low[c*D + d],
-// where high[] holds the shift and the directions of the gray-code bits shared by the
-// 256 points of one reference block (bits >= 8), and low[] the first 8 direction rows.
+// Sobol point: the bits of dimension d are high[d] ^ nib[d][g & 15] ^ nib[d][16 + (g >> 4)]
+// where high[] holds the shift and the directions of the gray-code bits >= 8 shared by
+// the 256 points of one reference block, g the low 8 gray-code bits of the point, and
+// nib[] the XORs of direction rows 0-3 and 4-7 for each 4-bit pattern.
 template <class Real>
 struct SobolSource {
     const uint64_t* high;
-    const uint64_t* low;
+    const uint64_t* __restrict__ nib;  // [dims][32]
     int dims;
     int used;
-    uint32_t gray_low;
+    uint32_t lo, hi;
 
     __device__ __forceinline__ void start(uint64_t sample) {
         uint64_t gray = sample ^ (sample >> 1);
-        gray_low = uint32_t(gray & 0xFF);
+        lo = uint32_t(gray & 0xF);
+        hi = uint32_t((gray >> 4) & 0xF) + 16;
         used = 0;
     }
     __device__ __forceinline__ uint64_t bits(int d) const {
-        uint64_t x = high[d];
-        uint32_t g = gray_low;
-        while (g) {
-            int c = __ffs(g) - 1;
-            x ^= low[c * dims + d];
-            g &= g - 1;
-        }
-        return x;
+        const uint64_t* row = nib + size_t(d) * 32;
+        return high[d] ^ __ldg(row + lo) ^ __ldg(row + hi);
     }
     __device__ __forceinline__ Real normal() { return sobol_normal(bits(used++), Real()); }
-    __device__ __forceinline__ void skip(int remaining) {
-        if (remaining > 0) used += remaining;
+    // Evaluates the next dimension whether or not it is needed (a pure function of the
+    // point), so the warp computes the quantile converged; consumes it only if needed.
+    __device__ __forceinline__ Real normal_if(bool need) {
+        const Real z = sobol_normal(bits(used < dims ? used : dims - 1), Real());
+        used += need ? 1 : 0;
+        return z;
     }
+    __device__ __forceinline__ void skip(int remaining) { used += remaining > 0 ? remaining : 0; }
+};
+
+// FP32 Sobol point from the top 32 of its 52 bits: high32[] and nib32[] hold the top 32
+// bits of the block's high part and of the nibble tables (truncation commutes with XOR),
+// halving the table bytes the path kernel reads.  The quantile needs the lower bits
+// only in the extreme tails (t < 2^-20, about 2e-6 of draws), where the full 52-bit
+// integer is rebuilt from the 64-bit directions.
+struct SobolSource32 {
+    const uint32_t* __restrict__ high32;  // this point's block row of the high table
+    const uint32_t* __restrict__ nib32;     // [dims][32]
+    const uint64_t* __restrict__ dirs64;    // [column * dims + dim]
+    const uint64_t* __restrict__ shifts64;  // [dim]
+    int dims;
+    int used;
+    uint32_t lo, hi;
+    uint64_t gray;
+
+    __device__ __forceinline__ void start(uint64_t sample) {
+        gray = sample ^ (sample >> 1);
+        lo = uint32_t(gray & 0xF);
+        hi = uint32_t((gray >> 4) & 0xF) + 16;
+        used = 0;
+    }
+    __device__ __forceinline__ float normal() {
+        const int d = used++;
+        const uint32_t* row = nib32 + size_t(d) * 32;
+        const uint32_t v = high32[d] ^ __ldg(row + lo) ^ __ldg(row + hi);
+        const bool upper = (v >> 31) != 0;
+        const uint32_t k = upper ? ~v : v;  // top 32 bits of the 52-bit tail integer
+        if (k < (1u << 12)) {
+            uint64_t x = shifts64[d];
+            for (uint64_t g = gray; g; g &= g - 1) x ^= dirs64[size_t(__ffsll(g) - 1) * dims + d];
+            return sobol_normal(x, 0.0f);
+        }
+        return normal_from_tail32(k, upper);
+    }
+    __device__ __forceinline__ float normal_if(bool need) { return need ? normal() : 0.0f; }
+    __device__ __forceinline__ void skip(int remaining) { used += remaining > 0 ? remaining : 0; }
 };
 
 // ------------------------------------------------------------------------------------
 // Arithmetic helpers: FP64 keeps the reference's rounding; FP32 uses fast intrinsics.
 // ------------------------------------------------------------------------------------
+__device__ __forceinline__ double xfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float xfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double xabs(double x) { return fabs(x); }
+__device__ __forceinline__ float xabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double xexp(double x) { return exp(x); }
 __device__ __forceinline__ float xexp(float x) { return __expf(x); }
 __device__ __forceinline__ double xexpm1(double x) { return expm1(x); }
 __device__ __forceinline__ float xexpm1(float x) { return expm1f(x); }
 __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float xsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double xinf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
+__device__ __forceinline__ float xinf(float) { return __int_as_float(0x7f800000); }
+__device__ __forceinline__ double xnan(double) { return __longlong_as_double(0x7ff8000000000000LL); }
+__device__ __forceinline__ float xnan(float) { return __int_as_float(0x7fc00000); }
 
 // scaled_value(initial, 1, log_return) for ordinary magnitudes (numerics.rs:226-238).
 template <class Real>
@@ -194,29 +307,31 @@ struct PathState {
     int i;         // next grid step
     int ev;        // next event (relative to the contract's first event)
     int k;         // next bridge interval
+    int end;       // grid step ending the current bridge interval (-1: not started)
     int fixings;
     int executed;  // grid steps simulated
     bool knocked_in;
     bool monitoring;
-    bool in_interval;
+    bool knocked_out;
 };
 
 template <class Real>
-__device__ __forceinline__ void path_init(PathState<Real>& s, const kgpu_contract& c, Real v0) {
+__device__ __forceinline__ void path_init(PathState<Real>& s, const ContractT<Real>& c, Real v0) {
     s.lr = Real(0);
     s.v = v0;
-    s.acc = Real(c.payoff == KGPU_PAYOFF_ACCUMULATOR ? c.quantity : 0.0);
-    s.cash = Real(c.initial_cash);
+    s.acc = c.payoff == KGPU_PAYOFF_ACCUMULATOR ? c.quantity : Real(0);
+    s.cash = c.initial_cash;
     s.target = Real(0);
     s.minimum = Real(0);
     s.i = 0;
     s.ev = 0;
     s.k = 0;
+    s.end = -1;
     s.fixings = 0;
     s.executed = 0;
     s.knocked_in = (c.flags & KGPU_C_KNOCKED_IN) != 0;
     s.monitoring = !s.knocked_in && (c.flags & KGPU_C_HAS_KNOCK_IN);
-    s.in_interval = false;
+    s.knocked_out = false;
 }
 
 // One grid step of the state.  BSM: `log_return += diffusion.mul_add(normal, drift)`;
@@ -224,15 +339,15 @@ __device__ __forceinline__ void path_init(PathState<Real>& s, const kgpu_contrac
 // independent variance shock); local volatility: Euler in log spot with the surface
 // read at the step's start.
 template <class Real, int MODEL, class Source>
-__device__ __forceinline__ void model_step(const DevModel<Real>& m, const kgpu_step& st,
+__device__ __forceinline__ void model_step(const DevModel<Real>& m, const StepT<Real>& st,
                                            PathState<Real>& s, Source& n) {
     if (MODEL == KGPU_MODEL_BSM) {
-        Real t = fma(Real(st.diffusion), n.normal(), Real(st.drift));
+        Real t = xfma(st.diffusion, n.normal(), st.drift);
         s.lr = s.lr + t;
     } else if (MODEL == KGPU_MODEL_HESTON) {
         Real z1 = n.normal();
         Real z2 = n.normal();
-        Real dt = Real(st.drift), sq = Real(st.diffusion);
+        Real dt = st.drift, sq = st.diffusion;
         Real vp = s.v > Real(0) ? s.v : Real(0);
         Real sv = xsqrt(vp) * sq;
         Real zv = m.rho * z1 + m.rho_bar * z2;
@@ -240,54 +355,129 @@ __device__ __forceinline__ void model_step(const DevModel<Real>& m, const kgpu_s
         s.v += m.kappa * (m.theta - vp) * dt + m.xi * sv * zv;
     } else {
         Real spot = m.spot * xexp(s.lr);
-        Real sigma = lv_at(m, Real(st.time), spot);
-        Real dt = Real(st.drift), sq = Real(st.diffusion);
+        Real sigma = lv_at(m, st.time, spot);
+        Real dt = st.drift, sq = st.diffusion;
         s.lr += (m.rate - m.dividend - Real(0.5) * sigma * sigma) * dt + sigma * sq * n.normal();
     }
 }
 
 // AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
 template <class Real>
-__device__ __forceinline__ Real autocallable_terminal(const kgpu_contract& c, Real spot, bool ki) {
+__device__ __forceinline__ Real autocallable_terminal(const ContractT<Real>& c, Real spot, bool ki) {
     if (ki) {
         if (c.flags & KGPU_C_DOWNSIDE) {
-            Real lower = Real(c.downside_lower), upper = Real(c.downside_upper);
-            Real clamped = spot < lower ? lower : (spot > upper ? upper : spot);
-            return Real(c.terminal_base) + (clamped - upper) / Real(c.downside_initial);
+            Real clamped = spot < c.downside_lower ? c.downside_lower
+                                                   : (spot > c.downside_upper ? c.downside_upper : spot);
+            return c.terminal_base + (clamped - c.downside_upper) / c.downside_initial;
         }
-        return Real(c.terminal_fixed);
+        return c.terminal_fixed;
     }
-    return Real(c.terminal_plain);
+    return c.terminal_plain;
 }
 
 template <class Real>
-__device__ __forceinline__ Real european_value(const kgpu_contract& c, Real z) {
-    Real distance = fma(Real(c.diffusion), z, Real(c.moneyness));
-    if (Real(c.sign) * distance <= Real(0)) return Real(0);
-    if (c.sign < 0.0) return -xexpm1(distance);
-    return -xexpm1(-distance) * xexp(fma(Real(c.diffusion), z, -Real(c.half_variance)));
+__device__ __forceinline__ Real european_value(const ContractT<Real>& c, Real z) {
+    Real distance = xfma(c.diffusion, z, c.moneyness);
+    if (c.sign * distance <= Real(0)) return Real(0);
+    if (c.sign < Real(0)) return -xexpm1(distance);
+    return -xexpm1(-distance) * xexp(xfma(c.diffusion, z, -c.half_variance));
 }
 
 template <class Real>
-__device__ __forceinline__ Real digital_value(const kgpu_contract& c, Real z) {
-    Real distance = Real(c.moneyness) + z;
-    bool call = c.sign > 0.0;
+__device__ __forceinline__ Real digital_value(const ContractT<Real>& c, Real z) {
+    Real distance = c.moneyness + z;
+    bool call = c.sign > Real(0);
     if (!(call ? distance > Real(0) : distance < Real(0))) return Real(0);
-    Real exponent = Real(c.log_scale) + ((c.flags & KGPU_C_ASSET_DIGITAL) ? Real(c.diffusion) * z : Real(0));
-    return Real(c.strike) * xexp(exponent);
+    Real exponent = c.log_scale + ((c.flags & KGPU_C_ASSET_DIGITAL) ? c.diffusion * z : Real(0));
+    return c.strike * xexp(exponent);
+}
+
+template <class Real>
+struct PlanPtrs {
+    const StepT<Real>* __restrict__ steps;
+    const uint8_t* __restrict__ flags;
+    const EventT<Real>* __restrict__ events;
+    const IntervalT<Real>* __restrict__ intervals;
+    const DailyT<Real>* __restrict__ daily;
+    const UnitT<Real>* __restrict__ units;
+    const EndT<Real>* __restrict__ ends;
+};
+
+template <class Real>
+__device__ __forceinline__ PlanPtrs<Real> plan_of(const DevBook<Real>& b, const ContractT<Real>& c) {
+    PlanPtrs<Real> p;
+    p.steps = b.steps + c.step_offset;
+    p.flags = b.flags + c.step_offset;
+    p.events = b.events ? b.events + c.event_offset : nullptr;
+    p.intervals = b.intervals ? b.intervals + c.bridge_offset : nullptr;
+    p.daily = b.daily ? b.daily + c.step_offset : nullptr;
+    p.units = b.units ? b.units + c.step_offset : nullptr;
+    p.ends = b.ends ? b.ends + c.step_offset : nullptr;
+    return p;
 }
 
 // Advances one path by one unit of work (a grid step, or a bridge interval end).
 // Returns true when the path has finished; its payoff is then in `value`.
 template <class Real, int MODEL, class Source>
-__device__ __forceinline__ bool path_step(const DevModel<Real>& m, const kgpu_contract& c,
-                                          const kgpu_step* __restrict__ steps,
-                                          const uint8_t* __restrict__ flags,
-                                          const kgpu_event* __restrict__ events,
-                                          const kgpu_bridge_interval* __restrict__ intervals,
-                                          const kgpu_bridge_daily* __restrict__ daily,
-                                          PathState<Real>& s, Source& n, Real& value) {
+__device__ __forceinline__ bool path_step(const DevModel<Real>& m, const ContractT<Real>& c,
+                                          const PlanPtrs<Real>& p, PathState<Real>& s, Source& n,
+                                          Real& value) {
     const int payoff = c.payoff;
+    if (payoff == KGPU_PAYOFF_AUTOCALLABLE && (c.flags & KGPU_C_BRIDGE)) {
+        // bridge_payoffs::<1, true>: the interval end is drawn first, then daily bridge
+        // steps until knock-in is decided, then the interval end.  Each call evaluates at
+        // most one normal, at a single call site, so lanes in different phases of their
+        // paths still share the quantile evaluation.
+        const Real level = c.knock_in;
+        const bool begin = s.end < 0;
+        const bool daily = !begin && s.i < s.end && s.monitoring && !(s.minimum < level);
+        const Real z = n.normal_if(begin || daily);
+        if (begin) {
+            const IntervalT<Real> iv = p.intervals[s.k];
+            s.target = s.lr + xfma(iv.diffusion, z, iv.drift);
+            s.minimum = xinf(Real());
+            s.end = iv.end;
+            if (s.i < s.end && s.monitoring) return false;
+        } else if (daily) {
+            const DailyT<Real> d = p.daily[s.i];
+            s.lr = s.lr + xfma(d.weight, s.target - s.lr, d.width * z);
+            s.minimum = s.lr < s.minimum ? s.lr : s.minimum;
+            ++s.i;
+            ++s.executed;
+            if (s.i < s.end) return false;
+        }
+        if (s.i < s.end) {
+            // knock-in decided (or never monitored): skip the interval's daily normals
+            n.skip(s.end - s.i);
+            s.i = s.end;
+        }
+        // interval end
+        const int end = s.end;
+        s.lr = s.target;
+        s.end = -1;
+        ++s.executed;
+        const uint8_t fl = p.flags[end];
+        if (s.monitoring && (s.minimum < level || ((fl & KGPU_STEP_KNOCK_IN) && s.lr < level))) {
+            s.monitoring = false;
+            s.knocked_in = true;
+        }
+        s.i = end + 1;
+        s.k += 1;
+        if (fl & KGPU_STEP_EVENT) {
+            const EventT<Real>& e = p.events[s.ev++];
+            const bool hit = e.has_knock_out && s.lr >= e.knock_out;
+            s.cash += e.payment[int(s.lr >= e.coupon_barrier) | (int(hit) << 1)];
+            if (hit) {
+                value = s.cash;
+                return true;
+            }
+        }
+        if (s.k < c.bridge_count) return false;
+        const bool hit = s.knocked_in ||
+                         ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) && (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < level);
+        value = s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), hit) * c.final_discount;
+        return true;
+    }
     if (payoff == KGPU_PAYOFF_EUROPEAN) {
         value = european_value(c, n.normal());
         s.executed = 1;
@@ -298,100 +488,48 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const kgpu_co
         s.executed = 1;
         return true;
     }
-    if (payoff == KGPU_PAYOFF_AUTOCALLABLE && (c.flags & KGPU_C_BRIDGE)) {
-        // bridge_payoffs::<1, true>: interval end drawn first, then daily bridge steps
-        // until knock-in is decided, then the interval end.
-        const kgpu_bridge_interval iv = intervals[s.k];
-        const Real level = Real(c.knock_in);
-        if (!s.in_interval) {
-            s.target = s.lr + fma(Real(iv.diffusion), n.normal(), Real(iv.drift));
-            s.minimum = Real(__int_as_float(0x7f800000));
-            s.in_interval = true;
-        }
-        if (s.i < iv.end) {
-            if (!s.monitoring || s.minimum < level) {
-                n.skip(iv.end - s.i);
-                s.i = iv.end;
-            } else {
-                Real z = n.normal();
-                const kgpu_bridge_daily d = daily[s.i];
-                s.lr = s.lr + fma(Real(d.weight), s.target - s.lr, Real(d.width) * z);
-                s.minimum = s.lr < s.minimum ? s.lr : s.minimum;
-                ++s.i;
-                ++s.executed;
-                if (s.i < iv.end) return false;
-            }
-        }
-        // interval end
-        s.lr = s.target;
-        s.in_interval = false;
-        ++s.executed;
-        const uint8_t fl = flags[iv.end];
-        if (s.monitoring && (s.minimum < level || ((fl & KGPU_STEP_KNOCK_IN) && s.lr < level))) {
-            s.monitoring = false;
-            s.knocked_in = true;
-        }
-        s.i = iv.end + 1;
-        s.k += 1;
-        if (fl & KGPU_STEP_EVENT) {
-            const kgpu_event& e = events[s.ev++];
-            bool hit = e.has_knock_out && s.lr >= Real(e.knock_out);
-            s.cash += Real(e.payment[int(s.lr >= Real(e.coupon_barrier)) | (int(hit) << 1)]);
-            if (hit) {
-                value = s.cash;
-                return true;
-            }
-        }
-        if (s.k < c.bridge_count) return false;
-        bool hit = s.knocked_in ||
-                   ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) && (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < level);
-        value = s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), hit) * Real(c.final_discount);
-        return true;
-    }
     // Grid-stepping families.
     const int i = s.i;
-    const kgpu_step st = steps[i];
+    const StepT<Real> st = p.steps[i];
     model_step<Real, MODEL>(m, st, s, n);
-    const uint8_t fl = flags[i];
+    const uint8_t fl = p.flags[i];
     s.i = i + 1;
     s.executed += 1;
     const bool last = s.i == c.step_count;
     if (payoff == KGPU_PAYOFF_AUTOCALLABLE) {
-        if (fl & KGPU_STEP_KNOCK_IN)
-            s.knocked_in |= (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < Real(c.knock_in);
+        if (fl & KGPU_STEP_KNOCK_IN) s.knocked_in |= (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < c.knock_in;
         if (fl & KGPU_STEP_EVENT) {
-            const kgpu_event& e = events[s.ev++];
-            bool coupon_due = s.lr >= Real(e.coupon_barrier);
-            bool knocked_out = e.has_knock_out && s.lr >= Real(e.knock_out);
-            s.cash += Real(e.payment[int(coupon_due) | (int(knocked_out) << 1)]);
+            const EventT<Real>& e = p.events[s.ev++];
+            const bool coupon_due = s.lr >= e.coupon_barrier;
+            const bool knocked_out = e.has_knock_out && s.lr >= e.knock_out;
+            s.cash += e.payment[int(coupon_due) | (int(knocked_out) << 1)];
             if (knocked_out) {
                 value = s.cash;
                 return true;
             }
         }
         if (!last) return false;
-        bool ki = s.knocked_in || ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) &&
-                                   (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < Real(c.knock_in));
-        value = s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), ki) * Real(c.final_discount);
+        const bool ki = s.knocked_in || ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) &&
+                                         (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < c.knock_in);
+        value = s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), ki) * c.final_discount;
         return true;
     }
     if (payoff == KGPU_PAYOFF_ACCUMULATOR) {
-        const Real sign = Real(c.sign);
+        const Real sign = c.sign;
         auto unit = [&](Real lr) {
-            Real distance = lr - Real(c.log_strike);
-            if (fabs(distance) < Real(0.5)) return sign * Real(c.strike) * xexpm1(distance);
+            Real distance = lr - c.log_strike;
+            if (xabs(distance) < Real(0.5)) return sign * c.strike * xexpm1(distance);
             Real spot = spot_at(m.spot, lr);
-            return c.sign > 0.0 ? spot - Real(c.strike) : Real(c.strike) - spot;
+            return sign > Real(0) ? spot - c.strike : c.strike - spot;
         };
-        if ((fl & KGPU_STEP_EVENT) && sign * s.lr >= sign * Real(c.knock_out)) {
-            value = s.acc * unit(s.lr) * Real(st.discount);
+        if ((fl & KGPU_STEP_EVENT) && sign * s.lr >= sign * c.knock_out) {
+            value = s.acc * unit(s.lr) * st.discount;
             return true;
         }
         if (fl & KGPU_STEP_ACCUMULATE)
-            s.acc += Real(c.daily_quantity) *
-                     (sign * s.lr < sign * Real(c.log_strike) ? Real(c.acceleration) : Real(1));
+            s.acc += c.daily_quantity * (sign * s.lr < sign * c.log_strike ? c.acceleration : Real(1));
         if (!last) return false;
-        value = s.acc * unit(s.lr) * Real(c.final_discount);
+        value = s.acc * unit(s.lr) * c.final_discount;
         return true;
     }
     if (payoff == KGPU_PAYOFF_ASIAN && (fl & KGPU_STEP_FIXING)) {
@@ -400,9 +538,66 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const kgpu_co
     }
     if (!last) return false;
     Real underlying = payoff == KGPU_PAYOFF_ASIAN ? s.acc / Real(s.fixings) : spot_at(m.spot, s.lr);
-    Real x = Real(c.sign) * (underlying - Real(c.strike));
-    value = (x > Real(0) ? x : Real(0)) * Real(c.final_discount);
+    Real x = c.sign * (underlying - c.strike);
+    value = (x > Real(0) ? x : Real(0)) * c.final_discount;
     return true;
+}
+
+// The bridged autocallable as one uniform unit of work per path position (persistent
+// kernels).  Same arithmetic and normal positions as the bridge branch of path_step: a
+// unit is the interval-end draw (the interval's first position) or one daily bridge
+// step.  Every call evaluates one normal and both unit formulas and selects; when the
+// interval's end is due (its last position, or knock-in decided so the remaining daily
+// normals are skipped) the interval end is settled in the same call, with selects and
+// predicated loads rather than a separate phase, so lanes at different positions of
+// their paths stay converged.  Returns true when the path has finished.
+template <class Real, class Source>
+__device__ __forceinline__ bool bridge_unit_step(const ContractT<Real>& c, const PlanPtrs<Real>& p,
+                                                 PathState<Real>& s, Source& n) {
+    const int q = s.i;
+    const UnitT<Real> u = p.units[q];
+    const Real z = n.normal();
+    const bool begin = (u.flags & kUnitBegin) != 0;
+    const Real target = s.lr + xfma(u.a, z, u.b);
+    const Real daily = s.lr + xfma(u.b, s.target - s.lr, u.a * z);
+    s.target = begin ? target : s.target;
+    s.lr = begin ? s.lr : daily;
+    s.minimum = begin ? xinf(Real()) : (daily < s.minimum ? daily : s.minimum);
+    s.executed += 1;
+    const Real level = c.knock_in;
+    const bool due = (u.flags & kUnitLast) || !s.monitoring || s.minimum < level;
+    // Interval end, evaluated with selects: skip the remaining daily normals, settle
+    // knock-in and the cash event.  Lanes without an event read one shared record.
+    const int end = u.end;
+    const int next = due ? end + 1 : q + 1;
+    n.skip(next - (q + 1));
+    s.i = next;
+    const Real lr = due ? s.target : s.lr;
+    s.lr = lr;
+    const int fl = u.flags >> 8;
+    const bool ki = due && s.monitoring && (s.minimum < level || ((fl & KGPU_STEP_KNOCK_IN) && lr < level));
+    s.knocked_in = s.knocked_in || ki;
+    s.monitoring = s.monitoring && !ki;
+    bool hit = false;
+    if (due && (fl & KGPU_STEP_EVENT)) {
+        const EndT<Real> e = p.ends[end];
+        hit = (u.flags & kUnitKnockOut) && lr >= e.knock_out;
+        const bool coupon = lr >= e.coupon_barrier;
+        s.cash += hit ? (coupon ? e.payment[3] : e.payment[2]) : (coupon ? e.payment[1] : e.payment[0]);
+    }
+    s.knocked_out = hit;
+    return due && (hit || end + 1 >= c.step_count);
+}
+
+// Payoff of a finished bridged path: the cash collected, plus the discounted terminal
+// redemption when the note reached expiry (discounted_terminal, autocallable.rs:797).
+template <class Real>
+__device__ __forceinline__ Real bridge_value(const DevModel<Real>& m, const ContractT<Real>& c,
+                                             const PathState<Real>& s) {
+    if (s.knocked_out) return s.cash;
+    const bool in = s.knocked_in || ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) && (c.flags & KGPU_C_HAS_KNOCK_IN) &&
+                                     s.lr < c.knock_in);
+    return s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), in) * c.final_discount;
 }
 
 // Scaled Welford moments (monte_carlo.rs:2155-2222), used by the plain schedule.

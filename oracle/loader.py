@@ -27,7 +27,8 @@ def load():
             return _LIB
         path = os.path.join(HERE, "liboracle.so")
         sources = [os.path.join(HERE, f) for f in ("oracle.cpp", "lsmc.cpp", "oracle_core.h",
-                                                  "heston_adi.cpp")]
+                                                  "heston_adi.cpp", "Makefile")]
+        sources.append(os.path.join(HERE, "..", "include", "kgpu.h"))
         newest = max(os.path.getmtime(s) for s in sources if os.path.exists(s))
         if not os.path.exists(path) or os.path.getmtime(path) < newest:
             build()
