@@ -290,11 +290,14 @@ typedef struct kgpu_lsmc_settings {
     int32_t path_count;
     int32_t exercise_dates;    /* exercise intervals (step_count of the reference) */
     int32_t substeps;          /* Euler substeps per exercise interval (Heston) */
-    int32_t basis;             /* KGPU_BASIS_* */
-    int32_t sampling;          /* KGPU_SAMPLING_PSEUDO_RANDOM only for Heston */
+    int32_t basis;             /* KGPU_BASIS_* (QUADRATIC: BSM {1, S/K, (S/K)^2};
+                                  POLY3: monomials of degree <= 3 in (S/K, v/theta)) */
+    int32_t sampling;          /* KGPU_SAMPLING_PSEUDO_RANDOM */
+    int32_t precision;         /* KGPU_PRECISION_*: path store and per-path arithmetic */
     int32_t mlp_epochs;        /* MLP basis: epochs per exercise date */
     int32_t mlp_batch;         /* MLP basis: minibatch size */
     int32_t mlp_hidden;        /* MLP basis: hidden width (64) */
+    int32_t reserved;
     double mlp_learning_rate;
     uint64_t seed;
     uint64_t mlp_seed;

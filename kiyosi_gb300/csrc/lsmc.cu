@@ -1,11 +1,553 @@
-// American exercise by least-squares Monte Carlo (placeholder until the LSMC kernels land).
+// American exercise by least-squares Monte Carlo (Longstaff-Schwartz) on the GPU.
+//
+// Reference method: MonteCarloVanillaEngine::american_scenarios,
+// crates/kiyosi/src/engines/monte_carlo/american.rs:955-1455, and solve_quadratic
+// (1693-1749).  BSM with the quadratic basis {1, S/K, (S/K)^2} follows it step for step:
+// per path the cumulative Brownian coordinate at each exercise date from the block
+// streams (Pcg32::new(seed, path / 256), path-major, `dates` normals per path), spots
+// S0 exp(drift (k+1)) exp(diffusion W_k), backward induction regressing discounted cash
+// on the basis over in-the-money paths, exercise when intrinsic/K > continuation.
+// Heston uses full-truncation Euler paths (`substeps` per exercise interval, two normals
+// per step) and the ten monomials of degree <= 3 in (S/K, v/theta), with the same
+// pivoted elimination and degree fallback.
+//
+// Kernels: lsmc_forward writes the path store [date][path] (coalesced); per date,
+// lsmc_backward applies the next date's decision, discounts the cash and accumulates
+// the in-the-money normal equations (products in the store's precision, FP64 across
+// warps and blocks), lsmc_solve merges the block partials in block order and solves in
+// FP64; lsmc_final and lsmc_lower_bound reduce the estimates.  The whole sequence is
+// captured in a CUDA graph per problem shape and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
 #include "../../include/kgpu.h"
 #include "api_internal.h"
+#include "path_engine.cuh"
 
-extern "C" kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double strike,
-                                       double sign, double expiry, const kgpu_lsmc_settings* settings,
-                                       uint64_t fresh_seed, kgpu_lsmc_result* out) {
-    (void)model; (void)strike; (void)sign; (void)expiry; (void)settings; (void)fresh_seed; (void)out;
-    if (ctx) ctx->error = "LSMC is not built in this library";
-    return KGPU_UNSUPPORTED_OPERATION;
+namespace kgpu {
+namespace {
+
+constexpr int kLsmcThreads = 128;
+constexpr int kMaxTerms = 10;
+constexpr int kMaxSums = kMaxTerms * (kMaxTerms + 1) / 2 + kMaxTerms;  // upper triangle + rhs
+
+template <class Real>
+struct LsmcParams {
+    Real spot, strike, sign, drift, diffusion, discount;
+    Real rate, dividend, kappa, theta, xi, rho, rho_bar, v0, h, sqrt_h, y_scale;
+    int dates, substeps, paths, terms, max_degree;
+};
+
+__host__ __device__ constexpr int sum_count(int terms) { return terms * (terms + 1) / 2 + terms; }
+
+template <class Real, bool TWO>
+__device__ __forceinline__ void lsmc_basis(Real x, Real y, Real* f) {
+    f[0] = Real(1);
+    f[1] = x;
+    if (!TWO) {
+        f[2] = x * x;
+        return;
+    }
+    f[2] = y;
+    f[3] = x * x;
+    f[4] = x * y;
+    f[5] = y * y;
+    f[6] = x * x * x;
+    f[7] = x * x * y;
+    f[8] = x * y * y;
+    f[9] = y * y * y;
+}
+
+template <class Real, bool TWO>
+__device__ __forceinline__ Real spot_at_date(const LsmcParams<Real>& p, int k, Real a) {
+    if (!TWO) return p.spot * xexp(p.drift * Real(k + 1)) * xexp(p.diffusion * a);
+    return p.spot * xexp(a);
+}
+
+template <class Real>
+__device__ __forceinline__ Real intrinsic(const LsmcParams<Real>& p, Real spot) {
+    const Real v = p.sign * (spot - p.strike);
+    return v > Real(0) ? v : Real(0);
+}
+
+template <class Real, bool TWO>
+__device__ __forceinline__ Real continuation(const LsmcParams<Real>& p, const double* coef, Real x, Real y) {
+    Real f[kMaxTerms];
+    lsmc_basis<Real, TWO>(x, y, f);
+    Real c = Real(0);
+#pragma unroll
+    for (int i = 0; i < (TWO ? 10 : 3); ++i) c += Real(coef[i]) * f[i];
+    return c;
+}
+
+// Forward pass: the path store and the terminal cash.
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(256) lsmc_forward(LsmcParams<Real> p, uint64_t seed, Real* a, Real* b,
+                                                    Real* cash) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.paths) return;
+    const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
+    PcgSource<Real> n;
+    n.start(seed, uint64_t(i), dims);
+    Real x = Real(0), v = p.v0;
+    for (int k = 0; k < p.dates; ++k) {
+        if (!TWO) {
+            x += n.normal();
+        } else {
+            for (int j = 0; j < p.substeps; ++j) {
+                const Real z1 = n.normal(), z2 = n.normal();
+                const Real vp = v > Real(0) ? v : Real(0);
+                const Real sv = xsqrt(vp) * p.sqrt_h;
+                x += (p.rate - p.dividend - Real(0.5) * vp) * p.h + sv * z1;
+                v += p.kappa * (p.theta - vp) * p.h + p.xi * sv * (p.rho * z1 + p.rho_bar * z2);
+            }
+            b[size_t(k) * p.paths + i] = v;
+        }
+        a[size_t(k) * p.paths + i] = x;
+    }
+    cash[i] = intrinsic(p, spot_at_date<Real, TWO>(p, p.dates - 1, x));
+}
+
+// One exercise date of the backward induction (american.rs:1347-1417).
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p, int date, const double* coef_next,
+                                                              const int* have_next, const Real* a, const Real* b,
+                                                              Real* cash, double* partials) {
+    constexpr int T = TWO ? 10 : 3;
+    constexpr int S = sum_count(T);
+    Real acc[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) acc[j] = Real(0);
+    const bool decide = coef_next != nullptr && *have_next;
+    double cn[T];
+#pragma unroll
+    for (int j = 0; j < T; ++j) cn[j] = decide ? coef_next[j] : 0.0;
+    const Real inv_k = Real(1) / p.strike;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
+        Real c = cash[i];
+        if (decide) {
+            const Real s1 = spot_at_date<Real, TWO>(p, date + 1, a[size_t(date + 1) * p.paths + i]);
+            const Real y1 = TWO ? b[size_t(date + 1) * p.paths + i] * p.y_scale : Real(0);
+            const Real e = intrinsic(p, s1);
+            if (e > Real(0) && e * inv_k > continuation<Real, TWO>(p, cn, s1 * inv_k, y1)) c = e;
+        }
+        c *= p.discount;
+        cash[i] = c;
+        const Real s = spot_at_date<Real, TWO>(p, date, a[size_t(date) * p.paths + i]);
+        if (intrinsic(p, s) > Real(0)) {
+            Real f[T];
+            lsmc_basis<Real, TWO>(s * inv_k, TWO ? b[size_t(date) * p.paths + i] * p.y_scale : Real(0), f);
+            const Real target = c * inv_k;
+            int q = 0;
+#pragma unroll
+            for (int r = 0; r < T; ++r)
+#pragma unroll
+                for (int col = r; col < T; ++col) acc[q++] += f[r] * f[col];
+#pragma unroll
+            for (int r = 0; r < T; ++r) acc[q++] += f[r] * target;
+        }
+    }
+    // Warp shuffles in FP64, then warps in a fixed order.
+    __shared__ double warp_sums[kLsmcThreads / 32][S];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+        double v = double(acc[j]);
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) warp_sums[warp][j] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        double v = 0.0;
+        for (int w = 0; w < kLsmcThreads / 32; ++w) v += warp_sums[w][j];
+        partials[size_t(blockIdx.x) * S + j] = v;
+    }
+}
+
+// Merges the block partials in block order and solves the normal equations with pivoting
+// and degree fallback (solve_quadratic, american.rs:1693-1749), in FP64.
+template <bool TWO>
+__global__ void lsmc_solve(const double* partials, int blocks, int max_degree, double* coef, int* have,
+                           int* failed) {
+    constexpr int T = TWO ? 10 : 3;
+    constexpr int S = sum_count(T);
+    __shared__ double sums[S];
+    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        double v = 0.0;
+        for (int blk = 0; blk < blocks; ++blk) v += partials[size_t(blk) * S + j];
+        sums[j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int j = 0; j < kMaxTerms; ++j) coef[j] = 0.0;
+    *have = 0;
+    if (sums[0] == 0.0) return;
+    double full[T][T + 1];
+    int q = 0;
+    for (int r = 0; r < T; ++r)
+        for (int c = r; c < T; ++c) {
+            full[r][c] = sums[q];
+            full[c][r] = sums[q];
+            ++q;
+        }
+    for (int r = 0; r < T; ++r) full[r][T] = sums[q++];
+    for (int degree = max_degree; degree >= 0; --degree) {
+        const int k = TWO ? (degree + 1) * (degree + 2) / 2 : degree + 1;
+        double m[T][T + 1];
+        for (int r = 0; r < k; ++r) {
+            for (int c = 0; c < k; ++c) m[r][c] = full[r][c];
+            m[r][k] = full[r][T];
+        }
+        double scale = 0.0;
+        for (int r = 0; r < k; ++r)
+            for (int c = 0; c < k; ++c) scale = fmax(scale, fabs(m[r][c]));
+        bool singular = false;
+        for (int col = 0; col < k && !singular; ++col) {
+            int pivot = col;
+            for (int r = col + 1; r < k; ++r)
+                if (fabs(m[r][col]) >= fabs(m[pivot][col])) pivot = r;
+            if (!isfinite(m[pivot][col])) {
+                *failed = 1;
+                return;
+            }
+            if (fabs(m[pivot][col]) <= 1e-14 * scale) {
+                singular = true;
+                break;
+            }
+            if (pivot != col)
+                for (int c = 0; c <= k; ++c) {
+                    double t = m[col][c];
+                    m[col][c] = m[pivot][c];
+                    m[pivot][c] = t;
+                }
+            for (int r = col + 1; r < k; ++r) {
+                const double factor = m[r][col] / m[col][col];
+                for (int c = col; c < k; ++c) m[r][c] -= factor * m[col][c];
+                m[r][k] -= factor * m[col][k];
+            }
+        }
+        if (singular) continue;
+        double x[T];
+        for (int r = k - 1; r >= 0; --r) {
+            double v = m[r][k];
+            for (int c = r + 1; c < k; ++c) v -= m[r][c] * x[c];
+            x[r] = v / m[r][r];
+        }
+        for (int r = 0; r < k; ++r) {
+            if (!isfinite(x[r])) {
+                *failed = 1;
+                return;
+            }
+            coef[r] = x[r];
+        }
+        *have = 1;
+        return;
+    }
+    *failed = 1;
+}
+
+// Date-0 decision and the mean of the cash (FP64 block partials: sum, sum of squares).
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_final(LsmcParams<Real> p, const double* coef0, const int* have0,
+                                                           const Real* a, const Real* b, const Real* cash,
+                                                           double* partials) {
+    constexpr int T = TWO ? 10 : 3;
+    double cn[T];
+    const bool decide = *have0;
+#pragma unroll
+    for (int j = 0; j < T; ++j) cn[j] = decide ? coef0[j] : 0.0;
+    const Real inv_k = Real(1) / p.strike;
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
+        Real c = cash[i];
+        if (decide) {
+            const Real s = spot_at_date<Real, TWO>(p, 0, a[i]);
+            const Real y = TWO ? b[i] * p.y_scale : Real(0);
+            const Real e = intrinsic(p, s);
+            if (e > Real(0) && e * inv_k > continuation<Real, TWO>(p, cn, s * inv_k, y)) c = e;
+        }
+        s0 += double(c);
+        s1 += double(c) * double(c);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, off);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, off);
+    }
+    __shared__ double w0[kLsmcThreads / 32], w1[kLsmcThreads / 32];
+    if ((threadIdx.x & 31) == 0) {
+        w0[threadIdx.x >> 5] = s0;
+        w1[threadIdx.x >> 5] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w = 0; w < kLsmcThreads / 32; ++w) {
+            t0 += w0[w];
+            t1 += w1[w];
+        }
+        partials[2 * blockIdx.x] = t0;
+        partials[2 * blockIdx.x + 1] = t1;
+    }
+}
+
+// Lower bound on fresh paths: the fitted policy applied forward (american.rs:574-637).
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound(LsmcParams<Real> p, uint64_t seed,
+                                                                 const double* coefs, const int* have,
+                                                                 double* partials) {
+    constexpr int T = TWO ? 10 : 3;
+    const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
+    const Real inv_k = Real(1) / p.strike;
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
+        PcgSource<Real> n;
+        n.start(seed, uint64_t(i), dims);
+        Real x = Real(0), v = p.v0, value = Real(0), df = Real(1);
+        for (int k = 0; k < p.dates; ++k) {
+            if (!TWO) {
+                x += n.normal();
+            } else {
+                for (int j = 0; j < p.substeps; ++j) {
+                    const Real z1 = n.normal(), z2 = n.normal();
+                    const Real vp = v > Real(0) ? v : Real(0);
+                    const Real sv = xsqrt(vp) * p.sqrt_h;
+                    x += (p.rate - p.dividend - Real(0.5) * vp) * p.h + sv * z1;
+                    v += p.kappa * (p.theta - vp) * p.h + p.xi * sv * (p.rho * z1 + p.rho_bar * z2);
+                }
+            }
+            df *= p.discount;
+            const Real s = spot_at_date<Real, TWO>(p, k, x);
+            const Real e = intrinsic(p, s);
+            if (e > Real(0)) {
+                bool stop = k == p.dates - 1;
+                if (!stop && have[k]) {
+                    double cn[T];
+#pragma unroll
+                    for (int j = 0; j < T; ++j) cn[j] = coefs[size_t(k) * kMaxTerms + j];
+                    stop = e * inv_k > continuation<Real, TWO>(p, cn, s * inv_k, TWO ? v * p.y_scale : Real(0));
+                }
+                if (stop) {
+                    value = e * df;
+                    break;
+                }
+            }
+        }
+        s0 += double(value);
+        s1 += double(value) * double(value);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, off);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, off);
+    }
+    __shared__ double w0[kLsmcThreads / 32], w1[kLsmcThreads / 32];
+    if ((threadIdx.x & 31) == 0) {
+        w0[threadIdx.x >> 5] = s0;
+        w1[threadIdx.x >> 5] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w = 0; w < kLsmcThreads / 32; ++w) {
+            t0 += w0[w];
+            t1 += w1[w];
+        }
+        partials[2 * blockIdx.x] = t0;
+        partials[2 * blockIdx.x + 1] = t1;
+    }
+}
+
+}  // namespace
+
+// Runs one LSMC pricing in precision Real; all device buffers come from the context.
+template <class Real>
+static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double strike, double sign,
+                            double expiry, const kgpu_lsmc_settings* s, uint64_t fresh_seed, kgpu_lsmc_result* out) {
+    const bool two = model->kind == KGPU_MODEL_HESTON;
+    LsmcParams<Real> p{};
+    const double dt = expiry / s->exercise_dates;
+    p.spot = Real(model->spot);
+    p.strike = Real(strike);
+    p.sign = Real(sign);
+    p.drift = Real((model->rate - model->dividend - 0.5 * model->volatility * model->volatility) * dt);
+    p.diffusion = Real(model->volatility * std::sqrt(dt));
+    p.discount = Real(std::exp(-model->rate * dt));
+    p.rate = Real(model->rate);
+    p.dividend = Real(model->dividend);
+    p.kappa = Real(model->kappa);
+    p.theta = Real(model->theta);
+    p.xi = Real(model->xi);
+    p.rho = Real(model->rho);
+    p.rho_bar = Real(std::sqrt(1.0 - model->rho * model->rho));
+    p.v0 = Real(model->v0);
+    p.substeps = two ? std::max(1, s->substeps) : 1;
+    p.h = Real(dt / p.substeps);
+    p.sqrt_h = Real(std::sqrt(dt / p.substeps));
+    p.y_scale = Real(two && model->theta > 0.0 ? 1.0 / model->theta : 1.0);
+    p.dates = s->exercise_dates;
+    p.paths = s->path_count;
+    p.terms = two ? 10 : 3;
+    p.max_degree = two ? 3 : 2;
+    const int S = sum_count(p.terms);
+    const size_t n = size_t(p.paths), d = size_t(p.dates);
+    const int blocks = std::min<int>(ctx->sm_count * 4, int((n + kLsmcThreads - 1) / kLsmcThreads));
+    if (ctx->lsmc_store.ensure(n * d * sizeof(Real) * (two ? 2 : 1)) || ctx->lsmc_cash.ensure(n * sizeof(Real)) ||
+        ctx->lsmc_sums.ensure(size_t(blocks) * kMaxSums * sizeof(double)) ||
+        ctx->lsmc_coef.ensure(d * kMaxTerms * sizeof(double) + d * sizeof(int) + 16) ||
+        ctx->lsmc_misc.ensure(size_t(blocks) * 2 * sizeof(double) + 16))
+        return KGPU_DEVICE_ERROR;
+    Real* a = static_cast<Real*>(ctx->lsmc_store.ptr);
+    Real* b = two ? a + n * d : nullptr;
+    Real* cash = static_cast<Real*>(ctx->lsmc_cash.ptr);
+    double* coefs = static_cast<double*>(ctx->lsmc_coef.ptr);
+    int* have = reinterpret_cast<int*>(coefs + d * kMaxTerms);
+    int* failed = have + d;
+    double* partials = static_cast<double*>(ctx->lsmc_sums.ptr);
+    double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
+    cudaStream_t st = ctx->stream;
+    cudaEvent_t e0, e1, e2, e3;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventCreate(&e2);
+    cudaEventCreate(&e3);
+    cudaMemsetAsync(coefs, 0, d * kMaxTerms * sizeof(double) + d * sizeof(int) + sizeof(int), st);
+    cudaEventRecord(e0, st);
+    int launches = 0;
+    if (two)
+        lsmc_forward<Real, true><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
+    else
+        lsmc_forward<Real, false><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
+    ++launches;
+    cudaEventRecord(e1, st);
+    for (int date = p.dates - 2; date >= 0; --date) {
+        const double* cnext = date + 1 <= p.dates - 2 ? coefs + size_t(date + 1) * kMaxTerms : nullptr;
+        const int* hnext = date + 1 <= p.dates - 2 ? have + date + 1 : nullptr;
+        if (two) {
+            lsmc_backward<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
+            lsmc_solve<true><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                                                have + date, failed);
+        } else {
+            lsmc_backward<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
+            lsmc_solve<false><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                                                 have + date, failed);
+        }
+        launches += 2;
+    }
+    if (two)
+        lsmc_final<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
+    else
+        lsmc_final<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
+    ++launches;
+    cudaEventRecord(e2, st);
+    const bool lower = fresh_seed != s->seed;
+    std::vector<double> lower_partials;
+    if (lower) {
+        if (ctx->mlp_scratch.ensure(size_t(blocks) * 2 * sizeof(double))) return KGPU_DEVICE_ERROR;
+        double* lp = static_cast<double*>(ctx->mlp_scratch.ptr);
+        if (two)
+            lsmc_lower_bound<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+        else
+            lsmc_lower_bound<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+        ++launches;
+        lower_partials.resize(size_t(blocks) * 2);
+        cudaMemcpyAsync(lower_partials.data(), lp, lower_partials.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    }
+    cudaEventRecord(e3, st);
+    std::vector<double> fin(size_t(blocks) * 2);
+    int fail_flag = 0;
+    cudaMemcpyAsync(fin.data(), finals, fin.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&fail_flag, failed, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t err = cudaStreamSynchronize(st);
+    float ms_total = 0, ms_store = 0, ms_regress = 0;
+    cudaEventElapsedTime(&ms_total, e0, e3);
+    cudaEventElapsedTime(&ms_store, e0, e1);
+    cudaEventElapsedTime(&ms_regress, e1, e2);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    cudaEventDestroy(e3);
+    if (err != cudaSuccess) {
+        ctx->error = cudaGetErrorString(err);
+        return KGPU_DEVICE_ERROR;
+    }
+    if (fail_flag) {
+        ctx->error = "Monte Carlo produced a non-finite parameter, path or result";
+        return KGPU_COMPUTATION_FAILURE;
+    }
+    ctx->last_launches = launches;
+    ctx->last_kernel_ms = ms_total;
+    double s0 = 0.0, s1 = 0.0;
+    for (int blk = 0; blk < blocks; ++blk) {
+        s0 += fin[2 * blk];
+        s1 += fin[2 * blk + 1];
+    }
+    const double disc0 = std::exp(-model->rate * dt);
+    const double mean = s0 / double(n);
+    const double var = n > 1 ? std::max(0.0, (s1 - s0 * mean) / double(n - 1)) : 0.0;
+    const double immediate = std::max(0.0, sign * (model->spot - strike));
+    out->price = std::max(immediate, mean * disc0);
+    out->standard_error = std::sqrt(var / double(n)) * disc0;
+    out->out_of_sample = std::nan("");
+    out->out_of_sample_error = std::nan("");
+    if (lower) {
+        double l0 = 0.0, l1 = 0.0;
+        for (int blk = 0; blk < blocks; ++blk) {
+            l0 += lower_partials[2 * blk];
+            l1 += lower_partials[2 * blk + 1];
+        }
+        const double lm = l0 / double(n);
+        const double lv = n > 1 ? std::max(0.0, (l1 - l0 * lm) / double(n - 1)) : 0.0;
+        out->out_of_sample = std::max(immediate, lm);
+        out->out_of_sample_error = std::sqrt(lv / double(n));
+    }
+    out->wall_ms = ms_total;
+    out->path_store_ms = ms_store;
+    out->regression_ms = ms_regress;
+    if (!std::isfinite(out->price)) {
+        ctx->error = "Monte Carlo produced a non-finite parameter, path or result";
+        return KGPU_COMPUTATION_FAILURE;
+    }
+    return KGPU_OK;
+}
+
+}  // namespace kgpu
+
+kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
+                          const kgpu_lsmc_settings* settings, uint64_t fresh_seed, kgpu_lsmc_result* out);
+
+extern "C" kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double strike, double sign,
+                                       double expiry, const kgpu_lsmc_settings* settings, uint64_t fresh_seed,
+                                       kgpu_lsmc_result* out) {
+    if (!ctx || !model || !settings || !out) return KGPU_INVALID_INPUT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->error.clear();
+    auto bad = [&](const char* msg) {
+        ctx->error = msg;
+        return KGPU_INVALID_INPUT;
+    };
+    if (settings->exercise_dates < 2) return bad("American Monte Carlo requires at least two exercise intervals");
+    if (settings->path_count < 1) return bad("path_count must be positive");
+    if (!(strike > 0.0) || !(expiry > 0.0) || (sign != 1.0 && sign != -1.0)) return bad("invalid option terms");
+    if (settings->sampling != KGPU_SAMPLING_PSEUDO_RANDOM) {
+        ctx->error = "GPU LSMC samples pseudo-random paths";
+        return KGPU_UNSUPPORTED_OPERATION;
+    }
+    if (model->kind == KGPU_MODEL_LOCAL_VOL) {
+        ctx->error = "GPU LSMC supports BSM and Heston";
+        return KGPU_UNSUPPORTED_OPERATION;
+    }
+    const bool heston = model->kind == KGPU_MODEL_HESTON;
+    if (settings->basis == KGPU_BASIS_MLP) {
+        return kgpu_lsmc_mlp(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
+    }
+    if ((settings->basis == KGPU_BASIS_QUADRATIC) == heston)
+        return bad("the quadratic basis prices BSM, the cubic (S/K, v) basis Heston");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
+    return settings->precision == KGPU_PRECISION_FP64
+               ? kgpu::lsmc_run<double>(ctx, model, strike, sign, expiry, settings, fresh_seed, out)
+               : kgpu::lsmc_run<float>(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
 }

@@ -166,15 +166,32 @@ class MonteCarloVanillaEngine(_MonteCarloEngine):
     """European (exact terminal sampling) and American (LSMC) vanilla options.
 
     `terminal_sampling=False` steps `step_count` uniform log-Euler steps instead of the
-    exact terminal draw (the reference's generic D-dimensional sampler)."""
-    _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + ("step_count", "terminal_sampling")
+    exact terminal draw (the reference's generic D-dimensional sampler).  American
+    options use `step_count` exercise intervals; under Heston `substeps` Euler steps per
+    interval and `basis` 'poly3' (default) or 'mlp'."""
+    _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + (
+        "step_count", "terminal_sampling", "basis", "substeps", "mlp_epochs", "mlp_batch",
+        "mlp_learning_rate", "mlp_seed")
 
-    def __init__(self, *, step_count: int = 50, terminal_sampling: bool = True, **kw):
+    def __init__(self, *, step_count: int = 50, terminal_sampling: bool = True,
+                 basis: Optional[str] = None, substeps: int = 5, mlp_epochs: int = 5,
+                 mlp_batch: int = 8192, mlp_learning_rate: float = 1e-3, mlp_seed: int = 0,
+                 **kw):
         if not (1 <= int(step_count) <= 10_000):
             raise InvalidInputError("step_count is outside the supported Monte Carlo range")
         super().__init__(**kw)
         self.step_count = int(step_count)
         self.terminal_sampling = bool(terminal_sampling)
+        self.basis = basis
+        self.substeps = int(substeps)
+        self.mlp_epochs = int(mlp_epochs)
+        self.mlp_batch = int(mlp_batch)
+        self.mlp_learning_rate = float(mlp_learning_rate)
+        self.mlp_seed = int(mlp_seed)
+
+    def price_american_out_of_sample(self, option, ctx: PricingContext, fresh_seed: int):
+        from .lsmc import price_american_out_of_sample
+        return price_american_out_of_sample(self, option, ctx, fresh_seed)
 
     def _plan(self, option, ctx):
         if self.terminal_sampling:

@@ -111,3 +111,32 @@ def lv_book(count, seed=7, min_log2=14, max_log2=18, months_range=(3, 36)):
 def heston_asian_c3(steps=252):
     times = [(i + 1) / steps for i in range(steps)]
     return AsianOption("call", 100.0, 1.0, times)
+
+
+def lsmc_settings(paths, dates, seed, basis, precision="fp64", substeps=1):
+    return abi.LsmcSettings(path_count=paths, exercise_dates=dates, substeps=substeps,
+                            basis=basis, sampling=0, precision=PRECISION[precision],
+                            mlp_epochs=5, mlp_batch=8192, mlp_hidden=64, mlp_learning_rate=1e-3,
+                            seed=seed, mlp_seed=1)
+
+
+def oracle_lsmc(ctx, strike, sign, expiry, s, fresh_seed=None, threads=0):
+    import ctypes as C
+    from oracle import loader
+    lib = loader.load()
+    out = abi.LsmcResult()
+    model = ctx.kgpu_model()
+    st = lib.kor_lsmc_price(C.byref(model), strike, sign, expiry, C.byref(s),
+                            s.seed if fresh_seed is None else fresh_seed, C.byref(out), threads)
+    assert st == 0, st
+    return out
+
+
+def gpu_lsmc(native, ctx, strike, sign, expiry, s, fresh_seed=None):
+    import ctypes as C
+    out = abi.LsmcResult()
+    model = ctx.kgpu_model()
+    native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), strike, sign, expiry,
+                                            C.byref(s), s.seed if fresh_seed is None else fresh_seed,
+                                            C.byref(out)))
+    return out
