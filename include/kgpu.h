@@ -320,6 +320,27 @@ kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double s
                             double sign, double expiry, const kgpu_lsmc_settings* settings,
                             uint64_t fresh_seed, kgpu_lsmc_result* out);
 
+/* Prices contract `contract` of `device_book` without allocating device memory, for
+ * callers that cannot call cudaMalloc (a host that reserves its device-memory budget up
+ * front and hands out slices itself, a plugin inside such a host, or a latency-critical
+ * loop that must never allocate).  It has no counterpart in the reference: kiyosi's CPU
+ * engines own their buffers per call.
+ *
+ * All pointers of `device_book`, including `contracts`, are device pointers; `model`,
+ * `settings` and `out` are host memory.  The call runs the FP64 plain schedule
+ * (results equal kgpu_price_book's for the same plan and settings) on `stream` (a
+ * cudaStream_t; NULL for the default stream) and returns when the estimate is in `out`.
+ * Limits: BSM or Heston models, pseudo-random sampling, at most 4,194,304 samples per
+ * call.  Its scratch is one fixed 1.7 MB array in device memory that every GPU loading
+ * this library holds until process exit; the first call on a device looks up the
+ * array's device address (make that first call before any stream capture).  Every call
+ * shares the array, so calls that overlap on the GPU -- on different streams or from
+ * different threads -- race; serialise them.  Errors are reported through
+ * kgpu_last_error_message(NULL). */
+kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book* device_book,
+                                        int32_t contract, const kgpu_settings* settings,
+                                        kgpu_estimate* out, void* stream);
+
 /* Instrumentation of the last call on `ctx`: device time from the first to the last
  * kernel of the call (CUDA events on the context's stream) and the number of kernel
  * launches it made. */

@@ -23,6 +23,7 @@ UNITS = {
     "kernels_fp32.cu": [],
     "lsmc.cu": [],
     "mlp.cu": [],
+    "noalloc.cu": [],
 }
 HEADERS = ["device_rng.cuh", "path_engine.cuh", "kernels.cuh", "kernels_impl.cuh", "launch.h",
            "api_internal.h", "joe_kuo_6_21201.inc", "lsmc_kernels.cuh", "mlp.cuh"]

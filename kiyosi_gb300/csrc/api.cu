@@ -66,11 +66,57 @@ void build_sobol(int dims, uint64_t seed, std::vector<uint64_t>& directions,
     }
 }
 
+// MonteCarloEstimate::from_sampling and sampling_standard_error (monte_carlo.rs:939-963,
+// 1435-1452), from merged scaled moments.
+void estimate_from_moments(const kgpu_contract& c, const kgpu_settings& s, int64_t paths,
+                           const BlockPartial& p, kgpu_estimate* out) {
+    const bool sobol = s.sampling == KGPU_SAMPLING_SOBOL;
+    const bool antithetic = s.antithetic != 0;
+    const bool statistics = !sobol && (!antithetic || paths % 2 == 0);
+    const double log_discount = c.payoff == KGPU_PAYOFF_EUROPEAN ? c.log_scale : 0.0;
+    auto scaled = [](double scale, double weight, double log_d) {
+        double value = scale * weight;
+        double discount = std::exp(log_d);
+        if (scale == 0.0 || weight == 0.0) return 0.0;
+        if (std::isnormal(discount) && std::isnormal(value)) return value * discount;
+        return std::copysign(std::exp(std::log(scale) + std::log(std::fabs(weight)) + log_d), weight);
+    };
+    out->price = scaled(p.moments.scale, p.moments.mean, log_discount);
+    const Moments& u = antithetic ? p.pairs : p.moments;
+    out->standard_error = 0.0;
+    if (statistics && u.count >= 2.0) {
+        double deviation = std::sqrt(std::max(u.m2, 0.0) / (u.count - 1.0) / u.count);
+        double se = scaled(u.scale, deviation, log_discount);
+        if (se == 0.0) {
+            out->uncertainty_status = KGPU_UNCERTAINTY_ZERO_OBSERVED_VARIANCE;
+        } else {
+            out->standard_error = se;
+            out->uncertainty_status = KGPU_UNCERTAINTY_AVAILABLE;
+        }
+    } else if (sobol) {
+        out->uncertainty_status = KGPU_UNCERTAINTY_UNSUPPORTED_SAMPLING;
+    } else if (antithetic && paths % 2 != 0) {
+        out->uncertainty_status = KGPU_UNCERTAINTY_INCOMPLETE_ANTITHETIC_PAIR;
+    } else {
+        out->uncertainty_status = KGPU_UNCERTAINTY_INSUFFICIENT_OBSERVATIONS;
+    }
+    const Moments& v = p.sample;
+    out->sample_error = v.count >= 2.0
+                            ? scaled(v.scale, std::sqrt(std::max(v.m2, 0.0) / (v.count - 1.0) / v.count),
+                                     log_discount)
+                            : 0.0;
+    out->seed = s.seed;
+}
+
 }  // namespace kgpu
 
 using namespace kgpu;
 
 static thread_local std::string g_thread_error;
+
+namespace kgpu {
+void set_thread_error(const char* message) { g_thread_error = message; }
+}  // namespace kgpu
 
 static kgpu_status fail(kgpu_context* ctx, kgpu_status status, const char* fmt, ...) {
     char buf[512];
@@ -199,48 +245,6 @@ int model_normals_per_step(const kgpu_model* m) { return m->kind == KGPU_MODEL_H
 int dims_of(const kgpu_contract& c, const kgpu_model* m) {
     if (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) return 1;
     return c.step_count * model_normals_per_step(m);
-}
-
-// MonteCarloEstimate::from_sampling and sampling_standard_error (monte_carlo.rs:939-963,
-// 1435-1452), from merged scaled moments.
-void estimate_from_moments(const kgpu_contract& c, const kgpu_settings& s, int64_t paths,
-                           const BlockPartial& p, kgpu_estimate* out) {
-    const bool sobol = s.sampling == KGPU_SAMPLING_SOBOL;
-    const bool antithetic = s.antithetic != 0;
-    const bool statistics = !sobol && (!antithetic || paths % 2 == 0);
-    const double log_discount = c.payoff == KGPU_PAYOFF_EUROPEAN ? c.log_scale : 0.0;
-    auto scaled = [](double scale, double weight, double log_d) {
-        double value = scale * weight;
-        double discount = std::exp(log_d);
-        if (scale == 0.0 || weight == 0.0) return 0.0;
-        if (std::isnormal(discount) && std::isnormal(value)) return value * discount;
-        return std::copysign(std::exp(std::log(scale) + std::log(std::fabs(weight)) + log_d), weight);
-    };
-    out->price = scaled(p.moments.scale, p.moments.mean, log_discount);
-    const Moments& u = antithetic ? p.pairs : p.moments;
-    out->standard_error = 0.0;
-    if (statistics && u.count >= 2.0) {
-        double deviation = std::sqrt(std::max(u.m2, 0.0) / (u.count - 1.0) / u.count);
-        double se = scaled(u.scale, deviation, log_discount);
-        if (se == 0.0) {
-            out->uncertainty_status = KGPU_UNCERTAINTY_ZERO_OBSERVED_VARIANCE;
-        } else {
-            out->standard_error = se;
-            out->uncertainty_status = KGPU_UNCERTAINTY_AVAILABLE;
-        }
-    } else if (sobol) {
-        out->uncertainty_status = KGPU_UNCERTAINTY_UNSUPPORTED_SAMPLING;
-    } else if (antithetic && paths % 2 != 0) {
-        out->uncertainty_status = KGPU_UNCERTAINTY_INCOMPLETE_ANTITHETIC_PAIR;
-    } else {
-        out->uncertainty_status = KGPU_UNCERTAINTY_INSUFFICIENT_OBSERVATIONS;
-    }
-    const Moments& v = p.sample;
-    out->sample_error = v.count >= 2.0
-                            ? scaled(v.scale, std::sqrt(std::max(v.m2, 0.0) / (v.count - 1.0) / v.count),
-                                     log_discount)
-                            : 0.0;
-    out->seed = s.seed;
 }
 
 void estimate_from_sums(const kgpu_contract& c, const kgpu_settings& s, int64_t paths,

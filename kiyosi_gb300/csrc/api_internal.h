@@ -22,6 +22,14 @@ struct DeviceBuffer {
 void build_sobol(int dims, uint64_t seed, std::vector<uint64_t>& directions,
                  std::vector<uint64_t>& shifts);
 
+// Records the calling thread's last error message (kgpu_last_error_message(NULL)).
+void set_thread_error(const char* message);
+
+struct BlockPartial;
+// MonteCarloEstimate of one contract from its block-merged scaled moments.
+void estimate_from_moments(const kgpu_contract& c, const kgpu_settings& s, int64_t paths,
+                           const BlockPartial& p, kgpu_estimate* out);
+
 }  // namespace kgpu
 
 struct kgpu_context {

@@ -1,0 +1,147 @@
+// Pricing one contract without allocating device memory.
+//
+// Some callers cannot call cudaMalloc: a host application that reserves its whole
+// device-memory budget up front and hands out slices itself, a plugin running inside
+// such a host, or a latency-critical pricing loop that must never pay an allocation or
+// risk an out-of-memory failure mid-session.  kgpu_price_contract_noalloc serves them:
+// it runs the FP64 plain schedule (one thread per sample, reference blocks as CUDA
+// blocks, block-ordered Welford merge) with all of its scratch -- the per-block moments,
+// the merged moments and the compiled contract record -- in one file-scope device array
+// of fixed size, which every GPU that loads this library holds until process exit.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/kgpu.h"
+#include "api_internal.h"
+#include "launch.h"
+
+namespace {
+
+using kgpu::BlockPartial;
+using kgpu::ContractT;
+
+// At most this many reference blocks of 256 samples per call (4,194,304 samples).
+constexpr int kNoAllocMaxBlocks = 16384;
+
+struct NoAllocScratch {
+    BlockPartial partials[kNoAllocMaxBlocks];
+    BlockPartial merged;
+    ContractT<double> contract;
+};
+
+// The scratch.  Its host-side name is only a stand-in: device code is handed the
+// address cudaGetSymbolAddress returns for the current device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+NoAllocScratch* g_noalloc_address[kMaxDevices] = {};
+
+// Failures are reported through kgpu_last_error_message(NULL) (thread-local).
+kgpu_status noalloc_fail(kgpu_status status, const char* message) {
+    kgpu::set_thread_error(message);
+    return status;
+}
+
+// Device address of the scratch on the current device, looked up once per device.
+kgpu_status scratch_address(NoAllocScratch** out) {
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices)
+        return noalloc_fail(KGPU_DEVICE_ERROR, "no usable current CUDA device");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[device]) {
+        void* ptr = nullptr;
+        const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (rc != cudaSuccess || !ptr) return noalloc_fail(KGPU_DEVICE_ERROR, cudaGetErrorString(rc));
+        g_noalloc_address[device] = static_cast<NoAllocScratch*>(ptr);
+    }
+    *out = g_noalloc_address[device];
+    return KGPU_OK;
+}
+
+}  // namespace
+
+extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book* device_book,
+                                                   int32_t contract, const kgpu_settings* settings,
+                                                   kgpu_estimate* out, void* stream) {
+    kgpu::set_thread_error("");
+    if (!model || !device_book || !settings || !out)
+        return noalloc_fail(KGPU_INVALID_INPUT, "null argument");
+    if (model->kind != KGPU_MODEL_BSM && model->kind != KGPU_MODEL_HESTON)
+        return noalloc_fail(KGPU_UNSUPPORTED_OPERATION, "the no-allocation entry point prices BSM and Heston");
+    if (settings->sampling != KGPU_SAMPLING_PSEUDO_RANDOM)
+        return noalloc_fail(KGPU_UNSUPPORTED_OPERATION, "the no-allocation entry point samples pseudo-random paths");
+    if (contract < 0 || contract >= device_book->contract_count)
+        return noalloc_fail(KGPU_INVALID_INPUT, "contract index out of range");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The contract record, read from device memory into this stack frame.
+    kgpu_contract c;
+    if (cudaMemcpyAsync(&c, device_book->contracts + contract, sizeof c, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return noalloc_fail(KGPU_DEVICE_ERROR, "cannot read the contract record");
+    const int64_t paths = c.path_count > 0 ? c.path_count : settings->path_count;
+    if (paths < 1 || paths > 2147483647LL) return noalloc_fail(KGPU_INVALID_INPUT, "path_count must be positive");
+    if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_DIGITAL)
+        return noalloc_fail(KGPU_INVALID_INPUT, "unknown payoff");
+    if ((c.flags & KGPU_C_BRIDGE) && model->kind != KGPU_MODEL_BSM)
+        return noalloc_fail(KGPU_INVALID_INPUT, "a bridge plan needs BSM");
+    if (c.step_count < 1 || c.step_offset < 0 || c.step_offset + c.step_count > device_book->step_total)
+        return noalloc_fail(KGPU_INVALID_INPUT, "steps out of range");
+    const int64_t samples = settings->antithetic ? (paths + 1) / 2 : paths;
+    const int64_t blocks = (samples + 255) / 256;
+    if (blocks > kNoAllocMaxBlocks)
+        return noalloc_fail(KGPU_INVALID_INPUT,
+                            "path count exceeds the no-allocation scratch limit of 4,194,304 samples");
+    NoAllocScratch* scratch = nullptr;
+    kgpu_status status = scratch_address(&scratch);
+    if (status != KGPU_OK) return status;
+    // Every field of the scratch is written before it is read (the compiled contract,
+    // one partial per block, the merged moments), so nothing needs clearing.
+    if (kgpu::launch_compile_contracts_fp64(device_book->contracts + contract, 1, &scratch->contract, st) !=
+        cudaSuccess)
+        return noalloc_fail(KGPU_DEVICE_ERROR, "contract compile launch failed");
+    kgpu::PlainArgs<double> a;
+    a.book.contracts = &scratch->contract;
+    a.book.steps = reinterpret_cast<const kgpu::StepT<double>*>(device_book->steps);
+    a.book.flags = device_book->step_flags;
+    a.book.events = device_book->event_total ? reinterpret_cast<const kgpu::EventT<double>*>(device_book->events) : nullptr;
+    a.book.intervals =
+        device_book->interval_total ? reinterpret_cast<const kgpu::IntervalT<double>*>(device_book->intervals) : nullptr;
+    a.book.daily = reinterpret_cast<const kgpu::DailyT<double>*>(device_book->bridge_daily);
+    a.book.units = nullptr;
+    a.book.ends = nullptr;
+    a.contract = 0;
+    a.dims = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL)
+                 ? 1
+                 : c.step_count * (model->kind == KGPU_MODEL_HESTON ? 2 : 1);
+    a.paths = paths;
+    a.samples = samples;
+    a.seed = settings->seed;
+    a.antithetic = settings->antithetic;
+    a.statistics = !settings->antithetic || paths % 2 == 0;
+    a.variance = a.statistics && !settings->antithetic;
+    a.sobol = kgpu::SobolTables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    a.partials = scratch->partials;
+    const size_t smem = kgpu::plain_smem_bytes(KGPU_PRECISION_FP64, false, a.dims, 0);
+    if (kgpu::launch_plain_fp64(model->kind, false, int(blocks), smem, st, a, *model, nullptr) != cudaSuccess)
+        return noalloc_fail(KGPU_DEVICE_ERROR, "pricing kernel launch failed");
+    kgpu::merge_blocks_kernel<<<1, 32, 0, st>>>(scratch->partials, int(blocks), a.variance, a.statistics,
+                                                 settings->antithetic, &scratch->merged);
+    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(KGPU_DEVICE_ERROR, "merge kernel launch failed");
+    BlockPartial merged;
+    if (cudaMemcpyAsync(&merged, &scratch->merged, sizeof merged, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return noalloc_fail(KGPU_DEVICE_ERROR, "cannot read the merged moments");
+    const cudaError_t rc = cudaStreamSynchronize(st);
+    if (rc != cudaSuccess) return noalloc_fail(KGPU_DEVICE_ERROR, cudaGetErrorString(rc));
+    kgpu_settings s = *settings;
+    s.sampling = KGPU_SAMPLING_PSEUDO_RANDOM;
+    kgpu::estimate_from_moments(c, s, paths, merged, out);
+    const int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
+    out->path_steps = double(paths) * grid;
+    out->executed_steps = merged.executed;
+    if (!(out->price == out->price) || out->price - out->price != 0.0)
+        return noalloc_fail(KGPU_COMPUTATION_FAILURE, "Monte Carlo produced a non-finite parameter, path or result");
+    return KGPU_OK;
+}
