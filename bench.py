@@ -35,11 +35,14 @@ sys.path.insert(0, ROOT)
 PATHS = 1 << 20
 STEPS = 504
 SEED = 42
-# Warp instructions issued per executed path-step by the FP32 persistent kernel on
-# this workload, measured with ncu (smsp__inst_executed.sum / executed path-steps,
-# profiles/persistent_kernel_snowball.txt).  Used to express the kernel's rate as a
-# fraction of the SM issue peak (4 warp-instructions per cycle per SM).
-WARP_INST_PER_EXECUTED_STEP = None
+# Warp instructions the FP32 persistent kernel issues per executed path position on
+# this workload, from one ncu capture (smsp__inst_executed.sum 354,077,385 over the
+# 41.7 M positions of a 2^19-path pricing; profiles/persistent_kernel_snowball.md).
+# The kernel is neither HBM- nor tensor-bound, so its roofline is the SM issue rate
+# (4 warp-instructions per cycle per SM).
+WARP_INST_PER_EXECUTED_STEP = 8.49
+# DRAM bytes per path of the same capture (4.44 MB read, 0 written, at 2^19 paths).
+DRAM_BYTES_PER_PATH = 4.4357e6 / (1 << 19)
 
 
 def snowball():
@@ -114,11 +117,15 @@ class Clocks:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    def __init__(self, device=0):
+        self.device = device
+
     def __enter__(self):
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+        self.path = os.path.join(ROOT, "gpurun_out", f"bench_clocks{self.device}.csv")
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device),
+                                          f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
@@ -150,15 +157,49 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class Ranks:
+    """Replicas under torchrun: one process per GPU, each pricing the full workload on
+    its own device (the pricing shards by reference block, but no cross-GPU merge is
+    built), a host barrier around the timed region and the maximum time over ranks."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.device = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, value):
+        if not self.dist:
+            return value
+        import torch
+        t = torch.tensor([float(value)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
 def run_ours(args):
     from kiyosi_gb300 import _native, abi
     from oracle import loader
-    native = _native.context(0)
+    ranks = Ranks()
+    native = _native.context(ranks.device)
     lib = native.lib
     ctx, packed = packed_plan()
     model = ctx.kgpu_model()
     host_book = packed.struct()
     cuda = Cuda()
+    cuda.rt.cudaSetDevice(ranks.device)
     # Device-resident plan for the kernel-only measurement.
     dev = abi.Book()
     dev.contract_count = 1
@@ -177,7 +218,8 @@ def run_ours(args):
         native.check(lib.kgpu_price_book_device(native.handle, C.byref(model), C.byref(dev),
                                                 C.byref(s), out))
         # Copy: `out` is reused by the next call.
-        return abi.Estimate.from_buffer_copy(out[0]), native.last_kernel_ms, native.last_launches
+        return (abi.Estimate.from_buffer_copy(out[0]), native.last_kernel_ms, native.last_launches,
+                native.last_path_kernel_ms)
 
     def host_call(s):
         native.check(lib.kgpu_price_book(native.handle, C.byref(model), C.byref(host_book),
@@ -188,18 +230,21 @@ def run_ours(args):
     s64 = settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN)
     for _ in range(args.warmup):
         device_call(s32)
-    kernel_ms, launches = [], 0
+    kernel_ms, path_ms, launches = [], [], 0
     est32 = None
-    with Clocks() as clocks:
+    with Clocks(ranks.device) as clocks:
+        ranks.barrier()
         for _ in range(args.steps):
             cuda.flush_l2()
-            est32, ms, nl = device_call(s32)
+            est32, ms, nl, pk = device_call(s32)
             kernel_ms.append(ms)
+            path_ms.append(pk)
             launches += nl
+        ranks.barrier()
     clock = clocks.summary()
-    total_ms = sum(kernel_ms)
+    total_ms = ranks.max(sum(kernel_ms))
     path_steps = est32.path_steps
-    value = path_steps * args.steps / (total_ms / 1e3)
+    value = ranks.world * path_steps * args.steps / (total_ms / 1e3)
     # End to end through the host-buffer C ABI call.
     h2d = (packed.steps.nbytes + packed.flags.nbytes + packed.events.nbytes
            + packed.intervals.nbytes + (packed.daily.nbytes if packed.daily is not None else 0)
@@ -207,37 +252,52 @@ def run_ours(args):
     d2h = C.sizeof(abi.Estimate)
     for _ in range(max(1, args.warmup // 2)):
         host_call(s32)
+    ranks.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         host_call(s32)
-    e2e_s = time.perf_counter() - t0
-    e2e = path_steps * args.steps / e2e_s
+    e2e_s = ranks.max(time.perf_counter() - t0)
+    e2e = ranks.world * path_steps * args.steps / e2e_s
+    if ranks.rank != 0:
+        ranks.close()
+        return
     # FP64 plain one-contract-per-launch path on the same random numbers.
     device_call(s64)
     f64_ms = []
     for _ in range(max(1, min(args.steps, 3))):
         cuda.flush_l2()
-        est64, ms, _ = device_call(s64)
+        est64, ms, _, _ = device_call(s64)
         f64_ms.append(ms)
     fp64_rate = path_steps / (statistics.median(f64_ms) / 1e3)
-    # FP64 CPU oracle at full size (parity) and timed as the CPU baseline.
+    # FP64 CPU oracle at full size (parity) and timed as the CPU baseline, on all host
+    # cores and on one.
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     ref = loader.price_book(ctx, packed, s64, threads=threads)[0]
     cpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loader.price_book(ctx, packed, settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN, 1 << 18),
+                      threads=1)
+    cpu1_rate = (1 << 18) * STEPS / (time.perf_counter() - t0)
     se = ref.sample_error
     executed = est32.executed_steps
     issue = None
-    if WARP_INST_PER_EXECUTED_STEP and clock["sm_mhz"]:
-        achieved = WARP_INST_PER_EXECUTED_STEP * executed / (total_ms / args.steps / 1e3)
+    kernel_s = sum(path_ms) / len(path_ms) / 1e3
+    if WARP_INST_PER_EXECUTED_STEP and clock["sm_mhz"] and kernel_s > 0:
+        achieved = WARP_INST_PER_EXECUTED_STEP * executed / kernel_s
         peak = 4.0 * native_sm_count(native) * clock["sm_mhz"] * 1e6
         issue = {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9,
-                 "unit": "Gwarp-inst/s", "frac": achieved / peak, "traffic": None}
+                 "unit": "Gwarp-inst/s", "frac": achieved / peak,
+                 "traffic": DRAM_BYTES_PER_PATH * PATHS,
+                 "kernel": "persistent_kernel<float, BSM, Sobol>",
+                 "kernel_ms": kernel_s * 1e3,
+                 "note": "peak = 4 warp-instructions/cycle x SMs x median SM clock sampled "
+                         "during the timed region; traffic = DRAM bytes per launch (ncu)"}
     line = {
         "metric": "path-steps/s (FP32 batched vs FP64 plain) at <=0.5 SE",
         "value": value,
         "unit": "path-steps/s",
-        "n_gpus": 1,
+        "n_gpus": ranks.world,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps,
@@ -266,9 +326,14 @@ def run_ours(args):
         "fp64_executed_steps_per_path": est64.executed_steps / PATHS,
         "cpu_baseline": {"value": path_steps / cpu_s, "unit": "path-steps/s", "cores": threads,
                          "kind": "port", "sample": "full workload (2^20 paths x 504 steps), "
-                                                   "one pricing, FP64 oracle"},
+                                                   "one pricing, FP64 oracle",
+                         "single_core_value": cpu1_rate,
+                         "single_core_sample": "2^18 paths x 504 steps, one thread"},
     }
+    if ranks.world > 1:
+        line["config"]["parallelism"] = f"replicas x{ranks.world} (one full pricing per GPU)"
     print(json.dumps(line))
+    ranks.close()
 
 
 def native_sm_count(native):
@@ -294,7 +359,8 @@ def run_kernel_only(args):
         native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book),
                                                 C.byref(s), out, None))
     print(json.dumps({"arm": args.kernel_only, "paths": args.paths, "price": out[0].price,
-                      "kernel_ms": native.last_kernel_ms}))
+                      "executed_steps": out[0].executed_steps, "kernel_ms": native.last_kernel_ms,
+                      "path_kernel_ms": native.last_path_kernel_ms}))
 
 
 def run_reference(args):
@@ -356,8 +422,6 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
-        return
-    if int(os.environ.get("RANK", "0")) != 0:
         return
     run_ours(args)
 

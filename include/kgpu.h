@@ -346,6 +346,9 @@ kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book
  * launches it made. */
 double kgpu_context_last_kernel_ms(const kgpu_context* ctx);
 int32_t kgpu_context_last_launches(const kgpu_context* ctx);
+/* Device time of the last pricing call's path kernels alone (the plain or persistent
+ * kernel launches, without plan compilation and reductions), summed over launches. */
+double kgpu_context_last_path_kernel_ms(const kgpu_context* ctx);
 
 /* Library identification. */
 int32_t kgpu_abi_version(void);

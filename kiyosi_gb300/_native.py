@@ -52,6 +52,10 @@ class Context:
         return self.lib.kgpu_context_last_kernel_ms(self.handle)
 
     @property
+    def last_path_kernel_ms(self) -> float:
+        return self.lib.kgpu_context_last_path_kernel_ms(self.handle)
+
+    @property
     def last_launches(self) -> int:
         return self.lib.kgpu_context_last_launches(self.handle)
 

@@ -150,6 +150,7 @@ EXPORTED_SYMBOLS = (
     "kgpu_context_create", "kgpu_context_destroy", "kgpu_last_error_message",
     "kgpu_price_book", "kgpu_price_book_device", "kgpu_pcg_normals", "kgpu_pcg_words",
     "kgpu_sobol_points", "kgpu_lsmc_price", "kgpu_context_last_kernel_ms",
+    "kgpu_context_last_path_kernel_ms",
     "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count",
     "kgpu_price_contract_noalloc",
 )
@@ -183,6 +184,8 @@ def declare(lib):
     lib.kgpu_lsmc_price.restype = _I
     lib.kgpu_context_last_kernel_ms.argtypes = [V]
     lib.kgpu_context_last_kernel_ms.restype = C.c_double
+    lib.kgpu_context_last_path_kernel_ms.argtypes = [V]
+    lib.kgpu_context_last_path_kernel_ms.restype = C.c_double
     lib.kgpu_context_last_launches.argtypes = [V]
     lib.kgpu_context_last_launches.restype = _I
     lib.kgpu_price_contract_noalloc.argtypes = [_P(Model), _P(Book), _I, _P(Settings),

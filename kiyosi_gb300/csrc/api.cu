@@ -216,6 +216,10 @@ void kgpu_context_destroy(kgpu_context* ctx) {
     if (ctx->cancel_host) cudaFreeHost((void*)ctx->cancel_host);
     cudaEventDestroy(ctx->ev_start);
     cudaEventDestroy(ctx->ev_stop);
+    for (auto& e : ctx->path_events) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -225,6 +229,7 @@ const char* kgpu_last_error_message(const kgpu_context* ctx) {
 }
 
 double kgpu_context_last_kernel_ms(const kgpu_context* ctx) { return ctx ? ctx->last_kernel_ms : 0.0; }
+double kgpu_context_last_path_kernel_ms(const kgpu_context* ctx) { return ctx ? ctx->last_path_kernel_ms : 0.0; }
 int32_t kgpu_context_last_launches(const kgpu_context* ctx) { return ctx ? ctx->last_launches : 0; }
 
 }  // extern "C"
@@ -233,6 +238,36 @@ int32_t kgpu_context_last_launches(const kgpu_context* ctx) { return ctx ? ctx->
 // Pricing
 // ------------------------------------------------------------------------------------
 namespace {
+
+// Records the start of one path-kernel launch; path_kernel_end records its end.
+cudaError_t path_kernel_begin(kgpu_context* ctx) {
+    if (ctx->path_events_used == ctx->path_events.size()) {
+        std::pair<cudaEvent_t, cudaEvent_t> e{nullptr, nullptr};
+        cudaError_t rc = cudaEventCreate(&e.first);
+        if (rc == cudaSuccess) rc = cudaEventCreate(&e.second);
+        if (rc != cudaSuccess) {
+            if (e.first) cudaEventDestroy(e.first);
+            return rc;
+        }
+        ctx->path_events.push_back(e);
+    }
+    return cudaEventRecord(ctx->path_events[ctx->path_events_used].first, ctx->stream);
+}
+
+cudaError_t path_kernel_end(kgpu_context* ctx) {
+    return cudaEventRecord(ctx->path_events[ctx->path_events_used++].second, ctx->stream);
+}
+
+// Sum of the recorded path-kernel times; call after the stream has been synchronised.
+double path_kernel_ms(kgpu_context* ctx) {
+    double total = 0.0;
+    for (size_t i = 0; i < ctx->path_events_used; ++i) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ctx->path_events[i].first, ctx->path_events[i].second) == cudaSuccess)
+            total += ms;
+    }
+    return total;
+}
 
 struct ContractInfo {
     int dims;
@@ -494,9 +529,11 @@ kgpu_status run_plain(Call& k, const DevBook<Real>& db, int& launches) {
         size_t smem = plain_smem_bytes(PrecisionOps<Real>::precision, k.sobol, ci.dims, k.lv_values);
         if (smem > 227 * 1024)
             return fail(ctx, KGPU_INVALID_INPUT, "dimension %d exceeds the plain kernel's shared memory", ci.dims);
+        CUDA_TRY(ctx, path_kernel_begin(ctx));
         CUDA_TRY(ctx, PrecisionOps<Real>::plain(k.model->kind, k.sobol, blocks, smem, ctx->stream, a, *k.model,
                                                 k.lv_dev));
-        merge_blocks_kernel<<<1, 32, 0, ctx->stream>>>(a.partials, blocks, a.variance, a.statistics, s.antithetic,
+        CUDA_TRY(ctx, path_kernel_end(ctx));
+        merge_blocks_kernel<<<1, kMergeThreads, 0, ctx->stream>>>(a.partials, blocks, a.variance, a.statistics, s.antithetic,
                                                         static_cast<BlockPartial*>(ctx->merged.ptr) + i);
         CUDA_TRY(ctx, cudaGetLastError());
         launches += 2;
@@ -654,8 +691,10 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
         if (s.ctas_per_sm > 0) per_sm = std::min(per_sm, s.ctas_per_sm);
         const int blocks = std::max(1, std::min(ctx->sm_count * per_sm, (a.item_count + kWarps - 1) / kWarps));
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->queue.ptr, 0, sizeof(int), ctx->stream));
+        CUDA_TRY(ctx, path_kernel_begin(ctx));
         CUDA_TRY(ctx, PrecisionOps<Real>::persistent(k.model->kind, k.sobol, blocks, smem, ctx->stream, a, *k.model,
                                                      k.lv_dev));
+        CUDA_TRY(ctx, path_kernel_end(ctx));
         launches += 1;
         // `order` is reused by the next group: wait for this launch's upload to be consumed.
         if (group_dims.size() > 1) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -699,6 +738,8 @@ template <class Real>
 kgpu_status run_book(Call& k) {
     kgpu_context* ctx = k.ctx;
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    ctx->path_events_used = 0;
+    ctx->last_path_kernel_ms = 0.0;
     DevBook<Real> db;
     kgpu_status st = compile_book<Real>(k, &db);
     if (st) return st;
@@ -707,6 +748,7 @@ kgpu_status run_book(Call& k) {
                                                   : run_plain<Real>(k, db, launches);
     float ms = 0;
     if (cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop) == cudaSuccess) ctx->last_kernel_ms = ms;
+    if (st == KGPU_OK) ctx->last_path_kernel_ms = path_kernel_ms(ctx);
     ctx->last_launches = launches;
     return st;
 }

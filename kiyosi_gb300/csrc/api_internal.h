@@ -61,7 +61,11 @@ struct kgpu_context {
     int* cancel_dev = nullptr;
     // instrumentation of the last call
     double last_kernel_ms = 0.0;
+    double last_path_kernel_ms = 0.0;  // the path kernels alone (plain or persistent)
     int last_launches = 0;
+    // Event pairs around each path-kernel launch of a call, grown on demand.
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> path_events;
+    size_t path_events_used = 0;
     size_t h2d_bytes = 0;
 
     std::vector<kgpu::DeviceBuffer*> buffers() {

@@ -414,21 +414,114 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs<Real> a, kgpu
 }
 
 // Merges the block partials of one contract in block order (monte_carlo.rs:1800-1809).
-static __global__ void merge_blocks_kernel(const BlockPartial* partials, int blocks, int variance,
-                                           int statistics, int antithetic, BlockPartial* out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    BlockPartial r;
-    r.moments = Moments{0, 0, 0, 0};
-    r.pairs = Moments{0, 0, 0, 0};
-    r.sample = Moments{0, 0, 0, 0};
-    r.executed = 0.0;
-    for (int b = 0; b < blocks; ++b) {
-        moments_merge(r.moments, partials[b].moments, variance);
-        moments_merge(r.sample, partials[b].sample, true);
-        if (statistics && antithetic) moments_merge(r.pairs, partials[b].pairs, true);
-        r.executed += partials[b].executed;
+// The merge is a dependent chain, but its divisions depend only on prefix sums of the
+// block counts and prefix maxima of the block scales, both exact in any order.  The
+// CTA's threads compute a chunk's weights in parallel; then one thread per chain (the
+// price moments, the i.i.d. sample moments, the antithetic pair moments) walks the
+// chunk with them.  Every operation is the sequential merge's, rounded separately
+// (__dmul_rn and friends, never contracted), so the result is bit-identical to it.
+constexpr int kMergeThreads = 256;
+
+struct MergeStep {
+    double left, right, w, u, mean, m2;  // left < 0 marks "copy the block" (empty state)
+};
+
+__device__ __forceinline__ const Moments& merge_chain(const BlockPartial& p, int c) {
+    return c == 0 ? p.moments : (c == 1 ? p.sample : p.pairs);
+}
+
+static __global__ void __launch_bounds__(kMergeThreads)
+    merge_blocks_kernel(const BlockPartial* partials, int blocks, int variance, int statistics, int antithetic,
+                        BlockPartial* out) {
+    __shared__ MergeStep steps[3][kMergeThreads];
+    __shared__ double scan_count[kMergeThreads], scan_scale[kMergeThreads];
+    __shared__ double carry_count[3], carry_scale[3], executed_part[kMergeThreads];
+    const int t = threadIdx.x;
+    const int chains = (statistics && antithetic) ? 3 : 2;
+    if (t < 3) {
+        carry_count[t] = 0.0;
+        carry_scale[t] = 0.0;
     }
-    *out = r;
+    double mean = 0.0, m2 = 0.0, executed = 0.0;  // chain state of threads 0..2
+    for (int base = 0; base < blocks; base += kMergeThreads) {
+        const int g = base + t;
+        const int n = min(kMergeThreads, blocks - base);
+        if (g < blocks) executed = __dadd_rn(executed, partials[g].executed);
+        for (int c = 0; c < chains; ++c) {
+            __syncthreads();
+            const Moments b = g < blocks ? merge_chain(partials[g], c) : Moments{0, 0, 0, 0};
+            scan_count[t] = b.count;
+            scan_scale[t] = b.scale;
+            __syncthreads();
+            // Inclusive scans (sum of integer counts, max of scales): exact.
+            for (int d = 1; d < kMergeThreads; d <<= 1) {
+                const double pc = t >= d ? scan_count[t - d] : 0.0;
+                const double ps = t >= d ? scan_scale[t - d] : 0.0;
+                __syncthreads();
+                scan_count[t] = __dadd_rn(scan_count[t], pc);
+                scan_scale[t] = fmax(scan_scale[t], ps);
+                __syncthreads();
+            }
+            if (g < blocks) {
+                const double a_count = __dadd_rn(carry_count[c], t > 0 ? scan_count[t - 1] : 0.0);
+                const double a_scale = fmax(carry_scale[c], t > 0 ? scan_scale[t - 1] : 0.0);
+                MergeStep st;
+                st.mean = b.mean;
+                st.m2 = b.m2;
+                if (a_count == 0.0) {
+                    st.left = -1.0;
+                    st.right = st.w = st.u = 0.0;
+                } else {
+                    const double sc = a_scale > b.scale ? a_scale : b.scale;
+                    st.left = sc == 0.0 ? 0.0 : __ddiv_rn(a_scale, sc);
+                    st.right = sc == 0.0 ? 0.0 : __ddiv_rn(b.scale, sc);
+                    const double total = __dadd_rn(a_count, b.count);
+                    st.w = __ddiv_rn(b.count, total);
+                    st.u = __dmul_rn(a_count, st.w);
+                }
+                steps[c][t] = st;
+            }
+            __syncthreads();
+            if (t == 0) {
+                carry_count[c] = __dadd_rn(carry_count[c], scan_count[n - 1]);
+                carry_scale[c] = fmax(carry_scale[c], scan_scale[n - 1]);
+            }
+        }
+        __syncthreads();
+        if (t < chains) {
+            const bool with_variance = t == 0 ? variance != 0 : true;
+            for (int i = 0; i < n; ++i) {
+                const MergeStep st = steps[t][i];
+                if (st.left < 0.0) {
+                    mean = st.mean;
+                    m2 = st.m2;
+                    continue;
+                }
+                const double ml = __dmul_rn(mean, st.left);
+                const double delta = __dsub_rn(__dmul_rn(st.mean, st.right), ml);
+                mean = __dadd_rn(ml, __dmul_rn(delta, st.w));
+                if (with_variance)
+                    m2 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(m2, st.left), st.left),
+                                             __dmul_rn(__dmul_rn(st.m2, st.right), st.right)),
+                                   __dmul_rn(__dmul_rn(delta, delta), st.u));
+            }
+        }
+    }
+    executed_part[t] = executed;
+    __syncthreads();
+    if (t < 3) {
+        Moments m{0, 0, 0, 0};
+        if (t < chains) m = Moments{carry_count[t], carry_scale[t], mean, m2};
+        if (t == 0) out->moments = m;
+        if (t == 1) out->sample = m;
+        if (t == 2) out->pairs = m;
+    }
+    if (t == 0) {
+        // Integer-valued counts: exact in any summation order.
+        double total = 0.0;
+        for (int i = 0; i < kMergeThreads; ++i) total = __dadd_rn(total, executed_part[i]);
+        out->executed = total;
+    }
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -127,7 +127,7 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
     const size_t smem = kgpu::plain_smem_bytes(KGPU_PRECISION_FP64, false, a.dims, 0);
     if (kgpu::launch_plain_fp64(model->kind, false, int(blocks), smem, st, a, *model, nullptr) != cudaSuccess)
         return noalloc_fail(KGPU_DEVICE_ERROR, "pricing kernel launch failed");
-    kgpu::merge_blocks_kernel<<<1, 32, 0, st>>>(scratch->partials, int(blocks), a.variance, a.statistics,
+    kgpu::merge_blocks_kernel<<<1, kgpu::kMergeThreads, 0, st>>>(scratch->partials, int(blocks), a.variance, a.statistics,
                                                  settings->antithetic, &scratch->merged);
     if (cudaGetLastError() != cudaSuccess) return noalloc_fail(KGPU_DEVICE_ERROR, "merge kernel launch failed");
     BlockPartial merged;
