@@ -102,7 +102,9 @@ enum {
     KGPU_PAYOFF_ASIAN = 2,        /* arithmetic average of the spots at FIXING steps */
     KGPU_PAYOFF_AUTOCALLABLE = 3, /* snowball / phoenix / binary / ternary (autocallable.rs:823-862) */
     KGPU_PAYOFF_ACCUMULATOR = 4,  /* accumulator.rs:160-216 */
-    KGPU_PAYOFF_DIGITAL = 5       /* terminal digital, one dimension (digital.rs:111-130) */
+    KGPU_PAYOFF_DIGITAL = 5,      /* terminal digital, one dimension (digital.rs:111-130) */
+    KGPU_PAYOFF_BARRIER = 6       /* continuously monitored single barrier: one terminal draw
+                                     and Brownian-bridge survival (barrier.rs:231-452) */
 };
 
 /* One simulated grid step of a contract.  For BSM the transition is the reference's
@@ -159,7 +161,9 @@ enum {
     KGPU_C_EXPIRY_KNOCK_IN = 4,  /* knock-in observed at expiry */
     KGPU_C_DOWNSIDE = 8,         /* knocked-in redemption is the capped downside */
     KGPU_C_BRIDGE = 16,          /* sample with the Brownian bridge plan */
-    KGPU_C_ASSET_DIGITAL = 32    /* digital pays the asset (no payout amount) */
+    KGPU_C_ASSET_DIGITAL = 32,   /* digital pays the asset (no payout amount) */
+    KGPU_C_BARRIER_UP = 64,      /* barrier above the spot (else below) */
+    KGPU_C_BARRIER_IN = 128      /* knock-in (else knock-out) */
 };
 
 /* A contract's plan.  Field groups are used by the payoff families named beside them. */
@@ -197,6 +201,15 @@ typedef struct kgpu_contract {
     double daily_quantity;
     double acceleration;
     double log_strike;       /* log_ratio(strike, spot) */
+    /* continuous single barrier (barrier.rs:231-452); strike, sign, diffusion (sigma
+     * sqrt(T)) and moneyness (log forward moneyness of the strike less sigma^2 T / 2)
+     * as above */
+    double barrier_drift;     /* (r - q - sigma^2 / 2) T: terminal log return = drift + diffusion z */
+    double barrier_distance;  /* |log(barrier / spot)| */
+    double barrier_moneyness; /* log forward moneyness of the barrier less sigma^2 T / 2 */
+    double rebate;            /* paid at expiry when the vanilla leg is not */
+    double spot;
+    double log_discount;      /* -r T */
 } kgpu_contract;
 
 /* A book of contracts sharing one model.  Arrays are indexed through the offsets in
@@ -340,6 +353,16 @@ kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double s
 kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book* device_book,
                                         int32_t contract, const kgpu_settings* settings,
                                         kgpu_estimate* out, void* stream);
+
+/* Loss and parameter gradients of the LSMC continuation network on one batch, computed
+ * by the tensor-core training kernel that the MLP basis of kgpu_lsmc_price runs (no
+ * counterpart in the reference: exposed so the kernels' gradients can be checked).
+ * params: KGPU_MLP_PARAMS floats, packed W1[64][3], b1[64], W2[64][64] (row = output
+ * unit), b2[64], w3[64], b3; samples: count x 4 floats (three inputs, then the target).
+ * grads receives d loss / d params of loss = mean((f(x) - target)^2); *loss that mean. */
+#define KGPU_MLP_PARAMS 4481
+kgpu_status kgpu_mlp_gradients(kgpu_context* ctx, const float* params, const float* samples, int32_t count,
+                               float* grads, double* loss);
 
 /* Instrumentation of the last call on `ctx`: device time from the first to the last
  * kernel of the call (CUDA events on the context's stream) and the number of kernel

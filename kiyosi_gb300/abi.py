@@ -32,6 +32,7 @@ PAYOFF_ASIAN = 2
 PAYOFF_AUTOCALLABLE = 3
 PAYOFF_ACCUMULATOR = 4
 PAYOFF_DIGITAL = 5
+PAYOFF_BARRIER = 6
 
 STEP_KNOCK_IN = 1
 STEP_EVENT = 2
@@ -44,6 +45,8 @@ C_EXPIRY_KNOCK_IN = 4
 C_DOWNSIDE = 8
 C_BRIDGE = 16
 C_ASSET_DIGITAL = 32
+C_BARRIER_UP = 64
+C_BARRIER_IN = 128
 
 UNCERTAINTY_NAMES = {
     0: "available",
@@ -102,7 +105,9 @@ class Contract(C.Structure):
                 ("terminal_plain", _D), ("terminal_fixed", _D), ("downside_lower", _D),
                 ("downside_upper", _D), ("downside_initial", _D), ("final_discount", _D),
                 ("knock_out", _D), ("quantity", _D), ("daily_quantity", _D),
-                ("acceleration", _D), ("log_strike", _D)]
+                ("acceleration", _D), ("log_strike", _D),
+                ("barrier_drift", _D), ("barrier_distance", _D), ("barrier_moneyness", _D),
+                ("rebate", _D), ("spot", _D), ("log_discount", _D)]
 
 
 class Book(C.Structure):
@@ -152,8 +157,9 @@ EXPORTED_SYMBOLS = (
     "kgpu_sobol_points", "kgpu_lsmc_price", "kgpu_context_last_kernel_ms",
     "kgpu_context_last_path_kernel_ms",
     "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count",
-    "kgpu_price_contract_noalloc",
+    "kgpu_price_contract_noalloc", "kgpu_mlp_gradients",
 )
+MLP_PARAMS = 4481
 
 
 def declare(lib):
@@ -191,6 +197,9 @@ def declare(lib):
     lib.kgpu_price_contract_noalloc.argtypes = [_P(Model), _P(Book), _I, _P(Settings),
                                                 _P(Estimate), V]
     lib.kgpu_price_contract_noalloc.restype = _I
+    lib.kgpu_mlp_gradients.argtypes = [V, _P(C.c_float), _P(C.c_float), _I, _P(C.c_float),
+                                       _P(_D)]
+    lib.kgpu_mlp_gradients.restype = _I
     lib.kgpu_abi_version.argtypes = []
     lib.kgpu_abi_version.restype = _I
     lib.kgpu_device_count.argtypes = []

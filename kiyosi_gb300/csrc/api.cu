@@ -277,8 +277,13 @@ struct ContractInfo {
 
 int model_normals_per_step(const kgpu_model* m) { return m->kind == KGPU_MODEL_HESTON ? 2 : 1; }
 
+// Payoffs sampled with one terminal draw per path (no grid).
+bool terminal_payoff(const kgpu_contract& c) {
+    return c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL || c.payoff == KGPU_PAYOFF_BARRIER;
+}
+
 int dims_of(const kgpu_contract& c, const kgpu_model* m) {
-    if (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) return 1;
+    if (terminal_payoff(c)) return 1;
     return c.step_count * model_normals_per_step(m);
 }
 
@@ -547,7 +552,7 @@ kgpu_status run_plain(Call& k, const DevBook<Real>& db, int& launches) {
     for (int i = 0; i < n; ++i) {
         const kgpu_contract& c = k.book->contracts[i];
         estimate_from_moments(c, s, k.info[i].paths, merged[i], &k.out[i]);
-        int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
+        int grid = terminal_payoff(c) ? 1 : c.step_count;
         k.out[i].path_steps = double(k.info[i].paths) * grid;
         k.out[i].executed_steps = merged[i].executed;
         if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].standard_error))
@@ -724,7 +729,7 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
         const kgpu_contract& c = k.book->contracts[i];
         sums[i].executed = double(executed[i]);
         estimate_from_sums(c, s, k.info[i].paths, sums[i], &k.out[i]);
-        int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
+        int grid = terminal_payoff(c) ? 1 : c.step_count;
         k.out[i].path_steps = double(k.info[i].paths) * grid;
         k.out[i].executed_steps = sums[i].executed;
         if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].standard_error))
@@ -797,8 +802,10 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: path_count must be positive", i);
         if (k.sobol && !is_pow2(paths))
             return fail(ctx, KGPU_INVALID_INPUT, "path_count must be a power of two for Sobol sampling");
-        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_DIGITAL)
+        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_BARRIER)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: unknown payoff %d", i, c.payoff);
+        if (c.payoff == KGPU_PAYOFF_BARRIER && (model->kind != KGPU_MODEL_BSM || !(c.diffusion > 0.0)))
+            return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "contract %d: the Monte Carlo barrier needs BSM volatility", i);
         if (c.step_count < 1 || c.step_offset < 0 || c.step_offset + c.step_count > book->step_total)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: steps out of range", i);
         if (c.event_count < 0 || c.event_offset < 0 || c.event_offset + c.event_count > book->event_total)

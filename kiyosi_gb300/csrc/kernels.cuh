@@ -121,6 +121,12 @@ __global__ void compile_contracts_kernel(const kgpu_contract* in, int n, Contrac
     o.daily_quantity = Real(c.daily_quantity);
     o.acceleration = Real(c.acceleration);
     o.log_strike = Real(c.log_strike);
+    o.barrier_drift = Real(c.barrier_drift);
+    o.barrier_distance = Real(c.barrier_distance);
+    o.barrier_moneyness = Real(c.barrier_moneyness);
+    o.rebate = Real(c.rebate);
+    o.spot = Real(c.spot);
+    o.log_discount = Real(c.log_discount);
     out[i] = o;
 }
 

@@ -1,9 +1,953 @@
-// MLP continuation regression for LSMC (placeholder until the tensor-core kernels land).
+// Least-squares Monte Carlo with a learned continuation value.
+//
+// At each exercise date the continuation value is the reference's least-squares
+// polynomial (crates/kiyosi/src/engines/monte_carlo/american.rs:1347-1417, the cubic
+// (S/K, v/theta) basis of the Heston path store) plus a small network
+// f(x) = w3 . relu(W2 relu(W1 x + b1) + b2) + b3 with 3 inputs (log moneyness, variance,
+// time), two hidden layers of 64 and one output, fitted by Adam on the mean squared error
+// to what the polynomial leaves unexplained: the in-the-money paths' discounted cash
+// flows minus the polynomial's fit.  A network that learns nothing leaves the
+// polynomial method exactly.  Exercise decisions, the date-0 estimate and the
+// out-of-sample lower bound follow the polynomial method step for step with the sum in
+// place of the polynomial.
+//
+// Training runs on the fifth-generation tensor cores: one CTA holds 128 samples; the
+// 64 x 64 layer's forward product, the backward product through it and its weight
+// gradient are tcgen05 MMAs (BF16 operands in shared memory, FP32 accumulators in
+// tensor memory); the 3 -> 64 and 64 -> 1 layers, the activations and the reductions run
+// on the CUDA cores in FP32.  Per-CTA gradient partials are summed in a fixed order by
+// the Adam kernel, so training is deterministic.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
 #include "../../include/kgpu.h"
 #include "api_internal.h"
+#include "lsmc_common.cuh"
+#include "tcgen05.cuh"
 
-kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model*, double, double, double,
-                          const kgpu_lsmc_settings*, uint64_t, kgpu_lsmc_result*) {
-    ctx->error = "the MLP continuation basis is not built in this library";
-    return KGPU_UNSUPPORTED_OPERATION;
+namespace kgpu {
+namespace {
+
+constexpr int kHidden = 64;
+constexpr int kRows = 128;  // samples per training CTA (the MMA's M)
+// Parameter vector: W1[64][3], b1[64], W2[64][64] (row = output unit), b2[64], w3[64], b3.
+constexpr int kPW1 = 0, kPB1 = 192, kPW2 = 256, kPB2 = 4352, kPW3 = 4416, kPB3 = 4480;
+constexpr int kParams = 4481;
+constexpr int kStride = 4484;  // per-CTA partial: kParams gradients, then the loss sum; also the
+                               // 16-byte-aligned stride of every parameter-sized region
+constexpr int kLossSlot = 4481;
+constexpr uint32_t kTmemColumns = 256;  // [0,64) Z2, [64,128) dH1, [128,192) dW2
+
+struct __align__(1024) TrainSmem {
+    __nv_bfloat16 h1[kRows * kHidden];       // A of the forward product: rows x inputs
+    __nv_bfloat16 h1t[kHidden * kRows];      // B of the weight gradient: inputs x rows
+    __nv_bfloat16 dz2[kRows * kHidden];      // A of the backward product: rows x outputs
+    __nv_bfloat16 dz2t[kRows * kRows];       // A of the weight gradient: outputs (64 + 64 zero) x rows
+    __nv_bfloat16 w2f[kHidden * kHidden];    // B forward: outputs x inputs
+    __nv_bfloat16 w2b[kHidden * kHidden];    // B backward: inputs x outputs
+    float w1[3 * kHidden], b1[kHidden], b2[kHidden], w3[kHidden];
+    float red[4][256];
+    uint64_t bar;
+    uint32_t tmem;
+    int failed;
+};
+
+constexpr size_t kTrainSmemBytes = sizeof(TrainSmem) + 1024;
+
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Sums N values across the warp: on return v[0 .. N/32) hold the warp totals of indices
+// (N/32) * lane + i.
+template <int N>
+__device__ __forceinline__ void warp_transpose_sum(float* v, int lane) {
+    int n = N;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+        n >>= 1;
+#pragma unroll
+        for (int i = 0; i < N / 2; ++i) {
+            if (i < n) {
+                const float send = upper ? v[i] : v[i + n];
+                const float keep = upper ? v[i + n] : v[i];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            }
+        }
+    }
+}
+
+// Reduces 128 per-thread values over the CTA's 128 threads; returns total t to thread t.
+__device__ __forceinline__ float cta_sum128(TrainSmem& s, float* v) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    warp_transpose_sum<128>(v, lane);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) s.red[warp][4 * lane + i] = v[i];
+    __syncthreads();
+    const int t = threadIdx.x;
+    const float out = ((s.red[0][t] + s.red[1][t]) + s.red[2][t]) + s.red[3][t];
+    __syncthreads();
+    return out;
+}
+
+// One batch's gradient partials: CTA b covers samples [first + 128 b, first + 128 b + 128)
+// of the batch [first, first + count); partials[b] receives the CTA's gradient of
+// (1 / count) sum (f(x) - y)^2 and its sum of squared residuals.
+__global__ void __launch_bounds__(kRows, 1) mlp_grad_kernel(const float* __restrict__ params,
+                                                            const float4* __restrict__ samples, int first,
+                                                            int count, float inv_count, float* __restrict__ partials,
+                                                            int* __restrict__ error) {
+    extern __shared__ unsigned char smem_raw[];
+    TrainSmem& s = *reinterpret_cast<TrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int t = threadIdx.x, warp = t >> 5;
+    if (warp == 0) {
+        tc::tmem_alloc(&s.tmem, kTmemColumns);
+        tc::tmem_relinquish();
+    }
+    if (t == 0) {
+        tc::mbar_init(&s.bar, 1);
+        s.failed = 0;
+    }
+    for (int i = t; i < 3 * kHidden; i += kRows) s.w1[i] = params[kPW1 + i];
+    if (t < kHidden) {
+        s.b1[t] = params[kPB1 + t];
+        s.b2[t] = params[kPB2 + t];
+        s.w3[t] = params[kPW3 + t];
+    }
+    const float b3 = params[kPB3];
+    for (int i = t; i < kHidden * kHidden; i += kRows) {
+        const int o = i >> 6, in = i & 63;
+        const __nv_bfloat16 w = __float2bfloat16_rn(params[kPW2 + i]);
+        s.w2f[tc::kmajor(o, in, kHidden)] = w;
+        s.w2b[tc::kmajor(in, o, kHidden)] = w;
+    }
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
+    for (int i = t; i < kHidden * kRows; i += kRows) s.dz2t[kHidden * kRows + i] = zero;  // rows 64..127
+    const int local = blockIdx.x * kRows + t;
+    const bool valid = local < count;
+    const float4 x = valid ? samples[first + local] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+
+    // Layer 1 on the CUDA cores; H1 goes to shared memory in both operand layouts.
+    uint64_t mask1 = 0;
+#pragma unroll 8
+    for (int j = 0; j < kHidden; ++j) {
+        const float z = fmaf(s.w1[3 * j], x.x, fmaf(s.w1[3 * j + 1], x.y, fmaf(s.w1[3 * j + 2], x.z, s.b1[j])));
+        if (z > 0.f) mask1 |= 1ull << j;
+        const __nv_bfloat16 h = __float2bfloat16_rn(valid && z > 0.f ? z : 0.f);
+        s.h1[tc::kmajor(t, j, kHidden)] = h;
+        s.h1t[tc::kmajor(j, t, kRows)] = h;
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = s.tmem;
+    const uint32_t idesc = tc::idesc_bf16(kRows, kHidden);
+    if (t == 0) {
+        const uint32_t a0 = tc::smem_u32(s.h1), b0 = tc::smem_u32(s.w2f);
+        for (int k = 0; k < kHidden / 16; ++k)
+            tc::mma_bf16(tmem, tc::smem_desc(a0 + 256 * k, 128, kHidden * 16), tc::smem_desc(b0 + 256 * k, 128, kHidden * 16),
+                         idesc, k > 0);
+        tc::mma_commit(&s.bar);
+    }
+    bool ok = tc::mbar_wait(&s.bar, 0);
+    if (__syncthreads_or(!ok)) {
+        if (t == 0) atomicExch(error, 1);
+        goto release;
+    }
+    tc::fence_after_sync();
+    {
+        // Z2 of this thread's sample (TMEM lane = row = thread).
+        float z2[kHidden];
+        const uint32_t lane_base = uint32_t(warp * 32) << 16;
+        tc::tmem_load32(tmem + lane_base, z2);
+        tc::tmem_load32(tmem + lane_base + 32, z2 + 32);
+        float out = b3;
+#pragma unroll
+        for (int j = 0; j < kHidden; ++j) {
+            z2[j] += s.b2[j];
+            out = fmaf(z2[j] > 0.f ? z2[j] : 0.f, s.w3[j], out);
+        }
+        const float res = valid ? out - x.w : 0.f;
+        const float dout = 2.f * res * inv_count;
+        // dW3 and db2 contributions (128 values), and dZ2 in both operand layouts.
+        float v[2 * kHidden];
+#pragma unroll
+        for (int j = 0; j < kHidden; ++j) {
+            const bool on = z2[j] > 0.f;
+            const float g = on ? dout * s.w3[j] : 0.f;
+            v[j] = dout * (on ? z2[j] : 0.f);
+            v[kHidden + j] = g;
+            const __nv_bfloat16 gb = __float2bfloat16_rn(g);
+            s.dz2[tc::kmajor(t, j, kHidden)] = gb;
+            s.dz2t[tc::kmajor(j, t, kRows)] = gb;
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        const float tot = cta_sum128(s, v);  // contains __syncthreads
+        tc::fence_after_sync();
+        float* part = partials + size_t(blockIdx.x) * kStride;
+        if (t < kHidden) part[kPW3 + t] = tot;
+        else part[kPB2 + (t - kHidden)] = tot;
+        // db3 and the loss: warp sums then warps in order.
+        float d3 = dout, l2 = res * res;
+        for (int o = 16; o >= 1; o >>= 1) {
+            d3 += __shfl_xor_sync(0xffffffffu, d3, o);
+            l2 += __shfl_xor_sync(0xffffffffu, l2, o);
+        }
+        if ((t & 31) == 0) {
+            s.red[0][warp] = d3;
+            s.red[1][warp] = l2;
+        }
+        if (t == 0) {
+            const uint32_t ad = tc::smem_u32(s.dz2), bw = tc::smem_u32(s.w2b);
+            for (int k = 0; k < kHidden / 16; ++k)
+                tc::mma_bf16(tmem + 64, tc::smem_desc(ad + 256 * k, 128, kHidden * 16),
+                             tc::smem_desc(bw + 256 * k, 128, kHidden * 16), idesc, k > 0);
+            const uint32_t at = tc::smem_u32(s.dz2t), bh = tc::smem_u32(s.h1t);
+            for (int k = 0; k < kRows / 16; ++k)
+                tc::mma_bf16(tmem + 128, tc::smem_desc(at + 256 * k, 128, kRows * 16),
+                             tc::smem_desc(bh + 256 * k, 128, kRows * 16), idesc, k > 0);
+            tc::mma_commit(&s.bar);
+        }
+        __syncthreads();
+        if (t == 0) {
+            part[kPB3] = ((s.red[0][0] + s.red[0][1]) + s.red[0][2]) + s.red[0][3];
+            part[kLossSlot] = ((s.red[1][0] + s.red[1][1]) + s.red[1][2]) + s.red[1][3];
+        }
+        ok = tc::mbar_wait(&s.bar, 1);
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(error, 1);
+            goto release;
+        }
+        tc::fence_after_sync();
+        // dH1 -> dZ1 -> dW1, db1 (256 values).
+        float dh1[kHidden];
+        tc::tmem_load32(tmem + lane_base + 64, dh1);
+        tc::tmem_load32(tmem + lane_base + 96, dh1 + 32);
+#pragma unroll
+        for (int j = 0; j < kHidden; ++j) dh1[j] = ((mask1 >> j) & 1ull) ? dh1[j] : 0.f;  // dZ1
+        float w[2 * kHidden];
+#pragma unroll
+        for (int j = 0; j < kHidden; ++j) {
+            w[j] = dh1[j] * x.x;
+            w[kHidden + j] = dh1[j] * x.y;
+        }
+        const float g01 = cta_sum128(s, w);
+#pragma unroll
+        for (int j = 0; j < kHidden; ++j) {
+            w[j] = dh1[j] * x.z;
+            w[kHidden + j] = dh1[j];
+        }
+        const float g2b = cta_sum128(s, w);
+        // W1 is row-major [64][3]: thread t < 64 owns column 0 (then 2) of unit t, thread
+        // t >= 64 column 1 of unit t - 64 (then the bias).
+        if (t < kHidden) {
+            part[kPW1 + 3 * t] = g01;
+            part[kPW1 + 3 * t + 2] = g2b;
+        } else {
+            part[kPW1 + 3 * (t - kHidden) + 1] = g01;
+            part[kPB1 + (t - kHidden)] = g2b;
+        }
+        // dW2: TMEM lanes 0..63 (warps 0 and 1) hold rows = output units.
+        if (warp < 2) {
+            float g2[kHidden];
+            tc::tmem_load32(tmem + lane_base + 128, g2);
+            tc::tmem_load32(tmem + lane_base + 160, g2 + 32);
+            float4* dst = reinterpret_cast<float4*>(part + kPW2 + t * kHidden);
+#pragma unroll
+            for (int q = 0; q < kHidden / 4; ++q) dst[q] = make_float4(g2[4 * q], g2[4 * q + 1], g2[4 * q + 2], g2[4 * q + 3]);
+        }
+    }
+release:
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemColumns);
+}
+
+// Adam (Kingma and Ba, 2015) on the summed CTA partials, in FP32.
+__global__ void mlp_adam_kernel(const float* __restrict__ partials, int blocks, float* __restrict__ params,
+                                float* __restrict__ m, float* __restrict__ v, float lr, float beta1, float beta2,
+                                float eps, float bias1, float bias2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    float g = 0.f;
+    for (int b = 0; b < blocks; ++b) g += partials[size_t(b) * kStride + i];
+    const float mi = beta1 * m[i] + (1.f - beta1) * g;
+    const float vi = beta2 * v[i] + (1.f - beta2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    params[i] -= lr * (mi / bias1) / (sqrtf(vi / bias2) + eps);
+}
+
+// The network on the CUDA cores with the training kernel's BF16 rounding of the
+// hidden layer's inputs; `P` holds a snapshot whose W2 is already rounded to BF16.
+__device__ __forceinline__ float mlp_eval(const float* P, float x0, float x1, float x2) {
+    float h1[kHidden];
+#pragma unroll
+    for (int j = 0; j < kHidden; ++j) {
+        const float z = fmaf(P[kPW1 + 3 * j], x0, fmaf(P[kPW1 + 3 * j + 1], x1, fmaf(P[kPW1 + 3 * j + 2], x2, P[kPB1 + j])));
+        h1[j] = bf16_round(z > 0.f ? z : 0.f);
+    }
+    float out = P[kPB3];
+#pragma unroll 1
+    for (int o = 0; o < kHidden; ++o) {
+        float z = 0.f;
+#pragma unroll
+        for (int i = 0; i < kHidden; ++i) z = fmaf(P[kPW2 + o * kHidden + i], h1[i], z);
+        z += P[kPB2 + o];
+        out = fmaf(z > 0.f ? z : 0.f, P[kPW3 + o], out);
+    }
+    return out;
+}
+
+// Target normalisation of one date: the network fits (y - mean) / scale.
+struct TargetNorm {
+    double mean, scale;
+};
+
+// Copies the trained parameters into the per-date store: W2 rounded to BF16 as the
+// training kernel multiplies it, the output layer scaled back to cash units
+// (w3 * scale, b3 * scale + mean), so the stored network predicts y itself.
+__global__ void mlp_snapshot_kernel(const float* __restrict__ params, const TargetNorm* __restrict__ norm,
+                                    float* __restrict__ net) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    const float scale = float(norm->scale), mean = float(norm->mean);
+    float w = params[i];
+    if (i >= kPW2 && i < kPB2) w = bf16_round(w);
+    else if (i >= kPW3 && i < kPB3) w *= scale;
+    else if (i == kPB3) w = fmaf(w, scale, mean);
+    net[i] = w;
+}
+
+__device__ __forceinline__ void load_net(float* dst, const float* src) {
+    for (int i = threadIdx.x; i < kParams; i += blockDim.x) dst[i] = src[i];
+}
+
+// Network inputs of a path at exercise date k.
+struct Features {
+    float spot_scale;  // 1 / (sigma_ref sqrt(T)) applied to log(S/K)
+    float v_center, v_scale;
+    float time_scale;  // dt / T
+};
+
+template <bool TWO>
+__device__ __forceinline__ float4 features(const LsmcParams<float>& p, const Features& f, int k, float a, float b) {
+    const float spot = spot_at_date<float, TWO>(p, k, a);
+    const float x0 = logf(spot / p.strike) * f.spot_scale;
+    const float x1 = TWO ? (b - f.v_center) * f.v_scale : 0.f;
+    return make_float4(x0, x1, float(k + 1) * f.time_scale, spot);
+}
+
+// Polynomial part of the continuation at date k (zero when the date has no fit).
+template <bool TWO>
+__device__ __forceinline__ float poly_part(const LsmcParams<float>& p, const double* coefs, const int* have, int k,
+                                           float spot, float v) {
+    if (!have[k]) return 0.f;
+    double cn[TWO ? 10 : 3];
+#pragma unroll
+    for (int j = 0; j < (TWO ? 10 : 3); ++j) cn[j] = coefs[size_t(k) * kMaxTerms + j];
+    return continuation<float, TWO>(p, cn, spot / p.strike, TWO ? v * p.y_scale : 0.f);
+}
+
+// Normal equations of the in-the-money paths at date k (the accumulation of
+// lsmc_backward, with the cash already decided and discounted to date k).
+template <bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) mlp_poly_sums_kernel(LsmcParams<float> p, int date,
+                                                                     const float* __restrict__ a,
+                                                                     const float* __restrict__ b,
+                                                                     const float* __restrict__ cash,
+                                                                     double* __restrict__ partials) {
+    constexpr int T = TWO ? 10 : 3;
+    constexpr int S = sum_count(T);
+    float acc[S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) acc[j] = 0.f;
+    const float inv_k = 1.f / p.strike;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
+        const size_t at = size_t(date) * p.paths + i;
+        const float s = spot_at_date<float, TWO>(p, date, a[at]);
+        if (intrinsic(p, s) > 0.f) {
+            float f[T];
+            lsmc_basis<float, TWO>(s * inv_k, TWO ? b[at] * p.y_scale : 0.f, f);
+            const float target = cash[i] * inv_k;
+            int q = 0;
+#pragma unroll
+            for (int r = 0; r < T; ++r)
+#pragma unroll
+                for (int col = r; col < T; ++col) acc[q++] += f[r] * f[col];
+#pragma unroll
+            for (int r = 0; r < T; ++r) acc[q++] += f[r] * target;
+        }
+    }
+    __shared__ double warp_sums[kLsmcThreads / 32][S];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+        double v = double(acc[j]);
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) warp_sums[warp][j] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        double v = 0.0;
+        for (int w = 0; w < kLsmcThreads / 32; ++w) v += warp_sums[w][j];
+        partials[size_t(blockIdx.x) * S + j] = v;
+    }
+}
+
+// Applies the exercise decision of date k + 1 with the continuation fitted there (when
+// `decide`), then discounts the cash to date k (american.rs:1347-1362).
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_decide_kernel(LsmcParams<float> p, Features f, int date, int decide,
+                                                         const float* __restrict__ net, const double* __restrict__ coefs,
+                                                         const int* __restrict__ have, const float* __restrict__ a,
+                                                         const float* __restrict__ b, float* __restrict__ cash) {
+    __shared__ float P[kParams];
+    if (decide) load_net(P, net);
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.paths) return;
+    float c = cash[i];
+    if (decide) {
+        const size_t at = size_t(date + 1) * p.paths + i;
+        const float v = TWO ? b[at] : 0.f;
+        const float4 x = features<TWO>(p, f, date + 1, a[at], v);
+        const float e = intrinsic(p, x.w);
+        if (e > 0.f &&
+            e / p.strike > poly_part<TWO>(p, coefs, have, date + 1, x.w, v) + mlp_eval(P, x.x, x.y, x.z))
+            c = e;
+    }
+    cash[i] = c * p.discount;
+}
+
+// In-the-money samples of date k in path order: per-block counts and target sums, a
+// block-ordered scan (offsets, the date's target mean and scale), then the scatter.
+struct BlockStats {
+    double count, sum, sumsq;
+};
+
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_count_kernel(LsmcParams<float> p, int date, const float* __restrict__ a,
+                                                        const float* __restrict__ b, const float* __restrict__ cash,
+                                                        const double* __restrict__ coefs, const int* __restrict__ have,
+                                                        BlockStats* __restrict__ stats) {
+    __shared__ double ws[8][3];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double c = 0.0, y = 0.0;
+    if (i < p.paths) {
+        const size_t at = size_t(date) * p.paths + i;
+        const float spot = spot_at_date<float, TWO>(p, date, a[at]);
+        if (intrinsic(p, spot) > 0.f) {
+            c = 1.0;
+            y = double(cash[i] / p.strike - poly_part<TWO>(p, coefs, have, date, spot, TWO ? b[at] : 0.f));
+        }
+    }
+    double y2 = y * y;
+    for (int o = 16; o >= 1; o >>= 1) {
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        ws[warp][0] = c;
+        ws[warp][1] = y;
+        ws[warp][2] = y2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        BlockStats b{0.0, 0.0, 0.0};
+        for (int w = 0; w < 8; ++w) {
+            b.count += ws[w][0];
+            b.sum += ws[w][1];
+            b.sumsq += ws[w][2];
+        }
+        stats[blockIdx.x] = b;
+    }
+}
+
+// Exclusive offsets in block order, the in-the-money total and the target normalisation.
+__global__ void mlp_scan_kernel(const BlockStats* __restrict__ stats, int blocks, int* __restrict__ offsets,
+                                int* __restrict__ total, TargetNorm* __restrict__ norm) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int run = 0;
+    double sum = 0.0, sumsq = 0.0;
+    for (int b = 0; b < blocks; ++b) {
+        offsets[b] = run;
+        run += int(stats[b].count);
+        sum += stats[b].sum;
+        sumsq += stats[b].sumsq;
+    }
+    *total = run;
+    TargetNorm t{0.0, 1.0};
+    if (run > 0) {
+        t.mean = sum / run;
+        const double var = sumsq / run - t.mean * t.mean;
+        t.scale = var > 1e-12 ? sqrt(var) : 1.0;
+    }
+    *norm = t;
+}
+
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_scatter_kernel(LsmcParams<float> p, Features f, int date,
+                                                          const float* __restrict__ a, const float* __restrict__ b,
+                                                          const float* __restrict__ cash, const double* __restrict__ coefs,
+                                                          const int* __restrict__ have, const int* __restrict__ offsets,
+                                                          const TargetNorm* __restrict__ norm,
+                                                          float4* __restrict__ samples) {
+    __shared__ int warp_base[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool itm = false;
+    float v = 0.f;
+    if (i < p.paths) {
+        const size_t at = size_t(date) * p.paths + i;
+        v = TWO ? b[at] : 0.f;
+        x = features<TWO>(p, f, date, a[at], v);
+        itm = intrinsic(p, x.w) > 0.f;
+    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, itm);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_base[warp] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int w = 0; w < 8; ++w) {
+            const int c = warp_base[w];
+            warp_base[w] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    if (itm) {
+        const int pos = offsets[blockIdx.x] + warp_base[warp] + __popc(ballot & ((1u << lane) - 1u));
+        const float y = cash[i] / p.strike - poly_part<TWO>(p, coefs, have, date, x.w, v);
+        samples[pos] = make_float4(x.x, x.y, x.z, float((double(y) - norm->mean) / norm->scale));
+    }
+}
+
+// Date-0 decision and the cash moments (FP64 partials per block).
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_final_kernel(LsmcParams<float> p, Features f, const float* __restrict__ net,
+                                                        const double* __restrict__ coefs, const int* __restrict__ have,
+                                                        const float* __restrict__ a, const float* __restrict__ b,
+                                                        const float* __restrict__ cash, double* __restrict__ partials) {
+    __shared__ float P[kParams];
+    __shared__ double w0[8], w1[8];
+    load_net(P, net);
+    __syncthreads();
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
+        float c = cash[i];
+        const float v = TWO ? b[i] : 0.f;
+        const float4 x = features<TWO>(p, f, 0, a[i], v);
+        const float e = intrinsic(p, x.w);
+        if (e > 0.f && e / p.strike > poly_part<TWO>(p, coefs, have, 0, x.w, v) + mlp_eval(P, x.x, x.y, x.z)) c = e;
+        s0 += double(c);
+        s1 += double(c) * double(c);
+    }
+    for (int o = 16; o >= 1; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        w0[threadIdx.x >> 5] = s0;
+        w1[threadIdx.x >> 5] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w = 0; w < 8; ++w) {
+            t0 += w0[w];
+            t1 += w1[w];
+        }
+        partials[2 * blockIdx.x] = t0;
+        partials[2 * blockIdx.x + 1] = t1;
+    }
+}
+
+// The fitted policy on fresh paths (american.rs:574-637): every thread walks its path
+// forward and stops at the first date whose intrinsic value beats the network.
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_lower_bound_kernel(LsmcParams<float> p, Features f, uint64_t seed,
+                                                              const float* __restrict__ nets,
+                                                              const double* __restrict__ coefs,
+                                                              const int* __restrict__ have,
+                                                              double* __restrict__ partials) {
+    __shared__ double w0[8], w1[8];
+    const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
+        PcgSource<float> n;
+        n.start(seed, uint64_t(i), dims);
+        float x = 0.f, v = p.v0, value = 0.f, df = 1.f;
+        for (int k = 0; k < p.dates; ++k) {
+            if (!TWO) {
+                x += n.normal();
+            } else {
+                for (int j = 0; j < p.substeps; ++j) {
+                    const float z1 = n.normal(), z2 = n.normal();
+                    const float vp = v > 0.f ? v : 0.f;
+                    const float sv = sqrtf(vp) * p.sqrt_h;
+                    x += (p.rate - p.dividend - 0.5f * vp) * p.h + sv * z1;
+                    v += p.kappa * (p.theta - vp) * p.h + p.xi * sv * (p.rho * z1 + p.rho_bar * z2);
+                }
+            }
+            df *= p.discount;
+            const float4 q = features<TWO>(p, f, k, x, v);
+            const float e = intrinsic(p, q.w);
+            if (e > 0.f) {
+                // The last date exercises whenever in the money; earlier ones consult the
+                // network of that date (weights read through L2, warp-uniform).
+                bool stop = k == p.dates - 1;
+                if (!stop)
+                    stop = e / p.strike >
+                           poly_part<TWO>(p, coefs, have, k, q.w, v) + mlp_eval(nets + size_t(k) * kStride, q.x, q.y, q.z);
+                if (stop) {
+                    value = e * df;
+                    break;
+                }
+            }
+        }
+        s0 += double(value);
+        s1 += double(value) * double(value);
+    }
+    for (int o = 16; o >= 1; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        w0[threadIdx.x >> 5] = s0;
+        w1[threadIdx.x >> 5] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w = 0; w < 8; ++w) {
+            t0 += w0[w];
+            t1 += w1[w];
+        }
+        partials[2 * blockIdx.x] = t0;
+        partials[2 * blockIdx.x + 1] = t1;
+    }
+}
+
+// Deterministic initial weights: uniform(-sqrt(6 / fan_in), sqrt(6 / fan_in)) from a
+// splitmix64 stream of `seed` for the hidden layers, zero biases and a zero output layer,
+// so the untrained network adds nothing to the polynomial.
+void initial_params(uint64_t seed, std::vector<float>& w) {
+    w.assign(kParams, 0.0f);
+    uint64_t state = seed;
+    auto next = [&]() {
+        uint64_t z = (state += 0x9E3779B97F4A7C15ULL);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        return double(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    auto fill = [&](int at, int n, double fan_in) {
+        const double r = std::sqrt(6.0 / fan_in);
+        for (int i = 0; i < n; ++i) w[at + i] = float((2.0 * next() - 1.0) * r);
+    };
+    fill(kPW1, 3 * kHidden, 3.0);
+    fill(kPW2, kHidden * kHidden, double(kHidden));
+}
+
+bool configure_train_kernel() {
+    static bool done = false;
+    if (done) return true;
+    done = cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmemBytes)) ==
+           cudaSuccess;
+    return done;
+}
+
+struct Adam {
+    float lr, beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+    int step = 0;
+};
+
+// One optimiser step on samples [first, first + count).
+cudaError_t train_step(cudaStream_t st, float* params, float* m, float* v, Adam& adam, const float4* samples, int first,
+                       int count, float* partials, int* error) {
+    const int blocks = (count + kRows - 1) / kRows;
+    mlp_grad_kernel<<<blocks, kRows, kTrainSmemBytes, st>>>(params, samples, first, count, 1.0f / float(count),
+                                                            partials, error);
+    adam.step += 1;
+    const float bias1 = 1.0f - std::pow(adam.beta1, float(adam.step));
+    const float bias2 = 1.0f - std::pow(adam.beta2, float(adam.step));
+    mlp_adam_kernel<<<(kParams + 255) / 256, 256, 0, st>>>(partials, blocks, params, m, v, adam.lr, adam.beta1,
+                                                           adam.beta2, adam.eps, bias1, bias2);
+    return cudaGetLastError();
+}
+
+template <bool TWO>
+kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
+                    const kgpu_lsmc_settings* s, uint64_t fresh_seed, kgpu_lsmc_result* out) {
+    const LsmcParams<float> p = make_lsmc_params<float>(model, strike, sign, expiry, s);
+    const size_t n = size_t(p.paths), d = size_t(p.dates);
+    const int batch = s->mlp_batch > 0 ? s->mlp_batch : 8192;
+    const int epochs = s->mlp_epochs > 0 ? s->mlp_epochs : 5;
+    if (s->mlp_hidden != 0 && s->mlp_hidden != kHidden) {
+        ctx->error = "the continuation network has 64 hidden units per layer";
+        return KGPU_UNSUPPORTED_OPERATION;
+    }
+    Features f;
+    const double sigma_ref = TWO ? std::sqrt(std::max(model->theta, 1e-8)) : model->volatility;
+    f.spot_scale = float(1.0 / (std::max(sigma_ref, 1e-4) * std::sqrt(expiry)));
+    f.v_center = TWO ? float(model->theta) : 0.f;
+    f.v_scale = TWO ? float(1.0 / std::max(model->theta, 1e-8)) : 0.f;
+    f.time_scale = float(1.0 / p.dates);
+    const int pblocks = int((n + 255) / 256);
+    const int max_train_blocks = (batch + kRows - 1) / kRows;
+    const int fblocks = std::min(ctx->sm_count * 8, pblocks);
+    const int sblocks = std::min<int>(ctx->sm_count * 4, int((n + kLsmcThreads - 1) / kLsmcThreads));
+    // Buffers: path store, cash, samples, counts, parameters and Adam state, per-date
+    // networks, gradient partials, estimate partials.
+    const size_t store_bytes = n * d * sizeof(float) * (TWO ? 2 : 1);
+    const size_t net_bytes = size_t(kParams) * sizeof(float);
+    const size_t misc_floats = (size_t(3) + d) * kStride + size_t(max_train_blocks) * kStride;
+    if (ctx->lsmc_store.ensure(store_bytes) || ctx->lsmc_cash.ensure(n * sizeof(float)) ||
+        ctx->mlp_scratch.ensure(n * sizeof(float4) + size_t(pblocks) * (sizeof(BlockStats) + sizeof(int)) +
+                                d * sizeof(TargetNorm) + 256) ||
+        ctx->mlp_params.ensure(misc_floats * sizeof(float)) ||
+        ctx->lsmc_misc.ensure(size_t(fblocks) * 2 * sizeof(double) * 2 + 64) ||
+        ctx->lsmc_sums.ensure(size_t(sblocks) * kMaxSums * sizeof(double)) ||
+        ctx->lsmc_coef.ensure(d * kMaxTerms * sizeof(double) + d * sizeof(int) + 16))
+        return KGPU_DEVICE_ERROR;
+    if (!configure_train_kernel()) {
+        ctx->error = "cannot configure the training kernel's shared memory";
+        return KGPU_DEVICE_ERROR;
+    }
+    float* a = static_cast<float*>(ctx->lsmc_store.ptr);
+    float* b = TWO ? a + n * d : nullptr;
+    float* cash = static_cast<float*>(ctx->lsmc_cash.ptr);
+    float4* samples = static_cast<float4*>(ctx->mlp_scratch.ptr);
+    BlockStats* stats = reinterpret_cast<BlockStats*>(samples + n);
+    TargetNorm* norms = reinterpret_cast<TargetNorm*>(stats + pblocks);
+    int* counts = reinterpret_cast<int*>(norms + d);
+    int* total = counts + pblocks;
+    int* error = total + 1;
+    // Regions of kStride floats keep every one 16-byte aligned (the gradient partials are
+    // written as float4).
+    float* params = static_cast<float*>(ctx->mlp_params.ptr);
+    float* m = params + kStride;
+    float* v = m + kStride;
+    float* nets = v + kStride;
+    float* partials = nets + d * kStride;
+    double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
+    double* lower_partials = finals + 2 * fblocks;
+    double* coefs = static_cast<double*>(ctx->lsmc_coef.ptr);
+    int* have = reinterpret_cast<int*>(coefs + d * kMaxTerms);
+    int* poly_failed = have + d;
+    double* poly_partials = static_cast<double*>(ctx->lsmc_sums.ptr);
+    cudaStream_t st = ctx->stream;
+    std::vector<float> init;
+    initial_params(s->mlp_seed, init);
+    Adam adam;
+    adam.lr = float(s->mlp_learning_rate > 0.0 ? s->mlp_learning_rate : 1e-3);
+    cudaEvent_t e0, e1, e2, e3;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventCreate(&e2);
+    cudaEventCreate(&e3);
+    auto cleanup = [&]() {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaEventDestroy(e2);
+        cudaEventDestroy(e3);
+    };
+#define MLP_TRY(x)                                       \
+    do {                                                 \
+        cudaError_t rc_ = (x);                           \
+        if (rc_ != cudaSuccess) {                        \
+            ctx->error = cudaGetErrorString(rc_);        \
+            cleanup();                                   \
+            return KGPU_DEVICE_ERROR;                    \
+        }                                                \
+    } while (0)
+    MLP_TRY(cudaMemcpyAsync(params, init.data(), net_bytes, cudaMemcpyHostToDevice, st));
+    MLP_TRY(cudaMemsetAsync(m, 0, 2 * kStride * sizeof(float), st));
+    MLP_TRY(cudaMemsetAsync(nets, 0, d * kStride * sizeof(float), st));
+    MLP_TRY(cudaMemsetAsync(error, 0, sizeof(int), st));
+    MLP_TRY(cudaMemsetAsync(coefs, 0, d * kMaxTerms * sizeof(double) + d * sizeof(int) + sizeof(int), st));
+    MLP_TRY(cudaEventRecord(e0, st));
+    lsmc_forward<float, TWO><<<unsigned(pblocks), 256, 0, st>>>(p, s->seed, a, b, cash);
+    MLP_TRY(cudaGetLastError());
+    MLP_TRY(cudaEventRecord(e1, st));
+    int launches = 1;
+    for (int date = p.dates - 2; date >= 0; --date) {
+        const int decide = date + 1 <= p.dates - 2;
+        mlp_decide_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, decide, nets + size_t(date + 1) * kStride, coefs,
+                                                       have, a, b, cash);
+        // The polynomial fit of this date (lsmc_solve: block-ordered merge, pivoted FP64
+        // elimination with degree fallback), then the residual samples.
+        mlp_poly_sums_kernel<TWO><<<sblocks, kLsmcThreads, 0, st>>>(p, date, a, b, cash, poly_partials);
+        lsmc_solve<TWO><<<1, 128, 0, st>>>(poly_partials, sblocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                                           have + date, poly_failed);
+        mlp_count_kernel<TWO><<<pblocks, 256, 0, st>>>(p, date, a, b, cash, coefs, have, stats);
+        mlp_scan_kernel<<<1, 32, 0, st>>>(stats, pblocks, counts, total, norms + date);
+        mlp_scatter_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, a, b, cash, coefs, have, counts, norms + date,
+                                                        samples);
+        launches += 6;
+        MLP_TRY(cudaGetLastError());
+        int itm = 0;
+        MLP_TRY(cudaMemcpyAsync(&itm, total, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MLP_TRY(cudaStreamSynchronize(st));
+        if (itm > 0) {
+            // The first fitted date starts from the initial weights: it trains four times
+            // as long; later dates start from the previous date's network.
+            const int date_epochs = adam.step == 0 ? 4 * epochs : epochs;
+            for (int epoch = 0; epoch < date_epochs; ++epoch)
+                for (int first = 0; first < itm; first += batch) {
+                    MLP_TRY(train_step(st, params, m, v, adam, samples, first, std::min(batch, itm - first), partials,
+                                       error));
+                    launches += 2;
+                }
+        }
+        // The network of this date (kept when no path is in the money: the previous
+        // date's weights continue).
+        mlp_snapshot_kernel<<<(kParams + 255) / 256, 256, 0, st>>>(params, norms + date, nets + size_t(date) * kStride);
+        ++launches;
+    }
+    mlp_final_kernel<TWO><<<fblocks, 256, 0, st>>>(p, f, nets, coefs, have, a, b, cash, finals);
+    ++launches;
+    MLP_TRY(cudaGetLastError());
+    MLP_TRY(cudaEventRecord(e2, st));
+    const bool lower = fresh_seed != s->seed;
+    if (lower) {
+        mlp_lower_bound_kernel<TWO><<<fblocks, 256, 0, st>>>(p, f, fresh_seed, nets, coefs, have, lower_partials);
+        ++launches;
+        MLP_TRY(cudaGetLastError());
+    }
+    MLP_TRY(cudaEventRecord(e3, st));
+    std::vector<double> fin(size_t(fblocks) * 4);
+    int failed = 0, fit_failed = 0;
+    MLP_TRY(cudaMemcpyAsync(fin.data(), finals, fin.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MLP_TRY(cudaMemcpyAsync(&failed, error, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MLP_TRY(cudaMemcpyAsync(&fit_failed, poly_failed, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MLP_TRY(cudaStreamSynchronize(st));
+    float ms_total = 0, ms_store = 0, ms_regress = 0;
+    cudaEventElapsedTime(&ms_total, e0, e3);
+    cudaEventElapsedTime(&ms_store, e0, e1);
+    cudaEventElapsedTime(&ms_regress, e1, e2);
+    cleanup();
+#undef MLP_TRY
+    if (failed) {
+        ctx->error = "a tensor-core wait gave up in the training kernel";
+        return KGPU_DEVICE_ERROR;
+    }
+    if (fit_failed) {
+        ctx->error = "Monte Carlo produced a non-finite parameter, path or result";
+        return KGPU_COMPUTATION_FAILURE;
+    }
+    ctx->last_launches = launches;
+    ctx->last_kernel_ms = ms_total;
+    auto moments = [&](const double* part, double* mean, double* err, double scale) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int blk = 0; blk < fblocks; ++blk) {
+            s0 += part[2 * blk];
+            s1 += part[2 * blk + 1];
+        }
+        const double mu = s0 / double(n);
+        const double var = n > 1 ? std::max(0.0, (s1 - s0 * mu) / double(n - 1)) : 0.0;
+        *mean = mu * scale;
+        *err = std::sqrt(var / double(n)) * scale;
+    };
+    const double disc0 = std::exp(-model->rate * (expiry / p.dates));
+    const double immediate = std::max(0.0, sign * (model->spot - strike));
+    double mean = 0.0, se = 0.0;
+    moments(fin.data(), &mean, &se, disc0);
+    out->price = std::max(immediate, mean);
+    out->standard_error = se;
+    out->out_of_sample = std::nan("");
+    out->out_of_sample_error = std::nan("");
+    if (lower) {
+        double lm = 0.0, le = 0.0;
+        moments(fin.data() + 2 * fblocks, &lm, &le, 1.0);
+        out->out_of_sample = std::max(immediate, lm);
+        out->out_of_sample_error = le;
+    }
+    out->wall_ms = ms_total;
+    out->path_store_ms = ms_store;
+    out->regression_ms = ms_regress;
+    if (!std::isfinite(out->price)) {
+        ctx->error = "Monte Carlo produced a non-finite parameter, path or result";
+        return KGPU_COMPUTATION_FAILURE;
+    }
+    return KGPU_OK;
+}
+
+}  // namespace
+}  // namespace kgpu
+
+// LSMC with the continuation network (called by kgpu_lsmc_price for KGPU_BASIS_MLP).
+kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
+                          const kgpu_lsmc_settings* settings, uint64_t fresh_seed, kgpu_lsmc_result* out) {
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
+    if (settings->precision != KGPU_PRECISION_FP32) {
+        ctx->error = "the continuation network trains on an FP32 path store (precision must be FP32)";
+        return KGPU_UNSUPPORTED_OPERATION;
+    }
+    return model->kind == KGPU_MODEL_HESTON
+               ? kgpu::mlp_run<true>(ctx, model, strike, sign, expiry, settings, fresh_seed, out)
+               : kgpu::mlp_run<false>(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
+}
+
+extern "C" kgpu_status kgpu_mlp_gradients(kgpu_context* ctx, const float* params, const float* samples, int32_t count,
+                                          float* grads, double* loss) {
+    using namespace kgpu;
+    if (!ctx || !params || !samples || !grads || !loss || count < 1) return KGPU_INVALID_INPUT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->error.clear();
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
+    if (!configure_train_kernel()) {
+        ctx->error = "cannot configure the training kernel's shared memory";
+        return KGPU_DEVICE_ERROR;
+    }
+    const int blocks = (count + kRows - 1) / kRows;
+    const size_t bytes = size_t(kParams) * 4 + size_t(count) * 16 + size_t(blocks) * kStride * 4 + 64;
+    if (ctx->mlp_scratch.ensure(bytes)) return KGPU_DEVICE_ERROR;
+    char* base = static_cast<char*>(ctx->mlp_scratch.ptr);
+    float4* dsamples = reinterpret_cast<float4*>(base);
+    float* dpartials = reinterpret_cast<float*>(base + size_t(count) * 16);
+    float* dparams = dpartials + size_t(blocks) * kStride;
+    int* derror = reinterpret_cast<int*>(dparams + kParams);
+    cudaStream_t st = ctx->stream;
+    std::vector<float> part(size_t(blocks) * kStride);
+    int failed = 0;
+    if (cudaMemcpyAsync(dsamples, samples, size_t(count) * 16, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dparams, params, size_t(kParams) * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(derror, 0, sizeof(int), st) != cudaSuccess)
+        return KGPU_DEVICE_ERROR;
+    mlp_grad_kernel<<<blocks, kRows, kTrainSmemBytes, st>>>(dparams, dsamples, 0, count, 1.0f / float(count), dpartials,
+                                                            derror);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(part.data(), dpartials, part.size() * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&failed, derror, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        ctx->error = "training kernel failed";
+        return KGPU_DEVICE_ERROR;
+    }
+    if (failed) {
+        ctx->error = "a tensor-core wait gave up in the training kernel";
+        return KGPU_DEVICE_ERROR;
+    }
+    double l = 0.0;
+    for (int i = 0; i < kParams; ++i) {
+        double g = 0.0;
+        for (int blk = 0; blk < blocks; ++blk) g += part[size_t(blk) * kStride + i];
+        grads[i] = float(g);
+    }
+    for (int blk = 0; blk < blocks; ++blk) l += part[size_t(blk) * kStride + kLossSlot];
+    *loss = l / double(count);
+    return KGPU_OK;
 }

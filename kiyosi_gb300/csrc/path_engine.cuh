@@ -81,6 +81,7 @@ struct ContractT {
     Real knock_in, initial_cash, terminal_base, terminal_plain, terminal_fixed;
     Real downside_lower, downside_upper, downside_initial, final_discount;
     Real knock_out, quantity, daily_quantity, acceleration, log_strike;
+    Real barrier_drift, barrier_distance, barrier_moneyness, rebate, spot, log_discount;
 };
 
 // Device view of the book in the kernel's precision.
@@ -240,6 +241,8 @@ __device__ __forceinline__ double xexp(double x) { return exp(x); }
 __device__ __forceinline__ float xexp(float x) { return __expf(x); }
 __device__ __forceinline__ double xexpm1(double x) { return expm1(x); }
 __device__ __forceinline__ float xexpm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double xlog(double x) { return log(x); }
+__device__ __forceinline__ float xlog(float x) { return __logf(x); }
 __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float xsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double xinf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
@@ -392,6 +395,53 @@ __device__ __forceinline__ Real digital_value(const ContractT<Real>& c, Real z) 
     return c.strike * xexp(exponent);
 }
 
+// Normal (finite, nonzero, not subnormal) test written with comparisons only; NaN fails
+// every comparison.
+__device__ __forceinline__ bool xnormal(double x) {
+    const double a = fabs(x);
+    return a >= 2.2250738585072014e-308 && a <= 1.7976931348623157e308;
+}
+__device__ __forceinline__ bool xnormal(float x) {
+    const float a = fabsf(x);
+    return a >= 1.17549435e-38f && a <= 3.40282347e38f;
+}
+
+// discounted_product(|amount|, signum(amount), log_weight) (numerics.rs:226-238), the
+// `weighted` helper of barrier.rs:328-330.
+template <class Real>
+__device__ __forceinline__ Real weighted_amount(Real amount, Real log_weight) {
+    const Real scale = xabs(amount);
+    const Real weight = amount < Real(0) ? Real(-1) : Real(1);
+    if (scale == Real(0)) return Real(0);
+    const Real discount = xexp(log_weight);
+    const Real value = scale * weight;
+    if (xnormal(discount) && xnormal(value)) return value * discount;
+    return copysign(xexp(xlog(scale) + log_weight), weight);
+}
+
+// Continuously monitored single barrier (barrier.rs:306-452): one terminal draw; the
+// vanilla leg is weighted by the Brownian-bridge survival probability (knock-out) or
+// the hit probability (knock-in), the expiry rebate by the other.
+template <class Real>
+__device__ __forceinline__ Real barrier_value(const ContractT<Real>& c, Real z) {
+    const Real noise = xfma(c.diffusion, z, Real(0));
+    const Real terminal = c.barrier_drift + noise;
+    const Real distance = c.moneyness + noise;
+    const Real payoff = xabs(distance) < Real(0.5) ? c.strike * xexpm1(distance)
+                                                   : weighted_amount(c.spot, terminal) - c.strike;
+    Real intrinsic = c.sign * payoff;
+    intrinsic = intrinsic > Real(0) ? intrinsic : Real(0);
+    const Real to_barrier = c.barrier_moneyness + noise;
+    const bool up = (c.flags & KGPU_C_BARRIER_UP) != 0;
+    const bool in = (c.flags & KGPU_C_BARRIER_IN) != 0;
+    const bool live = up ? to_barrier < Real(0) : to_barrier > Real(0);
+    const Real slope = live ? Real(2) * (xabs(to_barrier) / c.diffusion) / c.diffusion : Real(0);
+    const Real exponent = -c.barrier_distance * slope;
+    const Real survival = live ? xlog(-xexpm1(exponent)) : -xinf(Real(0));
+    return weighted_amount(intrinsic, c.log_discount + (in ? exponent : survival)) +
+           weighted_amount(c.rebate, c.log_discount + (in ? survival : exponent));
+}
+
 template <class Real>
 struct PlanPtrs {
     const StepT<Real>* __restrict__ steps;
@@ -485,6 +535,11 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
     }
     if (payoff == KGPU_PAYOFF_DIGITAL) {
         value = digital_value(c, n.normal());
+        s.executed = 1;
+        return true;
+    }
+    if (payoff == KGPU_PAYOFF_BARRIER) {
+        value = barrier_value(c, n.normal());
         s.executed = 1;
         return true;
     }

@@ -58,6 +58,39 @@ class DigitalOption(EuropeanOption):
     payout: Optional[float] = None  # cash amount; None pays the asset
 
 
+BARRIER_TYPES = ("down_and_out", "down_and_in", "up_and_out", "up_and_in")
+
+
+@dataclass(frozen=True)
+class BarrierOption(EuropeanOption):
+    """Continuously monitored single-barrier vanilla option (BarrierOption with
+    ObservationMode::Continuous, instruments/barrier.rs).  `rebate` is paid at expiry
+    unless `rebate_timing` is 'at_hit' (knock-outs only)."""
+    barrier: float = 0.0
+    barrier_type: str = "down_and_out"
+    rebate: float = 0.0
+    rebate_timing: str = "at_expiry"
+
+    def __post_init__(self):
+        super().__post_init__()
+        if self.barrier_type not in BARRIER_TYPES:
+            raise InvalidInputError(f"barrier_type must be one of {BARRIER_TYPES}")
+        if not (self.barrier > 0.0 and math.isfinite(self.barrier)):
+            raise InvalidInputError("barrier must be positive and finite")
+        if not (self.rebate >= 0.0 and math.isfinite(self.rebate)):
+            raise InvalidInputError("rebate must be nonnegative and finite")
+        if self.rebate_timing not in ("at_expiry", "at_hit"):
+            raise InvalidInputError("rebate_timing must be 'at_expiry' or 'at_hit'")
+
+    @property
+    def is_up(self) -> bool:
+        return self.barrier_type.startswith("up")
+
+    @property
+    def is_knock_in(self) -> bool:
+        return self.barrier_type.endswith("_in")
+
+
 @dataclass(frozen=True)
 class AsianOption:
     """Arithmetic average-price option on the spots at `fixings` (years)."""

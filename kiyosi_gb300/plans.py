@@ -20,9 +20,9 @@ from typing import List, Optional
 import numpy as np
 
 from . import abi
-from .errors import ComputationFailureError, InvalidInputError
-from .instruments import (Accumulator, AsianOption, AutocallableNote, DigitalOption,
-                          EuropeanOption)
+from .errors import UnsupportedOperationError, ComputationFailureError, InvalidInputError
+from .instruments import (Accumulator, AsianOption, AutocallableNote, BarrierOption,
+                          DigitalOption, EuropeanOption)
 from .market import (BlackScholesMertonParameters, HestonParameters, LocalVolatilitySurface,
                      PricingContext, discounted_product, log_ratio, safe_log_returns)
 
@@ -159,6 +159,59 @@ def digital(option: DigitalOption, ctx: PricingContext):
     c["step_count"] = 1
     steps = np.zeros(1, STEP_DTYPE)
     steps[0] = (drift, width, 0.0, math.exp(-rate * time))
+    return ContractPlan(c, steps, np.zeros(1, np.uint8))
+
+
+def barrier(option: BarrierOption, ctx: PricingContext):
+    """MonteCarloBarrierEngine::native for continuous monitoring (barrier.rs:231-452):
+    one terminal draw per path with Brownian-bridge survival.  Barriers already touched
+    at valuation resolve before sampling (analytic/barrier.rs:32-66): a knock-out pays
+    its rebate, a knock-in is the vanilla option."""
+    model = ctx.model
+    if not isinstance(model, BlackScholesMertonParameters):
+        raise UnsupportedOperationError("the Monte Carlo barrier engine requires BSM parameters")
+    rate, dividend, sigma = model.rate, model.dividend, model.volatility
+    spot, level, time = ctx.spot, option.barrier, option.expiry
+    up, knock_in = option.is_up, option.is_knock_in
+    at_hit = option.rebate_timing == "at_hit"
+    touched = spot >= level if up else spot <= level
+    expiry_rebate = option.rebate * math.exp(-rate * time)
+    if touched:
+        if knock_in:
+            return european(EuropeanOption(option.option_type, option.strike, time), ctx)
+        return Known(option.rebate if at_hit else expiry_rebate)
+    if time == 0.0:
+        return Known(option.rebate if knock_in else max(option.sign * (spot - option.strike), 0.0))
+    if sigma == 0.0:
+        raise UnsupportedOperationError("zero volatility: the barrier is deterministic")
+    if at_hit and not knock_in and option.rebate != 0.0:
+        raise UnsupportedOperationError("at-hit rebates of knock-out barriers are not sampled")
+    carry_rate = rate - dividend
+    half_variance_rate = 0.5 * sigma * sigma
+    drift = carry_rate - half_variance_rate
+    width = sigma * math.sqrt(time)
+    mean = drift * time
+    if not (width > 0.0 and math.isfinite(width) and math.isfinite(mean)):
+        raise _unstable()
+
+    def mean_distance(lvl):
+        return (log_ratio(spot, lvl) + carry_rate * time) - half_variance_rate * time
+
+    c = _new_contract(abi.PAYOFF_BARRIER)
+    c["flags"] = (abi.C_BARRIER_UP if up else 0) | (abi.C_BARRIER_IN if knock_in else 0)
+    c["strike"] = option.strike
+    c["sign"] = option.sign
+    c["diffusion"] = width
+    c["moneyness"] = mean_distance(option.strike)
+    c["barrier_drift"] = mean
+    c["barrier_distance"] = abs(log_ratio(level, spot))
+    c["barrier_moneyness"] = mean_distance(level)
+    c["rebate"] = option.rebate
+    c["spot"] = spot
+    c["log_discount"] = -rate * time
+    c["step_count"] = 1
+    steps = np.zeros(1, STEP_DTYPE)
+    steps[0] = (mean, width, 0.0, math.exp(-rate * time))
     return ContractPlan(c, steps, np.zeros(1, np.uint8))
 
 

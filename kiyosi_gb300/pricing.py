@@ -16,7 +16,7 @@ from . import abi, plans
 from ._native import context
 from .errors import InvalidInputError, UnsupportedOperationError
 from .instruments import (Accumulator, AmericanOption, AsianOption, AutocallableNote,
-                          DigitalOption, EuropeanOption)
+                          BarrierOption, DigitalOption, EuropeanOption)
 from .market import PricingContext
 
 PSEUDO_RANDOM = "pseudo_random"
@@ -248,3 +248,15 @@ class MonteCarloAccumulatorEngine(_MonteCarloEngine):
 class MonteCarloDigitalEngine(_MonteCarloEngine):
     def price_with_statistics(self, option: DigitalOption, ctx: PricingContext):
         return self._run(ctx, [plans.digital(option, ctx)])[0]
+
+
+class MonteCarloBarrierEngine(_MonteCarloEngine):
+    """Continuously monitored single barriers (barrier.rs): one terminal draw per path,
+    weighted by the Brownian-bridge survival or hit probability."""
+
+    def price_with_statistics(self, option: BarrierOption, ctx: PricingContext):
+        return self._run(ctx, [plans.barrier(option, ctx)])[0]
+
+    def price_strikes(self, option: BarrierOption, ctx: PricingContext, strikes: Sequence[float]):
+        opts = [replace(option, strike=float(k)) for k in strikes]
+        return [e.price for e in self._run(ctx, [plans.barrier(o, ctx) for o in opts])]

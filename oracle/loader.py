@@ -27,7 +27,7 @@ def load():
             return _LIB
         path = os.path.join(HERE, "liboracle.so")
         sources = [os.path.join(HERE, f) for f in ("oracle.cpp", "lsmc.cpp", "oracle_core.h",
-                                                  "heston_adi.cpp", "Makefile")]
+                                                  "heston_adi.cpp", "mlp.cpp", "Makefile")]
         sources.append(os.path.join(HERE, "..", "include", "kgpu.h"))
         newest = max(os.path.getmtime(s) for s in sources if os.path.exists(s))
         if not os.path.exists(path) or os.path.getmtime(path) < newest:
@@ -60,6 +60,9 @@ def load():
                                                     C.c_double, C.c_int, C.c_int, C.c_int,
                                                     C.c_int]
             lib.kor_heston_adi_american.restype = C.c_double
+        lib.kor_mlp_gradients.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int,
+                                          P(C.c_double)]
+        lib.kor_mlp_gradients.restype = C.c_double
         _LIB = lib
         return lib
 
@@ -100,3 +103,16 @@ def sobol_points(seed, dims, dim, first, count):
                          bits.ctypes.data_as(C.POINTER(C.c_uint64)),
                          normals.ctypes.data_as(C.POINTER(C.c_double)))
     return bits, normals
+
+
+def mlp_gradients(params, samples, bf16_operands=True):
+    """Loss and gradients of the LSMC continuation network on a batch (float32 inputs:
+    params[4481], samples[n][4] = (x0, x1, x2, target))."""
+    lib = load()
+    params = np.ascontiguousarray(params, np.float32)
+    samples = np.ascontiguousarray(samples, np.float32)
+    grads = np.zeros(params.size, np.float64)
+    loss = lib.kor_mlp_gradients(params.ctypes.data_as(C.POINTER(C.c_float)),
+                                 samples.ctypes.data_as(C.POINTER(C.c_float)), len(samples),
+                                 int(bf16_operands), grads.ctypes.data_as(C.POINTER(C.c_double)))
+    return loss, grads

@@ -282,6 +282,34 @@ static double digital_payoff(const kgpu_contract* c, double z) {
     return discounted_product(c->strike, 1.0, exponent);
 }
 
+// The `weighted` helper of the barrier sampler (barrier.rs:328-330):
+// scaled_value(|amount|, signum(amount), log_weight).
+static double weighted(double amount, double log_weight) {
+    return discounted_product(std::fabs(amount), std::signbit(amount) ? -1.0 : 1.0, log_weight);
+}
+
+// Continuously monitored single barrier (barrier.rs:306-452), one terminal draw.
+static double barrier_payoff(const kgpu_contract* c, double z, Failure& f) {
+    const double noise = std::fma(c->diffusion, z, 0.0);
+    const double terminal = c->barrier_drift + noise;
+    const double asset = discounted_product(c->spot, 1.0, terminal);
+    if (!std::isfinite(asset)) f.failed = true;
+    const double distance = c->moneyness + noise;
+    const double payoff = std::fabs(distance) < 0.5 ? c->strike * std::expm1(distance) : asset - c->strike;
+    const double intrinsic = std::max(c->sign * payoff, 0.0);
+    const double to_barrier = c->barrier_moneyness + noise;
+    const bool up = c->flags & KGPU_C_BARRIER_UP;
+    const bool in = c->flags & KGPU_C_BARRIER_IN;
+    const bool live = up ? to_barrier < 0.0 : to_barrier > 0.0;
+    const double slope = live ? 2.0 * (std::fabs(to_barrier) / c->diffusion) / c->diffusion : 0.0;
+    const double exponent = -c->barrier_distance * slope;
+    const double survival = live ? std::log(-std::expm1(exponent)) : -INFINITY;
+    const double value = weighted(intrinsic, c->log_discount + (in ? exponent : survival)) +
+                         weighted(c->rebate, c->log_discount + (in ? survival : exponent));
+    if (!std::isfinite(value)) f.failed = true;
+    return value;
+}
+
 // AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
 static inline double autocallable_terminal(const kgpu_contract* c, double spot, bool knocked_in) {
     if (knocked_in) {
@@ -409,8 +437,12 @@ static double accumulator_path(const Plan& p, const Model& model, PathNormals& n
     return quantity * unit(s.lr) * c->final_discount;
 }
 
+static bool terminal_payoff(const kgpu_contract* c) {
+    return c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL || c->payoff == KGPU_PAYOFF_BARRIER;
+}
+
 static int dimensions_of(const kgpu_contract* c, const Model& model) {
-    if (c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL) return 1;
+    if (terminal_payoff(c)) return 1;
     return c->step_count * model.normals_per_step();
 }
 
@@ -421,6 +453,8 @@ static double evaluate(const Plan& p, const Model& model, PathNormals& n, Failur
             return european_payoff(c, n.normal(), f);
         case KGPU_PAYOFF_DIGITAL:
             return digital_payoff(c, n.normal());
+        case KGPU_PAYOFF_BARRIER:
+            return barrier_payoff(c, n.normal(), f);
         case KGPU_PAYOFF_VANILLA_PATH:
             return path_vanilla(p, model, n, false);
         case KGPU_PAYOFF_ASIAN:
@@ -536,8 +570,7 @@ static int price_contract(const Model& model, const Plan& p, const kgpu_settings
                                            double(var.count)),
                                  log_discount)
             : 0.0;
-    int grid = (c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL) ? 1
-                                                                                        : c->step_count;
+    int grid = terminal_payoff(c) ? 1 : c->step_count;
     out->path_steps = double(paths) * double(grid);
     out->executed_steps = double(executed) / double(model.normals_per_step());
     return KGPU_OK;

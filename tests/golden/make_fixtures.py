@@ -4,7 +4,8 @@ calibration records (benchmarks/quantlib/calibration/*.json, produced by the kiy
 
 Run in a checkout that has the reference mounted:
     python tests/golden/make_fixtures.py /path/to/kiyosi
-Writes european_calibration.json, american_calibration.json and known_answers.json here.
+Writes european_calibration.json, barrier_calibration.json, american_calibration.json
+and known_answers.json here.
 """
 import ast
 import json
@@ -41,6 +42,25 @@ def main(root):
                          + mc["libraries"]["kiyosi"]["version"] + ")",
                "inputs": inputs, "samples": rows},
               open(os.path.join(HERE, "european_calibration.json"), "w"), indent=1)
+    # Continuously monitored barriers of the same calibration (one terminal draw).
+    cases = {c["id"]: c for c in json.load(open(os.path.join(root, "benchmarks", "quantlib", "cases",
+                                                             "monte_carlo.json")))["cases"]}
+    brows = []
+    for e in mc["experiments"]:
+        if e["backend"] != "kiyosi" or e["id"] not in ("mc-barrier-down-out-call", "mc-barrier-up-in-put"):
+            continue
+        ens = _parse(e["seed_ensemble"])
+        for s in ens["samples"]:
+            brows.append({"id": e["id"], "seed": s["seed"], "path_count": s["profile"]["path_count"],
+                          "price": s["price"]})
+        prof = _parse(e["profile"])
+        brows.append({"id": e["id"], "seed": prof["seed"], "path_count": prof["path_count"],
+                      "price": _parse(e["timing_seed_accuracy"])["price"]})
+    binputs = {k: cases[k]["inputs"] for k in ("mc-barrier-down-out-call", "mc-barrier-up-in-put")}
+    json.dump({"source": "benchmarks/quantlib/calibration/monte_carlo.json (kiyosi "
+                         + mc["libraries"]["kiyosi"]["version"] + ")",
+               "inputs": binputs, "samples": brows},
+              open(os.path.join(HERE, "barrier_calibration.json"), "w"), indent=1)
     am = json.load(open(os.path.join(cal, "american_monte_carlo.json")))
     arows = []
     for e in am["experiments"]:
@@ -69,7 +89,8 @@ def main(root):
                               "inputs": prov.get("inputs") if isinstance(prov, dict) else None}
     json.dump({"source": "benchmarks/quantlib/references/*.json", "values": known},
               open(os.path.join(HERE, "known_answers.json"), "w"), indent=1)
-    print(len(rows), "European rows,", len(arows), "American rows,", len(known), "known answers")
+    print(len(rows), "European rows,", len(brows), "barrier rows,", len(arows), "American rows,",
+          len(known), "known answers")
 
 
 if __name__ == "__main__":
