@@ -29,6 +29,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -348,6 +350,24 @@ def run_kernel_only(args):
     """Device-resident pricings of one arm only, for ncu captures of the kernels."""
     from kiyosi_gb300 import _native, abi
     native = _native.context(0)
+    if args.kernel_only.startswith("lsmc"):
+        from kiyosi_gb300 import workloads
+        ctx = workloads.heston_context()
+        model = ctx.kgpu_model()
+        basis = abi.BASIS_MLP if args.kernel_only == "lsmc-mlp" else abi.BASIS_POLY3
+        s = abi.LsmcSettings(path_count=args.paths, exercise_dates=args.dates, substeps=5,
+                             basis=basis, sampling=0, precision=abi.PRECISION_FP32, mlp_epochs=5,
+                             mlp_batch=8192, mlp_hidden=64, mlp_learning_rate=1e-3, seed=42,
+                             mlp_seed=7)
+        out = abi.LsmcResult()
+        for _ in range(args.warmup + args.steps):
+            native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0,
+                                                    1.0, C.byref(s), 43, C.byref(out)))
+        print(json.dumps({"arm": args.kernel_only, "paths": args.paths, "dates": args.dates,
+                          "price": out.price, "out_of_sample": out.out_of_sample,
+                          "wall_ms": out.wall_ms, "path_store_ms": out.path_store_ms,
+                          "regression_ms": out.regression_ms, "launches": native.last_launches}))
+        return
     ctx, packed = packed_plan()
     model = ctx.kgpu_model()
     book = packed.struct()
@@ -361,6 +381,175 @@ def run_kernel_only(args):
     print(json.dumps({"arm": args.kernel_only, "paths": args.paths, "price": out[0].price,
                       "executed_steps": out[0].executed_steps, "kernel_ms": native.last_kernel_ms,
                       "path_kernel_ms": native.last_path_kernel_ms}))
+
+
+def _host_pricing(native, ctx, packed, s):
+    """kgpu_price_book from host buffers: estimates, device time of the call's kernels,
+    of its path kernels alone, and the host wall time."""
+    from kiyosi_gb300 import abi
+    n = len(packed.contracts)
+    out = (abi.Estimate * n)()
+    model = ctx.kgpu_model()
+    book = packed.struct()
+    t0 = time.perf_counter()
+    native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book),
+                                            C.byref(s), out, None))
+    wall = time.perf_counter() - t0
+    return ([abi.Estimate.from_buffer_copy(e) for e in out], native.last_kernel_ms,
+            native.last_path_kernel_ms, wall)
+
+
+def _first(packed, n):
+    """The first n contracts of a packed book (the arrays they index stay shared)."""
+    return type(packed)(packed.contracts[:n].copy(), packed.steps, packed.flags, packed.events,
+                        packed.intervals, packed.daily)
+
+
+def _workload(name):
+    """(description, context, packed book, per-contract paths, sampling) of a named
+    benchmark configuration."""
+    from kiyosi_gb300 import plans, workloads
+    from kiyosi_gb300.market import PricingContext
+    b = plans.BookBuilder()
+    if name == "european":
+        ctx, opt = workloads.european()
+        b.add(plans.path_vanilla(opt, ctx, 252))
+        return ("European call, BSM, 2^16 PCG32 paths x 252 daily log-Euler steps", ctx,
+                b.build(), [1 << 16], 0)
+    if name == "heston-asian":
+        ctx = workloads.heston_context()
+        b.add(plans.asian(workloads.heston_asian_c3(), ctx))
+        return ("Heston arithmetic-average Asian call, 2^22 PCG32 paths x 252 full-truncation "
+                "Euler steps", ctx, b.build(), [1 << 22], 0)
+    if name == "lv-book":
+        ctx = PricingContext(workloads.lv_surface(), 100.0)
+        notes, paths = workloads.lv_book(4096)
+        for n in notes:
+            b.add(plans.autocallable(n, ctx))
+        return ("book of 4096 snowball/phoenix notes under local volatility (50x20 surface), "
+                "3-36 monthly observations, daily steps, 2^14-2^18 paths per note", ctx,
+                b.build(paths), paths, 0)
+    raise ValueError(name)
+
+
+def run_workload(args, name):
+    """One of the other benchmark configurations: FP32 persistent (one launch for the
+    whole book) against the FP64 plain path, with parity in standard errors."""
+    from kiyosi_gb300 import _native, abi
+    from oracle import loader
+    native = _native.context(0)
+    desc, ctx, packed, paths, sampling = _workload(name)
+    seed = 42 if name != "lv-book" else 7
+    s32 = abi.Settings(path_count=paths[0], sampling=sampling, antithetic=0,
+                       precision=abi.PRECISION_FP32, schedule=abi.SCHEDULE_PERSISTENT, seed=seed,
+                       **TUNING)
+    s64 = abi.Settings(path_count=paths[0], sampling=sampling, antithetic=0,
+                       precision=abi.PRECISION_FP64, schedule=abi.SCHEDULE_PLAIN, seed=seed)
+    for _ in range(args.warmup):
+        _host_pricing(native, ctx, packed, s32)
+    kernel, path, walls, launches = [], [], [], 0
+    with Clocks() as clocks:
+        for _ in range(args.steps):
+            est32, k, pk, w = _host_pricing(native, ctx, packed, s32)
+            kernel.append(k)
+            path.append(pk)
+            walls.append(w)
+            launches += native.last_launches
+    path_steps = sum(e.path_steps for e in est32)
+    # FP64 plain, one launch per contract: the whole book, or its first 128 notes for the
+    # local-volatility book (the FP64 path would take minutes on all 4096).
+    fp64_n = min(len(est32), 128)
+    est64, k64, _, _ = _host_pricing(native, ctx, _first(packed, fp64_n), s64)
+    fp64_path_steps = sum(e.path_steps for e in est64)
+    worst = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(est32, est64))
+    # CPU oracle on a bounded sample: the first contracts at up to 2^13 paths.
+    sample_n = min(len(est32), 16)
+    sub = _first(packed, sample_n)
+    sub.contracts["path_count"] = np.minimum(np.where(sub.contracts["path_count"] > 0,
+                                                      sub.contracts["path_count"], paths[0]), 1 << 13)
+    s_cpu = abi.Settings(path_count=min(paths[0], 1 << 13), sampling=sampling, antithetic=0,
+                         precision=abi.PRECISION_FP64, schedule=abi.SCHEDULE_PLAIN, seed=seed)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cpu = loader.price_book(ctx, sub, s_cpu, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    ms = statistics.median(kernel)
+    line = {
+        "metric": "path-steps/s (FP32 batched vs FP64 plain) at <=0.5 SE",
+        "value": path_steps / (ms / 1e3), "unit": "path-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded draws; benchmark contract parameters)",
+        "config": {"workload": desc, "contracts": len(est32), "sampling": "pcg32",
+                   "precision": "fp32", "schedule": "persistent",
+                   "l2": "inputs and per-path values exceed L2 (no flush)"},
+        "e2e": {"value": path_steps / statistics.median(walls), "unit": "path-steps/s",
+                "h2d_bytes_per_step": int(packed.steps.nbytes + packed.flags.nbytes
+                                          + packed.events.nbytes + packed.contracts.nbytes),
+                "d2h_bytes_per_step": int(len(est32) * C.sizeof(abi.Estimate))},
+        "gpu_launches": launches, "clocks": clocks.summary(),
+        "path_kernel_ms": statistics.median(path),
+        "fp64_plain": {"value": fp64_path_steps / (k64 / 1e3), "unit": "path-steps/s",
+                       "ms": k64, "contracts": fp64_n,
+                       "speedup_fp32_persistent": (path_steps / (ms / 1e3)) / (fp64_path_steps / (k64 / 1e3))},
+        "parity": {"max_fp32_vs_fp64_in_se": worst, "contracts": fp64_n},
+        "executed_steps_per_path_step": sum(e.executed_steps for e in est32) / path_steps,
+        "cpu_baseline": {"value": sum(e.path_steps for e in cpu) / cpu_s,
+                         "unit": "path-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample_n} contracts at up to 2^13 paths, FP64 oracle"},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_lsmc(args):
+    """American put under Heston (2^20 paths, 50 exercise dates, 5 Euler substeps): the
+    polynomial LSMC against the polynomial plus the fitted network, both judged by the
+    Heston ADI price; the polynomial is also run at the network's wall time."""
+    from kiyosi_gb300 import _native, abi, workloads
+    from oracle import loader
+    native = _native.context(0)
+    ctx = workloads.heston_context()
+    model = ctx.kgpu_model()
+    t0 = time.perf_counter()
+    adi = loader.load().kor_heston_adi_american(C.byref(model), 100.0, -1.0, 1.0, 400, 100, 400, 1)
+    adi_s = time.perf_counter() - t0
+
+    def price(basis, paths, precision=abi.PRECISION_FP32):
+        s = abi.LsmcSettings(path_count=paths, exercise_dates=50, substeps=5, basis=basis,
+                             sampling=0, precision=precision, mlp_epochs=5, mlp_batch=8192,
+                             mlp_hidden=64, mlp_learning_rate=1e-3, seed=42, mlp_seed=7)
+        out = abi.LsmcResult()
+        for _ in range(max(1, args.warmup // 3)):
+            native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0,
+                                                    1.0, C.byref(s), 43, C.byref(out)))
+        native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0, 1.0,
+                                                C.byref(s), 43, C.byref(out)))
+        return {"paths": paths, "price": out.price, "standard_error": out.standard_error,
+                "out_of_sample": out.out_of_sample,
+                "out_of_sample_error": out.out_of_sample_error,
+                "error_vs_adi": out.price - adi, "out_of_sample_error_vs_adi": out.out_of_sample - adi,
+                "wall_ms": out.wall_ms, "path_store_ms": out.path_store_ms,
+                "regression_ms": out.regression_ms}
+
+    poly = price(abi.BASIS_POLY3, 1 << 20)
+    poly64 = price(abi.BASIS_POLY3, 1 << 20, abi.PRECISION_FP64)
+    mlp = price(abi.BASIS_MLP, 1 << 20)
+    scale = max(1, int(round(math.log2(max(1.0, mlp["wall_ms"] / poly["wall_ms"])))))
+    equal = price(abi.BASIS_POLY3, 1 << min(26, 20 + scale))
+    line = {
+        "metric": "LSMC |price - ADI|: polynomial + fitted network vs polynomial at equal wall time",
+        "value": abs(mlp["out_of_sample_error_vs_adi"]), "unit": "price units (out-of-sample)",
+        "higher_is_better": False, "n_gpus": 1, "dtype": "f32 paths, bf16 network, f64 solve",
+        "data": "synthetic (seeded PCG32 draws; benchmark model parameters)",
+        "config": {"workload": "American put under Heston (S0=K=100, v0=theta=0.04, kappa=2, "
+                               "xi=0.5, rho=-0.7, r=0.03, T=1), 2^20 paths, 50 exercise dates "
+                               "x 5 Euler substeps; network 3-64-64-1, 5 epochs/date, batch 8192",
+                   "fresh_paths_seed": 43},
+        "adi": {"price": adi, "grid": "400 x 100 x 400 (MCS, Ikonen-Toivanen)", "cpu_s": adi_s},
+        "poly3_fp32": poly, "poly3_fp64": poly64, "poly3_plus_network": mlp,
+        "poly3_at_equal_wall_time": equal,
+    }
+    print(json.dumps(line), flush=True)
 
 
 def run_reference(args):
@@ -410,13 +599,25 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--paths", type=int, default=PATHS,
                     help="path count (profiling runs use smaller cases)")
-    ap.add_argument("--kernel-only", choices=["fp32", "fp64"],
+    ap.add_argument("--dates", type=int, default=50, help="LSMC exercise dates (profiling runs)")
+    ap.add_argument("--kernel-only", choices=["fp32", "fp64", "lsmc-poly", "lsmc-mlp"],
                     help="run only the device-resident pricing of one arm (for profilers)")
     ap.add_argument("--tile", type=int, default=0, help="persistent tile paths (0 = default)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")
     ap.add_argument("--refill", type=int, default=0, help="units between lane refills (0 = 16)")
+    ap.add_argument("--workload", default="snowball",
+                    choices=["snowball", "european", "heston-asian", "lv-book", "lsmc", "all"],
+                    help="benchmark configuration (default: the snowball headline)")
     args = ap.parse_args()
     TUNING.update(tile_paths=args.tile, ctas_per_sm=args.ctas_per_sm, refill=args.refill)
+    if args.workload != "snowball" and args.impl == "ours" and not args.kernel_only:
+        names = ["european", "heston-asian", "lv-book", "lsmc"] if args.workload == "all" else [args.workload]
+        for name in names:
+            if name == "lsmc":
+                run_lsmc(args)
+            else:
+                run_workload(args, name)
+        return
     if args.kernel_only:
         run_kernel_only(args)
         return

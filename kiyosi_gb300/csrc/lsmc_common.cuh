@@ -105,10 +105,14 @@ __global__ void lsmc_solve(const double* partials, int blocks, int max_degree, d
     constexpr int T = TWO ? 10 : 3;
     constexpr int S = sum_count(T);
     __shared__ double sums[S];
-    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+    // One warp per sum: lanes stride over the block partials, then a fixed shuffle tree
+    // (deterministic, and short enough that the solve is not latency-bound on it).
+    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (int j = threadIdx.x >> 5; j < S; j += warps) {
         double v = 0.0;
-        for (int blk = 0; blk < blocks; ++blk) v += partials[size_t(blk) * S + j];
-        sums[j] = v;
+        for (int blk = lane; blk < blocks; blk += 32) v += partials[size_t(blk) * S + j];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) sums[j] = v;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;

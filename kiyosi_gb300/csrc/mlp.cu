@@ -37,6 +37,7 @@ namespace {
 
 constexpr int kHidden = 64;
 constexpr int kRows = 128;  // samples per training CTA (the MMA's M)
+constexpr int kThreadsTrain = 256;  // two threads per sample, one per half of the hidden units
 // Parameter vector: W1[64][3], b1[64], W2[64][64] (row = output unit), b2[64], w3[64], b3.
 constexpr int kPW1 = 0, kPB1 = 192, kPW2 = 256, kPB2 = 4352, kPW3 = 4416, kPB3 = 4480;
 constexpr int kParams = 4481;
@@ -53,7 +54,9 @@ struct __align__(1024) TrainSmem {
     __nv_bfloat16 w2f[kHidden * kHidden];    // B forward: outputs x inputs
     __nv_bfloat16 w2b[kHidden * kHidden];    // B backward: inputs x outputs
     float w1[3 * kHidden], b1[kHidden], b2[kHidden], w3[kHidden];
-    float red[4][256];
+    float red[8][128];   // per-warp partial sums of half_sum
+    float tot[2][128];   // per-half totals of half_sum
+    float xch[256];      // output halves exchanged between the two threads of a row
     uint64_t bar;
     uint32_t tmem;
     int failed;
@@ -83,30 +86,11 @@ __device__ __forceinline__ void warp_transpose_sum(float* v, int lane) {
     }
 }
 
-// Reduces 128 per-thread values over the CTA's 128 threads; returns total t to thread t.
-__device__ __forceinline__ float cta_sum128(TrainSmem& s, float* v) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    warp_transpose_sum<128>(v, lane);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) s.red[warp][4 * lane + i] = v[i];
-    __syncthreads();
+// Prepares a training CTA: tensor memory, the completion barrier and the zero rows of
+// the weight-gradient operand (rows 64..127 of dz2t stay zero across steps).
+__device__ __forceinline__ void train_setup(TrainSmem& s) {
     const int t = threadIdx.x;
-    const float out = ((s.red[0][t] + s.red[1][t]) + s.red[2][t]) + s.red[3][t];
-    __syncthreads();
-    return out;
-}
-
-// One batch's gradient partials: CTA b covers samples [first + 128 b, first + 128 b + 128)
-// of the batch [first, first + count); partials[b] receives the CTA's gradient of
-// (1 / count) sum (f(x) - y)^2 and its sum of squared residuals.
-__global__ void __launch_bounds__(kRows, 1) mlp_grad_kernel(const float* __restrict__ params,
-                                                            const float4* __restrict__ samples, int first,
-                                                            int count, float inv_count, float* __restrict__ partials,
-                                                            int* __restrict__ error) {
-    extern __shared__ unsigned char smem_raw[];
-    TrainSmem& s = *reinterpret_cast<TrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const int t = threadIdx.x, warp = t >> 5;
-    if (warp == 0) {
+    if ((t >> 5) == 0) {
         tc::tmem_alloc(&s.tmem, kTmemColumns);
         tc::tmem_relinquish();
     }
@@ -114,35 +98,87 @@ __global__ void __launch_bounds__(kRows, 1) mlp_grad_kernel(const float* __restr
         tc::mbar_init(&s.bar, 1);
         s.failed = 0;
     }
-    for (int i = t; i < 3 * kHidden; i += kRows) s.w1[i] = params[kPW1 + i];
-    if (t < kHidden) {
-        s.b1[t] = params[kPB1 + t];
-        s.b2[t] = params[kPB2 + t];
-        s.w3[t] = params[kPW3 + t];
-    }
-    const float b3 = params[kPB3];
-    for (int i = t; i < kHidden * kHidden; i += kRows) {
-        const int o = i >> 6, in = i & 63;
-        const __nv_bfloat16 w = __float2bfloat16_rn(params[kPW2 + i]);
-        s.w2f[tc::kmajor(o, in, kHidden)] = w;
-        s.w2b[tc::kmajor(in, o, kHidden)] = w;
-    }
     const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
-    for (int i = t; i < kHidden * kRows; i += kRows) s.dz2t[kHidden * kRows + i] = zero;  // rows 64..127
-    const int local = blockIdx.x * kRows + t;
+    for (int i = t; i < kHidden * kRows; i += kThreadsTrain) s.dz2t[kHidden * kRows + i] = zero;
+}
+
+__device__ __forceinline__ void train_release(TrainSmem& s) {
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(s.tmem, kTmemColumns);
+}
+
+// Reduces, over the CTA's 128 rows, per-thread vectors of N values that belong to the
+// thread's column half: on return red[h][k] (h = half, k < N) holds the total of index k.
+// Threads t and t + 128 own the same row; the two halves are reduced separately.
+template <int N>
+__device__ __forceinline__ void half_sum(TrainSmem& s, float* v) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    warp_transpose_sum<N>(v, lane);
+#pragma unroll
+    for (int i = 0; i < N / 32; ++i) s.red[warp][(N / 32) * lane + i] = v[i];
+    __syncthreads();
+    for (int q = threadIdx.x; q < 2 * N; q += kThreadsTrain) {
+        const int h = q / N, k = q % N, w0 = 4 * h;
+        s.tot[h][k] = ((s.red[w0][k] + s.red[w0 + 1][k]) + s.red[w0 + 2][k]) + s.red[w0 + 3][k];
+    }
+    __syncthreads();
+}
+
+// One batch's gradient partial of this CTA: it covers samples
+// [first + 128 blockIdx.x, first + 128 blockIdx.x + 128) of the batch [first, first + count)
+// and writes to `partial` (element stride `pstride`) its share of the gradient of
+// (1 / count) sum (f(x) - y)^2 and its sum of squared residuals.  Thread t owns row
+// t % 128 and hidden units [32 h, 32 h + 32) with h = t / 128; warps w and w + 4 read the
+// same tensor-memory lanes, one column half each.  `phase` is the completion barrier's
+// next parity (two completions per step).  Returns false, on every thread, when a
+// tensor-core wait gave up.
+__device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const uint4* __restrict__ w2_tiles,
+                          const float4* __restrict__ samples, int first, int count, float inv_count,
+                          float* __restrict__ partial, int pstride, uint32_t& phase) {
+    const int t = threadIdx.x, warp = t >> 5;
+    const int row = t & (kRows - 1), half = t >> 7, j0 = 32 * half;
+    // Parameters are read past L1 (ld.global.cg): the persistent trainer rewrites them
+    // from other SMs between steps.
+    for (int i = t; i < 3 * kHidden; i += kThreadsTrain) s.w1[i] = __ldcg(params + kPW1 + i);
+    if (t < kHidden) {
+        s.b1[t] = __ldcg(params + kPB1 + t);
+        s.b2[t] = __ldcg(params + kPB2 + t);
+        s.w3[t] = __ldcg(params + kPW3 + t);
+    }
+    const float b3 = __ldcg(params + kPB3);
+    if (w2_tiles) {
+        // Both BF16 operand tiles of W2, already in shared-memory order (16 KB).
+        uint4* dst = reinterpret_cast<uint4*>(s.w2f);  // w2f and w2b are contiguous
+        for (int i = t; i < 2 * kHidden * kHidden / 8; i += kThreadsTrain) dst[i] = __ldcg(w2_tiles + i);
+    } else {
+        for (int i = t; i < kHidden * kHidden; i += kThreadsTrain) {
+            const int o = i >> 6, in = i & 63;
+            const __nv_bfloat16 w = __float2bfloat16_rn(__ldcg(params + kPW2 + i));
+            s.w2f[tc::kmajor(o, in, kHidden)] = w;
+            s.w2b[tc::kmajor(in, o, kHidden)] = w;
+        }
+    }
+    const int local = blockIdx.x * kRows + row;
     const bool valid = local < count;
     const float4 x = valid ? samples[first + local] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
 
-    // Layer 1 on the CUDA cores; H1 goes to shared memory in both operand layouts.
-    uint64_t mask1 = 0;
-#pragma unroll 8
-    for (int j = 0; j < kHidden; ++j) {
-        const float z = fmaf(s.w1[3 * j], x.x, fmaf(s.w1[3 * j + 1], x.y, fmaf(s.w1[3 * j + 2], x.z, s.b1[j])));
-        if (z > 0.f) mask1 |= 1ull << j;
-        const __nv_bfloat16 h = __float2bfloat16_rn(valid && z > 0.f ? z : 0.f);
-        s.h1[tc::kmajor(t, j, kHidden)] = h;
-        s.h1t[tc::kmajor(j, t, kRows)] = h;
+    // Layer 1 on the CUDA cores for this thread's 32 units; H1 goes to shared memory in
+    // both operand layouts (8 consecutive units of a row are one 16-byte store).
+    uint32_t mask1 = 0;
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        __align__(16) __nv_bfloat16 pack[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int j = j0 + 8 * g + u;
+            const float z = fmaf(s.w1[3 * j], x.x, fmaf(s.w1[3 * j + 1], x.y, fmaf(s.w1[3 * j + 2], x.z, s.b1[j])));
+            if (z > 0.f) mask1 |= 1u << (8 * g + u);
+            pack[u] = __float2bfloat16_rn(valid && z > 0.f ? z : 0.f);
+            s.h1t[tc::kmajor(j, row, kRows)] = pack[u];
+        }
+        *reinterpret_cast<uint4*>(&s.h1[tc::kmajor(row, j0 + 8 * g, kHidden)]) = *reinterpret_cast<const uint4*>(pack);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -157,119 +193,135 @@ __global__ void __launch_bounds__(kRows, 1) mlp_grad_kernel(const float* __restr
                          idesc, k > 0);
         tc::mma_commit(&s.bar);
     }
-    bool ok = tc::mbar_wait(&s.bar, 0);
-    if (__syncthreads_or(!ok)) {
-        if (t == 0) atomicExch(error, 1);
-        goto release;
-    }
+    bool ok = tc::mbar_wait(&s.bar, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) return false;
     tc::fence_after_sync();
-    {
-        // Z2 of this thread's sample (TMEM lane = row = thread).
-        float z2[kHidden];
-        const uint32_t lane_base = uint32_t(warp * 32) << 16;
-        tc::tmem_load32(tmem + lane_base, z2);
-        tc::tmem_load32(tmem + lane_base + 32, z2 + 32);
-        float out = b3;
+    // Z2 of this row's 32 units (TMEM lane = row).
+    const uint32_t lane_base = uint32_t((warp & 3) * 32) << 16;
+    float z2[32];
+    tc::tmem_load32(tmem + lane_base + j0, z2);
+    float out = 0.f;
 #pragma unroll
-        for (int j = 0; j < kHidden; ++j) {
-            z2[j] += s.b2[j];
-            out = fmaf(z2[j] > 0.f ? z2[j] : 0.f, s.w3[j], out);
-        }
-        const float res = valid ? out - x.w : 0.f;
-        const float dout = 2.f * res * inv_count;
-        // dW3 and db2 contributions (128 values), and dZ2 in both operand layouts.
-        float v[2 * kHidden];
+    for (int u = 0; u < 32; ++u) {
+        z2[u] += s.b2[j0 + u];
+        out = fmaf(z2[u] > 0.f ? z2[u] : 0.f, s.w3[j0 + u], out);
+    }
+    // The output needs both halves: exchange through shared memory.
+    s.xch[t] = out;
+    __syncthreads();
+    out = (b3 + s.xch[row]) + s.xch[row + kRows];
+    const float res = valid ? out - x.w : 0.f;
+    const float dout = 2.f * res * inv_count;
+    // dW3 and db2 contributions of this row (64 values), and dZ2 in both operand layouts.
+    float v[64];
 #pragma unroll
-        for (int j = 0; j < kHidden; ++j) {
-            const bool on = z2[j] > 0.f;
-            const float g = on ? dout * s.w3[j] : 0.f;
-            v[j] = dout * (on ? z2[j] : 0.f);
-            v[kHidden + j] = g;
-            const __nv_bfloat16 gb = __float2bfloat16_rn(g);
-            s.dz2[tc::kmajor(t, j, kHidden)] = gb;
-            s.dz2t[tc::kmajor(j, t, kRows)] = gb;
-        }
-        tc::fence_async_smem();
-        tc::fence_before_sync();
-        const float tot = cta_sum128(s, v);  // contains __syncthreads
-        tc::fence_after_sync();
-        float* part = partials + size_t(blockIdx.x) * kStride;
-        if (t < kHidden) part[kPW3 + t] = tot;
-        else part[kPB2 + (t - kHidden)] = tot;
-        // db3 and the loss: warp sums then warps in order.
-        float d3 = dout, l2 = res * res;
-        for (int o = 16; o >= 1; o >>= 1) {
-            d3 += __shfl_xor_sync(0xffffffffu, d3, o);
-            l2 += __shfl_xor_sync(0xffffffffu, l2, o);
-        }
-        if ((t & 31) == 0) {
-            s.red[0][warp] = d3;
-            s.red[1][warp] = l2;
-        }
-        if (t == 0) {
-            const uint32_t ad = tc::smem_u32(s.dz2), bw = tc::smem_u32(s.w2b);
-            for (int k = 0; k < kHidden / 16; ++k)
-                tc::mma_bf16(tmem + 64, tc::smem_desc(ad + 256 * k, 128, kHidden * 16),
-                             tc::smem_desc(bw + 256 * k, 128, kHidden * 16), idesc, k > 0);
-            const uint32_t at = tc::smem_u32(s.dz2t), bh = tc::smem_u32(s.h1t);
-            for (int k = 0; k < kRows / 16; ++k)
-                tc::mma_bf16(tmem + 128, tc::smem_desc(at + 256 * k, 128, kRows * 16),
-                             tc::smem_desc(bh + 256 * k, 128, kRows * 16), idesc, k > 0);
-            tc::mma_commit(&s.bar);
-        }
-        __syncthreads();
-        if (t == 0) {
-            part[kPB3] = ((s.red[0][0] + s.red[0][1]) + s.red[0][2]) + s.red[0][3];
-            part[kLossSlot] = ((s.red[1][0] + s.red[1][1]) + s.red[1][2]) + s.red[1][3];
-        }
-        ok = tc::mbar_wait(&s.bar, 1);
-        if (__syncthreads_or(!ok)) {
-            if (t == 0) atomicExch(error, 1);
-            goto release;
-        }
-        tc::fence_after_sync();
-        // dH1 -> dZ1 -> dW1, db1 (256 values).
-        float dh1[kHidden];
-        tc::tmem_load32(tmem + lane_base + 64, dh1);
-        tc::tmem_load32(tmem + lane_base + 96, dh1 + 32);
+    for (int g = 0; g < 4; ++g) {
+        __align__(16) __nv_bfloat16 pack[8];
 #pragma unroll
-        for (int j = 0; j < kHidden; ++j) dh1[j] = ((mask1 >> j) & 1ull) ? dh1[j] : 0.f;  // dZ1
-        float w[2 * kHidden];
-#pragma unroll
-        for (int j = 0; j < kHidden; ++j) {
-            w[j] = dh1[j] * x.x;
-            w[kHidden + j] = dh1[j] * x.y;
+        for (int u = 0; u < 8; ++u) {
+            const int k = 8 * g + u, j = j0 + k;
+            const bool on = z2[k] > 0.f;
+            const float gz = on ? dout * s.w3[j] : 0.f;
+            v[k] = dout * (on ? z2[k] : 0.f);
+            v[32 + k] = gz;
+            pack[u] = __float2bfloat16_rn(gz);
+            s.dz2t[tc::kmajor(j, row, kRows)] = pack[u];
         }
-        const float g01 = cta_sum128(s, w);
+        *reinterpret_cast<uint4*>(&s.dz2[tc::kmajor(row, j0 + 8 * g, kHidden)]) = *reinterpret_cast<const uint4*>(pack);
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    half_sum<64>(s, v);  // contains __syncthreads
+    tc::fence_after_sync();
+    if (t == 0) {
+        const uint32_t ad = tc::smem_u32(s.dz2), bw = tc::smem_u32(s.w2b);
+        for (int k = 0; k < kHidden / 16; ++k)
+            tc::mma_bf16(tmem + 64, tc::smem_desc(ad + 256 * k, 128, kHidden * 16),
+                         tc::smem_desc(bw + 256 * k, 128, kHidden * 16), idesc, k > 0);
+        const uint32_t at = tc::smem_u32(s.dz2t), bh = tc::smem_u32(s.h1t);
+        for (int k = 0; k < kRows / 16; ++k)
+            tc::mma_bf16(tmem + 128, tc::smem_desc(at + 256 * k, 128, kRows * 16),
+                         tc::smem_desc(bh + 256 * k, 128, kRows * 16), idesc, k > 0);
+        tc::mma_commit(&s.bar);
+    }
+    float* part = partial;
+    if (t < 2 * kHidden) {
+        // totals: [h][0..31] dW3 of units 32 h + k, [h][32..63] db2
+        const int h = t >> 6, k = t & 63;
+        const int unit = 32 * h + (k & 31);
+        part[size_t((k < 32 ? kPW3 : kPB2) + unit) * pstride] = s.tot[h][k];
+    }
+    // db3 and the loss: half 0 holds one copy of every row.
+    float d3 = half == 0 ? dout : 0.f, l2 = half == 0 ? res * res : 0.f;
+    for (int o = 16; o >= 1; o >>= 1) {
+        d3 += __shfl_xor_sync(0xffffffffu, d3, o);
+        l2 += __shfl_xor_sync(0xffffffffu, l2, o);
+    }
+    if ((t & 31) == 0 && half == 0) {
+        s.red[0][64 + warp] = d3;
+        s.red[0][96 + warp] = l2;
+    }
+    __syncthreads();
+    if (t == 0) {
+        part[size_t(kPB3) * pstride] = ((s.red[0][64] + s.red[0][65]) + s.red[0][66]) + s.red[0][67];
+        part[size_t(kLossSlot) * pstride] = ((s.red[0][96] + s.red[0][97]) + s.red[0][98]) + s.red[0][99];
+    }
+    ok = tc::mbar_wait(&s.bar, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) return false;
+    tc::fence_after_sync();
+    // dH1 -> dZ1 -> dW1, db1: 4 x 32 values per thread.
+    float dh1[32];
+    tc::tmem_load32(tmem + lane_base + 64 + j0, dh1);
+    float w[128];
 #pragma unroll
-        for (int j = 0; j < kHidden; ++j) {
-            w[j] = dh1[j] * x.z;
-            w[kHidden + j] = dh1[j];
-        }
-        const float g2b = cta_sum128(s, w);
-        // W1 is row-major [64][3]: thread t < 64 owns column 0 (then 2) of unit t, thread
-        // t >= 64 column 1 of unit t - 64 (then the bias).
-        if (t < kHidden) {
-            part[kPW1 + 3 * t] = g01;
-            part[kPW1 + 3 * t + 2] = g2b;
+    for (int k = 0; k < 32; ++k) {
+        const float g = ((mask1 >> k) & 1u) ? dh1[k] : 0.f;
+        w[k] = g * x.x;
+        w[32 + k] = g * x.y;
+        w[64 + k] = g * x.z;
+        w[96 + k] = g;
+    }
+    half_sum<128>(s, w);
+    for (int q = t; q < 256; q += kThreadsTrain) {
+        // totals: [h][c * 32 + k]: c = 0..2 column c of W1 (row-major [64][3]), c = 3 b1
+        const int h = q >> 7, k = q & 127, c = k >> 5, unit = 32 * h + (k & 31);
+        const int idx = c < 3 ? kPW1 + 3 * unit + c : kPB1 + unit;
+        part[size_t(idx) * pstride] = s.tot[h][k];
+    }
+    // dW2: TMEM lanes 0..63 hold rows = output units; warps 0, 1 (inputs 0..31) and 4, 5
+    // (inputs 32..63) read them.
+    if ((warp & 3) < 2) {
+        float g2[32];
+        tc::tmem_load32(tmem + lane_base + 128 + j0, g2);
+        const int unit = row;  // output unit
+        if (pstride == 1) {
+            float4* dst = reinterpret_cast<float4*>(part + kPW2 + unit * kHidden + j0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) dst[q] = make_float4(g2[4 * q], g2[4 * q + 1], g2[4 * q + 2], g2[4 * q + 3]);
         } else {
-            part[kPW1 + 3 * (t - kHidden) + 1] = g01;
-            part[kPB1 + (t - kHidden)] = g2b;
-        }
-        // dW2: TMEM lanes 0..63 (warps 0 and 1) hold rows = output units.
-        if (warp < 2) {
-            float g2[kHidden];
-            tc::tmem_load32(tmem + lane_base + 128, g2);
-            tc::tmem_load32(tmem + lane_base + 160, g2 + 32);
-            float4* dst = reinterpret_cast<float4*>(part + kPW2 + t * kHidden);
 #pragma unroll
-            for (int q = 0; q < kHidden / 4; ++q) dst[q] = make_float4(g2[4 * q], g2[4 * q + 1], g2[4 * q + 2], g2[4 * q + 3]);
+            for (int q = 0; q < 32; ++q) part[size_t(kPW2 + unit * kHidden + j0 + q) * pstride] = g2[q];
         }
     }
-release:
-    tc::fence_before_sync();
-    __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, kTmemColumns);
+    return true;
+}
+
+// One batch's gradient partials (partials[b] for CTA b); used for gradient checks.
+__global__ void __launch_bounds__(kThreadsTrain, 1) mlp_grad_kernel(const float* __restrict__ params,
+                                                            const float4* __restrict__ samples, int first,
+                                                            int count, float inv_count, float* __restrict__ partials,
+                                                            int* __restrict__ error) {
+    extern __shared__ unsigned char smem_raw[];
+    TrainSmem& s = *reinterpret_cast<TrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    train_setup(s);
+    uint32_t phase = 0;
+    if (!grad_step(s, params, nullptr, samples, first, count, inv_count, partials + size_t(blockIdx.x) * kStride, 1,
+                   phase) &&
+        threadIdx.x == 0)
+        atomicExch(error, 1);
+    train_release(s);
 }
 
 // Adam (Kingma and Ba, 2015) on the summed CTA partials, in FP32.
@@ -285,6 +337,138 @@ __global__ void mlp_adam_kernel(const float* __restrict__ partials, int blocks, 
     m[i] = mi;
     v[i] = vi;
     params[i] -= lr * (mi / bias1) / (sqrtf(vi / bias2) + eps);
+}
+
+// Grid barrier of a cooperative launch (every CTA resident): arrive on a counter, the
+// last arrival advances the generation.  A wait that outlives ~`max_cycles` sets
+// `*error` and returns false so the kernel can stop instead of hanging.
+struct GridBarrier {
+    unsigned int count;
+    unsigned int generation;
+};
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, unsigned int ctas, int* error,
+                                             long long max_cycles = 2000000000LL) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* gen = &bar->generation;
+        const unsigned int g = *gen;
+        __threadfence();
+        if (atomicAdd(&bar->count, 1u) == ctas - 1) {
+            bar->count = 0;
+            __threadfence();
+            atomicAdd(&bar->generation, 1u);
+        } else {
+            const long long start = clock64();
+            while (*gen == g) {
+                if (clock64() - start > max_cycles || *reinterpret_cast<volatile int*>(error)) {
+                    atomicExch(error, 1);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+struct TrainArgs {
+    float* params;
+    __nv_bfloat16* w2_tiles;  // [2][64 * 64]: forward then backward operand order
+    float* m;
+    float* v;
+    const float4* samples;
+    float* partials;
+    GridBarrier* barrier;
+    int* error;
+    int itm, batch, steps, first_step;  // first_step: Adam steps taken before this launch
+    float lr, beta1, beta2, eps;
+};
+
+// Every Adam step of one exercise date in one cooperative launch: each step computes
+// the batch's gradient partials (one CTA per 128 samples), then every CTA sums the
+// partials of its slice of the parameters in CTA order and applies Adam to it.
+__global__ void __launch_bounds__(kThreadsTrain, 1) mlp_train_kernel(TrainArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    TrainSmem& s = *reinterpret_cast<TrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    train_setup(s);
+    const unsigned int ctas = gridDim.x;
+    const int per_epoch = (a.itm + a.batch - 1) / a.batch;
+    const int chunk = (kParams + int(ctas) - 1) / int(ctas);
+    const int lo = int(blockIdx.x) * chunk, hi = min(kParams, lo + chunk);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // W2's BF16 operand tiles for the first step: each CTA lays out its slice.
+    for (int i = max(lo, kPW2) + int(threadIdx.x); i < min(hi, kPB2); i += kThreadsTrain) {
+        const int w = i - kPW2, o = w >> 6, in = w & 63;
+        const __nv_bfloat16 b = __float2bfloat16_rn(__ldcg(a.params + i));
+        a.w2_tiles[tc::kmajor(o, in, kHidden)] = b;
+        a.w2_tiles[kHidden * kHidden + tc::kmajor(in, o, kHidden)] = b;
+    }
+    __threadfence();
+    uint32_t phase = 0;
+    bool ok = grid_barrier(a.barrier, ctas, a.error);
+    for (int step = 0; ok && step < a.steps; ++step) {
+        const int first = (step % per_epoch) * a.batch;
+        const int count = min(a.batch, a.itm - first);
+        if (!grad_step(s, a.params, reinterpret_cast<const uint4*>(a.w2_tiles), a.samples, first, count,
+                       1.0f / float(count), a.partials + blockIdx.x, int(ctas), phase)) {
+            if (threadIdx.x == 0) atomicExch(a.error, 1);
+            break;
+        }
+        if (!grid_barrier(a.barrier, ctas, a.error)) break;
+        const float tstep = float(a.first_step + step + 1);
+        const float bias1 = 1.0f - powf(a.beta1, tstep), bias2 = 1.0f - powf(a.beta2, tstep);
+        const int blocks = (count + kRows - 1) / kRows;
+        // Adam on this CTA's slice.  Partials are parameter-major ([param][CTA], at most 64
+        // CTAs), so a warp fetches one parameter's partials with two coalesced loads per
+        // lane; six parameters per warp are in flight at once, with their Adam state.  The
+        // sums use a fixed shuffle tree (deterministic).  Everything here was written by
+        // other SMs: it is read past L1.
+        for (int i0 = lo + warp * 6; i0 < hi; i0 += (kThreadsTrain / 32) * 6) {
+            float g[6], state_m = 0.f, state_v = 0.f, state_w = 0.f;
+            const int mine = i0 + lane;
+            if (lane < 6 && mine < hi) {
+                state_m = __ldcg(a.m + mine);
+                state_v = __ldcg(a.v + mine);
+                state_w = __ldcg(a.params + mine);
+            }
+#pragma unroll
+            for (int u = 0; u < 6; ++u) {
+                const int i = i0 + u;
+                const float* row = a.partials + size_t(i < hi ? i : lo) * ctas;
+                const float x0 = (i < hi && lane < blocks) ? __ldcg(row + lane) : 0.f;
+                const float x1 = (i < hi && lane + 32 < blocks) ? __ldcg(row + lane + 32) : 0.f;
+                g[u] = x0 + x1;
+            }
+#pragma unroll
+            for (int u = 0; u < 6; ++u)
+                for (int off = 16; off > 0; off >>= 1) g[u] += __shfl_xor_sync(0xffffffffu, g[u], off);
+            float gi = g[0];
+#pragma unroll
+            for (int u = 1; u < 6; ++u) gi = lane == u ? g[u] : gi;
+            if (lane < 6 && mine < hi) {
+                const float mi = a.beta1 * state_m + (1.f - a.beta1) * gi;
+                const float vi = a.beta2 * state_v + (1.f - a.beta2) * gi * gi;
+                a.m[mine] = mi;
+                a.v[mine] = vi;
+                const float w = state_w - a.lr * (mi / bias1) / (sqrtf(vi / bias2) + a.eps);
+                a.params[mine] = w;
+                if (mine >= kPW2 && mine < kPB2) {
+                    const int k = mine - kPW2, o = k >> 6, in = k & 63;
+                    const __nv_bfloat16 b = __float2bfloat16_rn(w);
+                    a.w2_tiles[tc::kmajor(o, in, kHidden)] = b;
+                    a.w2_tiles[kHidden * kHidden + tc::kmajor(in, o, kHidden)] = b;
+                }
+            }
+        }
+        __threadfence();
+        ok = grid_barrier(a.barrier, ctas, a.error);
+    }
+    train_release(s);
 }
 
 // The network on the CUDA cores with the training kernel's BF16 rounding of the
@@ -475,26 +659,61 @@ __global__ void __launch_bounds__(256) mlp_count_kernel(LsmcParams<float> p, int
     }
 }
 
-// Exclusive offsets in block order, the in-the-money total and the target normalisation.
-__global__ void mlp_scan_kernel(const BlockStats* __restrict__ stats, int blocks, int* __restrict__ offsets,
-                                int* __restrict__ total, TargetNorm* __restrict__ norm) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int run = 0;
-    double sum = 0.0, sumsq = 0.0;
-    for (int b = 0; b < blocks; ++b) {
-        offsets[b] = run;
-        run += int(stats[b].count);
+// Exclusive offsets in block order, the in-the-money total and the target normalisation,
+// by one CTA of kScanThreads: each thread owns a contiguous run of blocks; counts are
+// scanned exactly, the sums reduced in a fixed tree (deterministic).
+constexpr int kScanThreads = 1024;
+
+__global__ void __launch_bounds__(kScanThreads) mlp_scan_kernel(const BlockStats* __restrict__ stats, int blocks,
+                                                                int* __restrict__ offsets, int* __restrict__ total,
+                                                                TargetNorm* __restrict__ norm) {
+    __shared__ int run_count[kScanThreads];
+    __shared__ double run_sum[kScanThreads], run_sq[kScanThreads];
+    const int t = threadIdx.x;
+    const int per = (blocks + kScanThreads - 1) / kScanThreads;
+    const int lo = min(blocks, t * per), hi = min(blocks, lo + per);
+    int c = 0;
+    double sum = 0.0, sq = 0.0;
+    for (int b = lo; b < hi; ++b) {
+        c += int(stats[b].count);
         sum += stats[b].sum;
-        sumsq += stats[b].sumsq;
+        sq += stats[b].sumsq;
     }
-    *total = run;
-    TargetNorm t{0.0, 1.0};
-    if (run > 0) {
-        t.mean = sum / run;
-        const double var = sumsq / run - t.mean * t.mean;
-        t.scale = var > 1e-12 ? sqrt(var) : 1.0;
+    run_count[t] = c;
+    run_sum[t] = sum;
+    run_sq[t] = sq;
+    __syncthreads();
+    // Inclusive scan of the counts (Hillis-Steele on integers).
+    for (int d = 1; d < kScanThreads; d <<= 1) {
+        const int add = t >= d ? run_count[t - d] : 0;
+        __syncthreads();
+        run_count[t] += add;
+        __syncthreads();
     }
-    *norm = t;
+    int base = t > 0 ? run_count[t - 1] : 0;
+    for (int b = lo; b < hi; ++b) {
+        offsets[b] = base;
+        base += int(stats[b].count);
+    }
+    // Tree reduction of the target sums.
+    for (int d = kScanThreads / 2; d > 0; d >>= 1) {
+        if (t < d) {
+            run_sum[t] += run_sum[t + d];
+            run_sq[t] += run_sq[t + d];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        const int n = run_count[kScanThreads - 1];
+        *total = n;
+        TargetNorm tn{0.0, 1.0};
+        if (n > 0) {
+            tn.mean = run_sum[0] / n;
+            const double var = run_sq[0] / n - tn.mean * tn.mean;
+            tn.scale = var > 1e-12 ? sqrt(var) : 1.0;
+        }
+        *norm = tn;
+    }
 }
 
 template <bool TWO>
@@ -666,8 +885,20 @@ bool configure_train_kernel() {
     static bool done = false;
     if (done) return true;
     done = cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmemBytes)) ==
-           cudaSuccess;
+               cudaSuccess &&
+           cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmemBytes)) ==
+               cudaSuccess;
     return done;
+}
+
+// Whether `ctas` training CTAs can all be resident at once (cooperative launch).
+bool cooperative_fits(int device, int ctas) {
+    int coop = 0, sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return false;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return false;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_train_kernel, kThreadsTrain, kTrainSmemBytes) != cudaSuccess)
+        return false;
+    return ctas <= per_sm * sms;
 }
 
 struct Adam {
@@ -679,7 +910,7 @@ struct Adam {
 cudaError_t train_step(cudaStream_t st, float* params, float* m, float* v, Adam& adam, const float4* samples, int first,
                        int count, float* partials, int* error) {
     const int blocks = (count + kRows - 1) / kRows;
-    mlp_grad_kernel<<<blocks, kRows, kTrainSmemBytes, st>>>(params, samples, first, count, 1.0f / float(count),
+    mlp_grad_kernel<<<blocks, kThreadsTrain, kTrainSmemBytes, st>>>(params, samples, first, count, 1.0f / float(count),
                                                             partials, error);
     adam.step += 1;
     const float bias1 = 1.0f - std::pow(adam.beta1, float(adam.step));
@@ -714,7 +945,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     // networks, gradient partials, estimate partials.
     const size_t store_bytes = n * d * sizeof(float) * (TWO ? 2 : 1);
     const size_t net_bytes = size_t(kParams) * sizeof(float);
-    const size_t misc_floats = (size_t(3) + d) * kStride + size_t(max_train_blocks) * kStride;
+    const size_t misc_floats = (size_t(3) + d) * kStride + size_t(max_train_blocks) * kStride + 2 * kHidden * kHidden;
     if (ctx->lsmc_store.ensure(store_bytes) || ctx->lsmc_cash.ensure(n * sizeof(float)) ||
         ctx->mlp_scratch.ensure(n * sizeof(float4) + size_t(pblocks) * (sizeof(BlockStats) + sizeof(int)) +
                                 d * sizeof(TargetNorm) + 256) ||
@@ -736,6 +967,8 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     int* counts = reinterpret_cast<int*>(norms + d);
     int* total = counts + pblocks;
     int* error = total + 1;
+    GridBarrier* barrier = reinterpret_cast<GridBarrier*>(error + 1);
+    const bool cooperative = max_train_blocks <= 64 && cooperative_fits(ctx->device, max_train_blocks);
     // Regions of kStride floats keep every one 16-byte aligned (the gradient partials are
     // written as float4).
     float* params = static_cast<float*>(ctx->mlp_params.ptr);
@@ -743,6 +976,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     float* v = m + kStride;
     float* nets = v + kStride;
     float* partials = nets + d * kStride;
+    __nv_bfloat16* w2_tiles = reinterpret_cast<__nv_bfloat16*>(partials + size_t(max_train_blocks) * kStride);
     double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
     double* lower_partials = finals + 2 * fblocks;
     double* coefs = static_cast<double*>(ctx->lsmc_coef.ptr);
@@ -777,7 +1011,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     MLP_TRY(cudaMemcpyAsync(params, init.data(), net_bytes, cudaMemcpyHostToDevice, st));
     MLP_TRY(cudaMemsetAsync(m, 0, 2 * kStride * sizeof(float), st));
     MLP_TRY(cudaMemsetAsync(nets, 0, d * kStride * sizeof(float), st));
-    MLP_TRY(cudaMemsetAsync(error, 0, sizeof(int), st));
+    MLP_TRY(cudaMemsetAsync(error, 0, sizeof(int) + sizeof(GridBarrier), st));
     MLP_TRY(cudaMemsetAsync(coefs, 0, d * kMaxTerms * sizeof(double) + d * sizeof(int) + sizeof(int), st));
     MLP_TRY(cudaEventRecord(e0, st));
     lsmc_forward<float, TWO><<<unsigned(pblocks), 256, 0, st>>>(p, s->seed, a, b, cash);
@@ -794,7 +1028,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         lsmc_solve<TWO><<<1, 128, 0, st>>>(poly_partials, sblocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                            have + date, poly_failed);
         mlp_count_kernel<TWO><<<pblocks, 256, 0, st>>>(p, date, a, b, cash, coefs, have, stats);
-        mlp_scan_kernel<<<1, 32, 0, st>>>(stats, pblocks, counts, total, norms + date);
+        mlp_scan_kernel<<<1, kScanThreads, 0, st>>>(stats, pblocks, counts, total, norms + date);
         mlp_scatter_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, a, b, cash, coefs, have, counts, norms + date,
                                                         samples);
         launches += 6;
@@ -806,12 +1040,23 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
             // The first fitted date starts from the initial weights: it trains four times
             // as long; later dates start from the previous date's network.
             const int date_epochs = adam.step == 0 ? 4 * epochs : epochs;
-            for (int epoch = 0; epoch < date_epochs; ++epoch)
-                for (int first = 0; first < itm; first += batch) {
-                    MLP_TRY(train_step(st, params, m, v, adam, samples, first, std::min(batch, itm - first), partials,
-                                       error));
-                    launches += 2;
-                }
+            const int steps = date_epochs * ((itm + batch - 1) / batch);
+            if (cooperative) {
+                TrainArgs ta{params, w2_tiles, m, v, samples, partials, barrier, error, itm, batch, steps,
+                             adam.step, adam.lr, adam.beta1, adam.beta2, adam.eps};
+                void* args[] = {&ta};
+                MLP_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel),
+                                                    dim3(max_train_blocks), dim3(kThreadsTrain), args, kTrainSmemBytes, st));
+                adam.step += steps;
+                launches += 1;
+            } else {
+                for (int epoch = 0; epoch < date_epochs; ++epoch)
+                    for (int first = 0; first < itm; first += batch) {
+                        MLP_TRY(train_step(st, params, m, v, adam, samples, first, std::min(batch, itm - first),
+                                           partials, error));
+                        launches += 2;
+                    }
+            }
         }
         // The network of this date (kept when no path is in the money: the previous
         // date's weights continue).
@@ -928,7 +1173,7 @@ extern "C" kgpu_status kgpu_mlp_gradients(kgpu_context* ctx, const float* params
         cudaMemcpyAsync(dparams, params, size_t(kParams) * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemsetAsync(derror, 0, sizeof(int), st) != cudaSuccess)
         return KGPU_DEVICE_ERROR;
-    mlp_grad_kernel<<<blocks, kRows, kTrainSmemBytes, st>>>(dparams, dsamples, 0, count, 1.0f / float(count), dpartials,
+    mlp_grad_kernel<<<blocks, kThreadsTrain, kTrainSmemBytes, st>>>(dparams, dsamples, 0, count, 1.0f / float(count), dpartials,
                                                             derror);
     if (cudaGetLastError() != cudaSuccess ||
         cudaMemcpyAsync(part.data(), dpartials, part.size() * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
