@@ -524,12 +524,14 @@ def run_lsmc(args):
                                                     1.0, C.byref(s), 43, C.byref(out)))
         native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0, 1.0,
                                                 C.byref(s), 43, C.byref(out)))
+        def num(x):
+            return None if x != x else x
         return {"paths": paths, "price": out.price, "standard_error": out.standard_error,
                 "out_of_sample": out.out_of_sample,
                 "out_of_sample_error": out.out_of_sample_error,
                 "error_vs_adi": out.price - adi, "out_of_sample_error_vs_adi": out.out_of_sample - adi,
-                "wall_ms": out.wall_ms, "path_store_ms": out.path_store_ms,
-                "regression_ms": out.regression_ms}
+                "wall_ms": out.wall_ms, "path_store_ms": num(out.path_store_ms),
+                "regression_ms": num(out.regression_ms)}
 
     poly = price(abi.BASIS_POLY3, 1 << 20)
     poly64 = price(abi.BASIS_POLY3, 1 << 20, abi.PRECISION_FP64)

@@ -220,6 +220,9 @@ void kgpu_context_destroy(kgpu_context* ctx) {
         cudaEventDestroy(e.first);
         cudaEventDestroy(e.second);
     }
+    if (ctx->lsmc_exec) cudaGraphExecDestroy(ctx->lsmc_exec);
+    for (cudaEvent_t e : ctx->lsmc_events)
+        if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -754,6 +757,7 @@ kgpu_status run_book(Call& k) {
     float ms = 0;
     if (cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop) == cudaSuccess) ctx->last_kernel_ms = ms;
     if (st == KGPU_OK) ctx->last_path_kernel_ms = path_kernel_ms(ctx);
+    cudaGetLastError();  // a refused timing query must not surface in the next call
     ctx->last_launches = launches;
     return st;
 }

@@ -56,6 +56,10 @@ struct kgpu_context {
         mlp_scratch;
     // raw streams
     kgpu::DeviceBuffer stream_out;
+    // polynomial LSMC: the captured launch sequence of the last problem and its key
+    cudaGraphExec_t lsmc_exec = nullptr;
+    std::vector<unsigned char> lsmc_key;
+    cudaEvent_t lsmc_events[4] = {nullptr, nullptr, nullptr, nullptr};
     // cancellation word mirrored into host-mapped memory for persistent kernels
     volatile int* cancel_host = nullptr;
     int* cancel_dev = nullptr;

@@ -16,12 +16,14 @@
 // the in-the-money normal equations (products in the store's precision, FP64 across
 // warps and blocks), lsmc_solve merges the block partials in block order and solves in
 // FP64; lsmc_final and lsmc_lower_bound reduce the estimates.  The whole sequence is
-// captured in a CUDA graph per problem shape and replayed.
+// captured in a CUDA graph and replayed while the problem is unchanged (a changed one is
+// re-captured and updates the executable graph in place).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -223,67 +225,118 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     double* partials = static_cast<double*>(ctx->lsmc_sums.ptr);
     double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
     cudaStream_t st = ctx->stream;
-    cudaEvent_t e0, e1, e2, e3;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventCreate(&e2);
-    cudaEventCreate(&e3);
-    cudaMemsetAsync(coefs, 0, d * kMaxTerms * sizeof(double) + d * sizeof(int) + sizeof(int), st);
-    cudaEventRecord(e0, st);
-    int launches = 0;
-    if (two)
-        lsmc_forward<Real, true><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
-    else
-        lsmc_forward<Real, false><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
-    ++launches;
-    cudaEventRecord(e1, st);
-    for (int date = p.dates - 2; date >= 0; --date) {
-        const double* cnext = date + 1 <= p.dates - 2 ? coefs + size_t(date + 1) * kMaxTerms : nullptr;
-        const int* hnext = date + 1 <= p.dates - 2 ? have + date + 1 : nullptr;
-        if (two) {
-            lsmc_backward<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
-            lsmc_solve<true><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
-                                                have + date, failed);
-        } else {
-            lsmc_backward<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
-            lsmc_solve<false><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
-                                                 have + date, failed);
-        }
-        launches += 2;
-    }
-    if (two)
-        lsmc_final<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
-    else
-        lsmc_final<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
-    ++launches;
-    cudaEventRecord(e2, st);
     const bool lower = fresh_seed != s->seed;
-    std::vector<double> lower_partials;
+    double* lp = nullptr;
     if (lower) {
         if (ctx->mlp_scratch.ensure(size_t(blocks) * 2 * sizeof(double))) return KGPU_DEVICE_ERROR;
-        double* lp = static_cast<double*>(ctx->mlp_scratch.ptr);
+        lp = static_cast<double*>(ctx->mlp_scratch.ptr);
+    }
+    for (cudaEvent_t& e : ctx->lsmc_events)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) return KGPU_DEVICE_ERROR;
+    cudaEvent_t e0 = ctx->lsmc_events[0], e1 = ctx->lsmc_events[1], e2 = ctx->lsmc_events[2],
+                e3 = ctx->lsmc_events[3];
+    int launches = 0;
+    // The whole launch sequence: captured once per problem into a CUDA graph and replayed.
+    auto enqueue = [&]() {
+        launches = 0;
+        cudaMemsetAsync(coefs, 0, d * kMaxTerms * sizeof(double) + d * sizeof(int) + sizeof(int), st);
         if (two)
-            lsmc_lower_bound<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+            lsmc_forward<Real, true><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
         else
-            lsmc_lower_bound<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+            lsmc_forward<Real, false><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
         ++launches;
+        cudaEventRecordWithFlags(e1, st, cudaEventRecordExternal);
+        for (int date = p.dates - 2; date >= 0; --date) {
+            const double* cnext = date + 1 <= p.dates - 2 ? coefs + size_t(date + 1) * kMaxTerms : nullptr;
+            const int* hnext = date + 1 <= p.dates - 2 ? have + date + 1 : nullptr;
+            if (two) {
+                lsmc_backward<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
+                lsmc_solve<true><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                                                    have + date, failed);
+            } else {
+                lsmc_backward<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash,
+                                                                            partials);
+                lsmc_solve<false><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                                                     have + date, failed);
+            }
+            launches += 2;
+        }
+        if (two)
+            lsmc_final<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
+        else
+            lsmc_final<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
+        ++launches;
+        cudaEventRecordWithFlags(e2, st, cudaEventRecordExternal);
+        if (lower) {
+            if (two)
+                lsmc_lower_bound<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+            else
+                lsmc_lower_bound<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+            ++launches;
+        }
+    };
+    // Key of the captured sequence: every argument its launches bake in.
+    std::vector<unsigned char> key(sizeof(p) + 64);
+    {
+        unsigned char* k = key.data();
+        std::memcpy(k, &p, sizeof(p));
+        const void* ptrs[] = {a, b, cash, coefs, partials, finals, lp};
+        std::memcpy(k + sizeof(p), ptrs, sizeof(ptrs));
+        const uint64_t tail[] = {s->seed, fresh_seed, uint64_t(blocks) | (uint64_t(sizeof(Real)) << 32)};
+        key.resize(sizeof(p) + sizeof(ptrs) + sizeof(tail));
+        std::memcpy(key.data() + sizeof(p) + sizeof(ptrs), tail, sizeof(tail));
+    }
+    if (!(ctx->lsmc_exec && ctx->lsmc_key == key)) {
+        cudaGraph_t graph = nullptr;
+        bool captured = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (captured) {
+            enqueue();
+            captured = cudaStreamEndCapture(st, &graph) == cudaSuccess && graph;
+        }
+        if (captured) {
+            cudaGraphExecUpdateResultInfo info;
+            if (!ctx->lsmc_exec || cudaGraphExecUpdate(ctx->lsmc_exec, graph, &info) != cudaSuccess) {
+                cudaGetLastError();
+                if (ctx->lsmc_exec) cudaGraphExecDestroy(ctx->lsmc_exec);
+                ctx->lsmc_exec = nullptr;
+                if (cudaGraphInstantiate(&ctx->lsmc_exec, graph, 0) != cudaSuccess) ctx->lsmc_exec = nullptr;
+            }
+            cudaGraphDestroy(graph);
+        }
+        ctx->lsmc_key = ctx->lsmc_exec ? key : std::vector<unsigned char>();
+    } else {
+        // Replaying: count the launches the sequence holds.
+        launches = 2 * (p.dates - 1) + 2 + (lower ? 1 : 0);
+    }
+    cudaGetLastError();  // a refused capture or update leaves nothing behind
+    cudaEventRecord(e0, st);
+    if (ctx->lsmc_exec) {
+        if (cudaGraphLaunch(ctx->lsmc_exec, st) != cudaSuccess) {
+            ctx->error = "CUDA graph launch failed";
+            return KGPU_DEVICE_ERROR;
+        }
+    } else {
+        enqueue();  // capture unavailable: launch directly
+    }
+    cudaEventRecord(e3, st);
+    std::vector<double> lower_partials;
+    if (lower) {
         lower_partials.resize(size_t(blocks) * 2);
         cudaMemcpyAsync(lower_partials.data(), lp, lower_partials.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     }
-    cudaEventRecord(e3, st);
     std::vector<double> fin(size_t(blocks) * 2);
     int fail_flag = 0;
     cudaMemcpyAsync(fin.data(), finals, fin.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&fail_flag, failed, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaError_t err = cudaStreamSynchronize(st);
+    // Timing: the whole call from stream events around the graph; the path store and the
+    // regression from the events the graph records (NaN when a query is refused; the
+    // refusal is cleared so it cannot surface in a later call).
     float ms_total = 0, ms_store = 0, ms_regress = 0;
-    cudaEventElapsedTime(&ms_total, e0, e3);
-    cudaEventElapsedTime(&ms_store, e0, e1);
-    cudaEventElapsedTime(&ms_regress, e1, e2);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaEventDestroy(e2);
-    cudaEventDestroy(e3);
+    if (cudaEventElapsedTime(&ms_total, e0, e3) != cudaSuccess) ms_total = std::nanf("");
+    if (cudaEventElapsedTime(&ms_store, e0, e1) != cudaSuccess) ms_store = std::nanf("");
+    if (cudaEventElapsedTime(&ms_regress, e1, e2) != cudaSuccess) ms_regress = std::nanf("");
+    cudaGetLastError();
     if (err != cudaSuccess) {
         ctx->error = cudaGetErrorString(err);
         return KGPU_DEVICE_ERROR;

@@ -115,72 +115,98 @@ __global__ void lsmc_solve(const double* partials, int blocks, int max_degree, d
         if (lane == 0) sums[j] = v;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    for (int j = 0; j < kMaxTerms; ++j) coef[j] = 0.0;
-    *have = 0;
+    // Pivoted elimination by one warp: lane r holds row r of the augmented system (the
+    // right-hand side at index T).  Each element is updated with the same operations as
+    // the sequential elimination; the pivot is the last row with the largest magnitude,
+    // as there.
+    if (threadIdx.x >= 32) return;
+    if (lane == 0) {
+        for (int j = 0; j < kMaxTerms; ++j) coef[j] = 0.0;
+        *have = 0;
+    }
     if (sums[0] == 0.0) return;
-    double full[T][T + 1];
-    int q = 0;
-    for (int r = 0; r < T; ++r)
-        for (int c = r; c < T; ++c) {
-            full[r][c] = sums[q];
-            full[c][r] = sums[q];
-            ++q;
-        }
-    for (int r = 0; r < T; ++r) full[r][T] = sums[q++];
+    double full[T + 1];
+#pragma unroll
+    for (int c = 0; c < T; ++c) {
+        const int r0 = lane < c ? lane : c, c0 = lane < c ? c : lane;
+        full[c] = lane < T ? sums[r0 * T - r0 * (r0 - 1) / 2 + (c0 - r0)] : 0.0;
+    }
+    full[T] = lane < T ? sums[T * (T + 1) / 2 + lane] : 0.0;
     for (int degree = max_degree; degree >= 0; --degree) {
         const int k = TWO ? (degree + 1) * (degree + 2) / 2 : degree + 1;
-        double m[T][T + 1];
-        for (int r = 0; r < k; ++r) {
-            for (int c = 0; c < k; ++c) m[r][c] = full[r][c];
-            m[r][k] = full[r][T];
-        }
+        double m[T + 1];
+#pragma unroll
+        for (int c = 0; c <= T; ++c) m[c] = (c < k || c == T) ? full[c] : 0.0;
         double scale = 0.0;
-        for (int r = 0; r < k; ++r)
-            for (int c = 0; c < k; ++c) scale = fmax(scale, fabs(m[r][c]));
+        if (lane < k) {
+#pragma unroll
+            for (int c = 0; c < T; ++c)
+                if (c < k) scale = fmax(scale, fabs(m[c]));
+        }
+        for (int off = 16; off > 0; off >>= 1) scale = fmax(scale, __shfl_xor_sync(0xffffffffu, scale, off));
         bool singular = false;
-        for (int col = 0; col < k && !singular; ++col) {
-            int pivot = col;
-            for (int r = col + 1; r < k; ++r)
-                if (fabs(m[r][col]) >= fabs(m[pivot][col])) pivot = r;
-            if (!isfinite(m[pivot][col])) {
-                *failed = 1;
+#pragma unroll
+        for (int col = 0; col < T; ++col) {
+            if (col >= k) break;
+            double best = (lane >= col && lane < k) ? fabs(m[col]) : -1.0;
+            int pivot = lane;
+            for (int off = 16; off > 0; off >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const int op = __shfl_xor_sync(0xffffffffu, pivot, off);
+                if (ob > best || (ob == best && op > pivot)) {
+                    best = ob;
+                    pivot = op;
+                }
+            }
+            const double pv = __shfl_sync(0xffffffffu, m[col], pivot);
+            if (!isfinite(pv)) {
+                if (lane == 0) *failed = 1;
                 return;
             }
-            if (fabs(m[pivot][col]) <= 1e-14 * scale) {
+            if (fabs(pv) <= 1e-14 * scale) {
                 singular = true;
                 break;
             }
-            if (pivot != col)
-                for (int c = 0; c <= k; ++c) {
-                    double t = m[col][c];
-                    m[col][c] = m[pivot][c];
-                    m[pivot][c] = t;
-                }
-            for (int r = col + 1; r < k; ++r) {
-                const double factor = m[r][col] / m[col][col];
-                for (int c = col; c < k; ++c) m[r][c] -= factor * m[col][c];
-                m[r][k] -= factor * m[col][k];
+            const int src = lane == col ? pivot : (lane == pivot ? col : lane);
+            double prow[T + 1];
+#pragma unroll
+            for (int c = 0; c <= T; ++c) {
+                m[c] = __shfl_sync(0xffffffffu, m[c], src);
+                prow[c] = __shfl_sync(0xffffffffu, m[c], col);
+            }
+            if (lane > col && lane < k) {
+                const double factor = m[col] / prow[col];
+#pragma unroll
+                for (int c = 0; c < T; ++c)
+                    if (c >= col && c < k) m[c] -= factor * prow[c];
+                m[T] -= factor * prow[T];
             }
         }
         if (singular) continue;
         double x[T];
-        for (int r = k - 1; r >= 0; --r) {
-            double v = m[r][k];
-            for (int c = r + 1; c < k; ++c) v -= m[r][c] * x[c];
-            x[r] = v / m[r][r];
+        bool finite = true;
+#pragma unroll
+        for (int r = T - 1; r >= 0; --r) {
+            x[r] = 0.0;
+            if (r >= k) continue;
+            double v = m[T];
+#pragma unroll
+            for (int c = 0; c < T; ++c)
+                if (c > r && c < k) v -= m[c] * x[c];
+            x[r] = __shfl_sync(0xffffffffu, v / m[r], r);
+            finite = finite && isfinite(x[r]);
         }
-        for (int r = 0; r < k; ++r) {
-            if (!isfinite(x[r])) {
+        if (lane == 0) {
+            if (!finite) {
                 *failed = 1;
                 return;
             }
-            coef[r] = x[r];
+            for (int r = 0; r < k; ++r) coef[r] = x[r];
+            *have = 1;
         }
-        *have = 1;
         return;
     }
-    *failed = 1;
+    if (lane == 0) *failed = 1;
 }
 
 // Forward pass: the path store and the terminal cash.

@@ -51,3 +51,18 @@ def test_engine_prices_american_options():
     lower, lower_se = engine.price_american_out_of_sample(AmericanOption("put", 100.0, 1.0), bsm(),
                                                           fresh_seed=77)
     assert lower < est.price + 3 * est.standard_error
+
+
+def test_graph_replay_and_update_give_the_same_prices(native):
+    """The polynomial LSMC sequence is a CUDA graph: replaying it for an unchanged
+    problem, updating it for a changed seed and going back all reproduce direct results."""
+    ctx = heston_context()
+    a = lsmc_settings(1 << 14, 8, 42, abi.BASIS_POLY3, precision="fp32", substeps=2)
+    b = lsmc_settings(1 << 14, 8, 77, abi.BASIS_POLY3, precision="fp32", substeps=2)
+    first = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, a, fresh_seed=5)
+    again = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, a, fresh_seed=5)
+    other = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, b, fresh_seed=5)
+    back = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, a, fresh_seed=5)
+    assert first.price == again.price == back.price
+    assert first.out_of_sample == again.out_of_sample == back.out_of_sample
+    assert other.price != first.price
