@@ -74,12 +74,12 @@ def _resolve_seed(seed):
 
 class _MonteCarloEngine:
     _STATE_FIELDS = ("path_count", "seed", "max_active_workers", "sampling", "antithetic",
-                     "precision", "schedule", "device", "tile_paths")
+                     "precision", "schedule", "device", "tile_paths", "tuning")
 
     def __init__(self, *, path_count: int = 131_072, seed: Optional[int] = None,
                  max_active_workers: int = 0, sampling: str = PSEUDO_RANDOM,
                  antithetic: bool = False, precision: str = "fp64", schedule: str = "plain",
-                 device: int = 0, tile_paths: int = 0):
+                 device: int = 0, tile_paths: int = 0, tuning: Optional[str] = None):
         if not (1 <= int(path_count) <= 2_147_483_647):
             raise InvalidInputError("path_count must be positive")
         if int(max_active_workers) < 0:
@@ -92,6 +92,8 @@ class _MonteCarloEngine:
             raise InvalidInputError(f"unknown precision {precision!r}")
         if schedule not in _SCHEDULE:
             raise InvalidInputError(f"unknown schedule {schedule!r}")
+        if tuning not in (None, "auto"):
+            raise InvalidInputError("tuning must be None or 'auto'")
         self.path_count = int(path_count)
         self.seed = None if seed is None else int(seed)
         self.max_active_workers = int(max_active_workers)
@@ -101,6 +103,9 @@ class _MonteCarloEngine:
         self.schedule = schedule
         self.device = int(device)
         self.tile_paths = int(tile_paths)
+        # 'auto': the persistent schedule's launch shape is tuned per kind of book
+        # (kiyosi_gb300.autotune); prices do not depend on it.
+        self.tuning = tuning
 
     def _kwargs(self):
         return {k: getattr(self, k) for k in self._STATE_FIELDS if hasattr(self, k)}
@@ -148,8 +153,13 @@ class _MonteCarloEngine:
             model = ctx.kgpu_model()
             book = packed.struct()
             flag = None if cancel is None else C.byref(cancel)
+            settings = self._settings(seed)
+            if self.tuning == "auto" and self.schedule == "persistent":
+                from . import autotune
+                shape, _ = autotune.tune(native, ctx, packed, settings)
+                settings = autotune.apply(settings, shape)
             native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book),
-                                                    C.byref(self._settings(seed)), out, flag))
+                                                    C.byref(settings), out, flag))
             for j, i in enumerate(index):
                 results[i] = MonteCarloEstimate.from_native(out[j])
         return results
