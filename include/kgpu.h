@@ -310,7 +310,8 @@ typedef struct kgpu_lsmc_settings {
     int32_t mlp_epochs;        /* MLP basis: epochs per exercise date */
     int32_t mlp_batch;         /* MLP basis: minibatch size */
     int32_t mlp_hidden;        /* MLP basis: hidden width (64) */
-    int32_t reserved;
+    int32_t mlp_samples;       /* MLP basis: in-the-money samples trained on per date, the
+                                  first ones in path order (0: all) */
     double mlp_learning_rate;
     uint64_t seed;
     uint64_t mlp_seed;

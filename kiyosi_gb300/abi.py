@@ -126,7 +126,7 @@ class Estimate(C.Structure):
 class LsmcSettings(C.Structure):
     _fields_ = [("path_count", _I), ("exercise_dates", _I), ("substeps", _I), ("basis", _I),
                 ("sampling", _I), ("precision", _I), ("mlp_epochs", _I), ("mlp_batch", _I),
-                ("mlp_hidden", _I), ("reserved", _I), ("mlp_learning_rate", _D),
+                ("mlp_hidden", _I), ("mlp_samples", _I), ("mlp_learning_rate", _D),
                 ("seed", C.c_uint64), ("mlp_seed", C.c_uint64)]
 
 

@@ -1036,6 +1036,9 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         int itm = 0;
         MLP_TRY(cudaMemcpyAsync(&itm, total, sizeof(int), cudaMemcpyDeviceToHost, st));
         MLP_TRY(cudaStreamSynchronize(st));
+        // Training samples: the first `mlp_samples` in-the-money paths (an i.i.d.
+        // subsample, the paths being independent), or all of them.
+        if (s->mlp_samples > 0 && itm > s->mlp_samples) itm = s->mlp_samples;
         if (itm > 0) {
             // The first fitted date starts from the initial weights: it trains four times
             // as long; later dates start from the previous date's network.
