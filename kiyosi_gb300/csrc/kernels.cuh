@@ -567,7 +567,7 @@ struct Compensated {
 // payoff to values[value_offset[contract] + sample]; reduce_values_kernel sums them in a
 // fixed order, so results do not depend on which warp ran which path.
 template <class Real, int MODEL, bool SOBOL>
-__global__ void __launch_bounds__(kThreads) persistent_kernel(PersistentArgs<Real> a, kgpu_model model,
+__global__ void __launch_bounds__(kThreads, 4) persistent_kernel(PersistentArgs<Real> a, kgpu_model model,
                                                               const double* lv_dev) {
     using Kind = SobolKind<Real>;
     using Word = typename Kind::Word;
