@@ -368,7 +368,7 @@ def run_kernel_only(args):
         s = abi.LsmcSettings(path_count=args.paths, exercise_dates=args.dates, substeps=5,
                              basis=basis, sampling=0, precision=abi.PRECISION_FP32, mlp_epochs=5,
                              mlp_batch=8192, mlp_hidden=64, mlp_learning_rate=1e-3, seed=42,
-                             mlp_seed=7)
+                             mlp_seed=7, mlp_samples=args.mlp_samples)
         out = abi.LsmcResult()
         for _ in range(args.warmup + args.steps):
             native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0,
@@ -612,6 +612,8 @@ def main():
     ap.add_argument("--paths", type=int, default=PATHS,
                     help="path count (profiling runs use smaller cases)")
     ap.add_argument("--dates", type=int, default=50, help="LSMC exercise dates (profiling runs)")
+    ap.add_argument("--mlp-samples", type=int, default=0,
+                    help="LSMC network: in-the-money samples trained on per date (0: all)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the kernel's default launch shape instead of the autotuner's")
     ap.add_argument("--kernel-only", choices=["fp32", "fp64", "lsmc-poly", "lsmc-mlp"],

@@ -512,9 +512,6 @@ __global__ void mlp_snapshot_kernel(const float* __restrict__ params, const Targ
     net[i] = w;
 }
 
-__device__ __forceinline__ void load_net(float* dst, const float* src) {
-    for (int i = threadIdx.x; i < kParams; i += blockDim.x) dst[i] = src[i];
-}
 
 // Network inputs of a path at exercise date k.
 struct Features {
@@ -540,6 +537,115 @@ __device__ __forceinline__ float poly_part(const LsmcParams<float>& p, const dou
 #pragma unroll
     for (int j = 0; j < (TWO ? 10 : 3); ++j) cn[j] = coefs[size_t(k) * kMaxTerms + j];
     return continuation<float, TWO>(p, cn, spot / p.strike, TWO ? v * p.y_scale : 0.f);
+}
+
+// The fitted network on compacted samples, on the tensor cores: 128 samples per CTA,
+// layer 1 on the CUDA cores, the 64 x 64 product as four tcgen05 MMAs (BF16 operands,
+// FP32 accumulator in 64 TMEM columns), the output layer in FP32 -- the training
+// kernel's forward arithmetic on a stored network (W2 already BF16-rounded, output
+// layer in cash units).  out[j] = f(samples[j].xyz).
+struct __align__(1024) InferSmem {
+    __nv_bfloat16 h1[kRows * kHidden];
+    __nv_bfloat16 w2f[kHidden * kHidden];
+    float w1[3 * kHidden], b1[kHidden], b2[kHidden], w3[kHidden];
+    uint64_t bar;
+    uint32_t tmem;
+};
+constexpr size_t kInferSmemBytes = sizeof(InferSmem) + 1024;
+
+__global__ void __launch_bounds__(kRows) mlp_infer_kernel(const float* __restrict__ net,
+                                                          const float4* __restrict__ samples, int count,
+                                                          float* __restrict__ out, int* __restrict__ error) {
+    extern __shared__ unsigned char smem_raw[];
+    InferSmem& s = *reinterpret_cast<InferSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int t = threadIdx.x, warp = t >> 5;
+    if (warp == 0) {
+        tc::tmem_alloc(&s.tmem, 64);
+        tc::tmem_relinquish();
+    }
+    if (t == 0) tc::mbar_init(&s.bar, 1);
+    for (int i = t; i < 3 * kHidden; i += kRows) s.w1[i] = net[kPW1 + i];
+    if (t < kHidden) {
+        s.b1[t] = net[kPB1 + t];
+        s.b2[t] = net[kPB2 + t];
+        s.w3[t] = net[kPW3 + t];
+    }
+    for (int i = t; i < kHidden * kHidden; i += kRows)
+        s.w2f[tc::kmajor(i >> 6, i & 63, kHidden)] = __float2bfloat16_rn(net[kPW2 + i]);
+    const int row = blockIdx.x * kRows + t;
+    const bool valid = row < count;
+    const float4 x = valid ? samples[row] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+        __align__(16) __nv_bfloat16 pack[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int j = 8 * g + u;
+            const float z = fmaf(s.w1[3 * j], x.x, fmaf(s.w1[3 * j + 1], x.y, fmaf(s.w1[3 * j + 2], x.z, s.b1[j])));
+            pack[u] = __float2bfloat16_rn(z > 0.f ? z : 0.f);
+        }
+        *reinterpret_cast<uint4*>(&s.h1[tc::kmajor(t, 8 * g, kHidden)]) = *reinterpret_cast<const uint4*>(pack);
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = s.tmem;
+    if (t == 0) {
+        const uint32_t a0 = tc::smem_u32(s.h1), b0 = tc::smem_u32(s.w2f);
+        for (int k = 0; k < kHidden / 16; ++k)
+            tc::mma_bf16(tmem, tc::smem_desc(a0 + 256 * k, 128, kHidden * 16), tc::smem_desc(b0 + 256 * k, 128, kHidden * 16),
+                         tc::idesc_bf16(kRows, kHidden), k > 0);
+        tc::mma_commit(&s.bar);
+    }
+    const bool ok = tc::mbar_wait(&s.bar, 0);
+    if (!__syncthreads_or(!ok)) {
+        tc::fence_after_sync();
+        float z2[32];
+        float y = net[kPB3];
+        const uint32_t lane_base = uint32_t(warp * 32) << 16;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            tc::tmem_load32(tmem + lane_base + 32 * h, z2);
+#pragma unroll
+            for (int u = 0; u < 32; ++u) {
+                const float z = z2[u] + s.b2[32 * h + u];
+                y = fmaf(z > 0.f ? z : 0.f, s.w3[32 * h + u], y);
+            }
+        }
+        if (valid) out[row] = y;
+    } else if (t == 0) {
+        atomicExch(error, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+// Exercise decisions of date k on its compacted in-the-money paths: exercise when the
+// intrinsic value beats the polynomial plus the network's output (computed by
+// mlp_infer_kernel into `net_out`).  Writes the cash of exercising paths.
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_exercise_kernel(LsmcParams<float> p, int date, int count,
+                                                           const int* __restrict__ sample_path,
+                                                           const float* __restrict__ net_out,
+                                                           const double* __restrict__ coefs,
+                                                           const int* __restrict__ have, const float* __restrict__ a,
+                                                           const float* __restrict__ b, float* __restrict__ cash) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= count) return;
+    const int i = sample_path[j];
+    const size_t at = size_t(date) * p.paths + i;
+    const float spot = spot_at_date<float, TWO>(p, date, a[at]);
+    const float v = TWO ? b[at] : 0.f;
+    const float e = intrinsic(p, spot);
+    if (e > 0.f && e / p.strike > poly_part<TWO>(p, coefs, have, date, spot, v) + net_out[j]) cash[i] = e;
+}
+
+__global__ void mlp_discount_kernel(float* __restrict__ cash, int n, float discount) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) cash[i] *= discount;
 }
 
 // Normal equations of the in-the-money paths at date k (the accumulation of
@@ -586,31 +692,6 @@ __global__ void __launch_bounds__(kLsmcThreads) mlp_poly_sums_kernel(LsmcParams<
         for (int w = 0; w < kLsmcThreads / 32; ++w) v += warp_sums[w][j];
         partials[size_t(blockIdx.x) * S + j] = v;
     }
-}
-
-// Applies the exercise decision of date k + 1 with the continuation fitted there (when
-// `decide`), then discounts the cash to date k (american.rs:1347-1362).
-template <bool TWO>
-__global__ void __launch_bounds__(256) mlp_decide_kernel(LsmcParams<float> p, Features f, int date, int decide,
-                                                         const float* __restrict__ net, const double* __restrict__ coefs,
-                                                         const int* __restrict__ have, const float* __restrict__ a,
-                                                         const float* __restrict__ b, float* __restrict__ cash) {
-    __shared__ float P[kParams];
-    if (decide) load_net(P, net);
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.paths) return;
-    float c = cash[i];
-    if (decide) {
-        const size_t at = size_t(date + 1) * p.paths + i;
-        const float v = TWO ? b[at] : 0.f;
-        const float4 x = features<TWO>(p, f, date + 1, a[at], v);
-        const float e = intrinsic(p, x.w);
-        if (e > 0.f &&
-            e / p.strike > poly_part<TWO>(p, coefs, have, date + 1, x.w, v) + mlp_eval(P, x.x, x.y, x.z))
-            c = e;
-    }
-    cash[i] = c * p.discount;
 }
 
 // In-the-money samples of date k in path order: per-block counts and target sums, a
@@ -722,7 +803,7 @@ __global__ void __launch_bounds__(256) mlp_scatter_kernel(LsmcParams<float> p, F
                                                           const float* __restrict__ cash, const double* __restrict__ coefs,
                                                           const int* __restrict__ have, const int* __restrict__ offsets,
                                                           const TargetNorm* __restrict__ norm,
-                                                          float4* __restrict__ samples) {
+                                                          float4* __restrict__ samples, int* __restrict__ sample_path) {
     __shared__ int warp_base[8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -751,28 +832,19 @@ __global__ void __launch_bounds__(256) mlp_scatter_kernel(LsmcParams<float> p, F
         const int pos = offsets[blockIdx.x] + warp_base[warp] + __popc(ballot & ((1u << lane) - 1u));
         const float y = cash[i] / p.strike - poly_part<TWO>(p, coefs, have, date, x.w, v);
         samples[pos] = make_float4(x.x, x.y, x.z, float((double(y) - norm->mean) / norm->scale));
+        sample_path[pos] = i;
     }
 }
 
-// Date-0 decision and the cash moments (FP64 partials per block).
-template <bool TWO>
-__global__ void __launch_bounds__(256) mlp_final_kernel(LsmcParams<float> p, Features f, const float* __restrict__ net,
-                                                        const double* __restrict__ coefs, const int* __restrict__ have,
-                                                        const float* __restrict__ a, const float* __restrict__ b,
-                                                        const float* __restrict__ cash, double* __restrict__ partials) {
-    __shared__ float P[kParams];
+// The cash moments at date 0, after its decision (FP64 partials per block).
+__global__ void __launch_bounds__(256) mlp_final_kernel(const float* __restrict__ cash, int paths,
+                                                        double* __restrict__ partials) {
     __shared__ double w0[8], w1[8];
-    load_net(P, net);
-    __syncthreads();
     double s0 = 0.0, s1 = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
-        float c = cash[i];
-        const float v = TWO ? b[i] : 0.f;
-        const float4 x = features<TWO>(p, f, 0, a[i], v);
-        const float e = intrinsic(p, x.w);
-        if (e > 0.f && e / p.strike > poly_part<TWO>(p, coefs, have, 0, x.w, v) + mlp_eval(P, x.x, x.y, x.z)) c = e;
-        s0 += double(c);
-        s1 += double(c) * double(c);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < paths; i += gridDim.x * blockDim.x) {
+        const double c = double(cash[i]);
+        s0 += c;
+        s1 += c * c;
     }
     for (int o = 16; o >= 1; o >>= 1) {
         s0 += __shfl_xor_sync(0xffffffffu, s0, o);
@@ -794,22 +866,42 @@ __global__ void __launch_bounds__(256) mlp_final_kernel(LsmcParams<float> p, Fea
     }
 }
 
-// The fitted policy on fresh paths (american.rs:574-637): every thread walks its path
-// forward and stops at the first date whose intrinsic value beats the network.
+// The fitted policy on fresh paths (american.rs:574-637), date by date so that the
+// network runs on the tensor cores: every path carries its state (log spot, variance,
+// value -- negative while alive -- and its PCG32 stream position) from one exercise
+// date to the next; at each date the alive in-the-money paths are compacted, the
+// network evaluates them (mlp_infer_kernel) and those whose intrinsic value beats the
+// continuation stop.
+struct FreshPaths {
+    float* x;
+    float* v;
+    float* value;
+    Pcg* pcg;
+    float* spare;
+    int* has_spare;
+};
+
 template <bool TWO>
-__global__ void __launch_bounds__(256) mlp_lower_bound_kernel(LsmcParams<float> p, Features f, uint64_t seed,
-                                                              const float* __restrict__ nets,
-                                                              const double* __restrict__ coefs,
-                                                              const int* __restrict__ have,
-                                                              double* __restrict__ partials) {
-    __shared__ double w0[8], w1[8];
-    const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
-    double s0 = 0.0, s1 = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
-        PcgSource<float> n;
-        n.start(seed, uint64_t(i), dims);
-        float x = 0.f, v = p.v0, value = 0.f, df = 1.f;
-        for (int k = 0; k < p.dates; ++k) {
+__global__ void __launch_bounds__(256) mlp_fresh_advance_kernel(LsmcParams<float> p, uint64_t seed, int date,
+                                                                float df, FreshPaths st, BlockStats* __restrict__ stats) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool itm = false;
+    if (i < p.paths) {
+        float value = date == 0 ? -1.f : st.value[i];
+        if (value < 0.f) {
+            PcgSource<float> n;
+            float x, v;
+            if (date == 0) {
+                n.start(seed, uint64_t(i), TWO ? p.dates * p.substeps * 2 : p.dates);
+                x = 0.f;
+                v = p.v0;
+            } else {
+                n.g = st.pcg[i];
+                n.spare = st.spare[i];
+                n.has_spare = st.has_spare[i] != 0;
+                x = st.x[i];
+                v = st.v[i];
+            }
             if (!TWO) {
                 x += n.normal();
             } else {
@@ -821,43 +913,70 @@ __global__ void __launch_bounds__(256) mlp_lower_bound_kernel(LsmcParams<float> 
                     v += p.kappa * (p.theta - vp) * p.h + p.xi * sv * (p.rho * z1 + p.rho_bar * z2);
                 }
             }
-            df *= p.discount;
-            const float4 q = features<TWO>(p, f, k, x, v);
-            const float e = intrinsic(p, q.w);
-            if (e > 0.f) {
-                // The last date exercises whenever in the money; earlier ones consult the
-                // network of that date (weights read through L2, warp-uniform).
-                bool stop = k == p.dates - 1;
-                if (!stop)
-                    stop = e / p.strike >
-                           poly_part<TWO>(p, coefs, have, k, q.w, v) + mlp_eval(nets + size_t(k) * kStride, q.x, q.y, q.z);
-                if (stop) {
-                    value = e * df;
-                    break;
-                }
+            const float e = intrinsic(p, spot_at_date<float, TWO>(p, date, x));
+            if (date == p.dates - 1) {
+                value = e > 0.f ? e * df : 0.f;  // the last date exercises whenever in the money
+            } else {
+                itm = e > 0.f;
+                st.pcg[i] = n.g;
+                st.spare[i] = n.spare;
+                st.has_spare[i] = n.has_spare;
             }
+            st.x[i] = x;
+            st.v[i] = v;
+            st.value[i] = value;
         }
-        s0 += double(value);
-        s1 += double(value) * double(value);
     }
-    for (int o = 16; o >= 1; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    const int c = __syncthreads_count(itm);
+    if (threadIdx.x == 0) stats[blockIdx.x] = BlockStats{double(c), 0.0, 0.0};
+}
+
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_fresh_scatter_kernel(LsmcParams<float> p, Features f, int date,
+                                                                FreshPaths st, const int* __restrict__ offsets,
+                                                                float4* __restrict__ samples,
+                                                                int* __restrict__ sample_path) {
+    __shared__ int warp_base[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool itm = false;
+    if (i < p.paths && st.value[i] < 0.f && date < p.dates - 1) {
+        x = features<TWO>(p, f, date, st.x[i], TWO ? st.v[i] : 0.f);
+        itm = intrinsic(p, x.w) > 0.f;
     }
-    if ((threadIdx.x & 31) == 0) {
-        w0[threadIdx.x >> 5] = s0;
-        w1[threadIdx.x >> 5] = s1;
-    }
+    const unsigned ballot = __ballot_sync(0xffffffffu, itm);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_base[warp] = __popc(ballot);
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t0 = 0.0, t1 = 0.0;
+        int run = 0;
         for (int w = 0; w < 8; ++w) {
-            t0 += w0[w];
-            t1 += w1[w];
+            const int c = warp_base[w];
+            warp_base[w] = run;
+            run += c;
         }
-        partials[2 * blockIdx.x] = t0;
-        partials[2 * blockIdx.x + 1] = t1;
     }
+    __syncthreads();
+    if (itm) {
+        const int pos = offsets[blockIdx.x] + warp_base[warp] + __popc(ballot & ((1u << lane) - 1u));
+        samples[pos] = make_float4(x.x, x.y, x.z, 0.f);
+        sample_path[pos] = i;
+    }
+}
+
+template <bool TWO>
+__global__ void __launch_bounds__(256) mlp_fresh_exercise_kernel(LsmcParams<float> p, int date, float df, int count,
+                                                                 const int* __restrict__ sample_path,
+                                                                 const float* __restrict__ net_out,
+                                                                 const double* __restrict__ coefs,
+                                                                 const int* __restrict__ have, FreshPaths st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= count) return;
+    const int i = sample_path[j];
+    const float spot = spot_at_date<float, TWO>(p, date, st.x[i]);
+    const float v = TWO ? st.v[i] : 0.f;
+    const float e = intrinsic(p, spot);
+    if (e > 0.f && e / p.strike > poly_part<TWO>(p, coefs, have, date, spot, v) + net_out[j]) st.value[i] = e * df;
 }
 
 // Deterministic initial weights: uniform(-sqrt(6 / fan_in), sqrt(6 / fan_in)) from a
@@ -887,6 +1006,8 @@ bool configure_train_kernel() {
     done = cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmemBytes)) ==
                cudaSuccess &&
            cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTrainSmemBytes)) ==
+               cudaSuccess &&
+           cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmemBytes)) ==
                cudaSuccess;
     return done;
 }
@@ -943,12 +1064,13 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     const int sblocks = std::min<int>(ctx->sm_count * 4, int((n + kLsmcThreads - 1) / kLsmcThreads));
     // Buffers: path store, cash, samples, counts, parameters and Adam state, per-date
     // networks, gradient partials, estimate partials.
-    const size_t store_bytes = n * d * sizeof(float) * (TWO ? 2 : 1);
+    // The path store; afterwards it holds the fresh paths' state (10 floats per path).
+    const size_t store_bytes = std::max(n * d * (TWO ? 2 : 1), 10 * n) * sizeof(float);
     const size_t net_bytes = size_t(kParams) * sizeof(float);
     const size_t misc_floats = (size_t(3) + d) * kStride + size_t(max_train_blocks) * kStride + 2 * kHidden * kHidden;
     if (ctx->lsmc_store.ensure(store_bytes) || ctx->lsmc_cash.ensure(n * sizeof(float)) ||
-        ctx->mlp_scratch.ensure(n * sizeof(float4) + size_t(pblocks) * (sizeof(BlockStats) + sizeof(int)) +
-                                d * sizeof(TargetNorm) + 256) ||
+        ctx->mlp_scratch.ensure(n * (sizeof(float4) + sizeof(int) + sizeof(float)) +
+                                size_t(pblocks) * (sizeof(BlockStats) + sizeof(int)) + d * sizeof(TargetNorm) + 256) ||
         ctx->mlp_params.ensure(misc_floats * sizeof(float)) ||
         ctx->lsmc_misc.ensure(size_t(fblocks) * 2 * sizeof(double) * 2 + 64) ||
         ctx->lsmc_sums.ensure(size_t(sblocks) * kMaxSums * sizeof(double)) ||
@@ -968,6 +1090,8 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     int* total = counts + pblocks;
     int* error = total + 1;
     GridBarrier* barrier = reinterpret_cast<GridBarrier*>(error + 1);
+    int* sample_path = reinterpret_cast<int*>(barrier + 1);  // path of each compacted sample
+    float* net_out = reinterpret_cast<float*>(sample_path + n);  // the network on the samples
     const bool cooperative = max_train_blocks <= 64 && cooperative_fits(ctx->device, max_train_blocks);
     // Regions of kStride floats keep every one 16-byte aligned (the gradient partials are
     // written as float4).
@@ -1018,10 +1142,25 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     MLP_TRY(cudaGetLastError());
     MLP_TRY(cudaEventRecord(e1, st));
     int launches = 1;
+    int itm_next = 0;  // in-the-money samples of date + 1, still compacted in `samples`
+    // Exercise decisions of date k with its fitted network on the tensor cores: the
+    // compacted in-the-money samples of k go through mlp_infer_kernel, then
+    // mlp_exercise_kernel compares with the intrinsic values.
+    auto decide_at = [&](int k, int count) -> cudaError_t {
+        if (count <= 0) return cudaSuccess;
+        mlp_infer_kernel<<<(count + kRows - 1) / kRows, kRows, kInferSmemBytes, st>>>(nets + size_t(k) * kStride,
+                                                                                      samples, count, net_out, error);
+        mlp_exercise_kernel<TWO><<<(count + 255) / 256, 256, 0, st>>>(p, k, count, sample_path, net_out, coefs, have,
+                                                                      a, b, cash);
+        launches += 2;
+        return cudaGetLastError();
+    };
     for (int date = p.dates - 2; date >= 0; --date) {
-        const int decide = date + 1 <= p.dates - 2;
-        mlp_decide_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, decide, nets + size_t(date + 1) * kStride, coefs,
-                                                       have, a, b, cash);
+        // Date + 1's decision (none at expiry, where the cash already is the intrinsic
+        // value), then the cash discounted to this date (american.rs:1347-1362).
+        if (date + 1 <= p.dates - 2) MLP_TRY(decide_at(date + 1, itm_next));
+        mlp_discount_kernel<<<pblocks, 256, 0, st>>>(cash, p.paths, p.discount);
+        ++launches;
         // The polynomial fit of this date (lsmc_solve: block-ordered merge, pivoted FP64
         // elimination with degree fallback), then the residual samples.
         mlp_poly_sums_kernel<TWO><<<sblocks, kLsmcThreads, 0, st>>>(p, date, a, b, cash, poly_partials);
@@ -1030,12 +1169,13 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         mlp_count_kernel<TWO><<<pblocks, 256, 0, st>>>(p, date, a, b, cash, coefs, have, stats);
         mlp_scan_kernel<<<1, kScanThreads, 0, st>>>(stats, pblocks, counts, total, norms + date);
         mlp_scatter_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, a, b, cash, coefs, have, counts, norms + date,
-                                                        samples);
-        launches += 6;
+                                                        samples, sample_path);
+        launches += 5;
         MLP_TRY(cudaGetLastError());
         int itm = 0;
         MLP_TRY(cudaMemcpyAsync(&itm, total, sizeof(int), cudaMemcpyDeviceToHost, st));
         MLP_TRY(cudaStreamSynchronize(st));
+        itm_next = itm;
         // Training samples: the first `mlp_samples` in-the-money paths (an i.i.d.
         // subsample, the paths being independent), or all of them.
         if (s->mlp_samples > 0 && itm > s->mlp_samples) itm = s->mlp_samples;
@@ -1066,13 +1206,45 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         mlp_snapshot_kernel<<<(kParams + 255) / 256, 256, 0, st>>>(params, norms + date, nets + size_t(date) * kStride);
         ++launches;
     }
-    mlp_final_kernel<TWO><<<fblocks, 256, 0, st>>>(p, f, nets, coefs, have, a, b, cash, finals);
+    // Date 0's decision on its compacted samples, then the cash moments.
+    MLP_TRY(decide_at(0, itm_next));
+    mlp_final_kernel<<<fblocks, 256, 0, st>>>(cash, p.paths, finals);
     ++launches;
     MLP_TRY(cudaGetLastError());
     MLP_TRY(cudaEventRecord(e2, st));
     const bool lower = fresh_seed != s->seed;
     if (lower) {
-        mlp_lower_bound_kernel<TWO><<<fblocks, 256, 0, st>>>(p, f, fresh_seed, nets, coefs, have, lower_partials);
+        // Fresh paths, date by date; the path store's buffer is free again and holds
+        // their state.
+        FreshPaths fp;
+        fp.x = a;
+        fp.v = a + n;
+        fp.value = a + 2 * n;
+        fp.pcg = reinterpret_cast<Pcg*>(a + 4 * n);  // 16-byte aligned: 4 n floats in
+        fp.spare = a + 8 * n;
+        fp.has_spare = reinterpret_cast<int*>(a + 9 * n);
+        float df = 1.f;
+        for (int k = 0; k < p.dates; ++k) {
+            df *= p.discount;
+            mlp_fresh_advance_kernel<TWO><<<pblocks, 256, 0, st>>>(p, fresh_seed, k, df, fp, stats);
+            launches += 1;
+            if (k == p.dates - 1) break;
+            mlp_scan_kernel<<<1, kScanThreads, 0, st>>>(stats, pblocks, counts, total, norms + k);
+            mlp_fresh_scatter_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, k, fp, counts, samples, sample_path);
+            launches += 2;
+            MLP_TRY(cudaGetLastError());
+            int alive = 0;
+            MLP_TRY(cudaMemcpyAsync(&alive, total, sizeof(int), cudaMemcpyDeviceToHost, st));
+            MLP_TRY(cudaStreamSynchronize(st));
+            if (alive > 0) {
+                mlp_infer_kernel<<<(alive + kRows - 1) / kRows, kRows, kInferSmemBytes, st>>>(
+                    nets + size_t(k) * kStride, samples, alive, net_out, error);
+                mlp_fresh_exercise_kernel<TWO><<<(alive + 255) / 256, 256, 0, st>>>(p, k, df, alive, sample_path,
+                                                                                    net_out, coefs, have, fp);
+                launches += 2;
+            }
+        }
+        mlp_final_kernel<<<fblocks, 256, 0, st>>>(fp.value, p.paths, lower_partials);
         ++launches;
         MLP_TRY(cudaGetLastError());
     }
