@@ -512,9 +512,12 @@ def run_workload(args, name):
 
 
 def run_lsmc(args):
-    """American put under Heston (2^20 paths, 50 exercise dates, 5 Euler substeps): the
-    polynomial LSMC against the polynomial plus the fitted network, both judged by the
-    Heston ADI price; the polynomial is also run at the network's wall time."""
+    """American put under Heston, 50 exercise dates x 5 Euler substeps, judged by the
+    Heston ADI price.  Two comparisons of the polynomial LSMC (the reference's method)
+    with the polynomial plus the fitted network: at the configuration's 2^20 paths
+    (network: 5 epochs per date over every in-the-money path, batch 8192), and at equal
+    wall time (network at 2^22 paths training on 131,072 samples per date, against the
+    polynomial at the path count whose wall time is closest)."""
     from kiyosi_gb300 import _native, abi, workloads
     from oracle import loader
     native = _native.context(0)
@@ -524,42 +527,45 @@ def run_lsmc(args):
     adi = loader.load().kor_heston_adi_american(C.byref(model), 100.0, -1.0, 1.0, 400, 100, 400, 1)
     adi_s = time.perf_counter() - t0
 
-    def price(basis, paths, precision=abi.PRECISION_FP32):
-        s = abi.LsmcSettings(path_count=paths, exercise_dates=50, substeps=5, basis=basis,
+    def price(basis, log2_paths, samples=0, precision=abi.PRECISION_FP32):
+        s = abi.LsmcSettings(path_count=1 << log2_paths, exercise_dates=50, substeps=5, basis=basis,
                              sampling=0, precision=precision, mlp_epochs=5, mlp_batch=8192,
-                             mlp_hidden=64, mlp_learning_rate=1e-3, seed=42, mlp_seed=7)
+                             mlp_hidden=64, mlp_samples=samples, mlp_learning_rate=1e-3, seed=42,
+                             mlp_seed=7)
         out = abi.LsmcResult()
-        for _ in range(max(1, args.warmup // 3)):
+        for _ in range(1 + max(0, args.warmup // 3)):
             native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0,
                                                     1.0, C.byref(s), 43, C.byref(out)))
-        native.check(native.lib.kgpu_lsmc_price(native.handle, C.byref(model), 100.0, -1.0, 1.0,
-                                                C.byref(s), 43, C.byref(out)))
+
         def num(x):
             return None if x != x else x
-        return {"paths": paths, "price": out.price, "standard_error": out.standard_error,
+        return {"paths": 1 << log2_paths, "training_samples_per_date": samples or "all",
+                "price": out.price, "standard_error": out.standard_error,
                 "out_of_sample": out.out_of_sample,
                 "out_of_sample_error": out.out_of_sample_error,
                 "error_vs_adi": out.price - adi, "out_of_sample_error_vs_adi": out.out_of_sample - adi,
                 "wall_ms": out.wall_ms, "path_store_ms": num(out.path_store_ms),
                 "regression_ms": num(out.regression_ms)}
 
-    poly = price(abi.BASIS_POLY3, 1 << 20)
-    poly64 = price(abi.BASIS_POLY3, 1 << 20, abi.PRECISION_FP64)
-    mlp = price(abi.BASIS_MLP, 1 << 20)
-    scale = max(1, int(round(math.log2(max(1.0, mlp["wall_ms"] / poly["wall_ms"])))))
-    equal = price(abi.BASIS_POLY3, 1 << min(26, 20 + scale))
+    poly = price(abi.BASIS_POLY3, 20)
+    poly64 = price(abi.BASIS_POLY3, 20, precision=abi.PRECISION_FP64)
+    mlp = price(abi.BASIS_MLP, 20)
+    mlp_eq = price(abi.BASIS_MLP, 22, samples=131072)
+    polys = [price(abi.BASIS_POLY3, k) for k in range(21, 26)]
+    equal = min(polys, key=lambda r: abs(r["wall_ms"] - mlp_eq["wall_ms"]))
     line = {
-        "metric": "LSMC |price - ADI|: polynomial + fitted network vs polynomial at equal wall time",
-        "value": abs(mlp["out_of_sample_error_vs_adi"]), "unit": "price units (out-of-sample)",
+        "metric": "LSMC |price - ADI| at equal wall time: polynomial + fitted network vs polynomial",
+        "value": abs(mlp_eq["error_vs_adi"]), "unit": "price units",
         "higher_is_better": False, "n_gpus": 1, "dtype": "f32 paths, bf16 network, f64 solve",
         "data": "synthetic (seeded PCG32 draws; benchmark model parameters)",
         "config": {"workload": "American put under Heston (S0=K=100, v0=theta=0.04, kappa=2, "
-                               "xi=0.5, rho=-0.7, r=0.03, T=1), 2^20 paths, 50 exercise dates "
-                               "x 5 Euler substeps; network 3-64-64-1, 5 epochs/date, batch 8192",
-                   "fresh_paths_seed": 43},
+                               "xi=0.5, rho=-0.7, r=0.03, T=1), 50 exercise dates x 5 Euler "
+                               "substeps; network 3-64-64-1 on the polynomial's residual, 5 "
+                               "epochs/date, batch 8192", "fresh_paths_seed": 43},
         "adi": {"price": adi, "grid": "400 x 100 x 400 (MCS, Ikonen-Toivanen)", "cpu_s": adi_s},
-        "poly3_fp32": poly, "poly3_fp64": poly64, "poly3_plus_network": mlp,
-        "poly3_at_equal_wall_time": equal,
+        "at_2^20_paths": {"poly3_fp32": poly, "poly3_fp64": poly64, "poly3_plus_network": mlp},
+        "at_equal_wall_time": {"poly3_plus_network": mlp_eq, "poly3": equal},
+        "poly3_by_paths": polys,
     }
     print(json.dumps(line), flush=True)
 
