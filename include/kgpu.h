@@ -103,8 +103,11 @@ enum {
     KGPU_PAYOFF_AUTOCALLABLE = 3, /* snowball / phoenix / binary / ternary (autocallable.rs:823-862) */
     KGPU_PAYOFF_ACCUMULATOR = 4,  /* accumulator.rs:160-216 */
     KGPU_PAYOFF_DIGITAL = 5,      /* terminal digital, one dimension (digital.rs:111-130) */
-    KGPU_PAYOFF_BARRIER = 6       /* continuously monitored single barrier: one terminal draw
+    KGPU_PAYOFF_BARRIER = 6,      /* continuously monitored single barrier: one terminal draw
                                      and Brownian-bridge survival (barrier.rs:231-452) */
+    KGPU_PAYOFF_BARRIER_DISCRETE = 7 /* single barrier observed on dates (barrier.rs:231-452):
+                                     one step per date; one kgpu_event per step holds the
+                                     date's record (see kgpu_contract) */
 };
 
 /* One simulated grid step of a contract.  For BSM the transition is the reference's
@@ -163,7 +166,13 @@ enum {
     KGPU_C_BRIDGE = 16,          /* sample with the Brownian bridge plan */
     KGPU_C_ASSET_DIGITAL = 32,   /* digital pays the asset (no payout amount) */
     KGPU_C_BARRIER_UP = 64,      /* barrier above the spot (else below) */
-    KGPU_C_BARRIER_IN = 128      /* knock-in (else knock-out) */
+    KGPU_C_BARRIER_IN = 128,     /* knock-in (else knock-out) */
+    KGPU_C_REBATE_AT_HIT = 256,  /* discrete knock-out: rebate paid on the hit date */
+    KGPU_C_CONDITION_ON_HIT = 512, /* discrete knock-in: after a hit with more than 8 dates left,
+                                     the vanilla is priced analytically from the hit */
+    KGPU_C_CHECK_STEPS = 1024     /* discrete barrier whose paths can leave the representable
+                                     range: a spot that overflows or underflows fails the
+                                     pricing (barrier.rs:280-289) */
 };
 
 /* A contract's plan.  Field groups are used by the payoff families named beside them. */
@@ -210,6 +219,15 @@ typedef struct kgpu_contract {
     double rebate;            /* paid at expiry when the vanilla leg is not */
     double spot;
     double log_discount;      /* -r T */
+    /* discretely observed barrier: steps hold drift = (r - q - sigma^2/2) t_i and
+     * diffusion = sigma sqrt(t_i - t_{i-1}); event i holds knock_out = the noise level
+     * sum(diffusion z) at which date i touches the barrier, coupon_barrier = T - t_i,
+     * payment[0] = -r t_i, payment[1] = -r t_i - q (T - t_i), payment[2] = sqrt(T - t_i),
+     * has_knock_out = 1 when date i is observed (the last step may be an unobserved
+     * expiry).  moneyness, half_variance (sigma^2 / 2), strike, sign, rebate, spot and
+     * log_discount as above. */
+    double volatility;
+    double dividend;
 } kgpu_contract;
 
 /* A book of contracts sharing one model.  Arrays are indexed through the offsets in

@@ -33,6 +33,7 @@ PAYOFF_AUTOCALLABLE = 3
 PAYOFF_ACCUMULATOR = 4
 PAYOFF_DIGITAL = 5
 PAYOFF_BARRIER = 6
+PAYOFF_BARRIER_DISCRETE = 7
 
 STEP_KNOCK_IN = 1
 STEP_EVENT = 2
@@ -47,6 +48,9 @@ C_BRIDGE = 16
 C_ASSET_DIGITAL = 32
 C_BARRIER_UP = 64
 C_BARRIER_IN = 128
+C_REBATE_AT_HIT = 256
+C_CONDITION_ON_HIT = 512
+C_CHECK_STEPS = 1024
 
 UNCERTAINTY_NAMES = {
     0: "available",
@@ -107,7 +111,8 @@ class Contract(C.Structure):
                 ("knock_out", _D), ("quantity", _D), ("daily_quantity", _D),
                 ("acceleration", _D), ("log_strike", _D),
                 ("barrier_drift", _D), ("barrier_distance", _D), ("barrier_moneyness", _D),
-                ("rebate", _D), ("spot", _D), ("log_discount", _D)]
+                ("rebate", _D), ("spot", _D), ("log_discount", _D), ("volatility", _D),
+                ("dividend", _D)]
 
 
 class Book(C.Structure):

@@ -806,10 +806,14 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: path_count must be positive", i);
         if (k.sobol && !is_pow2(paths))
             return fail(ctx, KGPU_INVALID_INPUT, "path_count must be a power of two for Sobol sampling");
-        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_BARRIER)
+        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_BARRIER_DISCRETE)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: unknown payoff %d", i, c.payoff);
         if (c.payoff == KGPU_PAYOFF_BARRIER && (model->kind != KGPU_MODEL_BSM || !(c.diffusion > 0.0)))
             return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "contract %d: the Monte Carlo barrier needs BSM volatility", i);
+        if (c.payoff == KGPU_PAYOFF_BARRIER_DISCRETE &&
+            (model->kind != KGPU_MODEL_BSM || c.event_count != c.step_count || !book->events))
+            return fail(ctx, KGPU_INVALID_INPUT,
+                        "contract %d: a scheduled barrier needs BSM and one event record per date", i);
         if (c.step_count < 1 || c.step_offset < 0 || c.step_offset + c.step_count > book->step_total)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: steps out of range", i);
         if (c.event_count < 0 || c.event_offset < 0 || c.event_offset + c.event_count > book->event_total)

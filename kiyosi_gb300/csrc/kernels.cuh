@@ -127,6 +127,8 @@ __global__ void compile_contracts_kernel(const kgpu_contract* in, int n, Contrac
     o.rebate = Real(c.rebate);
     o.spot = Real(c.spot);
     o.log_discount = Real(c.log_discount);
+    o.volatility = Real(c.volatility);
+    o.dividend = Real(c.dividend);
     out[i] = o;
 }
 

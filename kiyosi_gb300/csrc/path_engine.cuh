@@ -82,6 +82,7 @@ struct ContractT {
     Real downside_lower, downside_upper, downside_initial, final_discount;
     Real knock_out, quantity, daily_quantity, acceleration, log_strike;
     Real barrier_drift, barrier_distance, barrier_moneyness, rebate, spot, log_discount;
+    Real volatility, dividend;
 };
 
 // Device view of the book in the kernel's precision.
@@ -442,6 +443,56 @@ __device__ __forceinline__ Real barrier_value(const ContractT<Real>& c, Real z) 
            weighted_amount(c.rebate, c.log_discount + (in ? survival : exponent));
 }
 
+__device__ __forceinline__ double xerfc(double x) { return erfc(x); }
+__device__ __forceinline__ float xerfc(float x) { return erfcf(x); }
+
+// normal_cdf, log_normal_cdf, log_normal_tail, weighted_cdf (numerics.rs:192-224).
+template <class Real>
+__device__ __forceinline__ Real normal_cdf_of(Real x) {
+    return Real(0.5) * xerfc(-x * Real(0.70710678118654752440));
+}
+
+template <class Real>
+__device__ Real log_normal_cdf_of(Real x) {
+    if (x >= Real(-10)) return xlog(normal_cdf_of(x));
+    const Real inverse_square = (Real(1) / x) / x;
+    Real term = Real(1), sum = Real(1);
+    for (int k = 1; k <= 20; ++k) {
+        term *= -Real(2 * k - 1) * inverse_square;
+        sum += term;
+    }
+    return Real(-0.5) * x * x - xlog(-x) + xlog(sum / Real(2.5066282746310002));
+}
+
+template <class Real>
+__device__ __forceinline__ Real weighted_cdf_of(Real amount, Real exponent, Real argument) {
+    const Real discount = xexp(exponent);
+    const Real discounted = amount * discount;
+    if (argument < Real(-10) || !xnormal(discount) || !(xabs(discounted) <= xinf(Real(0))))
+        return xexp(xlog(amount) + exponent + log_normal_cdf_of(argument));
+    return discounted * normal_cdf_of(argument);
+}
+
+// lognormal_price (engines/analytic/european.rs:317-403) for widths of at least 1e-5
+// (narrower ones return NaN, reported as a computation failure).  Out of line: it runs
+// once per conditioned path, and inlining it would raise the stepping loop's registers.
+template <class Real>
+__device__ __noinline__ Real lognormal_price_of(Real spot, Real strike, Real log_moneyness, Real asset_log, Real risk_log,
+                                   Real volatility, Real root_time, Real sign) {
+    const Real width = volatility * root_time;
+    if (!(width >= Real(1e-5))) return xnan(Real(0));
+    const Real standardized = log_moneyness / width;
+    const Real d1 = standardized + Real(0.5) * width, d2 = standardized - Real(0.5) * width;
+    const Real asset = weighted_cdf_of(spot, asset_log, sign * d1);
+    const Real cash = weighted_cdf_of(strike, risk_log, sign * d2);
+    const Real direct = sign * (asset - cash);
+    if (xabs(direct) <= xinf(Real(0))) return direct;
+    const Real la = log_moneyness + log_normal_cdf_of(sign * d1), lc = log_normal_cdf_of(sign * d2);
+    const Real hi = sign > Real(0) ? la : lc, lo = sign > Real(0) ? lc : la;
+    const Real difference = hi == -xinf(Real(0)) ? hi : hi + xlog(-xexpm1(lo - hi));
+    return xexp(xlog(strike) + risk_log + difference);
+}
+
 template <class Real>
 struct PlanPtrs {
     const StepT<Real>* __restrict__ steps;
@@ -541,6 +592,47 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
     if (payoff == KGPU_PAYOFF_BARRIER) {
         value = barrier_value(c, n.normal());
         s.executed = 1;
+        return true;
+    }
+    if (payoff == KGPU_PAYOFF_BARRIER_DISCRETE) {
+        // Scheduled monitoring (barrier.rs:306-449): the noise sum(width z) against each
+        // observed date's touch level; a knock-out stops at its hit, a knock-in with more
+        // than 8 dates left is priced analytically from its hit.
+        const int i = s.i;
+        const StepT<Real> st = p.steps[i];
+        s.lr = xfma(st.diffusion, n.normal(), s.lr);
+        s.i = i + 1;
+        s.executed += 1;
+        if (c.flags & KGPU_C_CHECK_STEPS) {
+            const Real spot_now = weighted_amount(c.spot, st.drift + s.lr);
+            if (!(spot_now > Real(0) && spot_now < xinf(Real(0)))) {
+                value = xnan(Real(0));  // unrepresentable path: reported as a computation failure
+                return true;
+            }
+        }
+        const EventT<Real> e = p.events[i];
+        const bool in = (c.flags & KGPU_C_BARRIER_IN) != 0;
+        if (e.has_knock_out &&
+            ((c.flags & KGPU_C_BARRIER_UP) ? s.lr >= e.knock_out : s.lr <= e.knock_out)) {
+            s.knocked_in = true;  // touched
+            if ((c.flags & KGPU_C_CONDITION_ON_HIT) && c.step_count - i > 8) {
+                const Real asset = weighted_amount(c.spot, st.drift + s.lr);
+                value = lognormal_price_of(asset, c.strike, c.moneyness + s.lr + c.half_variance * e.coupon_barrier,
+                                           e.payment[1], c.log_discount, c.volatility, e.payment[2], c.sign);
+                return true;
+            }
+            if (!in) {
+                value = weighted_amount(c.rebate, (c.flags & KGPU_C_REBATE_AT_HIT) ? e.payment[0] : c.log_discount);
+                return true;
+            }
+        }
+        if (s.i < c.step_count) return false;
+        const Real asset = weighted_amount(c.spot, st.drift + s.lr);
+        const Real distance = c.moneyness + s.lr;
+        const Real payoff_value = xabs(distance) < Real(0.5) ? c.strike * xexpm1(distance) : asset - c.strike;
+        Real intrinsic = c.sign * payoff_value;
+        intrinsic = intrinsic > Real(0) ? intrinsic : Real(0);
+        value = weighted_amount(s.knocked_in == in ? intrinsic : c.rebate, c.log_discount);
         return true;
     }
     // Grid-stepping families.

@@ -63,13 +63,16 @@ BARRIER_TYPES = ("down_and_out", "down_and_in", "up_and_out", "up_and_in")
 
 @dataclass(frozen=True)
 class BarrierOption(EuropeanOption):
-    """Continuously monitored single-barrier vanilla option (BarrierOption with
-    ObservationMode::Continuous, instruments/barrier.rs).  `rebate` is paid at expiry
-    unless `rebate_timing` is 'at_hit' (knock-outs only)."""
+    """Single-barrier vanilla option (instruments/barrier.rs).  `observation_times`
+    (years after valuation, strictly increasing, within the option's life) makes the
+    monitoring scheduled; None monitors continuously (ObservationMode::Continuous).
+    `rebate` is paid at expiry unless `rebate_timing` is 'at_hit', which only knock-outs
+    may use (barrier.rs:198-202)."""
     barrier: float = 0.0
     barrier_type: str = "down_and_out"
     rebate: float = 0.0
     rebate_timing: str = "at_expiry"
+    observation_times: Optional[Sequence[float]] = None
 
     def __post_init__(self):
         super().__post_init__()
@@ -81,6 +84,17 @@ class BarrierOption(EuropeanOption):
             raise InvalidInputError("rebate must be nonnegative and finite")
         if self.rebate_timing not in ("at_expiry", "at_hit"):
             raise InvalidInputError("rebate_timing must be 'at_expiry' or 'at_hit'")
+        if self.is_knock_in and self.rebate_timing == "at_hit":
+            raise InvalidInputError("knock-in rebates cannot pay at hit")
+        if self.observation_times is not None:
+            times = tuple(_times(self.observation_times, self.expiry, "observation_times"))
+            if not times:
+                raise InvalidInputError("a scheduled barrier needs at least one observation time")
+            object.__setattr__(self, "observation_times", times)
+
+    @property
+    def continuous(self) -> bool:
+        return self.observation_times is None
 
     @property
     def is_up(self) -> bool:

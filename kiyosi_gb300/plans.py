@@ -19,7 +19,7 @@ from typing import List, Optional
 
 import numpy as np
 
-from . import abi
+from . import abi, analytic
 from .errors import UnsupportedOperationError, ComputationFailureError, InvalidInputError
 from .instruments import (Accumulator, AsianOption, AutocallableNote, BarrierOption,
                           DigitalOption, EuropeanOption)
@@ -162,50 +162,84 @@ def digital(option: DigitalOption, ctx: PricingContext):
     return ContractPlan(c, steps, np.zeros(1, np.uint8))
 
 
+def _barrier_resolution(option: BarrierOption, ctx: PricingContext):
+    """resolved_price (engines/analytic/barrier.rs:20-78) with the state of
+    instruments/monitoring.rs:293-320, valuation at the option's start: a barrier is
+    touched now when today is monitored (always for continuous monitoring, an
+    observation time of 0 for scheduled) and the spot is at or beyond it.  Returns the
+    settled price, or None when the option must be sampled."""
+    rate = ctx.model.rate
+    spot, level, time = ctx.spot, option.barrier, option.expiry
+    up, knock_in = option.is_up, option.is_knock_in
+    times = option.observation_times
+    monitored = option.continuous or times[0] == 0.0
+    hit = spot >= level if up else spot <= level
+    touched = monitored and hit
+    finished = time == 0.0 or (not option.continuous and times[-1] <= 0.0)
+
+    def cash():
+        if option.rebate == 0.0:
+            return 0.0
+        return analytic.discounted_product(option.rebate, 1.0, -rate * time)
+
+    if touched and not knock_in:
+        return option.rebate if option.rebate_timing == "at_hit" else cash()
+    if not touched and finished and knock_in:
+        return cash()
+    requires_touch = (option.continuous or times[-1] == time) and (
+        (option.sign > 0.0 and option.strike >= level) if up else
+        (option.sign < 0.0 and option.strike <= level))
+    fixed = option.rebate == 0.0 and requires_touch
+    if fixed and not knock_in:
+        return 0.0
+    if touched or finished or fixed:
+        return analytic.european_price(option.sign, option.strike, time, ctx)
+    return None
+
+
 def barrier(option: BarrierOption, ctx: PricingContext):
-    """MonteCarloBarrierEngine::native for continuous monitoring (barrier.rs:231-452):
-    one terminal draw per path with Brownian-bridge survival.  Barriers already touched
-    at valuation resolve before sampling (analytic/barrier.rs:32-66): a knock-out pays
-    its rebate, a knock-in is the vanilla option."""
+    """MonteCarloBarrierEngine::native (barrier.rs:231-452) for single barriers.
+    Barriers settled at valuation resolve first (analytic/barrier.rs:20-78): a touched
+    knock-out pays its rebate, a touched knock-in is the analytic vanilla option.
+    Continuous monitoring draws one terminal normal per path and weights it by the
+    Brownian-bridge survival; scheduled monitoring steps date by date (one normal per
+    observation, plus an unobserved expiry leg when the last observation is earlier)."""
     model = ctx.model
     if not isinstance(model, BlackScholesMertonParameters):
         raise UnsupportedOperationError("the Monte Carlo barrier engine requires BSM parameters")
+    resolved = _barrier_resolution(option, ctx)
+    if resolved is not None:
+        return Known(resolved)
     rate, dividend, sigma = model.rate, model.dividend, model.volatility
     spot, level, time = ctx.spot, option.barrier, option.expiry
     up, knock_in = option.is_up, option.is_knock_in
     at_hit = option.rebate_timing == "at_hit"
-    touched = spot >= level if up else spot <= level
-    expiry_rebate = option.rebate * math.exp(-rate * time)
-    if touched:
-        if knock_in:
-            return european(EuropeanOption(option.option_type, option.strike, time), ctx)
-        return Known(option.rebate if at_hit else expiry_rebate)
-    if time == 0.0:
-        return Known(option.rebate if knock_in else max(option.sign * (spot - option.strike), 0.0))
     if sigma == 0.0:
         raise UnsupportedOperationError("zero volatility: the barrier is deterministic")
-    if at_hit and not knock_in and option.rebate != 0.0:
-        raise UnsupportedOperationError("at-hit rebates of knock-out barriers are not sampled")
     carry_rate = rate - dividend
     half_variance_rate = 0.5 * sigma * sigma
     drift = carry_rate - half_variance_rate
+
+    def mean_distance(elapsed, lvl):
+        return (log_ratio(spot, lvl) + carry_rate * elapsed) - half_variance_rate * elapsed
+
+    if not option.continuous:
+        return _scheduled_barrier(option, ctx, drift, half_variance_rate, mean_distance)
+    if at_hit and not knock_in and option.rebate != 0.0:
+        raise UnsupportedOperationError("at-hit rebates of continuously monitored knock-outs are not sampled")
     width = sigma * math.sqrt(time)
     mean = drift * time
     if not (width > 0.0 and math.isfinite(width) and math.isfinite(mean)):
         raise _unstable()
-
-    def mean_distance(lvl):
-        return (log_ratio(spot, lvl) + carry_rate * time) - half_variance_rate * time
-
     c = _new_contract(abi.PAYOFF_BARRIER)
     c["flags"] = (abi.C_BARRIER_UP if up else 0) | (abi.C_BARRIER_IN if knock_in else 0)
     c["strike"] = option.strike
     c["sign"] = option.sign
     c["diffusion"] = width
-    c["moneyness"] = mean_distance(option.strike)
+    c["moneyness"] = mean_distance(time, option.strike)
     c["barrier_drift"] = mean
     c["barrier_distance"] = abs(log_ratio(level, spot))
-    c["barrier_moneyness"] = mean_distance(level)
+    c["barrier_moneyness"] = mean_distance(time, level)
     c["rebate"] = option.rebate
     c["spot"] = spot
     c["log_discount"] = -rate * time
@@ -213,6 +247,71 @@ def barrier(option: BarrierOption, ctx: PricingContext):
     steps = np.zeros(1, STEP_DTYPE)
     steps[0] = (mean, width, 0.0, math.exp(-rate * time))
     return ContractPlan(c, steps, np.zeros(1, np.uint8))
+
+
+def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_variance_rate,
+                       mean_distance):
+    """The scheduled branch of barrier.rs:240-449: one grid step and one event record per
+    remaining observation (plus the unobserved expiry leg).  Step i holds the cumulative
+    mean drift * t_i and the width sigma sqrt(t_i - t_(i-1)); event i holds the noise
+    level at which date i touches the barrier, the discount and asset log weights of a
+    hit, and the remaining time and its root for the conditioned vanilla."""
+    model = ctx.model
+    rate, dividend, sigma = model.rate, model.dividend, model.volatility
+    spot, level, time = ctx.spot, option.barrier, option.expiry
+    dates = [t for t in option.observation_times if t > 0.0]
+    legs = [(t, True) for t in dates]
+    if not dates or dates[-1] != time:
+        legs.append((time, False))
+    n = len(legs)
+    steps = np.zeros(n, STEP_DTYPE)
+    events = np.zeros(n, EVENT_DTYPE)
+    previous = 0.0
+    width_sum = 0.0
+    for i, (date, observe) in enumerate(legs):
+        dt = date - previous
+        width = sigma * math.sqrt(dt)
+        mean = drift * date
+        if not (width > 0.0 and math.isfinite(width) and math.isfinite(mean)):
+            raise _unstable()
+        remaining = time - date
+        discount = -rate * date
+        steps[i] = (mean, width, date, math.exp(discount))
+        events[i]["knock_out"] = -mean_distance(date, level) if observe else 0.0
+        events[i]["coupon_barrier"] = remaining
+        events[i]["payment"] = (discount, discount - dividend * remaining, math.sqrt(remaining), 0.0)
+        events[i]["has_knock_out"] = 1 if observe else 0
+        events[i]["step"] = i
+        width_sum += width
+        previous = date
+    # Both normal samplers stay within ten standard deviations; paths that could still
+    # leave the representable range are checked step by step.
+    bounded = abs(math.log(spot)) + 10.0 * width_sum + abs(drift * time) < 600.0
+    knock_in = option.is_knock_in
+    condition = knock_in and n > 8 and bounded
+    if condition:
+        # Conditioned hits price a vanilla of width sigma sqrt(remaining); the narrow-width
+        # regimes of that pricing are not sampled.
+        narrowest = min(sigma * float(events[i]["payment"][2]) for i in range(n - 8))
+        if not narrowest >= 1e-5:
+            raise UnsupportedOperationError("conditioned knock-in widths below 1e-5 are not sampled")
+    c = _new_contract(abi.PAYOFF_BARRIER_DISCRETE)
+    c["flags"] = ((abi.C_BARRIER_UP if option.is_up else 0) | (abi.C_BARRIER_IN if knock_in else 0)
+                  | (abi.C_REBATE_AT_HIT if option.rebate_timing == "at_hit" else 0)
+                  | (abi.C_CONDITION_ON_HIT if condition else 0)
+                  | (0 if bounded else abi.C_CHECK_STEPS))
+    c["strike"] = option.strike
+    c["sign"] = option.sign
+    c["moneyness"] = mean_distance(time, option.strike)
+    c["half_variance"] = half_variance_rate
+    c["rebate"] = option.rebate
+    c["spot"] = spot
+    c["log_discount"] = -rate * time
+    c["volatility"] = sigma
+    c["dividend"] = dividend
+    c["step_count"] = n
+    c["event_count"] = n
+    return ContractPlan(c, steps, np.zeros(n, np.uint8), events)
 
 
 def path_vanilla(option: EuropeanOption, ctx: PricingContext, step_count: int):

@@ -261,8 +261,11 @@ class MonteCarloDigitalEngine(_MonteCarloEngine):
 
 
 class MonteCarloBarrierEngine(_MonteCarloEngine):
-    """Continuously monitored single barriers (barrier.rs): one terminal draw per path,
-    weighted by the Brownian-bridge survival or hit probability."""
+    """Single barriers (barrier.rs:231-452).  Continuous monitoring: one terminal draw
+    per path, weighted by the Brownian-bridge survival or hit probability.  Scheduled
+    monitoring: one draw per observation date (plus an unobserved expiry leg); knock-outs
+    stop at the hit with their rebate (at expiry or at the hit), and dense knock-ins
+    price the vanilla analytically from the hit."""
 
     def price_with_statistics(self, option: BarrierOption, ctx: PricingContext):
         return self._run(ctx, [plans.barrier(option, ctx)])[0]

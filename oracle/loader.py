@@ -77,7 +77,8 @@ def price_book(ctx, packed, settings, threads=0):
     book = packed.struct()
     status = lib.kor_price_book(C.byref(model), C.byref(book), C.byref(settings), out, threads)
     if status != 0:
-        raise RuntimeError(f"oracle status {status}")
+        from kiyosi_gb300.errors import raise_for_status
+        raise_for_status(status, "oracle")
     return list(out)
 
 

@@ -310,6 +310,100 @@ static double barrier_payoff(const kgpu_contract* c, double z, Failure& f) {
     return value;
 }
 
+// normal_cdf, log_normal_cdf, log_normal_tail and weighted_cdf (numerics.rs:192-224).
+static double normal_cdf(double x) { return 0.5 * std::erfc(-x * 0.70710678118654752440); }
+
+static double log_normal_cdf(double x) {
+    if (x >= -10.0) return std::log(normal_cdf(x));
+    const double inverse_square = (1.0 / x) / x;
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k <= 20; ++k) {
+        term *= -double(2 * k - 1) * inverse_square;
+        sum += term;
+    }
+    return -0.5 * x * x - std::log(-x) + std::log(sum / std::sqrt(2.0 * M_PI));
+}
+
+static double weighted_cdf(double amount, double exponent, double argument) {
+    const double discount = std::exp(exponent);
+    const double discounted = amount * discount;
+    if (argument < -10.0 || !std::isnormal(discount) || !std::isfinite(discounted))
+        return std::exp(std::log(amount) + exponent + log_normal_cdf(argument));
+    return discounted * normal_cdf(argument);
+}
+
+// lognormal_price (engines/analytic/european.rs:317-403), the branch for widths of at
+// least 1e-5 (plans with narrower conditioned widths are rejected before sampling).
+static double lognormal_price(double spot, double strike, double log_moneyness, double asset_log,
+                              double risk_log, double volatility, double root_time, double sign,
+                              Failure& f) {
+    const double width = volatility * root_time;
+    if (!(width >= 1e-5)) {
+        f.failed = true;
+        return 0.0;
+    }
+    const double standardized = log_moneyness / width;
+    const double d1 = standardized + 0.5 * width, d2 = standardized - 0.5 * width;
+    const double asset = weighted_cdf(spot, asset_log, sign * d1);
+    const double cash = weighted_cdf(strike, risk_log, sign * d2);
+    const double direct = sign * (asset - cash);
+    if (std::isfinite(direct)) return direct;
+    const double la = log_moneyness + log_normal_cdf(sign * d1), lc = log_normal_cdf(sign * d2);
+    const double hi = sign > 0.0 ? la : lc, lo = sign > 0.0 ? lc : la;
+    const double difference = hi == -INFINITY ? -INFINITY : hi + std::log(-std::expm1(lo - hi));
+    const double value = std::exp(std::log(strike) + risk_log + difference);
+    if (!std::isfinite(value)) f.failed = true;
+    return value;
+}
+
+// Scheduled single barrier (barrier.rs:240-449 without Greeks): one normal per date,
+// noise = sum(width z) against each observed date's touch level; a knock-out stops at the
+// hit with its rebate; a knock-in hit with more than 8 dates left is priced analytically
+// from the hit (`condition_on_hit`); otherwise the expiry payoff or the expiry rebate.
+static double barrier_discrete_payoff(const Plan& p, PathNormals& n, Failure& f) {
+    const kgpu_contract* c = p.c;
+    const bool up = c->flags & KGPU_C_BARRIER_UP;
+    const bool in = c->flags & KGPU_C_BARRIER_IN;
+    const bool condition = c->flags & KGPU_C_CONDITION_ON_HIT;
+    double noise = 0.0, terminal = 0.0;
+    bool touched = false;
+    for (int i = 0; i < c->step_count; ++i) {
+        const kgpu_step& st = p.steps[i];
+        const kgpu_event& e = p.events[i];
+        noise = std::fma(st.diffusion, n.normal(), noise);
+        terminal = st.drift + noise;
+        if (c->flags & KGPU_C_CHECK_STEPS) {
+            const double spot_now = discounted_product(c->spot, 1.0, terminal);
+            if (!std::isfinite(spot_now) || spot_now <= 0.0) {
+                f.failed = true;
+                return 0.0;
+            }
+        }
+        if (e.has_knock_out && (up ? noise >= e.knock_out : noise <= e.knock_out)) {
+            touched = true;
+            if (condition && c->step_count - i > 8) {
+                const double asset = discounted_product(c->spot, 1.0, terminal);
+                return lognormal_price(asset, c->strike, c->moneyness + noise + c->half_variance * e.coupon_barrier,
+                                       e.payment[1], c->log_discount, c->volatility, e.payment[2], c->sign, f);
+            }
+        }
+        if (touched && !in) {
+            const double rebate =
+                discounted_product(c->rebate, 1.0, (c->flags & KGPU_C_REBATE_AT_HIT) ? e.payment[0] : c->log_discount);
+            if (!std::isfinite(rebate)) f.failed = true;
+            return rebate;
+        }
+    }
+    const double asset = discounted_product(c->spot, 1.0, terminal);
+    if (!std::isfinite(asset)) f.failed = true;
+    const double distance = c->moneyness + noise;
+    const double payoff = std::fabs(distance) < 0.5 ? c->strike * std::expm1(distance) : asset - c->strike;
+    const double intrinsic = std::max(c->sign * payoff, 0.0);
+    const double value = weighted(touched == in ? intrinsic : c->rebate, c->log_discount);
+    if (!std::isfinite(value)) f.failed = true;
+    return value;
+}
+
 // AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
 static inline double autocallable_terminal(const kgpu_contract* c, double spot, bool knocked_in) {
     if (knocked_in) {
@@ -455,6 +549,8 @@ static double evaluate(const Plan& p, const Model& model, PathNormals& n, Failur
             return digital_payoff(c, n.normal());
         case KGPU_PAYOFF_BARRIER:
             return barrier_payoff(c, n.normal(), f);
+        case KGPU_PAYOFF_BARRIER_DISCRETE:
+            return barrier_discrete_payoff(p, n, f);
         case KGPU_PAYOFF_VANILLA_PATH:
             return path_vanilla(p, model, n, false);
         case KGPU_PAYOFF_ASIAN:
@@ -484,6 +580,8 @@ static int price_contract(const Model& model, const Plan& p, const kgpu_settings
     bool sobol = settings->sampling == KGPU_SAMPLING_SOBOL;
     bool antithetic = settings->antithetic != 0;
     int dims = dimensions_of(c, model);
+    // sobol::sequence rejects dimensions beyond the Joe-Kuo table (sobol.rs).
+    if (sobol && (dims < 1 || dims > 21201)) return KGPU_INVALID_INPUT;
     int64_t samples = antithetic ? (paths + 1) / 2 : paths;
     size_t blocks = size_t((samples + kBlockSize - 1) / kBlockSize);
     std::unique_ptr<SobolSequence> seq;

@@ -10,7 +10,7 @@ import os
 
 import pytest
 
-from kiyosi_gb300 import abi, plans
+from kiyosi_gb300 import abi, analytic, plans
 from kiyosi_gb300.errors import InvalidInputError, UnsupportedOperationError
 from kiyosi_gb300.instruments import BarrierOption, EuropeanOption
 from oracle import loader
@@ -73,8 +73,18 @@ def test_in_out_parity_and_resolution():
     hit = plans.barrier(BarrierOption("put", 100.0, 1.0, barrier=95.0, barrier_type="up_and_out",
                                       rebate=2.0, rebate_timing="at_hit"), ctx)
     assert hit.value == 2.0
-    assert isinstance(plans.barrier(BarrierOption("put", 100.0, 1.0, barrier=100.0,
-                                                  barrier_type="down_and_in"), ctx), plans.ContractPlan)
+    # A touched knock-in is its vanilla option, priced analytically (analytic/barrier.rs:66-76).
+    touched_in = plans.barrier(BarrierOption("put", 100.0, 1.0, barrier=100.0,
+                                             barrier_type="down_and_in"), ctx)
+    assert isinstance(touched_in, plans.Known)
+    assert touched_in.value == analytic.european_price(-1.0, 100.0, 1.0, ctx)
+    assert abs(touched_in.value - 6.330080627549918) < 1e-12  # Black-Scholes put, scipy
+    # Payoffs that need the barrier crossed (analytic/barrier.rs:61-64): a knock-out is
+    # worthless without a rebate, the knock-in is the vanilla.
+    assert plans.barrier(BarrierOption("call", 130.0, 1.0, barrier=120.0,
+                                       barrier_type="up_and_out"), ctx).value == 0.0
+    assert plans.barrier(BarrierOption("call", 130.0, 1.0, barrier=120.0, barrier_type="up_and_in"),
+                         ctx).value == analytic.european_price(1.0, 130.0, 1.0, ctx)
     with pytest.raises(UnsupportedOperationError):
         plans.barrier(BarrierOption("call", 100.0, 1.0, barrier=90.0, barrier_type="down_and_out",
                                     rebate=1.0, rebate_timing="at_hit"), ctx)
