@@ -105,9 +105,14 @@ enum {
     KGPU_PAYOFF_DIGITAL = 5,      /* terminal digital, one dimension (digital.rs:111-130) */
     KGPU_PAYOFF_BARRIER = 6,      /* continuously monitored single barrier: one terminal draw
                                      and Brownian-bridge survival (barrier.rs:231-452) */
-    KGPU_PAYOFF_BARRIER_DISCRETE = 7 /* single barrier observed on dates (barrier.rs:231-452):
+    KGPU_PAYOFF_BARRIER_DISCRETE = 7, /* single barrier observed on dates (barrier.rs:231-452):
                                      one step per date; one kgpu_event per step holds the
                                      date's record (see kgpu_contract) */
+    KGPU_PAYOFF_AVERAGE_ARITHMETIC = 8, /* continuous arithmetic average (asian.rs:374-713,
+                                     1016-1257): trapezoid over n intervals, the first one
+                                     integrated analytically, n - 1 (+ lead) normals */
+    KGPU_PAYOFF_AVERAGE_GEOMETRIC = 9  /* continuous geometric average or single fixing:
+                                     one exact normal (asian.rs:740-784) */
 };
 
 /* One simulated grid step of a contract.  For BSM the transition is the reference's
@@ -170,9 +175,14 @@ enum {
     KGPU_C_REBATE_AT_HIT = 256,  /* discrete knock-out: rebate paid on the hit date */
     KGPU_C_CONDITION_ON_HIT = 512, /* discrete knock-in: after a hit with more than 8 dates left,
                                      the vanilla is priced analytically from the hit */
-    KGPU_C_CHECK_STEPS = 1024     /* discrete barrier whose paths can leave the representable
+    KGPU_C_CHECK_STEPS = 1024,    /* discrete barrier whose paths can leave the representable
                                      range: a spot that overflows or underflows fails the
                                      pricing (barrier.rs:280-289) */
+    KGPU_C_AVERAGE_LEAD = 2048,   /* arithmetic average starting after valuation: the first
+                                     normal draws the lead interval */
+    KGPU_C_AVERAGE_CONTROL = 4096 /* arithmetic average with the geometric control variate:
+                                     each sample is the residual against the geometric payoff
+                                     on the same path; control_mean is added to the mean */
 };
 
 /* A contract's plan.  Field groups are used by the payoff families named beside them. */
@@ -228,6 +238,32 @@ typedef struct kgpu_contract {
      * log_discount as above. */
     double volatility;
     double dividend;
+    /* continuous average (KGPU_PAYOFF_AVERAGE_*, asian.rs:374-1257), flat BSM rates, n
+     * integration intervals.  strike, sign, spot and log_discount as above.
+     * Arithmetic: growth += avg_drift + avg_width z per interval; the lead interval (if
+     * any) draws avg_lead_drift + avg_lead_width z.  Geometric: distance = moneyness +
+     * diffusion z with moneyness = initial moneyness + drift, diffusion = width and
+     * log_scale = log width. */
+    double avg_drift;             /* (r - q - sigma^2 / 2) dt */
+    double avg_width;             /* sigma sqrt(dt) */
+    double avg_lead_drift;        /* (r - q - sigma^2 / 2) lead */
+    double avg_lead_width;        /* sigma sqrt(lead) */
+    double avg_interval_forward;  /* (r - q) dt */
+    double avg_weight;            /* future / period */
+    double avg_log_spot;          /* ln(spot) */
+    double avg_log_scale;         /* ln(spot) + ln(weight) */
+    double avg_log_strike;        /* ln(strike) */
+    double avg_fraction;          /* 1 / n: trapezoid weight of an interior fixing */
+    double avg_half;              /* 0.5 / n: weight of the end fixings */
+    double avg_log_fraction;      /* ln(1 / n) */
+    double avg_log_half;          /* ln(0.5 / n) */
+    double avg_rest;              /* 1 - 0.5 / n */
+    double avg_log_rest;          /* ln(1 - 0.5 / n) */
+    double avg_baseline;          /* weight ((spot - strike) / spot) */
+    double control_log_strike;    /* geometric control (KGPU_C_AVERAGE_CONTROL) */
+    double control_log_asset_scale;
+    double control_first_weight;  /* 1 - 0.5 / n */
+    double control_mean;          /* exact expected value of the control */
 } kgpu_contract;
 
 /* A book of contracts sharing one model.  Arrays are indexed through the offsets in

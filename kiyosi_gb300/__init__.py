@@ -8,14 +8,16 @@ DeviceError when the CUDA library or a GPU is unavailable.
 from .errors import (ComputationFailureError, DeviceError, GreekUnavailableError,
                      InvalidInputError, KiyosiError, MissingHistoryError,
                      RootNotBracketedError, UnsupportedOperationError)
-from .instruments import (CALL, PUT, Accumulator, AmericanOption, AsianOption, AutocallableNote,
-                          DigitalOption, EuropeanOption, Observation, PhoenixOption,
-                          SnowballOption)
+from .instruments import (CALL, PUT, Accumulator, AmericanOption, ArithmeticAveragePriceOption,
+                          AsianOption, AutocallableNote, BarrierOption, DigitalOption,
+                          EuropeanOption, GeometricAveragePriceOption, Observation,
+                          PhoenixOption, SnowballOption)
 from .market import (BlackScholesMertonParameters, HestonParameters, LocalVolatilitySurface,
                      PricingContext)
 
 __all__ = [
-    "Accumulator", "AmericanOption", "AsianOption", "AutocallableNote",
+    "Accumulator", "AmericanOption", "ArithmeticAveragePriceOption", "AsianOption",
+    "AutocallableNote", "BarrierOption", "GeometricAveragePriceOption",
     "BlackScholesMertonParameters", "CALL", "ComputationFailureError", "DeviceError",
     "DigitalOption", "EuropeanOption", "GreekUnavailableError", "HestonParameters",
     "InvalidInputError", "KiyosiError", "LocalVolatilitySurface", "MissingHistoryError",

@@ -34,6 +34,8 @@ PAYOFF_ACCUMULATOR = 4
 PAYOFF_DIGITAL = 5
 PAYOFF_BARRIER = 6
 PAYOFF_BARRIER_DISCRETE = 7
+PAYOFF_AVERAGE_ARITHMETIC = 8
+PAYOFF_AVERAGE_GEOMETRIC = 9
 
 STEP_KNOCK_IN = 1
 STEP_EVENT = 2
@@ -51,6 +53,8 @@ C_BARRIER_IN = 128
 C_REBATE_AT_HIT = 256
 C_CONDITION_ON_HIT = 512
 C_CHECK_STEPS = 1024
+C_AVERAGE_LEAD = 2048
+C_AVERAGE_CONTROL = 4096
 
 UNCERTAINTY_NAMES = {
     0: "available",
@@ -112,7 +116,13 @@ class Contract(C.Structure):
                 ("acceleration", _D), ("log_strike", _D),
                 ("barrier_drift", _D), ("barrier_distance", _D), ("barrier_moneyness", _D),
                 ("rebate", _D), ("spot", _D), ("log_discount", _D), ("volatility", _D),
-                ("dividend", _D)]
+                ("dividend", _D), ("avg_drift", _D), ("avg_width", _D), ("avg_lead_drift", _D),
+                ("avg_lead_width", _D), ("avg_interval_forward", _D), ("avg_weight", _D),
+                ("avg_log_spot", _D), ("avg_log_scale", _D), ("avg_log_strike", _D), ("avg_fraction", _D),
+                ("avg_half", _D), ("avg_log_fraction", _D), ("avg_log_half", _D),
+                ("avg_rest", _D), ("avg_log_rest", _D), ("avg_baseline", _D),
+                ("control_log_strike", _D), ("control_log_asset_scale", _D),
+                ("control_first_weight", _D), ("control_mean", _D)]
 
 
 class Book(C.Structure):

@@ -54,6 +54,18 @@ def discounted_product(scale: float, weight: float, log_discount: float) -> floa
     return math.copysign(math.exp(_ln(scale) + _ln(abs(weight)) + log_discount), weight)
 
 
+def positive_difference(a: float, b: float) -> float:
+    """exp(a) - exp(b) floored at zero (engines/monte_carlo/asian.rs:972-985)."""
+    if a == math.inf:
+        return a
+    if b == -math.inf:
+        return math.exp(a)
+    difference = -math.expm1(b - a)
+    if difference > 0.0:
+        return math.exp(a + _ln(difference))
+    return 0.0
+
+
 def log_difference(high: float, low: float) -> float:
     if high == -math.inf:
         return -math.inf

@@ -82,6 +82,10 @@ void estimate_from_moments(const kgpu_contract& c, const kgpu_settings& s, int64
         return std::copysign(std::exp(std::log(scale) + std::log(std::fabs(weight)) + log_d), weight);
     };
     out->price = scaled(p.moments.scale, p.moments.mean, log_discount);
+    // The arithmetic average's samples are residuals against the geometric control;
+    // its exact mean is added back (ArithmeticGrid::sample, asian.rs:616-621).
+    if (c.payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC && (c.flags & KGPU_C_AVERAGE_CONTROL))
+        out->price += c.control_mean;
     const Moments& u = antithetic ? p.pairs : p.moments;
     out->standard_error = 0.0;
     if (statistics && u.count >= 2.0) {
@@ -282,7 +286,8 @@ int model_normals_per_step(const kgpu_model* m) { return m->kind == KGPU_MODEL_H
 
 // Payoffs sampled with one terminal draw per path (no grid).
 bool terminal_payoff(const kgpu_contract& c) {
-    return c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL || c.payoff == KGPU_PAYOFF_BARRIER;
+    return c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL || c.payoff == KGPU_PAYOFF_BARRIER ||
+           c.payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC;
 }
 
 int dims_of(const kgpu_contract& c, const kgpu_model* m) {
@@ -297,6 +302,8 @@ void estimate_from_sums(const kgpu_contract& c, const kgpu_settings& s, int64_t 
     const double n = t.count;
     const double mean = n > 0 ? t.sum / n : 0.0;
     out->price = mean * scale;
+    if (c.payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC && (c.flags & KGPU_C_AVERAGE_CONTROL))
+        out->price += c.control_mean;
     double se = 0.0;
     if (n >= 2) {
         double var = std::max(0.0, (t.sumsq - t.sum * mean) / (n - 1.0));
@@ -419,11 +426,11 @@ struct PrecisionOps<double> {
                              const kgpu_model& mo, const double* lv) {
         return launch_plain_fp64(m, so, b, sm, st, a, mo, lv);
     }
-    static cudaError_t persistent(int m, bool so, int b, size_t sm, cudaStream_t st,
+    static cudaError_t persistent(int m, bool so, bool ext, int b, size_t sm, cudaStream_t st,
                                   const PersistentArgs<double>& a, const kgpu_model& mo, const double* lv) {
-        return launch_persistent_fp64(m, so, b, sm, st, a, mo, lv);
+        return launch_persistent_fp64(m, so, ext, b, sm, st, a, mo, lv);
     }
-    static int occupancy(int m, bool so, size_t sm) { return persistent_occupancy_fp64(m, so, sm); }
+    static int occupancy(int m, bool so, bool ext, size_t sm) { return persistent_occupancy_fp64(m, so, ext, sm); }
     static cudaError_t contracts(const kgpu_contract* in, int n, ContractT<double>* out, cudaStream_t st) {
         return launch_compile_contracts_fp64(in, n, out, st);
     }
@@ -440,11 +447,11 @@ struct PrecisionOps<float> {
                              const kgpu_model& mo, const double* lv) {
         return launch_plain_fp32(m, so, b, sm, st, a, mo, lv);
     }
-    static cudaError_t persistent(int m, bool so, int b, size_t sm, cudaStream_t st,
+    static cudaError_t persistent(int m, bool so, bool ext, int b, size_t sm, cudaStream_t st,
                                   const PersistentArgs<float>& a, const kgpu_model& mo, const double* lv) {
-        return launch_persistent_fp32(m, so, b, sm, st, a, mo, lv);
+        return launch_persistent_fp32(m, so, ext, b, sm, st, a, mo, lv);
     }
-    static int occupancy(int m, bool so, size_t sm) { return persistent_occupancy_fp32(m, so, sm); }
+    static int occupancy(int m, bool so, bool ext, size_t sm) { return persistent_occupancy_fp32(m, so, ext, sm); }
     static cudaError_t contracts(const kgpu_contract* in, int n, ContractT<float>* out, cudaStream_t st) {
         return launch_compile_contracts_fp32(in, n, out, st);
     }
@@ -565,8 +572,20 @@ kgpu_status run_plain(Call& k, const DevBook<Real>& db, int& launches) {
     return KGPU_OK;
 }
 
+// Whether a book needs the persistent kernel's extended payoff set.
+bool extended_payoffs(const kgpu_book& b) {
+    for (int i = 0; i < b.contract_count; ++i) {
+        const int p = b.contracts[i].payoff;
+        if (p == KGPU_PAYOFF_BARRIER_DISCRETE || p == KGPU_PAYOFF_AVERAGE_ARITHMETIC ||
+            p == KGPU_PAYOFF_AVERAGE_GEOMETRIC)
+            return true;
+    }
+    return false;
+}
+
 template <class Real>
 kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
+    const bool ext = extended_payoffs(*k.book);
     kgpu_context* ctx = k.ctx;
     const kgpu_settings& s = k.s;
     const int n = k.raw.contract_count;
@@ -695,13 +714,13 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
             return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
                         "Sobol dimension %d exceeds the persistent kernel's shared memory; use the plain schedule",
                         group_dims[g]);
-        int per_sm = PrecisionOps<Real>::occupancy(k.model->kind, k.sobol, smem);
+        int per_sm = PrecisionOps<Real>::occupancy(k.model->kind, k.sobol, ext, smem);
         if (s.ctas_per_sm > 0) per_sm = std::min(per_sm, s.ctas_per_sm);
         const int blocks = std::max(1, std::min(ctx->sm_count * per_sm, (a.item_count + kWarps - 1) / kWarps));
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->queue.ptr, 0, sizeof(int), ctx->stream));
         CUDA_TRY(ctx, path_kernel_begin(ctx));
-        CUDA_TRY(ctx, PrecisionOps<Real>::persistent(k.model->kind, k.sobol, blocks, smem, ctx->stream, a, *k.model,
-                                                     k.lv_dev));
+        CUDA_TRY(ctx, PrecisionOps<Real>::persistent(k.model->kind, k.sobol, ext, blocks, smem, ctx->stream, a,
+                                                     *k.model, k.lv_dev));
         CUDA_TRY(ctx, path_kernel_end(ctx));
         launches += 1;
         // `order` is reused by the next group: wait for this launch's upload to be consumed.
@@ -806,10 +825,13 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: path_count must be positive", i);
         if (k.sobol && !is_pow2(paths))
             return fail(ctx, KGPU_INVALID_INPUT, "path_count must be a power of two for Sobol sampling");
-        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_BARRIER_DISCRETE)
+        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_AVERAGE_GEOMETRIC)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: unknown payoff %d", i, c.payoff);
         if (c.payoff == KGPU_PAYOFF_BARRIER && (model->kind != KGPU_MODEL_BSM || !(c.diffusion > 0.0)))
             return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "contract %d: the Monte Carlo barrier needs BSM volatility", i);
+        if ((c.payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC || c.payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC) &&
+            model->kind != KGPU_MODEL_BSM)
+            return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "contract %d: average-price sampling needs BSM", i);
         if (c.payoff == KGPU_PAYOFF_BARRIER_DISCRETE &&
             (model->kind != KGPU_MODEL_BSM || c.event_count != c.step_count || !book->events))
             return fail(ctx, KGPU_INVALID_INPUT,

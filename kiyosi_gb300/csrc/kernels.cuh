@@ -129,6 +129,26 @@ __global__ void compile_contracts_kernel(const kgpu_contract* in, int n, Contrac
     o.log_discount = Real(c.log_discount);
     o.volatility = Real(c.volatility);
     o.dividend = Real(c.dividend);
+    o.avg_drift = Real(c.avg_drift);
+    o.avg_width = Real(c.avg_width);
+    o.avg_lead_drift = Real(c.avg_lead_drift);
+    o.avg_lead_width = Real(c.avg_lead_width);
+    o.avg_interval_forward = Real(c.avg_interval_forward);
+    o.avg_weight = Real(c.avg_weight);
+    o.avg_log_spot = Real(c.avg_log_spot);
+    o.avg_log_scale = Real(c.avg_log_scale);
+    o.avg_log_strike = Real(c.avg_log_strike);
+    o.avg_fraction = Real(c.avg_fraction);
+    o.avg_half = Real(c.avg_half);
+    o.avg_log_fraction = Real(c.avg_log_fraction);
+    o.avg_log_half = Real(c.avg_log_half);
+    o.avg_rest = Real(c.avg_rest);
+    o.avg_log_rest = Real(c.avg_log_rest);
+    o.avg_baseline = Real(c.avg_baseline);
+    o.control_log_strike = Real(c.control_log_strike);
+    o.control_log_asset_scale = Real(c.control_log_asset_scale);
+    o.control_first_weight = Real(c.control_first_weight);
+    o.control_mean = Real(c.control_mean);
     out[i] = o;
 }
 
@@ -361,7 +381,9 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(PlainArgs<Real> a, kgpu
     const uint64_t block = blockIdx.x;
     if (SOBOL) sobol_high(a.sobol, block, high, threadIdx.x, blockDim.x);
     __syncthreads();
-    const ContractT<Real> c = a.book.contracts[a.contract];
+    // A reference into the compiled book (not a local copy): out-of-line payoff pieces
+    // receive it without a stack copy of the contract.
+    const ContractT<Real>& c = a.book.contracts[a.contract];
     const PlanPtrs<Real> plan = plan_of(a.book, c);
     const int64_t sample = int64_t(block) * kBlockSize + threadIdx.x;
     double positive = 0.0, negative = 0.0;
@@ -568,7 +590,7 @@ struct Compensated {
 // warp's shared copy (FP64 keeps one item per warp).  Each finished path writes its
 // payoff to values[value_offset[contract] + sample]; reduce_values_kernel sums them in a
 // fixed order, so results do not depend on which warp ran which path.
-template <class Real, int MODEL, bool SOBOL>
+template <class Real, int MODEL, bool SOBOL, bool EXT>
 __global__ void __launch_bounds__(kThreads, 4) persistent_kernel(PersistentArgs<Real> a, kgpu_model model,
                                                               const double* lv_dev) {
     using Kind = SobolKind<Real>;
@@ -686,8 +708,8 @@ __global__ void __launch_bounds__(kThreads, 4) persistent_kernel(PersistentArgs<
                     finished = SOBOL ? bridge_unit_step<Real>(c, plan, s, sn) : bridge_unit_step<Real>(c, plan, s, pn);
                     if (finished) value = bridge_value(m, c, s);
                 } else {
-                    finished = SOBOL ? path_step<Real, MODEL>(m, c, plan, s, sn, value)
-                                     : path_step<Real, MODEL>(m, c, plan, s, pn, value);
+                    finished = SOBOL ? path_step<Real, MODEL, EXT>(m, c, plan, s, sn, value)
+                                     : path_step<Real, MODEL, EXT>(m, c, plan, s, pn, value);
                 }
                 if (!finished && --guard == 0) {
                     finished = true;

@@ -14,19 +14,19 @@ static cudaError_t plain_one(int blocks, size_t smem, cudaStream_t s, const Plai
     return cudaGetLastError();
 }
 
-template <int MODEL, bool SOBOL>
+template <int MODEL, bool SOBOL, bool EXT>
 static cudaError_t persistent_one(int blocks, size_t smem, cudaStream_t s,
                                   const PersistentArgs<REAL>& a, const kgpu_model& m, const double* lv) {
-    auto k = persistent_kernel<REAL, MODEL, SOBOL>;
+    auto k = persistent_kernel<REAL, MODEL, SOBOL, EXT>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     k<<<blocks, kThreads, smem, s>>>(a, m, lv);
     return cudaGetLastError();
 }
 
-template <int MODEL, bool SOBOL>
+template <int MODEL, bool SOBOL, bool EXT>
 static int occupancy_one(size_t smem) {
-    auto k = persistent_kernel<REAL, MODEL, SOBOL>;
+    auto k = persistent_kernel<REAL, MODEL, SOBOL, EXT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
         return 1;
     int n = 0;
@@ -44,6 +44,19 @@ static int occupancy_one(size_t smem) {
         default: return FN<KGPU_MODEL_LOCAL_VOL, true>(__VA_ARGS__);                   \
     }
 
+// The extended payoffs are BSM-only: other models use the core instantiation.
+#define KGPU_DISPATCH_EXT(FN, ...)                                                     \
+    switch (model * 2 + int(sobol)) {                                                  \
+        case 0: return ext ? FN<KGPU_MODEL_BSM, false, true>(__VA_ARGS__)              \
+                           : FN<KGPU_MODEL_BSM, false, false>(__VA_ARGS__);            \
+        case 1: return ext ? FN<KGPU_MODEL_BSM, true, true>(__VA_ARGS__)               \
+                           : FN<KGPU_MODEL_BSM, true, false>(__VA_ARGS__);             \
+        case 2: return FN<KGPU_MODEL_HESTON, false, false>(__VA_ARGS__);               \
+        case 3: return FN<KGPU_MODEL_HESTON, true, false>(__VA_ARGS__);                \
+        case 4: return FN<KGPU_MODEL_LOCAL_VOL, false, false>(__VA_ARGS__);            \
+        default: return FN<KGPU_MODEL_LOCAL_VOL, true, false>(__VA_ARGS__);            \
+    }
+
 #define KGPU_CAT2(a, b) a##b
 #define KGPU_CAT(a, b) KGPU_CAT2(a, b)
 
@@ -53,14 +66,14 @@ cudaError_t KGPU_CAT(launch_plain_, PRECISION)(int model, bool sobol, int blocks
     KGPU_DISPATCH(plain_one, blocks, smem, s, a, m, lv)
 }
 
-cudaError_t KGPU_CAT(launch_persistent_, PRECISION)(int model, bool sobol, int blocks, size_t smem,
+cudaError_t KGPU_CAT(launch_persistent_, PRECISION)(int model, bool sobol, bool ext, int blocks, size_t smem,
                                                     cudaStream_t s, const PersistentArgs<REAL>& a,
                                                     const kgpu_model& m, const double* lv) {
-    KGPU_DISPATCH(persistent_one, blocks, smem, s, a, m, lv)
+    KGPU_DISPATCH_EXT(persistent_one, blocks, smem, s, a, m, lv)
 }
 
-int KGPU_CAT(persistent_occupancy_, PRECISION)(int model, bool sobol, size_t smem) {
-    KGPU_DISPATCH(occupancy_one, smem)
+int KGPU_CAT(persistent_occupancy_, PRECISION)(int model, bool sobol, bool ext, size_t smem) {
+    KGPU_DISPATCH_EXT(occupancy_one, smem)
 }
 
 cudaError_t KGPU_CAT(launch_compile_contracts_, PRECISION)(const kgpu_contract* in, int n,

@@ -14,14 +14,17 @@ cudaError_t launch_plain_fp64(int model, bool sobol, int blocks, size_t smem, cu
                               const PlainArgs<double>& a, const kgpu_model& m, const double* lv);
 cudaError_t launch_plain_fp32(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
                               const PlainArgs<float>& a, const kgpu_model& m, const double* lv);
-cudaError_t launch_persistent_fp64(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
+// `ext`: the book holds a payoff of the extended set (scheduled barriers, continuous
+// averages), which runs in its own instantiation so the core kernels keep their
+// register allocation.
+cudaError_t launch_persistent_fp64(int model, bool sobol, bool ext, int blocks, size_t smem, cudaStream_t s,
                                    const PersistentArgs<double>& a, const kgpu_model& m,
                                    const double* lv);
-cudaError_t launch_persistent_fp32(int model, bool sobol, int blocks, size_t smem, cudaStream_t s,
+cudaError_t launch_persistent_fp32(int model, bool sobol, bool ext, int blocks, size_t smem, cudaStream_t s,
                                    const PersistentArgs<float>& a, const kgpu_model& m,
                                    const double* lv);
-int persistent_occupancy_fp64(int model, bool sobol, size_t smem);
-int persistent_occupancy_fp32(int model, bool sobol, size_t smem);
+int persistent_occupancy_fp64(int model, bool sobol, bool ext, size_t smem);
+int persistent_occupancy_fp32(int model, bool sobol, bool ext, size_t smem);
 cudaError_t launch_compile_contracts_fp64(const kgpu_contract* in, int n, ContractT<double>* out,
                                           cudaStream_t s);
 cudaError_t launch_compile_contracts_fp32(const kgpu_contract* in, int n, ContractT<float>* out,

@@ -83,6 +83,10 @@ struct ContractT {
     Real knock_out, quantity, daily_quantity, acceleration, log_strike;
     Real barrier_drift, barrier_distance, barrier_moneyness, rebate, spot, log_discount;
     Real volatility, dividend;
+    Real avg_drift, avg_width, avg_lead_drift, avg_lead_width, avg_interval_forward, avg_weight;
+    Real avg_log_spot, avg_log_scale, avg_log_strike, avg_fraction, avg_half, avg_log_fraction, avg_log_half;
+    Real avg_rest, avg_log_rest, avg_baseline;
+    Real control_log_strike, control_log_asset_scale, control_first_weight, control_mean;
 };
 
 // Device view of the book in the kernel's precision.
@@ -244,6 +248,8 @@ __device__ __forceinline__ double xexpm1(double x) { return expm1(x); }
 __device__ __forceinline__ float xexpm1(float x) { return expm1f(x); }
 __device__ __forceinline__ double xlog(double x) { return log(x); }
 __device__ __forceinline__ float xlog(float x) { return __logf(x); }
+__device__ __forceinline__ double xlog1p(double x) { return log1p(x); }
+__device__ __forceinline__ float xlog1p(float x) { return log1pf(x); }
 __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float xsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double xinf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
@@ -336,6 +342,12 @@ __device__ __forceinline__ void path_init(PathState<Real>& s, const ContractT<Re
     s.knocked_in = (c.flags & KGPU_C_KNOCKED_IN) != 0;
     s.monitoring = !s.knocked_in && (c.flags & KGPU_C_HAS_KNOCK_IN);
     s.knocked_out = false;
+    if (c.payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC) {
+        // growth (lr), relative sum (acc), log sum (cash), geometric growth (target) and
+        // the lead growth (minimum; the lead normal is 0 without a lead interval).
+        s.cash = -xinf(Real(0));
+        s.minimum = c.avg_lead_drift + c.avg_lead_width * Real(0);
+    }
 }
 
 // One grid step of the state.  BSM: `log_return += diffusion.mul_add(normal, drift)`;
@@ -493,6 +505,97 @@ __device__ __noinline__ Real lognormal_price_of(Real spot, Real strike, Real log
     return xexp(xlog(strike) + risk_log + difference);
 }
 
+// log_add (numerics.rs:320-327) and positive_difference (asian.rs:972-985).
+template <class Real>
+__device__ __forceinline__ Real log_add_of(Real a, Real b) {
+    const Real high = a > b ? a : b;
+    if (high == -xinf(Real(0))) return high;
+    return high + xlog1p(xexp(-xabs(a - b)));
+}
+
+template <class Real>
+__device__ __forceinline__ Real positive_difference_of(Real a, Real b) {
+    if (a == xinf(Real(0))) return a;
+    if (b == -xinf(Real(0))) return xexp(a);
+    const Real difference = -xexpm1(b - a);
+    return difference > Real(0) ? xexp(a + xlog(difference)) : Real(0);
+}
+
+// ArithmeticParameters::geometric_values, price only (asian.rs:1062-1085).
+template <class Real>
+__device__ Real average_geometric_price(const ContractT<Real>& c, Real log_forward, Real log_strike, Real width) {
+    const Real d1 = (log_forward - log_strike) / width + Real(0.5) * width;
+    const Real d2 = d1 - width;
+    const Real log_asset = log_forward + c.log_discount + log_normal_cdf_of(c.sign * d1);
+    const Real log_cash = log_strike + c.log_discount + log_normal_cdf_of(c.sign * d2);
+    return c.sign > Real(0) ? positive_difference_of(log_asset, log_cash) : positive_difference_of(log_cash, log_asset);
+}
+
+// ArithmeticParameters::arithmetic, price only, without realized history, for widths of
+// at least 1e-5 (asian.rs:1087-1178): the first interval integrated in closed form given
+// the path's other increments, minus the geometric control on the same path.
+template <class Real>
+__device__ __noinline__ Real average_arithmetic_value(const ContractT<Real>& c, Real lead_growth, Real log_sum,
+                                                      Real relative_sum, Real geometric_growth) {
+    const bool summed = log_sum == -xinf(Real(0));
+    const Real log_rest = summed ? c.avg_log_rest + xlog1p(relative_sum / c.avg_rest) : log_sum;
+    const Real log_q = ((c.avg_log_scale + lead_growth) + log_rest) + c.avg_interval_forward;
+    const Real log_c = (c.avg_log_scale + lead_growth) + c.avg_log_half;
+    const Real log_accrued = log_c;  // log_add(no history, log_c)
+    Real control = Real(0);
+    if (c.flags & KGPU_C_AVERAGE_CONTROL) {
+        const Real width = c.control_first_weight * c.avg_width;
+        const Real log_forward = (((c.control_log_asset_scale + lead_growth) + geometric_growth) +
+                                  c.control_first_weight * c.avg_drift) +
+                                 Real(0.5) * width * width;
+        control = average_geometric_price(c, log_forward, c.control_log_strike, width);
+    }
+    const Real log_strike = c.avg_log_strike;
+    if (log_accrued >= log_strike) {
+        if (c.sign < Real(0)) return Real(0) - control;
+        const Real cash = positive_difference_of(log_accrued + c.log_discount, log_strike + c.log_discount);
+        return (xexp(log_q + c.log_discount) + cash) - control;
+    }
+    const Real log_b = log_strike + xlog(-xexpm1(log_accrued - log_strike));
+    Real forward = log_q - log_b;
+    if (summed) {
+        const Real extra = xexpm1(lead_growth) +
+                           xexp(lead_growth) * (c.avg_rest * xexpm1(c.avg_interval_forward) +
+                                                relative_sum * xexp(c.avg_interval_forward));
+        const Real excess = c.avg_baseline + c.avg_weight * extra;
+        const Real b = xexp(log_b - c.avg_log_spot);
+        if (b > Real(0) && xabs(excess / b) < Real(0.5)) forward = xlog1p(excess / b);
+    }
+    const Real center = forward / c.avg_width;
+    const Real d1 = center + Real(0.5) * c.avg_width, d2 = center - Real(0.5) * c.avg_width;
+    const Real log_asset = log_q + c.log_discount + log_normal_cdf_of(c.sign * d1);
+    const Real log_cash = log_b + c.log_discount + log_normal_cdf_of(c.sign * d2);
+    const Real price = c.sign > Real(0) ? positive_difference_of(log_asset, log_cash)
+                                        : positive_difference_of(log_cash, log_asset);
+    return price - control;
+}
+
+// GeometricParameters::geometric, price only (asian.rs:740-784): moneyness holds the
+// initial moneyness plus the drift, diffusion the width, log_scale the log width.
+template <class Real>
+__device__ __noinline__ Real average_geometric_value(const ContractT<Real>& c, Real normal) {
+    const Real distance = c.moneyness + c.diffusion * normal;
+    const Real center = c.moneyness / c.diffusion;
+    const Real standardized = center + normal;
+    if (c.sign * standardized <= Real(0)) return Real(0);
+    const Real log_strike = c.avg_log_strike;
+    Real log_payoff;
+    if (xabs(distance) < Real(1e-5) && xabs(standardized) < xinf(Real(0))) {
+        log_payoff = log_strike + c.log_scale + xlog(xabs(standardized)) +
+                     (distance == Real(0) ? Real(0) : xlog(xabs(xexpm1(distance)) / xabs(distance)));
+    } else if (c.sign > Real(0)) {
+        log_payoff = log_strike + distance + xlog(-xexpm1(-distance));
+    } else {
+        log_payoff = log_strike + xlog(-xexpm1(distance));
+    }
+    return xexp(log_payoff + c.log_discount);
+}
+
 template <class Real>
 struct PlanPtrs {
     const StepT<Real>* __restrict__ steps;
@@ -519,7 +622,8 @@ __device__ __forceinline__ PlanPtrs<Real> plan_of(const DevBook<Real>& b, const 
 
 // Advances one path by one unit of work (a grid step, or a bridge interval end).
 // Returns true when the path has finished; its payoff is then in `value`.
-template <class Real, int MODEL, class Source>
+// EXT: the extended payoff set (scheduled barriers, continuous averages) is compiled in.
+template <class Real, int MODEL, bool EXT = true, class Source>
 __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const ContractT<Real>& c,
                                           const PlanPtrs<Real>& p, PathState<Real>& s, Source& n,
                                           Real& value) {
@@ -594,7 +698,39 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         s.executed = 1;
         return true;
     }
-    if (payoff == KGPU_PAYOFF_BARRIER_DISCRETE) {
+    if (EXT && payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC) {
+        value = average_geometric_value(c, n.normal());
+        s.executed = 1;
+        return true;
+    }
+    if (EXT && payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC) {
+        // ArithmeticGrid::path (asian.rs:636-711): one normal per interval after the
+        // first; the last one carries the end fixing's half weight.
+        const Real z = n.normal();
+        const int i = s.i;
+        s.i = i + 1;
+        s.executed += 1;
+        if (i == 0 && (c.flags & KGPU_C_AVERAGE_LEAD)) {
+            s.minimum = c.avg_lead_drift + c.avg_lead_width * z;
+        } else {
+            const Real growth = s.lr + (c.avg_drift + c.avg_width * z);
+            s.lr = growth;
+            const Real fraction = s.i == c.step_count ? c.avg_half : c.avg_fraction;
+            if (c.flags & KGPU_C_AVERAGE_CONTROL) s.target += fraction * growth;
+            const Real growth_bound = sizeof(Real) == 8 ? Real(600) : Real(80);
+            if (growth > growth_bound || s.cash != -xinf(Real(0))) {
+                // Above the bound, unit offsets fall below the type's precision.
+                if (s.cash == -xinf(Real(0))) s.cash = xlog(c.avg_rest + s.acc);
+                s.cash = log_add_of(s.cash, (s.i == c.step_count ? c.avg_log_half : c.avg_log_fraction) + growth);
+            } else {
+                s.acc += fraction * xexpm1(growth);
+            }
+        }
+        if (s.i < c.step_count) return false;
+        value = average_arithmetic_value(c, s.minimum, s.cash, s.acc, s.target);
+        return true;
+    }
+    if (EXT && payoff == KGPU_PAYOFF_BARRIER_DISCRETE) {
         // Scheduled monitoring (barrier.rs:306-449): the noise sum(width z) against each
         // observed date's touch level; a knock-out stops at its hit, a knock-in with more
         // than 8 dates left is priced analytically from its hit.

@@ -106,6 +106,45 @@ class BarrierOption(EuropeanOption):
 
 
 @dataclass(frozen=True)
+class AveragePriceOption:
+    """Continuously averaged price option (instruments/asian.rs AverageTerms): the
+    average of the spot over [averaging_start, expiry] (years after valuation) against
+    `strike`.  Valuation is at the contract's effective time, so no realized average
+    exists yet; averaging may start later (a forward start)."""
+    option_type: str
+    strike: float
+    expiry: float
+    averaging_start: float = 0.0
+
+    def __post_init__(self):
+        _sign(self.option_type)
+        if not (self.strike > 0.0 and math.isfinite(self.strike)):
+            raise InvalidInputError("strike must be positive and finite")
+        if not (math.isfinite(self.expiry) and self.expiry >= 0.0):
+            raise InvalidInputError("expiry must be finite and nonnegative")
+        if not (0.0 <= self.averaging_start <= self.expiry):
+            raise InvalidInputError("averaging must start within the contract's life")
+
+    @property
+    def sign(self) -> float:
+        return _sign(self.option_type)
+
+    @property
+    def period(self) -> float:
+        return self.expiry - self.averaging_start
+
+
+@dataclass(frozen=True)
+class ArithmeticAveragePriceOption(AveragePriceOption):
+    """Arithmetic continuous average (ArithmeticAveragePriceOption)."""
+
+
+@dataclass(frozen=True)
+class GeometricAveragePriceOption(AveragePriceOption):
+    """Geometric continuous average (GeometricAveragePriceOption)."""
+
+
+@dataclass(frozen=True)
 class AsianOption:
     """Arithmetic average-price option on the spots at `fixings` (years)."""
     option_type: str

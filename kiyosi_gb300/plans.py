@@ -314,6 +314,140 @@ def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_v
     return ContractPlan(c, steps, np.zeros(n, np.uint8), events)
 
 
+def _geometric_control_price(sign, log_discount, log_forward, log_strike, width):
+    """ArithmeticParameters::geometric_values, price only (asian.rs:1062-1085)."""
+    d1 = (log_forward - log_strike) / width + 0.5 * width
+    d2 = d1 - width
+    log_asset = log_forward + log_discount + analytic.log_normal_cdf(sign * d1)
+    log_cash = log_strike + log_discount + analytic.log_normal_cdf(sign * d2)
+    if sign > 0.0:
+        return analytic.positive_difference(log_asset, log_cash)
+    return analytic.positive_difference(log_cash, log_asset)
+
+
+def average(option, ctx: PricingContext, step_count: int = 50, control: bool = True):
+    """MonteCarloAsianEngine::prepare (asian.rs:374-551) for flat BSM rates, valuation at
+    the contract's effective time (no realized average).
+
+    Geometric averages and single fixings sample their exact lognormal law in one
+    dimension.  Arithmetic averages integrate n = `step_count` trapezoid intervals.
+    The first interval is conditioned on the others and integrated in closed form, so
+    n - 1 normals are drawn, plus one for a lead interval when averaging starts later.
+    Near the money a geometric payoff on the same grid is the control variate
+    (geometric_control, asian.rs:1016-1060): samples are residuals and the control's
+    exact mean is carried in `control_mean`.  `control=False` builds the plan without
+    it, as the reference does when the controlled mean comes out negative."""
+    from .instruments import GeometricAveragePriceOption
+    model = ctx.model
+    if not isinstance(model, BlackScholesMertonParameters):
+        raise UnsupportedOperationError("the Monte Carlo Asian engine requires BSM parameters")
+    if not (2 <= int(step_count) <= 10_000):
+        raise InvalidInputError("step_count must be in 2..=10000")
+    geometric = isinstance(option, GeometricAveragePriceOption)
+    spot, strike, sign = ctx.spot, option.strike, option.sign
+    tau = option.expiry
+    if tau == 0.0:
+        return Known(max(sign * (spot - strike), 0.0))
+    rate, dividend, sigma = model.rate, model.dividend, model.volatility
+    if sigma == 0.0:
+        raise UnsupportedOperationError("zero volatility: the average is deterministic")
+    single = option.period == 0.0
+    lead = 0.0 if single else option.averaging_start
+    future = tau if single else tau - option.averaging_start
+    weight = 1.0 if single else future / option.period
+    carry = rate - dividend
+    drift_rate = carry - 0.5 * sigma * sigma
+    log_discount = -rate * tau
+    c_sign = sign
+    if geometric or single:
+        variance_time = tau if single else lead + future / 3.0
+        if single:
+            moneyness = log_ratio(spot, strike) + ((-dividend * tau) - log_discount)
+            drift = -0.5 * sigma * sigma * tau
+        else:
+            moneyness = weight * log_ratio(spot, strike)
+            drift = weight * drift_rate * (lead + future / 2.0)
+        width = sigma * (weight * math.sqrt(variance_time))
+        log_width = math.log(sigma) + math.log(weight) + 0.5 * math.log(variance_time)
+        initial_moneyness = moneyness + 0.0
+        if not (math.isfinite(drift) and math.isfinite(width)):
+            raise _unstable()
+        c = _new_contract(abi.PAYOFF_AVERAGE_GEOMETRIC)
+        c["strike"] = strike
+        c["sign"] = c_sign
+        c["moneyness"] = initial_moneyness + drift
+        c["diffusion"] = width
+        c["log_scale"] = log_width
+        c["avg_log_strike"] = math.log(strike)
+        c["log_discount"] = log_discount
+        c["spot"] = spot
+        c["step_count"] = 1
+        return ContractPlan(c, np.zeros(1, STEP_DTYPE), np.zeros(1, np.uint8))
+    n = int(step_count)
+    dt = future / float(n)
+    interval_forward = carry * dt
+    drift = drift_rate * dt
+    width = sigma * math.sqrt(dt)
+    lead_drift = drift_rate * lead
+    lead_width = sigma * math.sqrt(lead)
+    if not all(math.isfinite(v) for v in (drift, width, lead_drift, lead_width, interval_forward)):
+        raise _unstable()
+    if width < 1e-5:
+        raise UnsupportedOperationError("average-price intervals narrower than 1e-5 are not sampled")
+    has_lead = lead > 0.0
+    dims = n - 1 + (1 if has_lead else 0)
+    half = 0.5 / float(n)
+    rest = 1.0 - half
+    log_spot = math.log(spot)
+    c = _new_contract(abi.PAYOFF_AVERAGE_ARITHMETIC)
+    c["strike"] = strike
+    c["sign"] = c_sign
+    c["spot"] = spot
+    c["log_discount"] = log_discount
+    c["avg_drift"] = drift
+    c["avg_width"] = width
+    c["avg_lead_drift"] = lead_drift
+    c["avg_lead_width"] = lead_width
+    c["avg_interval_forward"] = interval_forward
+    c["avg_weight"] = weight
+    c["avg_log_spot"] = log_spot
+    c["avg_log_scale"] = log_spot + math.log(weight)
+    c["avg_log_strike"] = math.log(strike)
+    c["avg_fraction"] = 1.0 / float(n)
+    c["avg_half"] = half
+    c["avg_log_fraction"] = math.log(1.0 / float(n))
+    c["avg_log_half"] = math.log(half)
+    c["avg_rest"] = rest
+    c["avg_log_rest"] = math.log(rest)
+    # prior_weight ((realized - strike) / spot) + weight ((spot - strike) / spot), no history
+    c["avg_baseline"] = 0.0 * ((0.0 - strike) / spot) + weight * ((spot - strike) / spot)
+    c["step_count"] = dims
+    flags = abi.C_AVERAGE_LEAD if has_lead else 0
+    if control:
+        # geometric_control (asian.rs:1016-1060)
+        first_weight = 1.0 - 0.5 / float(n)
+        log_asset_scale = log_spot + math.log(weight)
+        log_strike = math.log(strike)
+        usable = not (width > 0.8 or abs(log_discount) > 50.0 or abs(log_spot) > 200.0
+                      or abs(log_asset_scale) > 200.0)
+        if usable:
+            mean = lead_drift + first_weight * drift
+            for step in range(1, n):
+                mean += (first_weight - float(step) / float(n)) * drift
+            variance = lead_width * lead_width + width * width * (float(n) / 3.0 - 1.0 / (12.0 * float(n)))
+            control_width = math.sqrt(variance)
+            log_forward = log_asset_scale + mean + 0.5 * variance
+            if 0.02 <= control_width <= 0.8 and abs(log_forward - log_strike) <= 2.0 * control_width:
+                flags |= abi.C_AVERAGE_CONTROL
+                c["control_log_strike"] = log_strike
+                c["control_log_asset_scale"] = log_asset_scale
+                c["control_first_weight"] = first_weight
+                c["control_mean"] = _geometric_control_price(c_sign, log_discount, log_forward,
+                                                             log_strike, control_width)
+    c["flags"] = flags
+    return ContractPlan(c, np.zeros(dims, STEP_DTYPE), np.zeros(dims, np.uint8))
+
+
 def path_vanilla(option: EuropeanOption, ctx: PricingContext, step_count: int):
     """Vanilla payoff after `step_count` uniform log-Euler steps (the reference's generic
     D-dimensional sampler path_samples, monte_carlo.rs:1498, with transition())."""

@@ -16,7 +16,7 @@ from . import abi, plans
 from ._native import context
 from .errors import InvalidInputError, UnsupportedOperationError
 from .instruments import (Accumulator, AmericanOption, AsianOption, AutocallableNote,
-                          BarrierOption, DigitalOption, EuropeanOption)
+                          AveragePriceOption, BarrierOption, DigitalOption, EuropeanOption)
 from .market import PricingContext
 
 PSEUDO_RANDOM = "pseudo_random"
@@ -222,16 +222,61 @@ class MonteCarloVanillaEngine(_MonteCarloEngine):
 
 
 class MonteCarloAsianEngine(_MonteCarloEngine):
-    """Arithmetic average-price options on their fixing dates (optionally refined to a
-    uniform `step_count` grid)."""
+    """kiyosi's MonteCarloAsianEngine (engines/monte_carlo/asian.rs) on continuously
+    averaged ArithmeticAveragePriceOption / GeometricAveragePriceOption contracts under
+    flat BSM rates:
+    - geometric averages sample their exact law with one normal;
+    - arithmetic averages integrate `step_count` trapezoid intervals (default 50, the
+      reference's grid default), with the first interval integrated in closed form and
+      a geometric control variate near the money.
+
+    AsianOption (the arithmetic mean of the spots on discrete fixing dates, under any
+    model) is priced on its fixing grid, refined to `step_count` uniform steps only
+    when one is given."""
     _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + ("step_count",)
 
-    def __init__(self, *, step_count: int = 0, **kw):
+    def __init__(self, *, step_count: Optional[int] = None, **kw):
         super().__init__(**kw)
-        self.step_count = int(step_count)
+        if step_count is not None and not (2 <= int(step_count) <= 10_000):
+            raise InvalidInputError("step_count must be in 2..=10000")
+        self.step_count = None if step_count is None else int(step_count)
 
-    def price_with_statistics(self, option: AsianOption, ctx: PricingContext):
-        return self._run(ctx, [plans.asian(option, ctx, self.step_count or None)])[0]
+    def _average(self, options, ctx: PricingContext):
+        """Prices average-price options with one resolved seed; a controlled mean that
+        comes out negative is priced again without the control on the same seed
+        (ArithmeticGrid::sample, asian.rs:602-633)."""
+        engine = self.with_resolved_seed()
+        steps = self.step_count or 50
+        first = [plans.average(o, ctx, steps) for o in options]
+        out = engine._run(ctx, first)
+        redo = [i for i, (p, e) in enumerate(zip(first, out))
+                if isinstance(p, plans.ContractPlan) and p.record["flags"] & abi.C_AVERAGE_CONTROL
+                and e.price < 0.0]
+        if redo:
+            again = engine._run(ctx, [plans.average(options[i], ctx, steps, control=False)
+                                      for i in redo])
+            for i, e in zip(redo, again):
+                out[i] = e
+        return out
+
+    def price_with_statistics(self, option, ctx: PricingContext):
+        if isinstance(option, AveragePriceOption):
+            return self._average([option], ctx)[0]
+        return self._run(ctx, [plans.asian(option, ctx, self.step_count)])[0]
+
+    def price_strikes(self, option: AveragePriceOption, ctx: PricingContext,
+                      strikes: Sequence[float]):
+        """Prices across strikes on common paths: every strike replays its scalar price
+        (price_strikes, asian.rs:197-340), duplicates included."""
+        if not isinstance(option, AveragePriceOption):
+            raise InvalidInputError("price_strikes takes an average-price option")
+        for k in strikes:
+            if not (math.isfinite(k) and k > 0.0):
+                raise InvalidInputError("strike must be positive and finite")
+        unique = sorted(set(float(k) for k in strikes))
+        prices = dict(zip(unique, (e.price for e in self._average(
+            [replace(option, strike=k) for k in unique], ctx))))
+        return [prices[float(k)] for k in strikes]
 
 
 class MonteCarloAutocallableEngine(_MonteCarloEngine):

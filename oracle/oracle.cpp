@@ -404,6 +404,114 @@ static double barrier_discrete_payoff(const Plan& p, PathNormals& n, Failure& f)
     return value;
 }
 
+// log_add (numerics.rs:320-327).
+static double log_add(double a, double b) {
+    const double high = std::max(a, b);
+    if (high == -INFINITY) return high;
+    return high + std::log1p(std::exp(-std::fabs(a - b)));
+}
+
+// positive_difference (asian.rs:972-985): exp(a) - exp(b), floored at zero.
+static double positive_difference(double a, double b) {
+    if (a == INFINITY) return a;
+    if (b == -INFINITY) return std::exp(a);
+    const double difference = -std::expm1(b - a);
+    return difference > 0.0 ? std::exp(a + std::log(difference)) : 0.0;
+}
+
+// ArithmeticParameters::geometric_values, price only (asian.rs:1062-1085).
+static double geometric_values(const kgpu_contract* c, double log_forward, double log_strike, double width) {
+    const double d1 = (log_forward - log_strike) / width + 0.5 * width;
+    const double d2 = d1 - width;
+    const double log_asset = log_forward + c->log_discount + log_normal_cdf(c->sign * d1);
+    const double log_cash = log_strike + c->log_discount + log_normal_cdf(c->sign * d2);
+    return c->sign > 0.0 ? positive_difference(log_asset, log_cash) : positive_difference(log_cash, log_asset);
+}
+
+// Continuous arithmetic average (asian.rs:636-711 ArithmeticGrid::path, then
+// 1087-1178 ArithmeticParameters::arithmetic), price only, flat rates, no realized
+// history, interval widths of at least 1e-5 (plans reject narrower ones).
+static double average_arithmetic_payoff(const kgpu_contract* c, PathNormals& n, Failure& f) {
+    const bool lead = c->flags & KGPU_C_AVERAGE_LEAD;
+    const bool control = c->flags & KGPU_C_AVERAGE_CONTROL;
+    const int normals = c->step_count - (lead ? 1 : 0);  // step_count (n) - 1 increments
+    const double lead_normal = lead ? n.normal() : 0.0;
+    const double lead_growth = c->avg_lead_drift + c->avg_lead_width * lead_normal;
+    double growth = 0.0, relative_sum = 0.0, log_sum = -INFINITY, geometric_growth = 0.0;
+    for (int index = 0; index < normals; ++index) {
+        const double normal = n.normal();
+        growth += c->avg_drift + c->avg_width * normal;
+        const bool last = index + 1 == normals;
+        const double fraction = last ? c->avg_half : c->avg_fraction;
+        if (control) geometric_growth += fraction * growth;
+        if (growth > 600.0 || log_sum != -INFINITY) {
+            if (log_sum == -INFINITY) log_sum = std::log(c->avg_rest + relative_sum);
+            log_sum = log_add(log_sum, (last ? c->avg_log_half : c->avg_log_fraction) + growth);
+        } else {
+            relative_sum += fraction * std::expm1(growth);
+        }
+    }
+    const double log_rest =
+        log_sum == -INFINITY ? c->avg_log_rest + std::log1p(relative_sum / c->avg_rest) : log_sum;
+    const double log_q = c->avg_log_scale + lead_growth + log_rest + c->avg_interval_forward;
+    const double log_c = c->avg_log_scale + lead_growth + c->avg_log_half;
+    const double log_accrued = log_add(-INFINITY, log_c);
+    double residual = 0.0;
+    if (control) {
+        const double width = c->control_first_weight * c->avg_width;
+        const double log_forward = c->control_log_asset_scale + lead_growth + geometric_growth +
+                                   c->control_first_weight * c->avg_drift + 0.5 * width * width;
+        residual = geometric_values(c, log_forward, c->control_log_strike, width);
+    }
+    double value;
+    const double log_strike = c->avg_log_strike;
+    if (log_accrued >= log_strike) {
+        value = c->sign < 0.0 ? 0.0
+                              : std::exp(log_q + c->log_discount) +
+                                    positive_difference(log_accrued + c->log_discount, log_strike + c->log_discount);
+    } else {
+        const double log_b = log_strike + std::log(-std::expm1(log_accrued - log_strike));
+        double forward = log_q - log_b;
+        if (log_sum == -INFINITY) {
+            const double extra = std::expm1(lead_growth) +
+                                 std::exp(lead_growth) * (c->avg_rest * std::expm1(c->avg_interval_forward) +
+                                                          relative_sum * std::exp(c->avg_interval_forward));
+            const double excess = c->avg_baseline + c->avg_weight * extra;
+            const double b = std::exp(log_b - c->avg_log_spot);
+            if (b > 0.0 && std::fabs(excess / b) < 0.5) forward = std::log1p(excess / b);
+        }
+        const double center = forward / c->avg_width;
+        const double d1 = center + 0.5 * c->avg_width;
+        const double d2 = center - 0.5 * c->avg_width;
+        const double log_asset = log_q + c->log_discount + log_normal_cdf(c->sign * d1);
+        const double log_cash = log_b + c->log_discount + log_normal_cdf(c->sign * d2);
+        value = c->sign > 0.0 ? positive_difference(log_asset, log_cash) : positive_difference(log_cash, log_asset);
+    }
+    value -= residual;
+    if (!std::isfinite(value)) f.failed = true;
+    return value;
+}
+
+// GeometricParameters::geometric, price only (asian.rs:740-784): moneyness = initial
+// moneyness + drift, diffusion = width, log_scale = log width.
+static double average_geometric_payoff(const kgpu_contract* c, double normal, Failure& f) {
+    const double distance = c->moneyness + c->diffusion * normal;
+    const double standardized = c->moneyness / c->diffusion + normal;
+    if (c->sign * standardized <= 0.0) return 0.0;
+    const double log_strike = c->avg_log_strike;
+    double log_payoff;
+    if (std::fabs(distance) < 1e-5 && std::isfinite(standardized))
+        log_payoff = log_strike + c->log_scale + std::log(std::fabs(standardized)) +
+                     (distance == 0.0 ? 0.0 : std::log(std::fabs(std::expm1(distance)) / std::fabs(distance)));
+    else if (c->sign > 0.0)
+        log_payoff = log_strike + distance + std::log(-std::expm1(-distance));
+    else
+        log_payoff = log_strike + std::log(-std::expm1(distance));
+    const double value = std::exp(log_payoff + c->log_discount);
+    if (!std::isfinite(value)) f.failed = true;
+    return value;
+}
+
 // AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
 static inline double autocallable_terminal(const kgpu_contract* c, double spot, bool knocked_in) {
     if (knocked_in) {
@@ -532,7 +640,8 @@ static double accumulator_path(const Plan& p, const Model& model, PathNormals& n
 }
 
 static bool terminal_payoff(const kgpu_contract* c) {
-    return c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL || c->payoff == KGPU_PAYOFF_BARRIER;
+    return c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL || c->payoff == KGPU_PAYOFF_BARRIER ||
+           c->payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC;
 }
 
 static int dimensions_of(const kgpu_contract* c, const Model& model) {
@@ -551,6 +660,10 @@ static double evaluate(const Plan& p, const Model& model, PathNormals& n, Failur
             return barrier_payoff(c, n.normal(), f);
         case KGPU_PAYOFF_BARRIER_DISCRETE:
             return barrier_discrete_payoff(p, n, f);
+        case KGPU_PAYOFF_AVERAGE_ARITHMETIC:
+            return average_arithmetic_payoff(c, n, f);
+        case KGPU_PAYOFF_AVERAGE_GEOMETRIC:
+            return average_geometric_payoff(c, n.normal(), f);
         case KGPU_PAYOFF_VANILLA_PATH:
             return path_vanilla(p, model, n, false);
         case KGPU_PAYOFF_ASIAN:
@@ -641,6 +754,9 @@ static int price_contract(const Model& model, const Plan& p, const kgpu_settings
     if (!std::isfinite(price)) return KGPU_COMPUTATION_FAILURE;
     // sampling_standard_error (monte_carlo.rs:1435-1452) and from_sampling (939-963).
     const Moments& u = antithetic ? pairs : total;
+    // ArithmeticGrid::sample (asian.rs:616-621): residual samples plus the control's mean.
+    if (c->payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC && (c->flags & KGPU_C_AVERAGE_CONTROL))
+        price += c->control_mean;
     out->price = price;
     out->seed = settings->seed;
     out->standard_error = 0.0;
