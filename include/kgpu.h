@@ -111,8 +111,11 @@ enum {
     KGPU_PAYOFF_AVERAGE_ARITHMETIC = 8, /* continuous arithmetic average (asian.rs:374-713,
                                      1016-1257): trapezoid over n intervals, the first one
                                      integrated analytically, n - 1 (+ lead) normals */
-    KGPU_PAYOFF_AVERAGE_GEOMETRIC = 9  /* continuous geometric average or single fixing:
+    KGPU_PAYOFF_AVERAGE_GEOMETRIC = 9, /* continuous geometric average or single fixing:
                                      one exact normal (asian.rs:740-784) */
+    KGPU_PAYOFF_DOUBLE_BARRIER = 10 /* continuously monitored double barrier: one terminal
+                                     draw weighted by the killed-density survival series
+                                     (barrier.rs:341-390, double_barrier.rs:6-112) */
 };
 
 /* One simulated grid step of a contract.  For BSM the transition is the reference's
@@ -180,9 +183,11 @@ enum {
                                      pricing (barrier.rs:280-289) */
     KGPU_C_AVERAGE_LEAD = 2048,   /* arithmetic average starting after valuation: the first
                                      normal draws the lead interval */
-    KGPU_C_AVERAGE_CONTROL = 4096 /* arithmetic average with the geometric control variate:
+    KGPU_C_AVERAGE_CONTROL = 4096, /* arithmetic average with the geometric control variate:
                                      each sample is the residual against the geometric payoff
                                      on the same path; control_mean is added to the mean */
+    KGPU_C_DOUBLE = 8192          /* scheduled double barrier: event payment[3] holds the upper
+                                     barrier's touch level (noise >= it touches) */
 };
 
 /* A contract's plan.  Field groups are used by the payoff families named beside them. */
@@ -264,6 +269,12 @@ typedef struct kgpu_contract {
     double control_log_asset_scale;
     double control_first_weight;  /* 1 - 0.5 / n */
     double control_mean;          /* exact expected value of the control */
+    /* continuous double barrier (KGPU_PAYOFF_DOUBLE_BARRIER): barrier_moneyness is the
+     * lower barrier's terminal distance, so log(S_T / lower) = barrier_moneyness + noise;
+     * strike, sign, diffusion, moneyness, barrier_drift, rebate, spot, log_discount as
+     * for the single barrier */
+    double band;                  /* log(upper / lower) */
+    double band_initial;          /* log(spot / lower) */
 } kgpu_contract;
 
 /* A book of contracts sharing one model.  Arrays are indexed through the offsets in

@@ -36,6 +36,7 @@ PAYOFF_BARRIER = 6
 PAYOFF_BARRIER_DISCRETE = 7
 PAYOFF_AVERAGE_ARITHMETIC = 8
 PAYOFF_AVERAGE_GEOMETRIC = 9
+PAYOFF_DOUBLE_BARRIER = 10
 
 STEP_KNOCK_IN = 1
 STEP_EVENT = 2
@@ -55,6 +56,7 @@ C_CONDITION_ON_HIT = 512
 C_CHECK_STEPS = 1024
 C_AVERAGE_LEAD = 2048
 C_AVERAGE_CONTROL = 4096
+C_DOUBLE = 8192
 
 UNCERTAINTY_NAMES = {
     0: "available",
@@ -122,7 +124,8 @@ class Contract(C.Structure):
                 ("avg_half", _D), ("avg_log_fraction", _D), ("avg_log_half", _D),
                 ("avg_rest", _D), ("avg_log_rest", _D), ("avg_baseline", _D),
                 ("control_log_strike", _D), ("control_log_asset_scale", _D),
-                ("control_first_weight", _D), ("control_mean", _D)]
+                ("control_first_weight", _D), ("control_mean", _D), ("band", _D),
+                ("band_initial", _D)]
 
 
 class Book(C.Structure):

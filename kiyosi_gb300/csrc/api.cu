@@ -287,7 +287,7 @@ int model_normals_per_step(const kgpu_model* m) { return m->kind == KGPU_MODEL_H
 // Payoffs sampled with one terminal draw per path (no grid).
 bool terminal_payoff(const kgpu_contract& c) {
     return c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL || c.payoff == KGPU_PAYOFF_BARRIER ||
-           c.payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC;
+           c.payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC || c.payoff == KGPU_PAYOFF_DOUBLE_BARRIER;
 }
 
 int dims_of(const kgpu_contract& c, const kgpu_model* m) {
@@ -577,7 +577,7 @@ bool extended_payoffs(const kgpu_book& b) {
     for (int i = 0; i < b.contract_count; ++i) {
         const int p = b.contracts[i].payoff;
         if (p == KGPU_PAYOFF_BARRIER_DISCRETE || p == KGPU_PAYOFF_AVERAGE_ARITHMETIC ||
-            p == KGPU_PAYOFF_AVERAGE_GEOMETRIC)
+            p == KGPU_PAYOFF_AVERAGE_GEOMETRIC || p == KGPU_PAYOFF_DOUBLE_BARRIER)
             return true;
     }
     return false;
@@ -825,9 +825,12 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: path_count must be positive", i);
         if (k.sobol && !is_pow2(paths))
             return fail(ctx, KGPU_INVALID_INPUT, "path_count must be a power of two for Sobol sampling");
-        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_AVERAGE_GEOMETRIC)
+        if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_DOUBLE_BARRIER)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: unknown payoff %d", i, c.payoff);
-        if (c.payoff == KGPU_PAYOFF_BARRIER && (model->kind != KGPU_MODEL_BSM || !(c.diffusion > 0.0)))
+        if (!(c.spot > 0.0) || !std::isfinite(c.spot))
+            return fail(ctx, KGPU_INVALID_INPUT, "contract %d: spot must be positive and finite", i);
+        if ((c.payoff == KGPU_PAYOFF_BARRIER || c.payoff == KGPU_PAYOFF_DOUBLE_BARRIER) &&
+            (model->kind != KGPU_MODEL_BSM || !(c.diffusion > 0.0)))
             return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "contract %d: the Monte Carlo barrier needs BSM volatility", i);
         if ((c.payoff == KGPU_PAYOFF_AVERAGE_ARITHMETIC || c.payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC) &&
             model->kind != KGPU_MODEL_BSM)

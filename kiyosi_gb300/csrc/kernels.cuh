@@ -149,6 +149,8 @@ __global__ void compile_contracts_kernel(const kgpu_contract* in, int n, Contrac
     o.control_log_asset_scale = Real(c.control_log_asset_scale);
     o.control_first_weight = Real(c.control_first_weight);
     o.control_mean = Real(c.control_mean);
+    o.band = Real(c.band);
+    o.band_initial = Real(c.band_initial);
     out[i] = o;
 }
 

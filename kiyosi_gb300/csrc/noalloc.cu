@@ -85,6 +85,8 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
     if (paths < 1 || paths > 2147483647LL) return noalloc_fail(KGPU_INVALID_INPUT, "path_count must be positive");
     if (c.payoff < KGPU_PAYOFF_EUROPEAN || c.payoff > KGPU_PAYOFF_DIGITAL)
         return noalloc_fail(KGPU_INVALID_INPUT, "unknown payoff");
+    if (!(c.spot > 0.0) || !std::isfinite(c.spot))
+        return noalloc_fail(KGPU_INVALID_INPUT, "spot must be positive and finite");
     if ((c.flags & KGPU_C_BRIDGE) && model->kind != KGPU_MODEL_BSM)
         return noalloc_fail(KGPU_INVALID_INPUT, "a bridge plan needs BSM");
     if (c.step_count < 1 || c.step_offset < 0 || c.step_offset + c.step_count > device_book->step_total)

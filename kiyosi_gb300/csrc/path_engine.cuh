@@ -87,6 +87,7 @@ struct ContractT {
     Real avg_log_spot, avg_log_scale, avg_log_strike, avg_fraction, avg_half, avg_log_fraction, avg_log_half;
     Real avg_rest, avg_log_rest, avg_baseline;
     Real control_log_strike, control_log_asset_scale, control_first_weight, control_mean;
+    Real band, band_initial;
 };
 
 // Device view of the book in the kernel's precision.
@@ -250,6 +251,8 @@ __device__ __forceinline__ double xlog(double x) { return log(x); }
 __device__ __forceinline__ float xlog(float x) { return __logf(x); }
 __device__ __forceinline__ double xlog1p(double x) { return log1p(x); }
 __device__ __forceinline__ float xlog1p(float x) { return log1pf(x); }
+__device__ __forceinline__ double xsin(double x) { return sin(x); }
+__device__ __forceinline__ float xsin(float x) { return sinf(x); }
 __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float xsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double xinf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
@@ -596,6 +599,81 @@ __device__ __noinline__ Real average_geometric_value(const ContractT<Real>& c, R
     return xexp(log_payoff + c.log_discount);
 }
 
+// survival (double_barrier.rs:6-112), value only: the probability that a Brownian path
+// from `initial` to `terminal` (log distances above the lower barrier) over a standard
+// deviation `deviation` stays inside (0, band).  Small variances sum the method of
+// images, large ones the spectral (sine) series.  NaN when the series does not converge
+// or leaves [0, 1] (a computation failure).
+template <class Real>
+__device__ __noinline__ Real double_survival(Real initial, Real terminal, Real band, Real deviation) {
+    if (terminal <= Real(0) || terminal >= band) return Real(0);
+    Real x = initial / band, y = terminal / band;
+    const Real ratio = deviation / band;
+    const Real variance = ratio * ratio;
+    if (variance == Real(0)) return Real(1);
+    if (!(variance > Real(0) && variance < xinf(Real(0)))) return xnan(Real(0));
+    if (x + y > Real(1)) {
+        x = Real(1) - x;
+        y = Real(1) - y;
+    }
+    Real sum = Real(0);
+    bool converged = false;
+    if (variance < Real(0.25)) {
+        // The k = 0 terms: the direct one is 1, the reflected one is folded into expm1.
+        sum = -xexpm1(Real(-2) * (x / ratio) * (y / ratio));
+        for (int n = 1; n <= 64; ++n) {
+            const Real k = Real(n);
+            const Real w1 = xexp(Real(-2) * (k / ratio) * ((y - x + k) / ratio));
+            const Real w2 = xexp(Real(-2) * ((x + k) / ratio) * ((y + k) / ratio));
+            const Real w3 = xexp(Real(-2) * (-k / ratio) * ((y - x - k) / ratio));
+            const Real w4 = xexp(Real(-2) * ((x - k) / ratio) * ((y - k) / ratio));
+            sum += w1;
+            sum -= w2;
+            sum += w3;
+            sum -= w4;
+            if (n >= 2 && ((w1 + w2) + w3) + w4 < Real(1e-18)) {
+                converged = true;
+                break;
+            }
+        }
+    } else {
+        const Real distance = y - x;
+        const Real log_scale = xlog(Real(2) * Real(2.5066282746310002) * ratio) + Real(0.5) * distance * distance / variance;
+        for (int n = 1; n <= 256; ++n) {
+            const Real frequency = Real(n) * Real(3.141592653589793);
+            const Real exponent = log_scale - Real(0.5) * frequency * frequency * variance;
+            const Real weight = xexp(exponent);
+            const Real sy = xsin(frequency * y);
+            const Real product = xsin(frequency * x) * sy;
+            sum += weight * product;
+            if (n >= 4 && exponent + Real(4) * xlog(frequency) < Real(-40)) {
+                converged = true;
+                break;
+            }
+        }
+    }
+    if (!converged || !(sum >= Real(-1e-13) && sum <= Real(1) + Real(1e-13))) return xnan(Real(0));
+    return sum < Real(0) ? Real(0) : (sum > Real(1) ? Real(1) : sum);
+}
+
+// The continuous double barrier's sample (barrier.rs:341-390), value only.
+template <class Real>
+__device__ __noinline__ Real double_barrier_value(const ContractT<Real>& c, Real z) {
+    const Real noise = xfma(c.diffusion, z, Real(0));
+    const Real terminal = c.barrier_drift + noise;
+    const Real distance = c.moneyness + noise;
+    const Real payoff = xabs(distance) < Real(0.5) ? c.strike * xexpm1(distance)
+                                                   : weighted_amount(c.spot, terminal) - c.strike;
+    Real intrinsic = c.sign * payoff;
+    intrinsic = intrinsic > Real(0) ? intrinsic : Real(0);
+    const Real survival = double_survival(c.band_initial, c.barrier_moneyness + noise, c.band, c.diffusion);
+    const bool in = (c.flags & KGPU_C_BARRIER_IN) != 0;
+    const Real rebate = (!in && (c.flags & KGPU_C_REBATE_AT_HIT)) ? Real(0) : c.rebate;
+    const Real log_survival = xlog(survival), log_hit = xlog1p(-survival);
+    return weighted_amount(intrinsic, c.log_discount + (in ? log_hit : log_survival)) +
+           weighted_amount(rebate, c.log_discount + (in ? log_survival : log_hit));
+}
+
 template <class Real>
 struct PlanPtrs {
     const StepT<Real>* __restrict__ steps;
@@ -680,7 +758,7 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         if (s.k < c.bridge_count) return false;
         const bool hit = s.knocked_in ||
                          ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) && (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < level);
-        value = s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), hit) * c.final_discount;
+        value = s.cash + autocallable_terminal(c, spot_at(c.spot, s.lr), hit) * c.final_discount;
         return true;
     }
     if (payoff == KGPU_PAYOFF_EUROPEAN) {
@@ -695,6 +773,11 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
     }
     if (payoff == KGPU_PAYOFF_BARRIER) {
         value = barrier_value(c, n.normal());
+        s.executed = 1;
+        return true;
+    }
+    if (EXT && payoff == KGPU_PAYOFF_DOUBLE_BARRIER) {
+        value = double_barrier_value(c, n.normal());
         s.executed = 1;
         return true;
     }
@@ -748,8 +831,10 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         }
         const EventT<Real> e = p.events[i];
         const bool in = (c.flags & KGPU_C_BARRIER_IN) != 0;
-        if (e.has_knock_out &&
-            ((c.flags & KGPU_C_BARRIER_UP) ? s.lr >= e.knock_out : s.lr <= e.knock_out)) {
+        const bool touched_now = (c.flags & KGPU_C_DOUBLE) ? (s.lr <= e.knock_out || s.lr >= e.payment[3])
+                                 : (c.flags & KGPU_C_BARRIER_UP) ? s.lr >= e.knock_out
+                                                                 : s.lr <= e.knock_out;
+        if (e.has_knock_out && touched_now) {
             s.knocked_in = true;  // touched
             if ((c.flags & KGPU_C_CONDITION_ON_HIT) && c.step_count - i > 8) {
                 const Real asset = weighted_amount(c.spot, st.drift + s.lr);
@@ -794,7 +879,7 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         if (!last) return false;
         const bool ki = s.knocked_in || ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) &&
                                          (c.flags & KGPU_C_HAS_KNOCK_IN) && s.lr < c.knock_in);
-        value = s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), ki) * c.final_discount;
+        value = s.cash + autocallable_terminal(c, spot_at(c.spot, s.lr), ki) * c.final_discount;
         return true;
     }
     if (payoff == KGPU_PAYOFF_ACCUMULATOR) {
@@ -802,7 +887,7 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         auto unit = [&](Real lr) {
             Real distance = lr - c.log_strike;
             if (xabs(distance) < Real(0.5)) return sign * c.strike * xexpm1(distance);
-            Real spot = spot_at(m.spot, lr);
+            Real spot = spot_at(c.spot, lr);
             return sign > Real(0) ? spot - c.strike : c.strike - spot;
         };
         if ((fl & KGPU_STEP_EVENT) && sign * s.lr >= sign * c.knock_out) {
@@ -816,11 +901,11 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         return true;
     }
     if (payoff == KGPU_PAYOFF_ASIAN && (fl & KGPU_STEP_FIXING)) {
-        s.acc += spot_at(m.spot, s.lr);
+        s.acc += spot_at(c.spot, s.lr);
         s.fixings += 1;
     }
     if (!last) return false;
-    Real underlying = payoff == KGPU_PAYOFF_ASIAN ? s.acc / Real(s.fixings) : spot_at(m.spot, s.lr);
+    Real underlying = payoff == KGPU_PAYOFF_ASIAN ? s.acc / Real(s.fixings) : spot_at(c.spot, s.lr);
     Real x = c.sign * (underlying - c.strike);
     value = (x > Real(0) ? x : Real(0)) * c.final_discount;
     return true;
@@ -880,7 +965,7 @@ __device__ __forceinline__ Real bridge_value(const DevModel<Real>& m, const Cont
     if (s.knocked_out) return s.cash;
     const bool in = s.knocked_in || ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) && (c.flags & KGPU_C_HAS_KNOCK_IN) &&
                                      s.lr < c.knock_in);
-    return s.cash + autocallable_terminal(c, spot_at(m.spot, s.lr), in) * c.final_discount;
+    return s.cash + autocallable_terminal(c, spot_at(c.spot, s.lr), in) * c.final_discount;
 }
 
 // Scaled Welford moments (monte_carlo.rs:2155-2222), used by the plain schedule.

@@ -105,6 +105,50 @@ class BarrierOption(EuropeanOption):
         return self.barrier_type.endswith("_in")
 
 
+DOUBLE_BARRIER_TYPES = ("knock_out", "knock_in")
+
+
+@dataclass(frozen=True)
+class DoubleBarrierOption(EuropeanOption):
+    """Double-barrier vanilla option (instruments/double_barrier.rs): knocked out (or in)
+    when the spot reaches `lower` or `upper`.  Monitoring, rebate and its timing follow
+    BarrierOption; kiyosi represents it as the lower down-barrier plus the upper level."""
+    lower: float = 0.0
+    upper: float = 0.0
+    barrier_type: str = "knock_out"
+    rebate: float = 0.0
+    rebate_timing: str = "at_expiry"
+    observation_times: Optional[Sequence[float]] = None
+
+    def __post_init__(self):
+        super().__post_init__()
+        if self.barrier_type not in DOUBLE_BARRIER_TYPES:
+            raise InvalidInputError(f"barrier_type must be one of {DOUBLE_BARRIER_TYPES}")
+        if not (self.lower > 0.0 and math.isfinite(self.lower)):
+            raise InvalidInputError("barrier must be positive and finite")
+        if not math.isfinite(self.upper) or self.upper <= self.lower:
+            raise InvalidInputError("double barriers require finite 0 < lower < upper")
+        if not (self.rebate >= 0.0 and math.isfinite(self.rebate)):
+            raise InvalidInputError("rebate must be nonnegative and finite")
+        if self.rebate_timing not in ("at_expiry", "at_hit"):
+            raise InvalidInputError("rebate_timing must be 'at_expiry' or 'at_hit'")
+        if self.is_knock_in and self.rebate_timing == "at_hit":
+            raise InvalidInputError("knock-in rebates cannot pay at hit")
+        if self.observation_times is not None:
+            times = tuple(_times(self.observation_times, self.expiry, "observation_times"))
+            if not times:
+                raise InvalidInputError("a scheduled barrier needs at least one observation time")
+            object.__setattr__(self, "observation_times", times)
+
+    @property
+    def is_knock_in(self) -> bool:
+        return self.barrier_type == "knock_in"
+
+    @property
+    def continuous(self) -> bool:
+        return self.observation_times is None
+
+
 @dataclass(frozen=True)
 class AveragePriceOption:
     """Continuously averaged price option (instruments/asian.rs AverageTerms): the

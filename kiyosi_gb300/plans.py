@@ -67,10 +67,13 @@ def transition(rate, dividend, sigma, time, discount_time):
     return drift, diffusion, log_discount
 
 
-def _new_contract(payoff: int) -> np.ndarray:
+def _new_contract(payoff: int, spot: float) -> np.ndarray:
+    """A zeroed contract record of `payoff` valued at `spot` (the scenario's spot: a
+    book may hold contracts valued at different spots, as Greek stencils do)."""
     c = np.zeros(1, CONTRACT_DTYPE)
     c["payoff"] = payoff
     c["sign"] = 1.0
+    c["spot"] = spot
     return c
 
 
@@ -118,7 +121,7 @@ def european(option: EuropeanOption, ctx: PricingContext):
     moneyness = (log_ratio(ctx.spot, option.strike) + carry) - half_variance
     log_scale = (math.log(ctx.spot) - dividend * time) if sign > 0 else (
         math.log(option.strike) - rate * time)
-    c = _new_contract(abi.PAYOFF_EUROPEAN)
+    c = _new_contract(abi.PAYOFF_EUROPEAN, ctx.spot)
     c["strike"] = option.strike
     c["sign"] = sign
     c["diffusion"] = diffusion
@@ -149,7 +152,7 @@ def digital(option: DigitalOption, ctx: PricingContext):
     asset = option.payout is None
     amount = ctx.spot if asset else option.payout
     drift = (-dividend - 0.5 * sigma * sigma) * time if asset else -rate * time
-    c = _new_contract(abi.PAYOFF_DIGITAL)
+    c = _new_contract(abi.PAYOFF_DIGITAL, ctx.spot)
     c["flags"] = abi.C_ASSET_DIGITAL if asset else 0
     c["strike"] = amount
     c["sign"] = sign
@@ -168,12 +171,16 @@ def _barrier_resolution(option: BarrierOption, ctx: PricingContext):
     touched now when today is monitored (always for continuous monitoring, an
     observation time of 0 for scheduled) and the spot is at or beyond it.  Returns the
     settled price, or None when the option must be sampled."""
+    from .instruments import DoubleBarrierOption
     rate = ctx.model.rate
-    spot, level, time = ctx.spot, option.barrier, option.expiry
-    up, knock_in = option.is_up, option.is_knock_in
+    spot, time = ctx.spot, option.expiry
+    knock_in = option.is_knock_in
     times = option.observation_times
     monitored = option.continuous or times[0] == 0.0
-    hit = spot >= level if up else spot <= level
+    if isinstance(option, DoubleBarrierOption):
+        hit = spot <= option.lower or spot >= option.upper
+    else:
+        hit = spot >= option.barrier if option.is_up else spot <= option.barrier
     touched = monitored and hit
     finished = time == 0.0 or (not option.continuous and times[-1] <= 0.0)
 
@@ -186,9 +193,14 @@ def _barrier_resolution(option: BarrierOption, ctx: PricingContext):
         return option.rebate if option.rebate_timing == "at_hit" else cash()
     if not touched and finished and knock_in:
         return cash()
-    requires_touch = (option.continuous or times[-1] == time) and (
-        (option.sign > 0.0 and option.strike >= level) if up else
-        (option.sign < 0.0 and option.strike <= level))
+    if isinstance(option, DoubleBarrierOption):
+        # DoubleBarrierOption::payoff_requires_touch (instruments/double_barrier.rs)
+        needs = option.strike >= option.upper if option.sign > 0.0 else option.strike <= option.lower
+    elif option.is_up:
+        needs = option.sign > 0.0 and option.strike >= option.barrier
+    else:
+        needs = option.sign < 0.0 and option.strike <= option.barrier
+    requires_touch = (option.continuous or times[-1] == time) and needs
     fixed = option.rebate == 0.0 and requires_touch
     if fixed and not knock_in:
         return 0.0
@@ -197,22 +209,27 @@ def _barrier_resolution(option: BarrierOption, ctx: PricingContext):
     return None
 
 
-def barrier(option: BarrierOption, ctx: PricingContext):
-    """MonteCarloBarrierEngine::native (barrier.rs:231-452) for single barriers.
+def barrier(option, ctx: PricingContext):
+    """MonteCarloBarrierEngine::native (barrier.rs:231-452) for single and double barriers.
     Barriers settled at valuation resolve first (analytic/barrier.rs:20-78): a touched
     knock-out pays its rebate, a touched knock-in is the analytic vanilla option.
     Continuous monitoring draws one terminal normal per path and weights it by the
-    Brownian-bridge survival; scheduled monitoring steps date by date (one normal per
+    Brownian-bridge survival (single) or the killed-density series (double,
+    double_barrier.rs); scheduled monitoring steps date by date (one normal per
     observation, plus an unobserved expiry leg when the last observation is earlier)."""
+    from .instruments import DoubleBarrierOption
     model = ctx.model
     if not isinstance(model, BlackScholesMertonParameters):
         raise UnsupportedOperationError("the Monte Carlo barrier engine requires BSM parameters")
     resolved = _barrier_resolution(option, ctx)
     if resolved is not None:
         return Known(resolved)
+    double = isinstance(option, DoubleBarrierOption)
     rate, dividend, sigma = model.rate, model.dividend, model.volatility
-    spot, level, time = ctx.spot, option.barrier, option.expiry
-    up, knock_in = option.is_up, option.is_knock_in
+    spot, time = ctx.spot, option.expiry
+    level = option.lower if double else option.barrier
+    up = False if double else option.is_up
+    knock_in = option.is_knock_in
     at_hit = option.rebate_timing == "at_hit"
     if sigma == 0.0:
         raise UnsupportedOperationError("zero volatility: the barrier is deterministic")
@@ -231,8 +248,11 @@ def barrier(option: BarrierOption, ctx: PricingContext):
     mean = drift * time
     if not (width > 0.0 and math.isfinite(width) and math.isfinite(mean)):
         raise _unstable()
-    c = _new_contract(abi.PAYOFF_BARRIER)
+    c = _new_contract(abi.PAYOFF_DOUBLE_BARRIER if double else abi.PAYOFF_BARRIER, ctx.spot)
     c["flags"] = (abi.C_BARRIER_UP if up else 0) | (abi.C_BARRIER_IN if knock_in else 0)
+    if double:
+        c["band"] = log_ratio(option.upper, level)
+        c["band_initial"] = -log_ratio(level, spot)
     c["strike"] = option.strike
     c["sign"] = option.sign
     c["diffusion"] = width
@@ -256,9 +276,12 @@ def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_v
     mean drift * t_i and the width sigma sqrt(t_i - t_(i-1)); event i holds the noise
     level at which date i touches the barrier, the discount and asset log weights of a
     hit, and the remaining time and its root for the conditioned vanilla."""
+    from .instruments import DoubleBarrierOption
     model = ctx.model
     rate, dividend, sigma = model.rate, model.dividend, model.volatility
-    spot, level, time = ctx.spot, option.barrier, option.expiry
+    double = isinstance(option, DoubleBarrierOption)
+    spot, time = ctx.spot, option.expiry
+    level = option.lower if double else option.barrier
     dates = [t for t in option.observation_times if t > 0.0]
     legs = [(t, True) for t in dates]
     if not dates or dates[-1] != time:
@@ -279,7 +302,9 @@ def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_v
         steps[i] = (mean, width, date, math.exp(discount))
         events[i]["knock_out"] = -mean_distance(date, level) if observe else 0.0
         events[i]["coupon_barrier"] = remaining
-        events[i]["payment"] = (discount, discount - dividend * remaining, math.sqrt(remaining), 0.0)
+        upper_touch = -mean_distance(date, option.upper) if (double and observe) else 0.0
+        events[i]["payment"] = (discount, discount - dividend * remaining, math.sqrt(remaining),
+                                upper_touch)
         events[i]["has_knock_out"] = 1 if observe else 0
         events[i]["step"] = i
         width_sum += width
@@ -295,8 +320,9 @@ def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_v
         narrowest = min(sigma * float(events[i]["payment"][2]) for i in range(n - 8))
         if not narrowest >= 1e-5:
             raise UnsupportedOperationError("conditioned knock-in widths below 1e-5 are not sampled")
-    c = _new_contract(abi.PAYOFF_BARRIER_DISCRETE)
-    c["flags"] = ((abi.C_BARRIER_UP if option.is_up else 0) | (abi.C_BARRIER_IN if knock_in else 0)
+    c = _new_contract(abi.PAYOFF_BARRIER_DISCRETE, ctx.spot)
+    c["flags"] = ((abi.C_BARRIER_UP if (not double and option.is_up) else 0)
+                  | (abi.C_DOUBLE if double else 0) | (abi.C_BARRIER_IN if knock_in else 0)
                   | (abi.C_REBATE_AT_HIT if option.rebate_timing == "at_hit" else 0)
                   | (abi.C_CONDITION_ON_HIT if condition else 0)
                   | (0 if bounded else abi.C_CHECK_STEPS))
@@ -372,7 +398,7 @@ def average(option, ctx: PricingContext, step_count: int = 50, control: bool = T
         initial_moneyness = moneyness + 0.0
         if not (math.isfinite(drift) and math.isfinite(width)):
             raise _unstable()
-        c = _new_contract(abi.PAYOFF_AVERAGE_GEOMETRIC)
+        c = _new_contract(abi.PAYOFF_AVERAGE_GEOMETRIC, ctx.spot)
         c["strike"] = strike
         c["sign"] = c_sign
         c["moneyness"] = initial_moneyness + drift
@@ -399,7 +425,7 @@ def average(option, ctx: PricingContext, step_count: int = 50, control: bool = T
     half = 0.5 / float(n)
     rest = 1.0 - half
     log_spot = math.log(spot)
-    c = _new_contract(abi.PAYOFF_AVERAGE_ARITHMETIC)
+    c = _new_contract(abi.PAYOFF_AVERAGE_ARITHMETIC, ctx.spot)
     c["strike"] = strike
     c["sign"] = c_sign
     c["spot"] = spot
@@ -455,7 +481,7 @@ def path_vanilla(option: EuropeanOption, ctx: PricingContext, step_count: int):
         raise InvalidInputError("step_count must be positive")
     times = _uniform_times(option.expiry, step_count)
     steps = _grid_steps(ctx, times)
-    c = _new_contract(abi.PAYOFF_VANILLA_PATH)
+    c = _new_contract(abi.PAYOFF_VANILLA_PATH, ctx.spot)
     c["strike"] = option.strike
     c["sign"] = option.sign
     c["step_count"] = step_count
@@ -479,7 +505,7 @@ def asian(option: AsianOption, ctx: PricingContext, step_count: Optional[int] = 
         if i is None:
             raise InvalidInputError("every fixing must lie on the simulation grid")
         flags[i] |= abi.STEP_FIXING
-    c = _new_contract(abi.PAYOFF_ASIAN)
+    c = _new_contract(abi.PAYOFF_ASIAN, ctx.spot)
     c["strike"] = option.strike
     c["sign"] = option.sign
     c["step_count"] = len(times)
@@ -537,7 +563,7 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
                 payments.append(discounted_product(1.0, amount, log_discount))
             ev[k] = (ko, barrier, tuple(payments), int(has_ko), i)
             k += 1
-    c = _new_contract(abi.PAYOFF_AUTOCALLABLE)
+    c = _new_contract(abi.PAYOFF_AUTOCALLABLE, ctx.spot)
     flag = 0
     if note.knock_in_level is not None:
         flag |= abi.C_HAS_KNOCK_IN
@@ -620,7 +646,7 @@ def accumulator(option: Accumulator, ctx: PricingContext):
             flags[i] |= abi.STEP_EVENT
         if t in acc:
             flags[i] |= abi.STEP_ACCUMULATE
-    c = _new_contract(abi.PAYOFF_ACCUMULATOR)
+    c = _new_contract(abi.PAYOFF_ACCUMULATOR, ctx.spot)
     c["strike"] = option.strike
     c["sign"] = option.sign
     c["step_count"] = len(times)

@@ -379,7 +379,9 @@ static double barrier_discrete_payoff(const Plan& p, PathNormals& n, Failure& f)
                 return 0.0;
             }
         }
-        if (e.has_knock_out && (up ? noise >= e.knock_out : noise <= e.knock_out)) {
+        const bool touch = (c->flags & KGPU_C_DOUBLE) ? (noise <= e.knock_out || noise >= e.payment[3])
+                                                       : (up ? noise >= e.knock_out : noise <= e.knock_out);
+        if (e.has_knock_out && touch) {
             touched = true;
             if (condition && c->step_count - i > 8) {
                 const double asset = discounted_product(c->spot, 1.0, terminal);
@@ -512,6 +514,93 @@ static double average_geometric_payoff(const kgpu_contract* c, double normal, Fa
     return value;
 }
 
+// survival (double_barrier.rs:6-112) without derivatives: the probability that a
+// Brownian bridge between log distances `initial` and `terminal` above the lower barrier
+// stays inside (0, band).  Returns false when the series does not converge or leaves
+// [0, 1] (the reference's unstable() error).
+static bool double_survival(double initial, double terminal, double band, double deviation, double* out) {
+    if (terminal <= 0.0 || terminal >= band) {
+        *out = 0.0;
+        return true;
+    }
+    double x = initial / band, y = terminal / band;
+    const double ratio = deviation / band;
+    const double variance = ratio * ratio;
+    if (variance == 0.0) {
+        *out = 1.0;
+        return true;
+    }
+    if (!std::isfinite(variance) || variance <= 0.0) return false;
+    if (x + y > 1.0) {
+        x = 1.0 - x;
+        y = 1.0 - y;
+    }
+    double sum = 0.0;
+    bool converged = false;
+    if (variance < 0.25) {
+        sum = -std::expm1(-2.0 * (x / ratio) * (y / ratio));
+        // One image term: k shifts the band; direct images add, reflected ones subtract.
+        auto term = [&](double k, bool direct) {
+            const double exponent = direct ? -2.0 * (k / ratio) * ((y - x + k) / ratio)
+                                           : -2.0 * ((x + k) / ratio) * ((y + k) / ratio);
+            const double weight = std::exp(exponent);
+            if (k != 0.0) sum += (direct ? 1.0 : -1.0) * weight;
+            return weight;
+        };
+        term(0.0, false);
+        for (int n = 1; n <= 64; ++n) {
+            const double k = double(n);
+            const double a = term(k, true);
+            const double b = term(k, false);
+            const double c = term(-k, true);
+            const double d = term(-k, false);
+            if (n >= 2 && a + b + c + d < 1e-18) {
+                converged = true;
+                break;
+            }
+        }
+    } else {
+        const double distance = y - x;
+        const double log_scale = std::log(2.0 * std::sqrt(2.0 * M_PI) * ratio) + 0.5 * distance * distance / variance;
+        for (int n = 1; n <= 256; ++n) {
+            const double frequency = double(n) * M_PI;
+            const double exponent = log_scale - 0.5 * frequency * frequency * variance;
+            const double weight = std::exp(exponent);
+            const double sy = std::sin(frequency * y);
+            sum += weight * (std::sin(frequency * x) * sy);
+            if (n >= 4 && exponent + 4.0 * std::log(frequency) < -40.0) {
+                converged = true;
+                break;
+            }
+        }
+    }
+    if (!converged || !(sum >= -1e-13 && sum <= 1.0 + 1e-13)) return false;
+    *out = std::min(std::max(sum, 0.0), 1.0);
+    return true;
+}
+
+// Continuously monitored double barrier (barrier.rs:341-390), value only.
+static double double_barrier_payoff(const kgpu_contract* c, double z, Failure& f) {
+    const double noise = std::fma(c->diffusion, z, 0.0);
+    const double terminal = c->barrier_drift + noise;
+    const double asset = discounted_product(c->spot, 1.0, terminal);
+    if (!std::isfinite(asset)) f.failed = true;
+    const double distance = c->moneyness + noise;
+    const double payoff = std::fabs(distance) < 0.5 ? c->strike * std::expm1(distance) : asset - c->strike;
+    const double intrinsic = std::max(c->sign * payoff, 0.0);
+    double survival;
+    if (!double_survival(c->band_initial, c->barrier_moneyness + noise, c->band, c->diffusion, &survival)) {
+        f.failed = true;
+        return 0.0;
+    }
+    const bool in = c->flags & KGPU_C_BARRIER_IN;
+    const double rebate = (!in && (c->flags & KGPU_C_REBATE_AT_HIT)) ? 0.0 : c->rebate;
+    const double value = weighted(intrinsic, c->log_discount + (in ? std::log1p(-survival) : std::log(survival))) +
+                         weighted(rebate, c->log_discount + (in ? std::log(survival) : std::log1p(-survival)));
+    if (!std::isfinite(value)) f.failed = true;
+    return value;
+}
+
 // AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
 static inline double autocallable_terminal(const kgpu_contract* c, double spot, bool knocked_in) {
     if (knocked_in) {
@@ -546,7 +635,7 @@ static double autocallable_forward(const Plan& p, const Model& model, PathNormal
         }
     }
     knocked_in |= (c->flags & KGPU_C_EXPIRY_KNOCK_IN) && has_ki && s.lr < c->knock_in;
-    double spot = spot_at(model.m->spot, s.lr);
+    double spot = spot_at(c->spot, s.lr);
     cash += autocallable_terminal(c, spot, knocked_in) * c->final_discount;
     return cash;
 }
@@ -591,7 +680,7 @@ static double autocallable_bridge(const Plan& p, const Model& model, PathNormals
         }
     }
     bool hit = knocked_in || ((c->flags & KGPU_C_EXPIRY_KNOCK_IN) && has_ki && lr < level);
-    cash += autocallable_terminal(c, spot_at(model.m->spot, lr), hit) * c->final_discount;
+    cash += autocallable_terminal(c, spot_at(c->spot, lr), hit) * c->final_discount;
     return cash;
 }
 
@@ -606,11 +695,11 @@ static double path_vanilla(const Plan& p, const Model& model, PathNormals& n, bo
     for (int i = 0; i < c->step_count; ++i) {
         step_state(model, p.steps[i], s, n);
         if (asian && (p.flags[i] & KGPU_STEP_FIXING)) {
-            sum += spot_at(model.m->spot, s.lr);
+            sum += spot_at(c->spot, s.lr);
             ++fixings;
         }
     }
-    double underlying = asian ? sum / double(fixings) : spot_at(model.m->spot, s.lr);
+    double underlying = asian ? sum / double(fixings) : spot_at(c->spot, s.lr);
     double value = c->sign * (underlying - c->strike);
     return (value > 0.0 ? value : 0.0) * c->final_discount;
 }
@@ -624,7 +713,7 @@ static double accumulator_path(const Plan& p, const Model& model, PathNormals& n
     auto unit = [&](double lr) {
         double distance = lr - c->log_strike;
         if (std::fabs(distance) < 0.5) return c->sign * c->strike * std::expm1(distance);
-        double spot = spot_at(model.m->spot, lr);
+        double spot = spot_at(c->spot, lr);
         return c->sign > 0.0 ? spot - c->strike : c->strike - spot;
     };
     for (int i = 0; i < c->step_count; ++i) {
@@ -641,7 +730,7 @@ static double accumulator_path(const Plan& p, const Model& model, PathNormals& n
 
 static bool terminal_payoff(const kgpu_contract* c) {
     return c->payoff == KGPU_PAYOFF_EUROPEAN || c->payoff == KGPU_PAYOFF_DIGITAL || c->payoff == KGPU_PAYOFF_BARRIER ||
-           c->payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC;
+           c->payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC || c->payoff == KGPU_PAYOFF_DOUBLE_BARRIER;
 }
 
 static int dimensions_of(const kgpu_contract* c, const Model& model) {
@@ -664,6 +753,8 @@ static double evaluate(const Plan& p, const Model& model, PathNormals& n, Failur
             return average_arithmetic_payoff(c, n, f);
         case KGPU_PAYOFF_AVERAGE_GEOMETRIC:
             return average_geometric_payoff(c, n.normal(), f);
+        case KGPU_PAYOFF_DOUBLE_BARRIER:
+            return double_barrier_payoff(c, n.normal(), f);
         case KGPU_PAYOFF_VANILLA_PATH:
             return path_vanilla(p, model, n, false);
         case KGPU_PAYOFF_ASIAN:
