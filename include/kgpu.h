@@ -186,8 +186,13 @@ enum {
     KGPU_C_AVERAGE_CONTROL = 4096, /* arithmetic average with the geometric control variate:
                                      each sample is the residual against the geometric payoff
                                      on the same path; control_mean is added to the mean */
-    KGPU_C_DOUBLE = 8192          /* scheduled double barrier: event payment[3] holds the upper
+    KGPU_C_DOUBLE = 8192,         /* scheduled double barrier: event payment[3] holds the upper
                                      barrier's touch level (noise >= it touches) */
+    KGPU_C_OUTPUT_DELTA = 16384,  /* report each path's likelihood-ratio / pathwise delta sample
+                                     instead of its payoff (digital, barrier and average payoffs:
+                                     their native delta, digital.rs:116-140, barrier.rs:455-472,
+                                     asian.rs:740-784, 1163-1177); the estimate is its mean */
+    KGPU_C_OUTPUT_GAMMA = 32768   /* likewise for the gamma sample */
 };
 
 /* A contract's plan.  Field groups are used by the payoff families named beside them. */
@@ -275,6 +280,13 @@ typedef struct kgpu_contract {
      * for the single barrier */
     double band;                  /* log(upper / lower) */
     double band_initial;          /* log(spot / lower) */
+    /* native delta / gamma samples (KGPU_C_OUTPUT_*) */
+    double greek_log_spot;        /* ln(spot) */
+    double greek_log_width;       /* digital: ln(sigma) + ln(sqrt(T)); arithmetic average:
+                                     log width of an interval; geometric: log width */
+    double greek_log_amount;      /* digital: ln(paid amount) */
+    double greek_log_base_width;  /* geometric average: ln(sigma) + ln(sqrt(variance time)) */
+    double greek_log_weight;      /* geometric average: ln(weight) */
 } kgpu_contract;
 
 /* A book of contracts sharing one model.  Arrays are indexed through the offsets in

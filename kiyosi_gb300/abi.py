@@ -57,6 +57,8 @@ C_CHECK_STEPS = 1024
 C_AVERAGE_LEAD = 2048
 C_AVERAGE_CONTROL = 4096
 C_DOUBLE = 8192
+C_OUTPUT_DELTA = 16384
+C_OUTPUT_GAMMA = 32768
 
 UNCERTAINTY_NAMES = {
     0: "available",
@@ -125,7 +127,8 @@ class Contract(C.Structure):
                 ("avg_rest", _D), ("avg_log_rest", _D), ("avg_baseline", _D),
                 ("control_log_strike", _D), ("control_log_asset_scale", _D),
                 ("control_first_weight", _D), ("control_mean", _D), ("band", _D),
-                ("band_initial", _D)]
+                ("band_initial", _D), ("greek_log_spot", _D), ("greek_log_width", _D),
+                ("greek_log_amount", _D), ("greek_log_base_width", _D), ("greek_log_weight", _D)]
 
 
 class Book(C.Structure):

@@ -178,3 +178,16 @@ def european_price(option_type_sign: float, strike: float, expiry: float, ctx: P
     return lognormal_price(spot, strike, log_ratio(spot, strike) + (dividend_log - risk_log),
                            dividend_log, risk_log, model.volatility, math.sqrt(expiry),
                            option_type_sign)
+
+
+def european_delta_gamma(sign: float, strike: float, expiry: float, ctx: PricingContext):
+    """Black-Scholes delta and gamma of a European option with flat rates (the analytic
+    Greeks a settled knock-in barrier reports, engines/monte_carlo/barrier.rs:199-206)."""
+    model = ctx.model
+    spot, sigma = ctx.spot, model.volatility
+    width = sigma * math.sqrt(expiry)
+    d1 = (log_ratio(spot, strike) + (model.rate - model.dividend) * expiry) / width + 0.5 * width
+    carry = math.exp(-model.dividend * expiry)
+    delta = sign * carry * normal_cdf(sign * d1)
+    gamma = carry * math.exp(-0.5 * d1 * d1) / math.sqrt(2.0 * math.pi) / (spot * width)
+    return {"delta": delta, "gamma": gamma}

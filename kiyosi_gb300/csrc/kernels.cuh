@@ -151,6 +151,11 @@ __global__ void compile_contracts_kernel(const kgpu_contract* in, int n, Contrac
     o.control_mean = Real(c.control_mean);
     o.band = Real(c.band);
     o.band_initial = Real(c.band_initial);
+    o.greek_log_spot = Real(c.greek_log_spot);
+    o.greek_log_width = Real(c.greek_log_width);
+    o.greek_log_amount = Real(c.greek_log_amount);
+    o.greek_log_base_width = Real(c.greek_log_base_width);
+    o.greek_log_weight = Real(c.greek_log_weight);
     out[i] = o;
 }
 

@@ -88,6 +88,7 @@ struct ContractT {
     Real avg_rest, avg_log_rest, avg_baseline;
     Real control_log_strike, control_log_asset_scale, control_first_weight, control_mean;
     Real band, band_initial;
+    Real greek_log_spot, greek_log_width, greek_log_amount, greek_log_base_width, greek_log_weight;
 };
 
 // Device view of the book in the kernel's precision.
@@ -402,12 +403,44 @@ __device__ __forceinline__ Real european_value(const ContractT<Real>& c, Real z)
     return -xexpm1(-distance) * xexp(xfma(c.diffusion, z, -c.half_variance));
 }
 
+// Which sample a path reports: 0 its payoff, 1 its delta sample, 2 its gamma sample.
+__device__ __forceinline__ int output_of(int flags) {
+    return (flags & KGPU_C_OUTPUT_DELTA) ? 1 : ((flags & KGPU_C_OUTPUT_GAMMA) ? 2 : 0);
+}
+
+// The barrier sampler's likelihood-ratio delta and gamma (barrier.rs:455-470): `z` is
+// the first normal and `width` its standard deviation; `first` and `second` are the
+// survival weight's spot derivatives (zero for scheduled monitoring).
+template <class Real>
+__device__ __forceinline__ Real likelihood_greek(int output, Real value, Real first, Real second, Real z, Real width,
+                                                 Real spot) {
+    const Real score = z / width;
+    if (output == 1) return (value * score + first) / spot;
+    const Real second_score = ((z * z - Real(1)) / width - z) / width;
+    return ((value * second_score + first * (Real(2) * score - Real(1)) + second) / spot) / spot;
+}
+
+// MonteCarloDigitalEngine's native delta and gamma samples (digital.rs:116-140).
+template <class Real>
+__device__ __noinline__ Real digital_greek(const ContractT<Real>& c, Real z, Real exponent) {
+    const Real log_payoff = c.greek_log_amount + exponent;
+    if (output_of(c.flags) == 1) {
+        if (z == Real(0)) return Real(0);
+        return copysign(xexp(log_payoff + xlog(xabs(z)) - c.greek_log_spot - c.greek_log_width), z);
+    }
+    const Real score = xfma(-c.diffusion, z, z * z - Real(1));
+    if (score == Real(0)) return Real(0);
+    return copysign(xexp(log_payoff + xlog(xabs(score)) - Real(2) * c.greek_log_spot - Real(2) * c.greek_log_width),
+                    score);
+}
+
 template <class Real>
 __device__ __forceinline__ Real digital_value(const ContractT<Real>& c, Real z) {
     Real distance = c.moneyness + z;
     bool call = c.sign > Real(0);
     if (!(call ? distance > Real(0) : distance < Real(0))) return Real(0);
     Real exponent = c.log_scale + ((c.flags & KGPU_C_ASSET_DIGITAL) ? c.diffusion * z : Real(0));
+    if (c.flags & (KGPU_C_OUTPUT_DELTA | KGPU_C_OUTPUT_GAMMA)) return digital_greek(c, z, exponent);
     return c.strike * xexp(exponent);
 }
 
@@ -454,8 +487,17 @@ __device__ __forceinline__ Real barrier_value(const ContractT<Real>& c, Real z) 
     const Real slope = live ? Real(2) * (xabs(to_barrier) / c.diffusion) / c.diffusion : Real(0);
     const Real exponent = -c.barrier_distance * slope;
     const Real survival = live ? xlog(-xexpm1(exponent)) : -xinf(Real(0));
-    return weighted_amount(intrinsic, c.log_discount + (in ? exponent : survival)) +
-           weighted_amount(c.rebate, c.log_discount + (in ? survival : exponent));
+    const Real value = weighted_amount(intrinsic, c.log_discount + (in ? exponent : survival)) +
+                       weighted_amount(c.rebate, c.log_discount + (in ? survival : exponent));
+    const int output = output_of(c.flags);
+    if (output == 0) return value;
+    Real first = Real(0), second = Real(0);
+    if (slope > Real(0) && exponent > -xinf(Real(0))) {
+        const Real difference = (in ? Real(-1) : Real(1)) * (intrinsic - c.rebate);
+        first = weighted_amount(up ? -difference : difference, c.log_discount + (exponent + xlog(slope)));
+        if (output == 2) second = weighted_amount(-difference, c.log_discount + (exponent + Real(2) * xlog(slope)));
+    }
+    return likelihood_greek(output, value, first, second, z, c.diffusion, c.spot);
 }
 
 __device__ __forceinline__ double xerfc(double x) { return erfc(x); }
@@ -524,22 +566,32 @@ __device__ __forceinline__ Real positive_difference_of(Real a, Real b) {
     return difference > Real(0) ? xexp(a + xlog(difference)) : Real(0);
 }
 
-// ArithmeticParameters::geometric_values, price only (asian.rs:1062-1085).
+constexpr double kHalfLog2Pi = 0.9189385332046727;  // ln(2 pi) / 2
+
+// ArithmeticParameters::geometric_values (asian.rs:1062-1085): the geometric control's
+// price, delta or gamma (`output` 0, 1, 2).
 template <class Real>
-__device__ Real average_geometric_price(const ContractT<Real>& c, Real log_forward, Real log_strike, Real width) {
+__device__ Real average_geometric_values(const ContractT<Real>& c, Real log_forward, Real log_strike, Real width,
+                                         int output) {
     const Real d1 = (log_forward - log_strike) / width + Real(0.5) * width;
     const Real d2 = d1 - width;
     const Real log_asset = log_forward + c.log_discount + log_normal_cdf_of(c.sign * d1);
+    if (output == 1) return c.sign * xexp(log_asset - c.avg_log_spot);
+    if (output == 2)
+        return xexp(log_forward + c.log_discount - Real(2) * c.avg_log_spot - xlog(width) - Real(0.5) * d1 * d1 -
+                    Real(kHalfLog2Pi));
     const Real log_cash = log_strike + c.log_discount + log_normal_cdf_of(c.sign * d2);
     return c.sign > Real(0) ? positive_difference_of(log_asset, log_cash) : positive_difference_of(log_cash, log_asset);
 }
 
-// ArithmeticParameters::arithmetic, price only, without realized history, for widths of
-// at least 1e-5 (asian.rs:1087-1178): the first interval integrated in closed form given
-// the path's other increments, minus the geometric control on the same path.
+// ArithmeticParameters::arithmetic without realized history, for widths of at least
+// 1e-5 (asian.rs:1087-1178): the first interval integrated in closed form given the
+// path's other increments, minus the geometric control on the same path.  Returns the
+// price, or the native delta or gamma sample (KGPU_C_OUTPUT_*).
 template <class Real>
 __device__ __noinline__ Real average_arithmetic_value(const ContractT<Real>& c, Real lead_growth, Real log_sum,
                                                       Real relative_sum, Real geometric_growth) {
+    const int output = output_of(c.flags);
     const bool summed = log_sum == -xinf(Real(0));
     const Real log_rest = summed ? c.avg_log_rest + xlog1p(relative_sum / c.avg_rest) : log_sum;
     const Real log_q = ((c.avg_log_scale + lead_growth) + log_rest) + c.avg_interval_forward;
@@ -551,13 +603,16 @@ __device__ __noinline__ Real average_arithmetic_value(const ContractT<Real>& c, 
         const Real log_forward = (((c.control_log_asset_scale + lead_growth) + geometric_growth) +
                                   c.control_first_weight * c.avg_drift) +
                                  Real(0.5) * width * width;
-        control = average_geometric_price(c, log_forward, c.control_log_strike, width);
+        control = average_geometric_values(c, log_forward, c.control_log_strike, width, output);
     }
     const Real log_strike = c.avg_log_strike;
+    const Real ld = c.log_discount;
     if (log_accrued >= log_strike) {
         if (c.sign < Real(0)) return Real(0) - control;
-        const Real cash = positive_difference_of(log_accrued + c.log_discount, log_strike + c.log_discount);
-        return (xexp(log_q + c.log_discount) + cash) - control;
+        if (output == 1) return (xexp(log_q + ld - c.avg_log_spot) + xexp(log_c + ld - c.avg_log_spot)) - control;
+        if (output == 2) return Real(0) - control;
+        const Real cash = positive_difference_of(log_accrued + ld, log_strike + ld);
+        return (xexp(log_q + ld) + cash) - control;
     }
     const Real log_b = log_strike + xlog(-xexpm1(log_accrued - log_strike));
     Real forward = log_q - log_b;
@@ -571,15 +626,24 @@ __device__ __noinline__ Real average_arithmetic_value(const ContractT<Real>& c, 
     }
     const Real center = forward / c.avg_width;
     const Real d1 = center + Real(0.5) * c.avg_width, d2 = center - Real(0.5) * c.avg_width;
-    const Real log_asset = log_q + c.log_discount + log_normal_cdf_of(c.sign * d1);
-    const Real log_cash = log_b + c.log_discount + log_normal_cdf_of(c.sign * d2);
+    if (output == 1)
+        return c.sign * (xexp(log_c + ld - c.avg_log_spot + log_normal_cdf_of(c.sign * d2)) +
+                         xexp(log_q + ld - c.avg_log_spot + log_normal_cdf_of(c.sign * d1))) -
+               control;
+    if (output == 2)
+        return xexp(ld + Real(2) * log_strike - Real(2) * c.avg_log_spot - log_b - c.greek_log_width -
+                    Real(0.5) * d2 * d2 - Real(kHalfLog2Pi)) -
+               control;
+    const Real log_asset = log_q + ld + log_normal_cdf_of(c.sign * d1);
+    const Real log_cash = log_b + ld + log_normal_cdf_of(c.sign * d2);
     const Real price = c.sign > Real(0) ? positive_difference_of(log_asset, log_cash)
                                         : positive_difference_of(log_cash, log_asset);
     return price - control;
 }
 
-// GeometricParameters::geometric, price only (asian.rs:740-784): moneyness holds the
-// initial moneyness plus the drift, diffusion the width, log_scale the log width.
+// GeometricParameters::geometric (asian.rs:740-784): moneyness holds the initial
+// moneyness plus the drift, diffusion the width, log_scale the log width.  Returns the
+// price, or the native delta or gamma sample.
 template <class Real>
 __device__ __noinline__ Real average_geometric_value(const ContractT<Real>& c, Real normal) {
     const Real distance = c.moneyness + c.diffusion * normal;
@@ -587,6 +651,16 @@ __device__ __noinline__ Real average_geometric_value(const ContractT<Real>& c, R
     const Real standardized = center + normal;
     if (c.sign * standardized <= Real(0)) return Real(0);
     const Real log_strike = c.avg_log_strike;
+    const int output = output_of(c.flags);
+    if (output != 0) {
+        const Real log_asset = log_strike + distance + c.log_discount + c.greek_log_weight;
+        if (output == 1) return c.sign * xexp(log_asset - c.greek_log_spot);
+        const Real numerator = normal - xexp(c.greek_log_base_width);
+        if (numerator == Real(0)) return Real(0);
+        return c.sign * copysign(xexp(log_asset - Real(2) * c.greek_log_spot + xlog(xabs(numerator)) -
+                                      c.greek_log_base_width),
+                                 numerator);
+    }
     Real log_payoff;
     if (xabs(distance) < Real(1e-5) && xabs(standardized) < xinf(Real(0))) {
         log_payoff = log_strike + c.log_scale + xlog(xabs(standardized)) +
@@ -599,38 +673,72 @@ __device__ __noinline__ Real average_geometric_value(const ContractT<Real>& c, R
     return xexp(log_payoff + c.log_discount);
 }
 
-// survival (double_barrier.rs:6-112), value only: the probability that a Brownian path
-// from `initial` to `terminal` (log distances above the lower barrier) over a standard
-// deviation `deviation` stays inside (0, band).  Small variances sum the method of
-// images, large ones the spectral (sine) series.  NaN when the series does not converge
-// or leaves [0, 1] (a computation failure).
+// One image term's contribution to the survival derivatives (double_barrier.rs:37-65).
 template <class Real>
-__device__ __noinline__ Real double_survival(Real initial, Real terminal, Real band, Real deviation) {
+__device__ __forceinline__ void image_derivatives(Real exponent, Real weight, Real numerator, Real sign,
+                                                  Real inverse_variance, Real ratio, Real* d1, Real* d2) {
+    if (numerator == Real(0)) return;
+    const Real slope = numerator * inverse_variance;
+    const Real first = weight * slope;
+    const Real second = first * slope;
+    if (xnormal(weight) && xnormal(first) && xnormal(second)) {
+        *d1 += sign * first;
+        *d2 += sign * second;
+    } else {
+        // Preserve derivatives when variance or weight underflows.
+        const Real log_slope = xlog(xabs(numerator)) - Real(2) * xlog(ratio);
+        *d1 += sign * copysign(xexp(exponent + log_slope), numerator);
+        *d2 += sign * xexp(exponent + Real(2) * log_slope);
+    }
+}
+
+// survival (double_barrier.rs:6-112): the probability that a Brownian path from
+// `initial` to `terminal` (log distances above the lower barrier) over a standard
+// deviation `deviation` stays inside (0, band), and with `derivatives` its first and
+// second derivatives in the initial log spot.  Small variances sum the method of images,
+// large ones the spectral (sine) series.  NaN when the series does not converge or
+// leaves [0, 1] (a computation failure).
+template <class Real>
+__device__ __noinline__ Real double_survival(Real initial, Real terminal, Real band, Real deviation, bool derivatives,
+                                             Real* d1, Real* d2) {
+    *d1 = Real(0);
+    *d2 = Real(0);
     if (terminal <= Real(0) || terminal >= band) return Real(0);
     Real x = initial / band, y = terminal / band;
     const Real ratio = deviation / band;
     const Real variance = ratio * ratio;
     if (variance == Real(0)) return Real(1);
     if (!(variance > Real(0) && variance < xinf(Real(0)))) return xnan(Real(0));
-    if (x + y > Real(1)) {
+    const bool reflected = x + y > Real(1);
+    if (reflected) {
         x = Real(1) - x;
         y = Real(1) - y;
     }
     Real sum = Real(0);
     bool converged = false;
     if (variance < Real(0.25)) {
+        const Real inverse_variance = xnormal(variance) ? Real(1) / variance : xinf(Real(0));
         // The k = 0 terms: the direct one is 1, the reflected one is folded into expm1.
         sum = -xexpm1(Real(-2) * (x / ratio) * (y / ratio));
+        if (derivatives) {
+            const Real e0 = Real(-2) * ((x + Real(0)) / ratio) * ((y + Real(0)) / ratio);
+            image_derivatives(e0, xexp(e0), Real(-2) * (y + Real(0)), Real(-1), inverse_variance, ratio, d1, d2);
+        }
         for (int n = 1; n <= 64; ++n) {
             const Real k = Real(n);
-            const Real w1 = xexp(Real(-2) * (k / ratio) * ((y - x + k) / ratio));
-            const Real w2 = xexp(Real(-2) * ((x + k) / ratio) * ((y + k) / ratio));
-            const Real w3 = xexp(Real(-2) * (-k / ratio) * ((y - x - k) / ratio));
-            const Real w4 = xexp(Real(-2) * ((x - k) / ratio) * ((y - k) / ratio));
+            const Real e1 = Real(-2) * (k / ratio) * ((y - x + k) / ratio);
+            const Real e2 = Real(-2) * ((x + k) / ratio) * ((y + k) / ratio);
+            const Real e3 = Real(-2) * (-k / ratio) * ((y - x - k) / ratio);
+            const Real e4 = Real(-2) * ((x - k) / ratio) * ((y - k) / ratio);
+            const Real w1 = xexp(e1), w2 = xexp(e2), w3 = xexp(e3), w4 = xexp(e4);
             sum += w1;
+            if (derivatives) image_derivatives(e1, w1, Real(2) * k, Real(1), inverse_variance, ratio, d1, d2);
             sum -= w2;
+            if (derivatives) image_derivatives(e2, w2, Real(-2) * (y + k), Real(-1), inverse_variance, ratio, d1, d2);
             sum += w3;
+            if (derivatives) image_derivatives(e3, w3, Real(2) * -k, Real(1), inverse_variance, ratio, d1, d2);
             sum -= w4;
+            if (derivatives) image_derivatives(e4, w4, Real(-2) * (y - k), Real(-1), inverse_variance, ratio, d1, d2);
             if (n >= 2 && ((w1 + w2) + w3) + w4 < Real(1e-18)) {
                 converged = true;
                 break;
@@ -646,6 +754,12 @@ __device__ __noinline__ Real double_survival(Real initial, Real terminal, Real b
             const Real sy = xsin(frequency * y);
             const Real product = xsin(frequency * x) * sy;
             sum += weight * product;
+            if (derivatives) {
+                const Real first = frequency * cos(frequency * x) * sy;
+                const Real score = -distance / variance;
+                *d1 += weight * (first + score * product);
+                *d2 += weight * (Real(2) * score * first + (score * score + Real(1) / variance - frequency * frequency) * product);
+            }
             if (n >= 4 && exponent + Real(4) * xlog(frequency) < Real(-40)) {
                 converged = true;
                 break;
@@ -653,6 +767,10 @@ __device__ __noinline__ Real double_survival(Real initial, Real terminal, Real b
         }
     }
     if (!converged || !(sum >= Real(-1e-13) && sum <= Real(1) + Real(1e-13))) return xnan(Real(0));
+    if (derivatives) {
+        *d1 = (reflected ? -*d1 : *d1) / band;
+        *d2 = (*d2 / band) / band;
+    }
     return sum < Real(0) ? Real(0) : (sum > Real(1) ? Real(1) : sum);
 }
 
@@ -666,12 +784,25 @@ __device__ __noinline__ Real double_barrier_value(const ContractT<Real>& c, Real
                                                    : weighted_amount(c.spot, terminal) - c.strike;
     Real intrinsic = c.sign * payoff;
     intrinsic = intrinsic > Real(0) ? intrinsic : Real(0);
-    const Real survival = double_survival(c.band_initial, c.barrier_moneyness + noise, c.band, c.diffusion);
+    const int output = output_of(c.flags);
+    Real ds1, ds2;
+    const Real survival =
+        double_survival(c.band_initial, c.barrier_moneyness + noise, c.band, c.diffusion, output != 0, &ds1, &ds2);
     const bool in = (c.flags & KGPU_C_BARRIER_IN) != 0;
     const Real rebate = (!in && (c.flags & KGPU_C_REBATE_AT_HIT)) ? Real(0) : c.rebate;
     const Real log_survival = xlog(survival), log_hit = xlog1p(-survival);
-    return weighted_amount(intrinsic, c.log_discount + (in ? log_hit : log_survival)) +
-           weighted_amount(rebate, c.log_discount + (in ? log_survival : log_hit));
+    const Real value = weighted_amount(intrinsic, c.log_discount + (in ? log_hit : log_survival)) +
+                       weighted_amount(rebate, c.log_discount + (in ? log_survival : log_hit));
+    if (output == 0) return value;
+    // derivative(weight) of barrier.rs:366-372
+    const Real difference = (in ? Real(-1) : Real(1)) * (intrinsic - rebate);
+    const Real ad = xabs(difference), sd = difference < Real(0) ? Real(-1) : Real(1);
+    const Real first =
+        weighted_amount(ad * (sd * (ds1 < Real(0) ? Real(-1) : Real(1))), c.log_discount + xlog(xabs(ds1)));
+    const Real second = output == 2 ? weighted_amount(ad * (sd * (ds2 < Real(0) ? Real(-1) : Real(1))),
+                                                      c.log_discount + xlog(xabs(ds2)))
+                                    : Real(0);
+    return likelihood_greek(output, value, first, second, z, c.diffusion, c.spot);
 }
 
 template <class Real>
@@ -819,9 +950,18 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         // than 8 dates left is priced analytically from its hit.
         const int i = s.i;
         const StepT<Real> st = p.steps[i];
-        s.lr = xfma(st.diffusion, n.normal(), s.lr);
+        const Real z = n.normal();
+        if (i == 0) s.v = z;  // the first normal carries the likelihood-ratio score
+        s.lr = xfma(st.diffusion, z, s.lr);
         s.i = i + 1;
         s.executed += 1;
+        // Native delta / gamma samples: the first normal's score (barrier.rs:455-470).
+        const auto finish = [&]() {
+            const int output = output_of(c.flags);
+            if (output != 0)
+                value = likelihood_greek(output, value, Real(0), Real(0), s.v, p.steps[0].diffusion, c.spot);
+            return true;
+        };
         if (c.flags & KGPU_C_CHECK_STEPS) {
             const Real spot_now = weighted_amount(c.spot, st.drift + s.lr);
             if (!(spot_now > Real(0) && spot_now < xinf(Real(0)))) {
@@ -840,11 +980,11 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
                 const Real asset = weighted_amount(c.spot, st.drift + s.lr);
                 value = lognormal_price_of(asset, c.strike, c.moneyness + s.lr + c.half_variance * e.coupon_barrier,
                                            e.payment[1], c.log_discount, c.volatility, e.payment[2], c.sign);
-                return true;
+                return finish();
             }
             if (!in) {
                 value = weighted_amount(c.rebate, (c.flags & KGPU_C_REBATE_AT_HIT) ? e.payment[0] : c.log_discount);
-                return true;
+                return finish();
             }
         }
         if (s.i < c.step_count) return false;
@@ -854,7 +994,7 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         Real intrinsic = c.sign * payoff_value;
         intrinsic = intrinsic > Real(0) ? intrinsic : Real(0);
         value = weighted_amount(s.knocked_in == in ? intrinsic : c.rebate, c.log_discount);
-        return true;
+        return finish();
     }
     // Grid-stepping families.
     const int i = s.i;

@@ -14,7 +14,7 @@ A builder returns either a Known value (no sampling) or a ContractPlan; BookBuil
 packs plans into one kgpu_book.
 """
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 from typing import List, Optional
 
 import numpy as np
@@ -47,6 +47,8 @@ class ContractPlan:
     events: np.ndarray = field(default_factory=lambda: np.zeros(0, EVENT_DTYPE))
     intervals: np.ndarray = field(default_factory=lambda: np.zeros(0, INTERVAL_DTYPE))
     daily: Optional[np.ndarray] = None   # DAILY_DTYPE[step_count] when bridged
+    # exact [price, delta, gamma] of an arithmetic average's geometric control
+    control_expected: Optional[tuple] = None
 
     @property
     def record(self):
@@ -160,6 +162,10 @@ def digital(option: DigitalOption, ctx: PricingContext):
     c["moneyness"] = d2
     c["log_scale"] = drift
     c["step_count"] = 1
+    # native delta / gamma samples (digital.rs:110-140)
+    c["greek_log_spot"] = math.log(ctx.spot)
+    c["greek_log_width"] = math.log(sigma) + math.log(root)
+    c["greek_log_amount"] = math.log(amount)
     steps = np.zeros(1, STEP_DTYPE)
     steps[0] = (drift, width, 0.0, math.exp(-rate * time))
     return ContractPlan(c, steps, np.zeros(1, np.uint8))
@@ -340,15 +346,21 @@ def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_v
     return ContractPlan(c, steps, np.zeros(n, np.uint8), events)
 
 
-def _geometric_control_price(sign, log_discount, log_forward, log_strike, width):
-    """ArithmeticParameters::geometric_values, price only (asian.rs:1062-1085)."""
+def _geometric_control_values(sign, log_discount, log_spot, log_forward, log_strike, width):
+    """ArithmeticParameters::geometric_values (asian.rs:1062-1085): the control's exact
+    [price, delta, gamma]."""
     d1 = (log_forward - log_strike) / width + 0.5 * width
     d2 = d1 - width
     log_asset = log_forward + log_discount + analytic.log_normal_cdf(sign * d1)
     log_cash = log_strike + log_discount + analytic.log_normal_cdf(sign * d2)
     if sign > 0.0:
-        return analytic.positive_difference(log_asset, log_cash)
-    return analytic.positive_difference(log_cash, log_asset)
+        price = analytic.positive_difference(log_asset, log_cash)
+    else:
+        price = analytic.positive_difference(log_cash, log_asset)
+    delta = sign * math.exp(log_asset - log_spot)
+    gamma = math.exp(log_forward + log_discount - 2.0 * log_spot - math.log(width) - 0.5 * d1 * d1
+                     - 0.5 * math.log(2.0 * math.pi))
+    return (price, delta, gamma)
 
 
 def average(option, ctx: PricingContext, step_count: int = 50, control: bool = True):
@@ -408,6 +420,10 @@ def average(option, ctx: PricingContext, step_count: int = 50, control: bool = T
         c["log_discount"] = log_discount
         c["spot"] = spot
         c["step_count"] = 1
+        # native delta / gamma samples (GeometricParameters::geometric)
+        c["greek_log_spot"] = math.log(spot)
+        c["greek_log_weight"] = math.log(weight)
+        c["greek_log_base_width"] = math.log(sigma) + 0.5 * math.log(variance_time)
         return ContractPlan(c, np.zeros(1, STEP_DTYPE), np.zeros(1, np.uint8))
     n = int(step_count)
     dt = future / float(n)
@@ -447,7 +463,9 @@ def average(option, ctx: PricingContext, step_count: int = 50, control: bool = T
     c["avg_log_rest"] = math.log(rest)
     # prior_weight ((realized - strike) / spot) + weight ((spot - strike) / spot), no history
     c["avg_baseline"] = 0.0 * ((0.0 - strike) / spot) + weight * ((spot - strike) / spot)
+    c["greek_log_width"] = math.log(sigma) + 0.5 * math.log(dt)  # ArithmeticParameters::log_width
     c["step_count"] = dims
+    expected = None
     flags = abi.C_AVERAGE_LEAD if has_lead else 0
     if control:
         # geometric_control (asian.rs:1016-1060)
@@ -468,10 +486,26 @@ def average(option, ctx: PricingContext, step_count: int = 50, control: bool = T
                 c["control_log_strike"] = log_strike
                 c["control_log_asset_scale"] = log_asset_scale
                 c["control_first_weight"] = first_weight
-                c["control_mean"] = _geometric_control_price(c_sign, log_discount, log_forward,
-                                                             log_strike, control_width)
+                expected = _geometric_control_values(c_sign, log_discount, log_spot, log_forward,
+                                                     log_strike, control_width)
+                c["control_mean"] = expected[0]
     c["flags"] = flags
-    return ContractPlan(c, np.zeros(dims, STEP_DTYPE), np.zeros(dims, np.uint8))
+    return ContractPlan(c, np.zeros(dims, STEP_DTYPE), np.zeros(dims, np.uint8),
+                        control_expected=expected)
+
+
+def greek_output(plan, output: str):
+    """A copy of `plan` whose paths report their native delta or gamma sample instead
+    of the payoff (digital, barrier and average payoffs); an arithmetic average's control
+    mean becomes the control's exact delta or gamma."""
+    if isinstance(plan, Known):
+        return plan
+    index = {"delta": 1, "gamma": 2}[output]
+    c = plan.contract.copy()
+    c["flags"] = c["flags"] | (abi.C_OUTPUT_DELTA if index == 1 else abi.C_OUTPUT_GAMMA)
+    if plan.control_expected is not None:
+        c["control_mean"] = plan.control_expected[index]
+    return replace(plan, contract=c)
 
 
 def path_vanilla(option: EuropeanOption, ctx: PricingContext, step_count: int):

@@ -171,6 +171,15 @@ class _MonteCarloEngine:
         e = self.price_with_statistics(contract, ctx)
         return e.price, e.seed
 
+    def _scenario_prices(self, contract, contexts):
+        """Prices `contract` in each context with this engine's seed.  Engines with a
+        per-contract plan price every context in one book (one launch, shared random
+        numbers); the others price them one by one."""
+        plan = getattr(self, "_plan", None)
+        if plan is None:
+            return [self.price(contract, c) for c in contexts]
+        return [e.price for e in self._run(contexts[0], [plan(contract, c) for c in contexts])]
+
 
 class MonteCarloVanillaEngine(_MonteCarloEngine):
     """European (exact terminal sampling) and American (LSMC) vanilla options.
@@ -215,6 +224,15 @@ class MonteCarloVanillaEngine(_MonteCarloEngine):
             from .lsmc import price_american
             return price_american(self, option, ctx)
         return self._run(ctx, [self._plan(option, ctx)])[0]
+
+    def price_with_greeks(self, option, ctx: PricingContext, request, shifts=None):
+        """European Greeks by bump-and-reprice with a pinned seed, every scenario in one
+        launch (monte_carlo.rs:1334-1409, european_greek_prices).  American options are
+        not supported."""
+        if isinstance(option, AmericanOption):
+            raise UnsupportedOperationError("American Monte Carlo Greeks are not built")
+        from .greeks import numerical_greeks
+        return numerical_greeks(self, option, ctx, request, shifts)
 
     def price_strikes(self, option, ctx: PricingContext, strikes: Sequence[float]):
         opts = [replace(option, strike=float(k)) for k in strikes]
@@ -264,6 +282,30 @@ class MonteCarloAsianEngine(_MonteCarloEngine):
             return self._average([option], ctx)[0]
         return self._run(ctx, [plans.asian(option, ctx, self.step_count)])[0]
 
+    def price_with_greeks(self, option, ctx: PricingContext, request, shifts=None):
+        """Native delta and gamma from the price's normals (asian.rs:740-784, 1087-1178,
+        with the geometric control's exact delta and gamma added back)."""
+        if not isinstance(option, AveragePriceOption):
+            raise UnsupportedOperationError("Greeks of discrete-fixing Asian options are not built")
+        from .greeks import native_greeks
+        steps = self.step_count or 50
+
+        def plan_for(option, ctx):
+            return plans.average(option, ctx, steps)
+
+        def without_control(option, ctx):
+            return plans.average(option, ctx, steps, control=False)
+
+        def discontinuity(radius):
+            return option.expiry == 0.0 and ctx.spot - radius <= option.strike <= ctx.spot + radius
+        return native_greeks(self, option, ctx, request, plan_for, shifts, discontinuity=discontinuity,
+                             redo_without_control=without_control)
+
+    def _scenario_prices(self, option, contexts):
+        if isinstance(option, AveragePriceOption):
+            return [self._average([option], c)[0].price for c in contexts]
+        return super()._scenario_prices(option, contexts)
+
     def price_strikes(self, option: AveragePriceOption, ctx: PricingContext,
                       strikes: Sequence[float]):
         """Prices across strikes on common paths: every strike replays its scalar price
@@ -282,8 +324,18 @@ class MonteCarloAsianEngine(_MonteCarloEngine):
 class MonteCarloAutocallableEngine(_MonteCarloEngine):
     """Snowball / Phoenix notes (autocallable.rs), singly or as a batched book."""
 
+    def _plan(self, note: AutocallableNote, ctx: PricingContext):
+        return plans.autocallable(note, ctx)
+
     def price_with_statistics(self, note: AutocallableNote, ctx: PricingContext):
         return self._run(ctx, [plans.autocallable(note, ctx)])[0]
+
+    def price_with_greeks(self, note: AutocallableNote, ctx: PricingContext, request, shifts=None):
+        """Numerical Greeks with a pinned seed (autocallable.rs:174-283: the reference
+        drives the base and bumped notes with shared paths); all scenarios in one
+        launch."""
+        from .greeks import numerical_greeks
+        return numerical_greeks(self, note, ctx, request, shifts)
 
     def price_many(self, notes: Sequence[AutocallableNote], ctx: PricingContext,
                    path_counts: Optional[Sequence[int]] = None):
@@ -296,13 +348,30 @@ class MonteCarloAutocallableEngine(_MonteCarloEngine):
 
 
 class MonteCarloAccumulatorEngine(_MonteCarloEngine):
+    def _plan(self, option: Accumulator, ctx: PricingContext):
+        return plans.accumulator(option, ctx)
+
     def price_with_statistics(self, option: Accumulator, ctx: PricingContext):
         return self._run(ctx, [plans.accumulator(option, ctx)])[0]
 
+    def price_with_greeks(self, option: Accumulator, ctx: PricingContext, request, shifts=None):
+        from .greeks import numerical_greeks
+        return numerical_greeks(self, option, ctx, request, shifts)
+
 
 class MonteCarloDigitalEngine(_MonteCarloEngine):
+    def _plan(self, option: DigitalOption, ctx: PricingContext):
+        return plans.digital(option, ctx)
+
     def price_with_statistics(self, option: DigitalOption, ctx: PricingContext):
         return self._run(ctx, [plans.digital(option, ctx)])[0]
+
+    def price_with_greeks(self, option: DigitalOption, ctx: PricingContext, request, shifts=None):
+        """Delta and gamma as the means of the likelihood-ratio samples of the price's
+        normals (digital.rs:110-150), priced with the price in one book."""
+        from .greeks import native_greeks, vanilla_discontinuity
+        return native_greeks(self, option, ctx, request, plans.digital, shifts,
+                             discontinuity=vanilla_discontinuity(option, ctx))
 
 
 class MonteCarloBarrierEngine(_MonteCarloEngine):
@@ -312,8 +381,29 @@ class MonteCarloBarrierEngine(_MonteCarloEngine):
     stop at the hit with their rebate (at expiry or at the hit), and dense knock-ins
     price the vanilla analytically from the hit."""
 
+    def _plan(self, option, ctx: PricingContext):
+        return plans.barrier(option, ctx)
+
     def price_with_statistics(self, option: BarrierOption, ctx: PricingContext):
         return self._run(ctx, [plans.barrier(option, ctx)])[0]
+
+    def price_with_greeks(self, option, ctx: PricingContext, request, shifts=None):
+        """Likelihood-ratio delta and gamma from the price's normals (barrier.rs:180-214,
+        455-470): continuous barriers add the survival weight's spot derivatives.  They
+        are absent when a spot stencil reaches a barrier monitored now; settled knock-ins
+        report the vanilla's analytic delta and gamma, settled knock-outs zero."""
+        from . import analytic
+        from .greeks import NumericalShiftSettings, barrier_discontinuity, native_greeks
+
+        def settled(option, ctx):
+            if option.is_knock_in:
+                return analytic.european_delta_gamma(option.sign, option.strike, option.expiry, ctx)
+            return {"delta": 0.0, "gamma": 0.0}
+
+        def discontinuity(radius):
+            return option.expiry == 0.0 or barrier_discontinuity(option, ctx, radius)
+        return native_greeks(self, option, ctx, request, plans.barrier, shifts,
+                             discontinuity=discontinuity, resolved_greeks=settled)
 
     def price_strikes(self, option: BarrierOption, ctx: PricingContext, strikes: Sequence[float]):
         opts = [replace(option, strike=float(k)) for k in strikes]

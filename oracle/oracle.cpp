@@ -272,14 +272,42 @@ static double european_payoff(const kgpu_contract* c, double z, Failure& f) {
     return payoff;
 }
 
-// Digital terminal payoff (digital.rs:111-121): moneyness = d2, diffusion = width,
-// log_scale = exponent offset, strike = paid amount.
+// The sample a path reports: its payoff, or its native delta or gamma sample.
+static int output_of(const kgpu_contract* c) {
+    return (c->flags & KGPU_C_OUTPUT_DELTA) ? 1 : ((c->flags & KGPU_C_OUTPUT_GAMMA) ? 2 : 0);
+}
+
+// Digital terminal payoff (digital.rs:111-140): moneyness = d2, diffusion = width,
+// log_scale = exponent offset, strike = paid amount; with the likelihood-ratio delta
+// and gamma samples of the same normal.
 static double digital_payoff(const kgpu_contract* c, double z) {
     double distance = c->moneyness + z;
     bool call = c->sign > 0.0;
     if (!(call ? distance > 0.0 : distance < 0.0)) return 0.0;
     double exponent = c->log_scale + ((c->flags & KGPU_C_ASSET_DIGITAL) ? c->diffusion * z : 0.0);
-    return discounted_product(c->strike, 1.0, exponent);
+    const int output = output_of(c);
+    if (output == 0) return discounted_product(c->strike, 1.0, exponent);
+    const double log_payoff = c->greek_log_amount + exponent;
+    if (output == 1)
+        return z != 0.0 ? std::copysign(std::exp(log_payoff + std::log(std::fabs(z)) - c->greek_log_spot -
+                                                 c->greek_log_width),
+                                        z)
+                        : 0.0;
+    const double score = std::fma(-c->diffusion, z, z * z - 1.0);
+    return score != 0.0 ? std::copysign(std::exp(log_payoff + std::log(std::fabs(score)) - 2.0 * c->greek_log_spot -
+                                                 2.0 * c->greek_log_width),
+                                        score)
+                        : 0.0;
+}
+
+// The barrier sampler's delta and gamma from the first normal's score plus the survival
+// weight's spot derivatives (barrier.rs:455-470).
+static double barrier_greek(int output, double value, double first, double second, double z, double width,
+                            double spot) {
+    const double score = z / width;
+    if (output == 1) return (value * score + first) / spot;
+    const double second_score = ((z * z - 1.0) / width - z) / width;
+    return ((value * second_score + first * (2.0 * score - 1.0) + second) / spot) / spot;
 }
 
 // The `weighted` helper of the barrier sampler (barrier.rs:328-330):
@@ -307,7 +335,17 @@ static double barrier_payoff(const kgpu_contract* c, double z, Failure& f) {
     const double value = weighted(intrinsic, c->log_discount + (in ? exponent : survival)) +
                          weighted(c->rebate, c->log_discount + (in ? survival : exponent));
     if (!std::isfinite(value)) f.failed = true;
-    return value;
+    const int output = output_of(c);
+    if (output == 0) return value;
+    double first = 0.0, second = 0.0;
+    if (slope > 0.0 && exponent > -INFINITY) {
+        const double difference = (in ? -1.0 : 1.0) * (intrinsic - c->rebate);
+        first = weighted(up ? -difference : difference, c->log_discount + (exponent + std::log(slope)));
+        if (output == 2) second = weighted(-difference, c->log_discount + (exponent + 2.0 * std::log(slope)));
+    }
+    const double greek = barrier_greek(output, value, first, second, z, c->diffusion, c->spot);
+    if (!std::isfinite(greek)) f.failed = true;
+    return greek;
 }
 
 // normal_cdf, log_normal_cdf, log_normal_tail and weighted_cdf (numerics.rs:192-224).
@@ -365,12 +403,20 @@ static double barrier_discrete_payoff(const Plan& p, PathNormals& n, Failure& f)
     const bool up = c->flags & KGPU_C_BARRIER_UP;
     const bool in = c->flags & KGPU_C_BARRIER_IN;
     const bool condition = c->flags & KGPU_C_CONDITION_ON_HIT;
-    double noise = 0.0, terminal = 0.0;
+    double noise = 0.0, terminal = 0.0, first_normal = 0.0;
     bool touched = false;
+    const int output = output_of(c);
+    // The delta / gamma samples score the first normal (barrier.rs:455-470).
+    auto finish = [&](double value) {
+        return output == 0 ? value
+                           : barrier_greek(output, value, 0.0, 0.0, first_normal, p.steps[0].diffusion, c->spot);
+    };
     for (int i = 0; i < c->step_count; ++i) {
         const kgpu_step& st = p.steps[i];
         const kgpu_event& e = p.events[i];
-        noise = std::fma(st.diffusion, n.normal(), noise);
+        const double z = n.normal();
+        if (i == 0) first_normal = z;
+        noise = std::fma(st.diffusion, z, noise);
         terminal = st.drift + noise;
         if (c->flags & KGPU_C_CHECK_STEPS) {
             const double spot_now = discounted_product(c->spot, 1.0, terminal);
@@ -385,15 +431,16 @@ static double barrier_discrete_payoff(const Plan& p, PathNormals& n, Failure& f)
             touched = true;
             if (condition && c->step_count - i > 8) {
                 const double asset = discounted_product(c->spot, 1.0, terminal);
-                return lognormal_price(asset, c->strike, c->moneyness + noise + c->half_variance * e.coupon_barrier,
-                                       e.payment[1], c->log_discount, c->volatility, e.payment[2], c->sign, f);
+                return finish(lognormal_price(asset, c->strike,
+                                              c->moneyness + noise + c->half_variance * e.coupon_barrier,
+                                              e.payment[1], c->log_discount, c->volatility, e.payment[2], c->sign, f));
             }
         }
         if (touched && !in) {
             const double rebate =
                 discounted_product(c->rebate, 1.0, (c->flags & KGPU_C_REBATE_AT_HIT) ? e.payment[0] : c->log_discount);
             if (!std::isfinite(rebate)) f.failed = true;
-            return rebate;
+            return finish(rebate);
         }
     }
     const double asset = discounted_product(c->spot, 1.0, terminal);
@@ -403,7 +450,7 @@ static double barrier_discrete_payoff(const Plan& p, PathNormals& n, Failure& f)
     const double intrinsic = std::max(c->sign * payoff, 0.0);
     const double value = weighted(touched == in ? intrinsic : c->rebate, c->log_discount);
     if (!std::isfinite(value)) f.failed = true;
-    return value;
+    return finish(value);
 }
 
 // log_add (numerics.rs:320-327).
@@ -421,21 +468,29 @@ static double positive_difference(double a, double b) {
     return difference > 0.0 ? std::exp(a + std::log(difference)) : 0.0;
 }
 
-// ArithmeticParameters::geometric_values, price only (asian.rs:1062-1085).
-static double geometric_values(const kgpu_contract* c, double log_forward, double log_strike, double width) {
+// ArithmeticParameters::geometric_values (asian.rs:1062-1085): the geometric
+// control's [price, delta, gamma].
+static void geometric_values(const kgpu_contract* c, double log_forward, double log_strike, double width,
+                             double out[3]) {
     const double d1 = (log_forward - log_strike) / width + 0.5 * width;
     const double d2 = d1 - width;
     const double log_asset = log_forward + c->log_discount + log_normal_cdf(c->sign * d1);
     const double log_cash = log_strike + c->log_discount + log_normal_cdf(c->sign * d2);
-    return c->sign > 0.0 ? positive_difference(log_asset, log_cash) : positive_difference(log_cash, log_asset);
+    out[0] = c->sign > 0.0 ? positive_difference(log_asset, log_cash) : positive_difference(log_cash, log_asset);
+    const double log_spot = c->avg_log_spot;
+    out[1] = c->sign * std::exp(log_asset - log_spot);
+    out[2] = std::exp(log_forward + c->log_discount - 2.0 * log_spot - std::log(width) - 0.5 * d1 * d1 -
+                      0.5 * std::log(2.0 * M_PI));
 }
 
 // Continuous arithmetic average (asian.rs:636-711 ArithmeticGrid::path, then
-// 1087-1178 ArithmeticParameters::arithmetic), price only, flat rates, no realized
-// history, interval widths of at least 1e-5 (plans reject narrower ones).
+// 1087-1178 ArithmeticParameters::arithmetic), flat rates, no realized history,
+// interval widths of at least 1e-5 (plans reject narrower ones): the price or its native
+// delta / gamma sample.
 static double average_arithmetic_payoff(const kgpu_contract* c, PathNormals& n, Failure& f) {
     const bool lead = c->flags & KGPU_C_AVERAGE_LEAD;
     const bool control = c->flags & KGPU_C_AVERAGE_CONTROL;
+    const int output = output_of(c);
     const int normals = c->step_count - (lead ? 1 : 0);  // step_count (n) - 1 increments
     const double lead_normal = lead ? n.normal() : 0.0;
     const double lead_growth = c->avg_lead_drift + c->avg_lead_width * lead_normal;
@@ -453,24 +508,27 @@ static double average_arithmetic_payoff(const kgpu_contract* c, PathNormals& n, 
             relative_sum += fraction * std::expm1(growth);
         }
     }
+    const double log_spot = c->avg_log_spot;
     const double log_rest =
         log_sum == -INFINITY ? c->avg_log_rest + std::log1p(relative_sum / c->avg_rest) : log_sum;
     const double log_q = c->avg_log_scale + lead_growth + log_rest + c->avg_interval_forward;
     const double log_c = c->avg_log_scale + lead_growth + c->avg_log_half;
     const double log_accrued = log_add(-INFINITY, log_c);
-    double residual = 0.0;
+    double residual[3] = {0.0, 0.0, 0.0};
     if (control) {
         const double width = c->control_first_weight * c->avg_width;
         const double log_forward = c->control_log_asset_scale + lead_growth + geometric_growth +
                                    c->control_first_weight * c->avg_drift + 0.5 * width * width;
-        residual = geometric_values(c, log_forward, c->control_log_strike, width);
+        geometric_values(c, log_forward, c->control_log_strike, width, residual);
     }
-    double value;
+    double values[3] = {0.0, 0.0, 0.0};
     const double log_strike = c->avg_log_strike;
+    const double ld = c->log_discount;
     if (log_accrued >= log_strike) {
-        value = c->sign < 0.0 ? 0.0
-                              : std::exp(log_q + c->log_discount) +
-                                    positive_difference(log_accrued + c->log_discount, log_strike + c->log_discount);
+        if (c->sign > 0.0) {
+            values[0] = std::exp(log_q + ld) + positive_difference(log_accrued + ld, log_strike + ld);
+            values[1] = std::exp(log_q + ld - log_spot) + std::exp(log_c + ld - log_spot);
+        }
     } else {
         const double log_b = log_strike + std::log(-std::expm1(log_accrued - log_strike));
         double forward = log_q - log_b;
@@ -479,23 +537,27 @@ static double average_arithmetic_payoff(const kgpu_contract* c, PathNormals& n, 
                                  std::exp(lead_growth) * (c->avg_rest * std::expm1(c->avg_interval_forward) +
                                                           relative_sum * std::exp(c->avg_interval_forward));
             const double excess = c->avg_baseline + c->avg_weight * extra;
-            const double b = std::exp(log_b - c->avg_log_spot);
+            const double b = std::exp(log_b - log_spot);
             if (b > 0.0 && std::fabs(excess / b) < 0.5) forward = std::log1p(excess / b);
         }
         const double center = forward / c->avg_width;
         const double d1 = center + 0.5 * c->avg_width;
         const double d2 = center - 0.5 * c->avg_width;
-        const double log_asset = log_q + c->log_discount + log_normal_cdf(c->sign * d1);
-        const double log_cash = log_b + c->log_discount + log_normal_cdf(c->sign * d2);
-        value = c->sign > 0.0 ? positive_difference(log_asset, log_cash) : positive_difference(log_cash, log_asset);
+        const double log_asset = log_q + ld + log_normal_cdf(c->sign * d1);
+        const double log_cash = log_b + ld + log_normal_cdf(c->sign * d2);
+        values[0] = c->sign > 0.0 ? positive_difference(log_asset, log_cash) : positive_difference(log_cash, log_asset);
+        values[1] = c->sign * (std::exp(log_c + ld - log_spot + log_normal_cdf(c->sign * d2)) +
+                               std::exp(log_q + ld - log_spot + log_normal_cdf(c->sign * d1)));
+        values[2] = std::exp(ld + 2.0 * log_strike - 2.0 * log_spot - log_b - c->greek_log_width - 0.5 * d2 * d2 -
+                             0.5 * std::log(2.0 * M_PI));
     }
-    value -= residual;
+    const double value = values[output] - residual[output];
     if (!std::isfinite(value)) f.failed = true;
     return value;
 }
 
-// GeometricParameters::geometric, price only (asian.rs:740-784): moneyness = initial
-// moneyness + drift, diffusion = width, log_scale = log width.
+// GeometricParameters::geometric (asian.rs:740-784): moneyness = initial moneyness +
+// drift, diffusion = width, log_scale = log width; the price or its delta / gamma.
 static double average_geometric_payoff(const kgpu_contract* c, double normal, Failure& f) {
     const double distance = c->moneyness + c->diffusion * normal;
     const double standardized = c->moneyness / c->diffusion + normal;
@@ -509,42 +571,77 @@ static double average_geometric_payoff(const kgpu_contract* c, double normal, Fa
         log_payoff = log_strike + distance + std::log(-std::expm1(-distance));
     else
         log_payoff = log_strike + std::log(-std::expm1(distance));
-    const double value = std::exp(log_payoff + c->log_discount);
+    const double log_asset = log_strike + distance + c->log_discount + c->greek_log_weight;
+    const double numerator = normal - std::exp(c->greek_log_base_width);
+    double value;
+    switch (output_of(c)) {
+        case 1:
+            value = c->sign * std::exp(log_asset - c->greek_log_spot);
+            break;
+        case 2:
+            value = numerator != 0.0 ? c->sign * std::copysign(std::exp(log_asset - 2.0 * c->greek_log_spot +
+                                                                        std::log(std::fabs(numerator)) -
+                                                                        c->greek_log_base_width),
+                                                               numerator)
+                                     : 0.0;
+            break;
+        default:
+            value = std::exp(log_payoff + c->log_discount);
+    }
     if (!std::isfinite(value)) f.failed = true;
     return value;
 }
 
-// survival (double_barrier.rs:6-112) without derivatives: the probability that a
-// Brownian bridge between log distances `initial` and `terminal` above the lower barrier
-// stays inside (0, band).  Returns false when the series does not converge or leaves
+// survival (double_barrier.rs:6-112): the probability that a Brownian bridge between
+// log distances `initial` and `terminal` above the lower barrier stays inside (0, band),
+// in out[0], and with `derivatives` its first and second derivatives in the initial log
+// spot in out[1], out[2].  Returns false when the series does not converge or leaves
 // [0, 1] (the reference's unstable() error).
-static bool double_survival(double initial, double terminal, double band, double deviation, double* out) {
-    if (terminal <= 0.0 || terminal >= band) {
-        *out = 0.0;
-        return true;
-    }
+static bool double_survival(double initial, double terminal, double band, double deviation, bool derivatives,
+                            double out[3]) {
+    out[0] = out[1] = out[2] = 0.0;
+    if (terminal <= 0.0 || terminal >= band) return true;
     double x = initial / band, y = terminal / band;
     const double ratio = deviation / band;
     const double variance = ratio * ratio;
     if (variance == 0.0) {
-        *out = 1.0;
+        out[0] = 1.0;
         return true;
     }
     if (!std::isfinite(variance) || variance <= 0.0) return false;
-    if (x + y > 1.0) {
+    const bool reflected = x + y > 1.0;
+    if (reflected) {
         x = 1.0 - x;
         y = 1.0 - y;
     }
-    double sum = 0.0;
+    double sum[3] = {0.0, 0.0, 0.0};
     bool converged = false;
     if (variance < 0.25) {
-        sum = -std::expm1(-2.0 * (x / ratio) * (y / ratio));
+        const double inverse_variance = std::isnormal(variance) ? 1.0 / variance : INFINITY;
+        sum[0] = -std::expm1(-2.0 * (x / ratio) * (y / ratio));
         // One image term: k shifts the band; direct images add, reflected ones subtract.
         auto term = [&](double k, bool direct) {
             const double exponent = direct ? -2.0 * (k / ratio) * ((y - x + k) / ratio)
                                            : -2.0 * ((x + k) / ratio) * ((y + k) / ratio);
+            const double sign = direct ? 1.0 : -1.0;
             const double weight = std::exp(exponent);
-            if (k != 0.0) sum += (direct ? 1.0 : -1.0) * weight;
+            if (k != 0.0) sum[0] += sign * weight;
+            if (derivatives) {
+                const double numerator = direct ? 2.0 * k : -2.0 * (y + k);
+                if (numerator != 0.0) {
+                    const double slope = numerator * inverse_variance;
+                    const double first = weight * slope;
+                    const double second = first * slope;
+                    if (std::isnormal(weight) && std::isnormal(first) && std::isnormal(second)) {
+                        sum[1] += sign * first;
+                        sum[2] += sign * second;
+                    } else {
+                        const double log_slope = std::log(std::fabs(numerator)) - 2.0 * std::log(ratio);
+                        sum[1] += sign * std::copysign(std::exp(exponent + log_slope), numerator);
+                        sum[2] += sign * std::exp(exponent + 2.0 * log_slope);
+                    }
+                }
+            }
             return weight;
         };
         term(0.0, false);
@@ -567,15 +664,26 @@ static bool double_survival(double initial, double terminal, double band, double
             const double exponent = log_scale - 0.5 * frequency * frequency * variance;
             const double weight = std::exp(exponent);
             const double sy = std::sin(frequency * y);
-            sum += weight * (std::sin(frequency * x) * sy);
+            const double product = std::sin(frequency * x) * sy;
+            sum[0] += weight * product;
+            if (derivatives) {
+                const double first = frequency * std::cos(frequency * x) * sy;
+                const double score = -distance / variance;
+                sum[1] += weight * (first + score * product);
+                sum[2] += weight * (2.0 * score * first + (score * score + 1.0 / variance - frequency * frequency) * product);
+            }
             if (n >= 4 && exponent + 4.0 * std::log(frequency) < -40.0) {
                 converged = true;
                 break;
             }
         }
     }
-    if (!converged || !(sum >= -1e-13 && sum <= 1.0 + 1e-13)) return false;
-    *out = std::min(std::max(sum, 0.0), 1.0);
+    if (!converged || !(sum[0] >= -1e-13 && sum[0] <= 1.0 + 1e-13)) return false;
+    out[0] = std::min(std::max(sum[0], 0.0), 1.0);
+    if (derivatives) {
+        out[1] = (reflected ? -sum[1] : sum[1]) / band;
+        out[2] = (sum[2] / band) / band;
+    }
     return true;
 }
 
@@ -588,17 +696,31 @@ static double double_barrier_payoff(const kgpu_contract* c, double z, Failure& f
     const double distance = c->moneyness + noise;
     const double payoff = std::fabs(distance) < 0.5 ? c->strike * std::expm1(distance) : asset - c->strike;
     const double intrinsic = std::max(c->sign * payoff, 0.0);
-    double survival;
-    if (!double_survival(c->band_initial, c->barrier_moneyness + noise, c->band, c->diffusion, &survival)) {
+    const int output = output_of(c);
+    double survival[3];
+    if (!double_survival(c->band_initial, c->barrier_moneyness + noise, c->band, c->diffusion, output != 0,
+                         survival)) {
         f.failed = true;
         return 0.0;
     }
     const bool in = c->flags & KGPU_C_BARRIER_IN;
     const double rebate = (!in && (c->flags & KGPU_C_REBATE_AT_HIT)) ? 0.0 : c->rebate;
-    const double value = weighted(intrinsic, c->log_discount + (in ? std::log1p(-survival) : std::log(survival))) +
-                         weighted(rebate, c->log_discount + (in ? std::log(survival) : std::log1p(-survival)));
+    const double value =
+        weighted(intrinsic, c->log_discount + (in ? std::log1p(-survival[0]) : std::log(survival[0]))) +
+        weighted(rebate, c->log_discount + (in ? std::log(survival[0]) : std::log1p(-survival[0])));
     if (!std::isfinite(value)) f.failed = true;
-    return value;
+    if (output == 0) return value;
+    // derivative(weight) of barrier.rs:366-372
+    const double difference = (in ? -1.0 : 1.0) * (intrinsic - rebate);
+    auto derivative = [&](double weight) {
+        const double sign = (std::signbit(difference) ? -1.0 : 1.0) * (std::signbit(weight) ? -1.0 : 1.0);
+        return discounted_product(std::fabs(difference), sign, c->log_discount + std::log(std::fabs(weight)));
+    };
+    const double first = derivative(survival[1]);
+    const double second = output == 2 ? derivative(survival[2]) : 0.0;
+    const double greek = barrier_greek(output, value, first, second, z, c->diffusion, c->spot);
+    if (!std::isfinite(greek)) f.failed = true;
+    return greek;
 }
 
 // AutocallableNote::terminal (instruments/autocallable.rs:1396-1414)
