@@ -191,3 +191,39 @@ def european_delta_gamma(sign: float, strike: float, expiry: float, ctx: Pricing
     delta = sign * carry * normal_cdf(sign * d1)
     gamma = carry * math.exp(-0.5 * d1 * d1) / math.sqrt(2.0 * math.pi) / (spot * width)
     return {"delta": delta, "gamma": gamma}
+
+
+def scaled_cdf(amount: float, exponent: float, argument: float) -> float:
+    """numerics.rs:168-174."""
+    if amount == 0.0:
+        return 0.0
+    return math.exp(_ln(amount) + exponent + log_normal_cdf(argument))
+
+
+def hit_value(amount: float, distance: float, upper: bool, drift: float, sigma: float, t: float,
+              rate: float) -> float:
+    """hit_value (engines/analytic/barrier.rs:361-425): the value of `amount` paid when a
+    continuously monitored barrier `distance` (absolute log distance) away is first
+    touched before `t`.  The closed form with both exponential terms is restated; the
+    negative-discriminant quadrature and the reflection tail are not built."""
+    from .errors import UnsupportedOperationError
+    variance = sigma * sigma
+    drift = -drift if upper else drift
+    if variance == 0.0:
+        raise UnsupportedOperationError("zero-volatility at-hit rebates are not sampled")
+    discriminant = drift * drift + 2.0 * rate * variance
+    scale = max(1.0, abs(drift * drift), abs(2.0 * rate * variance))
+    if discriminant < 0.0 or (rate < 0.0 and discriminant <= 16.0 * 2.220446049250313e-16 * scale):
+        raise UnsupportedOperationError("at-hit rebates with a non-positive discriminant are not sampled")
+    root = math.sqrt(discriminant)
+    width = sigma * math.sqrt(t)
+    first_exponent = -2.0 * rate / (root - drift) if drift < 0.0 else (-drift - root) / variance
+    second_exponent = 2.0 * rate / (root + drift) if drift > 0.0 else (-drift + root) / variance
+    if not math.isfinite(second_exponent):
+        raise UnsupportedOperationError("at-hit rebates needing the reflection tail are not sampled")
+    first = scaled_cdf(amount, first_exponent * distance, (root * t - distance) / width)
+    second = scaled_cdf(amount, second_exponent * distance, (-root * t - distance) / width)
+    value = first + second
+    if not math.isfinite(value):
+        raise ComputationFailureError("analytic pricing produced a non-finite result")
+    return value

@@ -319,6 +319,19 @@ def native_greeks(engine, option, ctx: PricingContext, request, plan_for,
             result = PricingResult(estimates[0].price)
             for g, e in zip(wanted, estimates[1:]):
                 result.greeks[g] = e.price
+            if plan.addend is not None and wanted:
+                # The analytic part's own spot stencils (barrier.rs:489-523).
+                def addend_price(key):
+                    return plan.addend(scenario_context(key))
+                key0 = (ctx.spot, ctx.model.volatility, ctx.model.rate, ctx.model.dividend)
+                extra = _stencils(ctx, option.expiry, wanted, shifts,
+                                  discontinuity if discontinuity is not None else (lambda r: False),
+                                  addend_price, addend_price(key0))
+                for g in wanted:
+                    if g in extra.greeks:
+                        result.greeks[g] += extra.greeks[g]
+                    else:
+                        result.greeks.pop(g, None)
         for g in supported:
             if g not in result.greeks:
                 result.status[g] = "stencil_unavailable"

@@ -15,7 +15,7 @@ packs plans into one kgpu_book.
 """
 import math
 from dataclasses import dataclass, field, replace
-from typing import List, Optional
+from typing import Callable, List, Optional
 
 import numpy as np
 
@@ -49,6 +49,9 @@ class ContractPlan:
     daily: Optional[np.ndarray] = None   # DAILY_DTYPE[step_count] when bridged
     # exact [price, delta, gamma] of an arithmetic average's geometric control
     control_expected: Optional[tuple] = None
+    # an analytic part added to the sampled mean (a continuous knock-out's at-hit
+    # rebate, barrier.rs:484-498), as a function of the context
+    addend: Optional[Callable] = None
 
     @property
     def record(self):
@@ -248,8 +251,18 @@ def barrier(option, ctx: PricingContext):
 
     if not option.continuous:
         return _scheduled_barrier(option, ctx, drift, half_variance_rate, mean_distance)
+    addend = None
     if at_hit and not knock_in and option.rebate != 0.0:
-        raise UnsupportedOperationError("at-hit rebates of continuously monitored knock-outs are not sampled")
+        if double:
+            raise UnsupportedOperationError("at-hit rebates of continuous double knock-outs are not sampled")
+
+        def addend(scenario: PricingContext, option=option, up=up):
+            # hit_value (analytic/barrier.rs:361-425) at the scenario's market
+            m = scenario.model
+            return analytic.hit_value(option.rebate, abs(log_ratio(option.barrier, scenario.spot)), up,
+                                      m.rate - m.dividend - 0.5 * m.volatility * m.volatility,
+                                      m.volatility, option.expiry, m.rate)
+        addend(ctx)  # unsupported branches fail before sampling
     width = sigma * math.sqrt(time)
     mean = drift * time
     if not (width > 0.0 and math.isfinite(width) and math.isfinite(mean)):
@@ -266,13 +279,14 @@ def barrier(option, ctx: PricingContext):
     c["barrier_drift"] = mean
     c["barrier_distance"] = abs(log_ratio(level, spot))
     c["barrier_moneyness"] = mean_distance(time, level)
-    c["rebate"] = option.rebate
+    # An at-hit knock-out rebate is valued analytically, not on the paths.
+    c["rebate"] = 0.0 if addend is not None else option.rebate
     c["spot"] = spot
     c["log_discount"] = -rate * time
     c["step_count"] = 1
     steps = np.zeros(1, STEP_DTYPE)
     steps[0] = (mean, width, 0.0, math.exp(-rate * time))
-    return ContractPlan(c, steps, np.zeros(1, np.uint8))
+    return ContractPlan(c, steps, np.zeros(1, np.uint8), addend=addend)
 
 
 def _scheduled_barrier(option: BarrierOption, ctx: PricingContext, drift, half_variance_rate,

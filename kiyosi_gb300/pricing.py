@@ -162,6 +162,9 @@ class _MonteCarloEngine:
                                                     C.byref(settings), out, flag))
             for j, i in enumerate(index):
                 results[i] = MonteCarloEstimate.from_native(out[j])
+                addend = getattr(contract_plans[i], "addend", None)
+                if addend is not None:
+                    results[i] = replace(results[i], price=results[i].price + addend(ctx))
         return results
 
     def price(self, contract, ctx: PricingContext) -> float:
