@@ -38,13 +38,13 @@ PATHS = 1 << 20
 STEPS = 504
 SEED = 42
 # Warp instructions the FP32 persistent kernel issues per executed path position on
-# this workload, from one ncu capture (smsp__inst_executed.sum 354,077,385 over the
-# 41.7 M positions of a 2^19-path pricing; profiles/persistent_kernel_snowball.md).
+# this workload, from one ncu capture (smsp__inst_executed.sum 403,176,851 over the
+# 41,683,020 positions of a 2^19-path pricing; profiles/persistent_kernel_snowball.md).
 # The kernel is neither HBM- nor tensor-bound, so its roofline is the SM issue rate
 # (4 warp-instructions per cycle per SM).
-WARP_INST_PER_EXECUTED_STEP = 8.49
-# DRAM bytes per path of the same capture (4.44 MB read, 0 written, at 2^19 paths).
-DRAM_BYTES_PER_PATH = 4.4357e6 / (1 << 19)
+WARP_INST_PER_EXECUTED_STEP = 403176851 / 41683020
+# DRAM bytes per path of the same capture (5.07 MB read, 512 B written, at 2^19 paths).
+DRAM_BYTES_PER_PATH = (5.069568e6 + 512) / (1 << 19)
 
 
 def snowball():
