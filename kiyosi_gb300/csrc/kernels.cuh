@@ -597,8 +597,14 @@ struct Compensated {
 // warp's shared copy (FP64 keeps one item per warp).  Each finished path writes its
 // payoff to values[value_offset[contract] + sample]; reduce_values_kernel sums them in a
 // fixed order, so results do not depend on which warp ran which path.
+// Resident CTAs the register budget is cut for: FP32 paths fit 64 registers (four
+// CTAs per SM); FP64 state needs twice the registers, so it keeps two CTAs.
+template <class Real>
+constexpr int kPersistentMinBlocks = sizeof(Real) == 4 ? 4 : 2;
+
 template <class Real, int MODEL, bool SOBOL, bool EXT>
-__global__ void __launch_bounds__(kThreads, 4) persistent_kernel(PersistentArgs<Real> a, kgpu_model model,
+__global__ void __launch_bounds__(kThreads, kPersistentMinBlocks<Real>) persistent_kernel(PersistentArgs<Real> a,
+                                                                                          kgpu_model model,
                                                               const double* lv_dev) {
     using Kind = SobolKind<Real>;
     using Word = typename Kind::Word;

@@ -49,28 +49,50 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p
 #pragma unroll
     for (int j = 0; j < T; ++j) cn[j] = decide ? coef_next[j] : 0.0;
     const Real inv_k = Real(1) / p.strike;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
-        Real c = cash[i];
-        if (decide) {
-            const Real s1 = spot_at_date<Real, TWO>(p, date + 1, a[size_t(date + 1) * p.paths + i]);
-            const Real y1 = TWO ? b[size_t(date + 1) * p.paths + i] * p.y_scale : Real(0);
-            const Real e = intrinsic(p, s1);
-            if (e > Real(0) && e * inv_k > continuation<Real, TWO>(p, cn, s1 * inv_k, y1)) c = e;
+    // The 65-sum accumulator allows one CTA per SM, so the loop is latency-bound; each
+    // thread loads kPrefetch paths before working through them in grid-stride order,
+    // which keeps every thread's accumulation order (and the sums) unchanged.
+    constexpr int kPrefetch = 4;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < p.paths; base += kPrefetch * stride) {
+        Real c_in[kPrefetch], a0[kPrefetch], b0[kPrefetch], a1[kPrefetch], b1[kPrefetch];
+#pragma unroll
+        for (int u = 0; u < kPrefetch; ++u) {
+            const int i = base + u * stride;
+            if (i < p.paths) {
+                c_in[u] = cash[i];
+                a0[u] = a[size_t(date) * p.paths + i];
+                b0[u] = TWO ? b[size_t(date) * p.paths + i] : Real(0);
+                a1[u] = decide ? a[size_t(date + 1) * p.paths + i] : Real(0);
+                b1[u] = (decide && TWO) ? b[size_t(date + 1) * p.paths + i] : Real(0);
+            }
         }
-        c *= p.discount;
-        cash[i] = c;
-        const Real s = spot_at_date<Real, TWO>(p, date, a[size_t(date) * p.paths + i]);
-        if (intrinsic(p, s) > Real(0)) {
-            Real f[T];
-            lsmc_basis<Real, TWO>(s * inv_k, TWO ? b[size_t(date) * p.paths + i] * p.y_scale : Real(0), f);
-            const Real target = c * inv_k;
-            int q = 0;
 #pragma unroll
-            for (int r = 0; r < T; ++r)
+        for (int u = 0; u < kPrefetch; ++u) {
+            const int i = base + u * stride;
+            if (i >= p.paths) break;
+            Real c = c_in[u];
+            if (decide) {
+                const Real s1 = spot_at_date<Real, TWO>(p, date + 1, a1[u]);
+                const Real y1 = TWO ? b1[u] * p.y_scale : Real(0);
+                const Real e = intrinsic(p, s1);
+                if (e > Real(0) && e * inv_k > continuation<Real, TWO>(p, cn, s1 * inv_k, y1)) c = e;
+            }
+            c *= p.discount;
+            cash[i] = c;
+            const Real s = spot_at_date<Real, TWO>(p, date, a0[u]);
+            if (intrinsic(p, s) > Real(0)) {
+                Real f[T];
+                lsmc_basis<Real, TWO>(s * inv_k, TWO ? b0[u] * p.y_scale : Real(0), f);
+                const Real target = c * inv_k;
+                int q = 0;
 #pragma unroll
-                for (int col = r; col < T; ++col) acc[q++] += f[r] * f[col];
+                for (int r = 0; r < T; ++r)
 #pragma unroll
-            for (int r = 0; r < T; ++r) acc[q++] += f[r] * target;
+                    for (int col = r; col < T; ++col) acc[q++] += f[r] * f[col];
+#pragma unroll
+                for (int r = 0; r < T; ++r) acc[q++] += f[r] * target;
+            }
         }
     }
     // Warp shuffles in FP64, then warps in a fixed order.
@@ -251,12 +273,12 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
             const int* hnext = date + 1 <= p.dates - 2 ? have + date + 1 : nullptr;
             if (two) {
                 lsmc_backward<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
-                lsmc_solve<true><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                lsmc_solve<true><<<1, kSolveThreads, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                                     have + date, failed);
             } else {
                 lsmc_backward<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash,
                                                                             partials);
-                lsmc_solve<false><<<1, 128, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                lsmc_solve<false><<<1, kSolveThreads, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                                      have + date, failed);
             }
             launches += 2;

@@ -99,8 +99,13 @@ __device__ __forceinline__ Real continuation(const LsmcParams<Real>& p, const do
 
 // Merges the block partials in block order and solves the normal equations with pivoting
 // and degree fallback (solve_quadratic, american.rs:1693-1749), in FP64.
+// Threads of the solve's launch: 16 warps read the block partials of the normal-equation
+// sums concurrently (the order of each sum's additions does not depend on the warp
+// count); 512 threads leave the elimination its 128 registers.
+constexpr int kSolveThreads = 512;
+
 template <bool TWO>
-__global__ void lsmc_solve(const double* partials, int blocks, int max_degree, double* coef, int* have,
+__global__ void __launch_bounds__(kSolveThreads) lsmc_solve(const double* partials, int blocks, int max_degree, double* coef, int* have,
                            int* failed) {
     constexpr int T = TWO ? 10 : 3;
     constexpr int S = sum_count(T);

@@ -662,20 +662,38 @@ __global__ void __launch_bounds__(kLsmcThreads) mlp_poly_sums_kernel(LsmcParams<
 #pragma unroll
     for (int j = 0; j < S; ++j) acc[j] = 0.f;
     const float inv_k = 1.f / p.strike;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
-        const size_t at = size_t(date) * p.paths + i;
-        const float s = spot_at_date<float, TWO>(p, date, a[at]);
-        if (intrinsic(p, s) > 0.f) {
-            float f[T];
-            lsmc_basis<float, TWO>(s * inv_k, TWO ? b[at] * p.y_scale : 0.f, f);
-            const float target = cash[i] * inv_k;
-            int q = 0;
+    // One CTA per SM fits the accumulators: loads of kPrefetch paths are issued before
+    // the sums, in grid-stride order (the accumulation order is unchanged).
+    constexpr int kPrefetch = 4;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < p.paths; base += kPrefetch * stride) {
+        float av[kPrefetch], bv[kPrefetch], cv[kPrefetch];
 #pragma unroll
-            for (int r = 0; r < T; ++r)
+        for (int u = 0; u < kPrefetch; ++u) {
+            const int i = base + u * stride;
+            if (i < p.paths) {
+                const size_t at = size_t(date) * p.paths + i;
+                av[u] = a[at];
+                bv[u] = TWO ? b[at] : 0.f;
+                cv[u] = cash[i];
+            }
+        }
 #pragma unroll
-                for (int col = r; col < T; ++col) acc[q++] += f[r] * f[col];
+        for (int u = 0; u < kPrefetch; ++u) {
+            if (base + u * stride >= p.paths) break;
+            const float s = spot_at_date<float, TWO>(p, date, av[u]);
+            if (intrinsic(p, s) > 0.f) {
+                float f[T];
+                lsmc_basis<float, TWO>(s * inv_k, TWO ? bv[u] * p.y_scale : 0.f, f);
+                const float target = cv[u] * inv_k;
+                int q = 0;
 #pragma unroll
-            for (int r = 0; r < T; ++r) acc[q++] += f[r] * target;
+                for (int r = 0; r < T; ++r)
+#pragma unroll
+                    for (int col = r; col < T; ++col) acc[q++] += f[r] * f[col];
+#pragma unroll
+                for (int r = 0; r < T; ++r) acc[q++] += f[r] * target;
+            }
         }
     }
     __shared__ double warp_sums[kLsmcThreads / 32][S];
@@ -1164,7 +1182,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         // The polynomial fit of this date (lsmc_solve: block-ordered merge, pivoted FP64
         // elimination with degree fallback), then the residual samples.
         mlp_poly_sums_kernel<TWO><<<sblocks, kLsmcThreads, 0, st>>>(p, date, a, b, cash, poly_partials);
-        lsmc_solve<TWO><<<1, 128, 0, st>>>(poly_partials, sblocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+        lsmc_solve<TWO><<<1, kSolveThreads, 0, st>>>(poly_partials, sblocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                            have + date, poly_failed);
         mlp_count_kernel<TWO><<<pblocks, 256, 0, st>>>(p, date, a, b, cash, coefs, have, stats);
         mlp_scan_kernel<<<1, kScanThreads, 0, st>>>(stats, pblocks, counts, total, norms + date);

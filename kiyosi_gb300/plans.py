@@ -519,7 +519,8 @@ def greek_output(plan, output: str):
     c["flags"] = c["flags"] | (abi.C_OUTPUT_DELTA if index == 1 else abi.C_OUTPUT_GAMMA)
     if plan.control_expected is not None:
         c["control_mean"] = plan.control_expected[index]
-    return replace(plan, contract=c)
+    # An analytic addend's Greeks come from its own stencils, not from this sample.
+    return replace(plan, contract=c, addend=None)
 
 
 def path_vanilla(option: EuropeanOption, ctx: PricingContext, step_count: int):

@@ -88,6 +88,8 @@ def test_in_out_parity_and_resolution():
     at_hit = plans.barrier(BarrierOption("call", 100.0, 1.0, barrier=90.0, barrier_type="down_and_out",
                                          rebate=1.0, rebate_timing="at_hit"), ctx)
     assert at_hit.record["rebate"] == 0.0 and at_hit.addend is not None
+    # The delta / gamma copies carry no addend: its Greeks come from its own stencils.
+    assert plans.greek_output(at_hit, "delta").addend is None
     with pytest.raises(InvalidInputError):
         BarrierOption("call", 100.0, 1.0, barrier=90.0, barrier_type="sideways")
 
