@@ -45,9 +45,9 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p
 #pragma unroll
     for (int j = 0; j < S; ++j) acc[j] = Real(0);
     const bool decide = coef_next != nullptr && *have_next;
-    double cn[T];
+    Real cn[T];
 #pragma unroll
-    for (int j = 0; j < T; ++j) cn[j] = decide ? coef_next[j] : 0.0;
+    for (int j = 0; j < T; ++j) cn[j] = decide ? Real(coef_next[j]) : Real(0);
     const Real inv_k = Real(1) / p.strike;
     // The 65-sum accumulator allows one CTA per SM, so the loop is latency-bound; each
     // thread loads kPrefetch paths before working through them in grid-stride order,
@@ -95,21 +95,7 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p
             }
         }
     }
-    // Warp shuffles in FP64, then warps in a fixed order.
-    __shared__ double warp_sums[kLsmcThreads / 32][S];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < S; ++j) {
-        double v = double(acc[j]);
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) warp_sums[warp][j] = v;
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < S; j += blockDim.x) {
-        double v = 0.0;
-        for (int w = 0; w < kLsmcThreads / 32; ++w) v += warp_sums[w][j];
-        partials[size_t(blockIdx.x) * S + j] = v;
-    }
+    block_sums<Real, S>(acc, partials);
 }
 
 // Date-0 decision and the mean of the cash (FP64 block partials: sum, sum of squares).
@@ -118,10 +104,10 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_final(LsmcParams<Real> p, c
                                                            const Real* a, const Real* b, const Real* cash,
                                                            double* partials) {
     constexpr int T = TWO ? 10 : 3;
-    double cn[T];
+    Real cn[T];
     const bool decide = *have0;
 #pragma unroll
-    for (int j = 0; j < T; ++j) cn[j] = decide ? coef0[j] : 0.0;
+    for (int j = 0; j < T; ++j) cn[j] = decide ? Real(coef0[j]) : Real(0);
     const Real inv_k = Real(1) / p.strike;
     double s0 = 0.0, s1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.paths; i += gridDim.x * blockDim.x) {
@@ -157,9 +143,16 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_final(LsmcParams<Real> p, c
 }
 
 // Lower bound on fresh paths: the fitted policy applied forward (american.rs:574-637).
+// The fitted FP64 coefficients in the path store's precision, for the forward pass.
+template <class Real>
+__global__ void coef_table_kernel(const double* coefs, Real* table, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) table[i] = Real(coefs[i]);
+}
+
 template <class Real, bool TWO>
 __global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound(LsmcParams<Real> p, uint64_t seed,
-                                                                 const double* coefs, const int* have,
+                                                                 const Real* table, const int* have,
                                                                  double* partials) {
     constexpr int T = TWO ? 10 : 3;
     const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
@@ -187,10 +180,8 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound(LsmcParams<Real
             if (e > Real(0)) {
                 bool stop = k == p.dates - 1;
                 if (!stop && have[k]) {
-                    double cn[T];
-#pragma unroll
-                    for (int j = 0; j < T; ++j) cn[j] = coefs[size_t(k) * kMaxTerms + j];
-                    stop = e * inv_k > continuation<Real, TWO>(p, cn, s * inv_k, TWO ? v * p.y_scale : Real(0));
+                    stop = e * inv_k > continuation<Real, TWO>(p, table + k * kMaxTerms, s * inv_k,
+                                                               TWO ? v * p.y_scale : Real(0));
                 }
                 if (stop) {
                     value = e * df;
@@ -235,7 +226,7 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     const int blocks = std::min<int>(ctx->sm_count * 4, int((n + kLsmcThreads - 1) / kLsmcThreads));
     if (ctx->lsmc_store.ensure(n * d * sizeof(Real) * (two ? 2 : 1)) || ctx->lsmc_cash.ensure(n * sizeof(Real)) ||
         ctx->lsmc_sums.ensure(size_t(blocks) * kMaxSums * sizeof(double)) ||
-        ctx->lsmc_coef.ensure(d * kMaxTerms * sizeof(double) + d * sizeof(int) + 16) ||
+        ctx->lsmc_coef.ensure(d * kMaxTerms * (sizeof(double) + sizeof(Real)) + d * sizeof(int) + 64) ||
         ctx->lsmc_misc.ensure(size_t(blocks) * 2 * sizeof(double) + 16))
         return KGPU_DEVICE_ERROR;
     Real* a = static_cast<Real*>(ctx->lsmc_store.ptr);
@@ -244,6 +235,9 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     double* coefs = static_cast<double*>(ctx->lsmc_coef.ptr);
     int* have = reinterpret_cast<int*>(coefs + d * kMaxTerms);
     int* failed = have + d;
+    // Converted coefficients after `failed`, aligned to 16 bytes.
+    Real* table = reinterpret_cast<Real*>(
+        (reinterpret_cast<uintptr_t>(failed + 1) + 15) & ~uintptr_t(15));
     double* partials = static_cast<double*>(ctx->lsmc_sums.ptr);
     double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
     cudaStream_t st = ctx->stream;
@@ -290,11 +284,13 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
         ++launches;
         cudaEventRecordWithFlags(e2, st, cudaEventRecordExternal);
         if (lower) {
+            const int terms = int(d) * kMaxTerms;
+            coef_table_kernel<Real><<<(terms + 255) / 256, 256, 0, st>>>(coefs, table, terms);
             if (two)
-                lsmc_lower_bound<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
+                lsmc_lower_bound<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, table, have, lp);
             else
-                lsmc_lower_bound<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, coefs, have, lp);
-            ++launches;
+                lsmc_lower_bound<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, table, have, lp);
+            launches += 2;
         }
     };
     // Key of the captured sequence: every argument its launches bake in.

@@ -87,14 +87,51 @@ __device__ __forceinline__ void lsmc_basis(Real x, Real y, Real* f) {
     f[9] = y * y * y;
 }
 
+// `coef` in the path store's precision (converted from the FP64 fit once per thread or
+// block, not per path: on GB300 a double-to-float conversion issues on the FP64 pipe).
 template <class Real, bool TWO>
-__device__ __forceinline__ Real continuation(const LsmcParams<Real>& p, const double* coef, Real x, Real y) {
+__device__ __forceinline__ Real continuation(const LsmcParams<Real>& p, const Real* coef, Real x, Real y) {
     Real f[kMaxTerms];
     lsmc_basis<Real, TWO>(x, y, f);
     Real c = Real(0);
 #pragma unroll
-    for (int i = 0; i < (TWO ? 10 : 3); ++i) c += Real(coef[i]) * f[i];
+    for (int i = 0; i < (TWO ? 10 : 3); ++i) c += coef[i] * f[i];
     return c;
+}
+
+// The block's FP64 partial of each normal-equation sum, written sum-major (the solve
+// reads each sum coalesced).  FP32 accumulators go through shared memory and each sum
+// is added by one thread in thread order: 65 x 128 FP64 additions per block instead of
+// a 5-step butterfly on every lane (GB300's FP64 pipe is the slow one).  FP64
+// accumulators keep the butterfly (their staging would not fit in shared memory).
+template <class Real, int S>
+__device__ __forceinline__ void block_sums(const Real (&acc)[S], double* partials) {
+    if constexpr (sizeof(Real) == 4) {
+        __shared__ float staged[S][kLsmcThreads + 1];  // padded: row reads hit distinct banks
+#pragma unroll
+        for (int j = 0; j < S; ++j) staged[j][threadIdx.x] = acc[j];
+        __syncthreads();
+        for (int j = threadIdx.x; j < S; j += blockDim.x) {
+            double v = 0.0;
+            for (int t = 0; t < kLsmcThreads; ++t) v += double(staged[j][t]);
+            partials[size_t(j) * gridDim.x + blockIdx.x] = v;
+        }
+    } else {
+        __shared__ double warp_sums[kLsmcThreads / 32][S];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int j = 0; j < S; ++j) {
+            double v = double(acc[j]);
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) warp_sums[warp][j] = v;
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < S; j += blockDim.x) {
+            double v = 0.0;
+            for (int w = 0; w < kLsmcThreads / 32; ++w) v += warp_sums[w][j];
+            partials[size_t(j) * gridDim.x + blockIdx.x] = v;
+        }
+    }
 }
 
 // Merges the block partials in block order and solves the normal equations with pivoting
@@ -115,7 +152,18 @@ __global__ void __launch_bounds__(kSolveThreads) lsmc_solve(const double* partia
     const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
     for (int j = threadIdx.x >> 5; j < S; j += warps) {
         double v = 0.0;
-        for (int blk = lane; blk < blocks; blk += 32) v += partials[size_t(blk) * S + j];
+        // Loads of eight partials are issued before they are added, in the same order.
+        for (int base = lane; base < blocks; base += 8 * 32) {
+            double chunk[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int blk = base + 32 * u;
+                chunk[u] = blk < blocks ? partials[size_t(j) * blocks + blk] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (base + 32 * u < blocks) v += chunk[u];
+        }
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         if (lane == 0) sums[j] = v;
     }

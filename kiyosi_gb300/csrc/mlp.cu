@@ -533,9 +533,9 @@ template <bool TWO>
 __device__ __forceinline__ float poly_part(const LsmcParams<float>& p, const double* coefs, const int* have, int k,
                                            float spot, float v) {
     if (!have[k]) return 0.f;
-    double cn[TWO ? 10 : 3];
+    float cn[TWO ? 10 : 3];
 #pragma unroll
-    for (int j = 0; j < (TWO ? 10 : 3); ++j) cn[j] = coefs[size_t(k) * kMaxTerms + j];
+    for (int j = 0; j < (TWO ? 10 : 3); ++j) cn[j] = float(coefs[size_t(k) * kMaxTerms + j]);
     return continuation<float, TWO>(p, cn, spot / p.strike, TWO ? v * p.y_scale : 0.f);
 }
 
@@ -696,20 +696,7 @@ __global__ void __launch_bounds__(kLsmcThreads) mlp_poly_sums_kernel(LsmcParams<
             }
         }
     }
-    __shared__ double warp_sums[kLsmcThreads / 32][S];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < S; ++j) {
-        double v = double(acc[j]);
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) warp_sums[warp][j] = v;
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < S; j += blockDim.x) {
-        double v = 0.0;
-        for (int w = 0; w < kLsmcThreads / 32; ++w) v += warp_sums[w][j];
-        partials[size_t(blockIdx.x) * S + j] = v;
-    }
+    block_sums<float, S>(acc, partials);
 }
 
 // In-the-money samples of date k in path order: per-block counts and target sums, a
