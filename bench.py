@@ -551,7 +551,7 @@ def run_lsmc(args):
     poly64 = price(abi.BASIS_POLY3, 20, precision=abi.PRECISION_FP64)
     mlp = price(abi.BASIS_MLP, 20)
     mlp_eq = price(abi.BASIS_MLP, 22, samples=131072)
-    polys = [price(abi.BASIS_POLY3, k) for k in range(21, 26)]
+    polys = [price(abi.BASIS_POLY3, k) for k in range(21, 27)]
     equal = min(polys, key=lambda r: abs(r["wall_ms"] - mlp_eq["wall_ms"]))
     line = {
         "metric": "LSMC |price - ADI| at equal wall time: polynomial + fitted network vs polynomial",
