@@ -225,7 +225,7 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     const size_t n = size_t(p.paths), d = size_t(p.dates);
     const int blocks = std::min<int>(ctx->sm_count * 4, int((n + kLsmcThreads - 1) / kLsmcThreads));
     if (ctx->lsmc_store.ensure(n * d * sizeof(Real) * (two ? 2 : 1)) || ctx->lsmc_cash.ensure(n * sizeof(Real)) ||
-        ctx->lsmc_sums.ensure(size_t(blocks) * kMaxSums * sizeof(double)) ||
+        ctx->lsmc_sums.ensure((size_t(blocks) + 1) * kMaxSums * sizeof(double)) ||
         ctx->lsmc_coef.ensure(d * kMaxTerms * (sizeof(double) + sizeof(Real)) + d * sizeof(int) + 64) ||
         ctx->lsmc_misc.ensure(size_t(blocks) * 2 * sizeof(double) + 16))
         return KGPU_DEVICE_ERROR;
@@ -239,6 +239,7 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     Real* table = reinterpret_cast<Real*>(
         (reinterpret_cast<uintptr_t>(failed + 1) + 15) & ~uintptr_t(15));
     double* partials = static_cast<double*>(ctx->lsmc_sums.ptr);
+    double* reduced = partials + size_t(blocks) * kMaxSums;  // one partial per sum
     double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
     cudaStream_t st = ctx->stream;
     const bool lower = fresh_seed != s->seed;
@@ -267,15 +268,17 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
             const int* hnext = date + 1 <= p.dates - 2 ? have + date + 1 : nullptr;
             if (two) {
                 lsmc_backward<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
-                lsmc_solve<true><<<1, kSolveThreads, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                reduce_partials_kernel<<<S, 32, 0, st>>>(partials, blocks, reduced);
+                lsmc_solve<true><<<1, kSolveThreads, 0, st>>>(reduced, 1, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                                     have + date, failed);
             } else {
                 lsmc_backward<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash,
                                                                             partials);
-                lsmc_solve<false><<<1, kSolveThreads, 0, st>>>(partials, blocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+                reduce_partials_kernel<<<S, 32, 0, st>>>(partials, blocks, reduced);
+                lsmc_solve<false><<<1, kSolveThreads, 0, st>>>(reduced, 1, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                                      have + date, failed);
             }
-            launches += 2;
+            launches += 3;
         }
         if (two)
             lsmc_final<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);

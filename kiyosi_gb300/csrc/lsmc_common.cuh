@@ -134,6 +134,28 @@ __device__ __forceinline__ void block_sums(const Real (&acc)[S], double* partial
     }
 }
 
+// Sums each normal-equation sum's block partials, one warp per sum on its own SM: lanes
+// stride over the partials in a fixed order and a fixed shuffle tree adds the lanes.
+// The solve then reads one partial per sum, so these sums are its inputs bit for bit,
+// while the FP64 additions are spread over many SMs (one SM's FP64 pipe is slow).
+__global__ void __launch_bounds__(32) reduce_partials_kernel(const double* partials, int blocks, double* sums) {
+    const int j = blockIdx.x, lane = threadIdx.x;
+    double v = 0.0;
+    for (int base = lane; base < blocks; base += 8 * 32) {
+        double chunk[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int blk = base + 32 * u;
+            chunk[u] = blk < blocks ? partials[size_t(j) * blocks + blk] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (base + 32 * u < blocks) v += chunk[u];
+    }
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) sums[j] = v;
+}
+
 // Merges the block partials in block order and solves the normal equations with pivoting
 // and degree fallback (solve_quadratic, american.rs:1693-1749), in FP64.
 // Threads of the solve's launch: 16 warps read the block partials of the normal-equation
@@ -147,25 +169,38 @@ __global__ void __launch_bounds__(kSolveThreads) lsmc_solve(const double* partia
     constexpr int T = TWO ? 10 : 3;
     constexpr int S = sum_count(T);
     __shared__ double sums[S];
-    // One warp per sum: lanes stride over the block partials, then a fixed shuffle tree
-    // (deterministic, and short enough that the solve is not latency-bound on it).
-    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-    for (int j = threadIdx.x >> 5; j < S; j += warps) {
-        double v = 0.0;
-        // Loads of eight partials are issued before they are added, in the same order.
-        for (int base = lane; base < blocks; base += 8 * 32) {
-            double chunk[8];
+    // Each warp owns the sums j = warp + 16 q.  Lanes stride over the block partials of
+    // a sum in a fixed order, then a fixed shuffle tree adds the lanes (deterministic).
+    // The loads of eight partials of all of a warp's sums are issued before they are
+    // added, so the reduction is not one load latency per partial.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    constexpr int kPerWarp = (S + kSolveThreads / 32 - 1) / (kSolveThreads / 32);
+    double v[kPerWarp];
+#pragma unroll
+    for (int q = 0; q < kPerWarp; ++q) v[q] = 0.0;
+    for (int base = lane; base < blocks; base += 8 * 32) {
+        double chunk[kPerWarp][8];
+#pragma unroll
+        for (int q = 0; q < kPerWarp; ++q) {
+            const int j = warp + warps * q;
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 const int blk = base + 32 * u;
-                chunk[u] = blk < blocks ? partials[size_t(j) * blocks + blk] : 0.0;
+                chunk[q][u] = (j < S && blk < blocks) ? partials[size_t(j) * blocks + blk] : 0.0;
             }
+        }
+#pragma unroll
+        for (int q = 0; q < kPerWarp; ++q)
 #pragma unroll
             for (int u = 0; u < 8; ++u)
-                if (base + 32 * u < blocks) v += chunk[u];
-        }
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) sums[j] = v;
+                if (base + 32 * u < blocks) v[q] += chunk[q][u];
+    }
+#pragma unroll
+    for (int q = 0; q < kPerWarp; ++q) {
+        const int j = warp + warps * q;
+        double t = v[q];
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+        if (lane == 0 && j < S) sums[j] = t;
     }
     __syncthreads();
     // Pivoted elimination by one warp: lane r holds row r of the augmented system (the

@@ -1078,7 +1078,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
                                 size_t(pblocks) * (sizeof(BlockStats) + sizeof(int)) + d * sizeof(TargetNorm) + 256) ||
         ctx->mlp_params.ensure(misc_floats * sizeof(float)) ||
         ctx->lsmc_misc.ensure(size_t(fblocks) * 2 * sizeof(double) * 2 + 64) ||
-        ctx->lsmc_sums.ensure(size_t(sblocks) * kMaxSums * sizeof(double)) ||
+        ctx->lsmc_sums.ensure((size_t(sblocks) + 1) * kMaxSums * sizeof(double)) ||
         ctx->lsmc_coef.ensure(d * kMaxTerms * sizeof(double) + d * sizeof(int) + 16))
         return KGPU_DEVICE_ERROR;
     if (!configure_train_kernel()) {
@@ -1112,6 +1112,7 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     int* have = reinterpret_cast<int*>(coefs + d * kMaxTerms);
     int* poly_failed = have + d;
     double* poly_partials = static_cast<double*>(ctx->lsmc_sums.ptr);
+    double* poly_reduced = poly_partials + size_t(sblocks) * kMaxSums;  // one partial per sum
     cudaStream_t st = ctx->stream;
     std::vector<float> init;
     initial_params(s->mlp_seed, init);
@@ -1169,13 +1170,14 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         // The polynomial fit of this date (lsmc_solve: block-ordered merge, pivoted FP64
         // elimination with degree fallback), then the residual samples.
         mlp_poly_sums_kernel<TWO><<<sblocks, kLsmcThreads, 0, st>>>(p, date, a, b, cash, poly_partials);
-        lsmc_solve<TWO><<<1, kSolveThreads, 0, st>>>(poly_partials, sblocks, p.max_degree, coefs + size_t(date) * kMaxTerms,
+        reduce_partials_kernel<<<sum_count(TWO ? 10 : 3), 32, 0, st>>>(poly_partials, sblocks, poly_reduced);
+        lsmc_solve<TWO><<<1, kSolveThreads, 0, st>>>(poly_reduced, 1, p.max_degree, coefs + size_t(date) * kMaxTerms,
                                            have + date, poly_failed);
         mlp_count_kernel<TWO><<<pblocks, 256, 0, st>>>(p, date, a, b, cash, coefs, have, stats);
         mlp_scan_kernel<<<1, kScanThreads, 0, st>>>(stats, pblocks, counts, total, norms + date);
         mlp_scatter_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, a, b, cash, coefs, have, counts, norms + date,
                                                         samples, sample_path);
-        launches += 5;
+        launches += 6;
         MLP_TRY(cudaGetLastError());
         int itm = 0;
         MLP_TRY(cudaMemcpyAsync(&itm, total, sizeof(int), cudaMemcpyDeviceToHost, st));
