@@ -127,7 +127,9 @@ __device__ __forceinline__ void box_muller(uint64_t b1, uint64_t b2, float* cosi
     float u1 = unit52f(b1);
     float u2 = unit52f(b2);
     float radius = sqrtf(-2.0f * __logf(u1));
-    float turns = u2 - rintf(u2);
+    // u2 - rint(u2) for u2 in [0, 1] (rint(0.5) = 0) as a compare and select; the
+    // result is the same float for every u2 in that range.
+    float turns = u2 > 0.5f ? u2 - 1.0f : u2;
     float s, c;
     __sincosf(6.28318530717958647692f * turns, &s, &c);
     *cosine = radius * c;
