@@ -287,6 +287,12 @@ typedef struct kgpu_contract {
     double greek_log_amount;      /* digital: ln(paid amount) */
     double greek_log_base_width;  /* geometric average: ln(sigma) + ln(sqrt(variance time)) */
     double greek_log_weight;      /* geometric average: ln(weight) */
+    /* sampling dimensions per path: 0 = step_count x the model's normals per step.  A
+     * larger value lays every path out over that many normals, so a contract whose grid
+     * is a prefix of a longer one draws the longer grid's numbers (the lanes of a shared
+     * daily grid, autocallable/portfolio.rs:1180-1190). */
+    int32_t dimensions;
+    int32_t reserved_tail;
 } kgpu_contract;
 
 /* A book of contracts sharing one model.  Arrays are indexed through the offsets in

@@ -128,7 +128,8 @@ class Contract(C.Structure):
                 ("control_log_strike", _D), ("control_log_asset_scale", _D),
                 ("control_first_weight", _D), ("control_mean", _D), ("band", _D),
                 ("band_initial", _D), ("greek_log_spot", _D), ("greek_log_width", _D),
-                ("greek_log_amount", _D), ("greek_log_base_width", _D), ("greek_log_weight", _D)]
+                ("greek_log_amount", _D), ("greek_log_base_width", _D), ("greek_log_weight", _D),
+                ("dimensions", _I), ("reserved_tail", _I)]
 
 
 class Book(C.Structure):

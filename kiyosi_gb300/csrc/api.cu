@@ -292,6 +292,7 @@ bool terminal_payoff(const kgpu_contract& c) {
 
 int dims_of(const kgpu_contract& c, const kgpu_model* m) {
     if (terminal_payoff(c)) return 1;
+    if (c.dimensions > 0) return c.dimensions;
     return c.step_count * model_normals_per_step(m);
 }
 
@@ -845,10 +846,25 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: events out of range", i);
         if (c.event_count > 0 && !book->events)
             return fail(ctx, KGPU_INVALID_INPUT, "contract %d: events missing", i);
+        if (c.dimensions < 0 ||
+            (c.dimensions > 0 && (terminal_payoff(c) || c.dimensions < c.step_count * model_normals_per_step(model))))
+            return fail(ctx, KGPU_INVALID_INPUT, "contract %d: dimensions must cover every step's normals", i);
         if (c.flags & KGPU_C_BRIDGE) {
             if (model->kind != KGPU_MODEL_BSM || !book->bridge_daily || !book->intervals || c.bridge_count < 1 ||
                 c.bridge_offset < 0 || c.bridge_offset + c.bridge_count > book->interval_total)
                 return fail(ctx, KGPU_INVALID_INPUT, "contract %d: invalid bridge plan", i);
+            if (!device_resident) {
+                // Interval ends ascend strictly and the last one is the final step.
+                int previous = -1;
+                for (int q = 0; q < c.bridge_count; ++q) {
+                    const int end = book->intervals[c.bridge_offset + q].end;
+                    if (end <= previous || end >= c.step_count)
+                        return fail(ctx, KGPU_INVALID_INPUT, "contract %d: bridge interval %d ends out of order", i, q);
+                    previous = end;
+                }
+                if (previous != c.step_count - 1)
+                    return fail(ctx, KGPU_INVALID_INPUT, "contract %d: the last bridge interval must end the grid", i);
+            }
         }
         if (!device_resident && c.payoff == KGPU_PAYOFF_AUTOCALLABLE) {
             // Every event step must be backed by an event record.

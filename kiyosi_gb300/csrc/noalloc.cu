@@ -115,9 +115,12 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
     a.book.units = nullptr;
     a.book.ends = nullptr;
     a.contract = 0;
-    a.dims = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL)
-                 ? 1
-                 : c.step_count * (model->kind == KGPU_MODEL_HESTON ? 2 : 1);
+    const int step_dims = c.step_count * (model->kind == KGPU_MODEL_HESTON ? 2 : 1);
+    if (c.dimensions < 0 || (c.dimensions > 0 && c.dimensions < step_dims))
+        return noalloc_fail(KGPU_INVALID_INPUT, "dimensions must cover every step's normals");
+    a.dims = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1
+             : c.dimensions > 0                                                    ? c.dimensions
+                                                                                   : step_dims;
     a.paths = paths;
     a.samples = samples;
     a.seed = settings->seed;

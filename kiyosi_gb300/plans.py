@@ -562,6 +562,26 @@ def asian(option: AsianOption, ctx: PricingContext, step_count: Optional[int] = 
     return ContractPlan(c, _grid_steps(ctx, times), flags)
 
 
+def cash_event(note: AutocallableNote, o, spot: float, rate: float, step: int):
+    """CashEvent::new and discounted_payment (autocallable.rs:532-562): one observation's
+    log-space knock-out and coupon thresholds and its four discounted payments, indexed
+    coupon_due | knocked_out << 1, as an EVENT_DTYPE record at grid step `step`."""
+    has_ko = o.knock_out_level is not None
+    ko = log_ratio(o.knock_out_level, spot) if has_ko else 0.0
+    barrier = log_ratio(o.coupon_barrier_level if o.coupon_barrier_level is not None
+                        else 0.0, spot)
+    period_coupon = note.period_coupon if o.coupon_barrier_level is not None else 0.0
+    redemption = note.knock_out_payment(o) if has_ko else 0.0
+    log_discount = -rate * o.time
+    payments = []
+    for outcome in range(4):
+        coupon_due, knocked_out = outcome & 1, outcome >> 1
+        coupon = period_coupon if coupon_due else 0.0
+        amount = redemption + coupon if knocked_out else coupon
+        payments.append(discounted_product(1.0, amount, log_discount))
+    return (ko, barrier, tuple(payments), int(has_ko), step)
+
+
 def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool = True):
     """prepare_sample_on_grid (autocallable.rs:293-430) for a note valued before its first
     observation: merged event and daily knock-in grid, log-space thresholds, discounted
@@ -596,21 +616,7 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
         o = event_at.get(t)
         if o is not None:
             flags[i] |= abi.STEP_EVENT
-            # CashEvent::new (autocallable.rs:532-550)
-            has_ko = o.knock_out_level is not None
-            ko = log_ratio(o.knock_out_level, spot) if has_ko else 0.0
-            barrier = log_ratio(o.coupon_barrier_level if o.coupon_barrier_level is not None
-                                else 0.0, spot)
-            period_coupon = note.period_coupon if o.coupon_barrier_level is not None else 0.0
-            redemption = note.knock_out_payment(o) if has_ko else 0.0
-            log_discount = -rate * t
-            payments = []
-            for outcome in range(4):
-                coupon_due, knocked_out = outcome & 1, outcome >> 1
-                coupon = period_coupon if coupon_due else 0.0
-                amount = redemption + coupon if knocked_out else coupon
-                payments.append(discounted_product(1.0, amount, log_discount))
-            ev[k] = (ko, barrier, tuple(payments), int(has_ko), i)
+            ev[k] = cash_event(note, o, spot, rate, i)
             k += 1
     c = _new_contract(abi.PAYOFF_AUTOCALLABLE, ctx.spot)
     flag = 0

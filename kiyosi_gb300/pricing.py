@@ -341,10 +341,24 @@ class MonteCarloAutocallableEngine(_MonteCarloEngine):
         return numerical_greeks(self, note, ctx, request, shifts)
 
     def price_many(self, notes: Sequence[AutocallableNote], ctx: PricingContext,
-                   path_counts: Optional[Sequence[int]] = None):
-        """Prices a book of notes in input order.  Unlike the reference's price_many,
-        each note may carry its own path count."""
+                   path_counts: Optional[Sequence[int]] = None, shared_grid: bool = False):
+        """Prices a book of notes in input order (autocallable.rs:119-152).  Unlike the
+        reference's price_many, each note may carry its own path count.  With
+        `shared_grid`, daily-knock-in notes of one daily grid share their paths and
+        coupon families are interpolated (portfolio.rs); see `portfolio`."""
+        if shared_grid:
+            if path_counts is not None:
+                raise InvalidInputError("a shared daily grid takes the engine's path count")
+            from . import portfolio
+            return portfolio.price_many(self, notes, ctx, True)
+        if len(notes) > (1 << 20):
+            raise InvalidInputError("contract batch exceeds 1,048,576 instruments")
         return [e.price for e in self.price_many_with_statistics(notes, ctx, path_counts)]
+
+    def price_many_on_shared_grid(self, notes: Sequence[AutocallableNote], ctx: PricingContext):
+        """MonteCarloAutocallableEngine::price_many_on_shared_grid (autocallable.rs:
+        127-152)."""
+        return self.price_many(notes, ctx, shared_grid=True)
 
     def price_many_with_statistics(self, notes, ctx: PricingContext, path_counts=None):
         return self._run(ctx, [plans.autocallable(n, ctx) for n in notes], path_counts)

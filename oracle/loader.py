@@ -60,6 +60,11 @@ def load():
                                                     C.c_double, C.c_int, C.c_int, C.c_int,
                                                     C.c_int]
             lib.kor_heston_adi_american.restype = C.c_double
+        lib.kor_price_shared_group.argtypes = [P(abi.Model), P(abi.Book), P(abi.Settings),
+                                               C.c_double, C.c_double, P(C.c_int32),
+                                               P(C.c_int32), P(C.c_int32), P(C.c_double),
+                                               C.c_int, P(C.c_double), P(C.c_double), C.c_int]
+        lib.kor_price_shared_group.restype = C.c_int
         lib.kor_mlp_gradients.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int,
                                           P(C.c_double)]
         lib.kor_mlp_gradients.restype = C.c_double
@@ -80,6 +85,44 @@ def price_book(ctx, packed, settings, threads=0):
         from kiyosi_gb300.errors import raise_for_status
         raise_for_status(status, "oracle")
     return list(out)
+
+
+def price_shared_group(ctx, packed, settings, strips=None, threads=0):
+    """One shared daily grid's lanes (the contracts of `packed`) walked by the oracle's
+    restatement of the multi-lane path loop.  `strips` gives per lane None or
+    (kind, ascending log levels) with kind 1 = knock-out, 2 = knock-in.  Returns the lane
+    prices and, per lane, the strip members' prices (or None)."""
+    from kiyosi_gb300 import abi
+    from kiyosi_gb300.market import safe_log_returns
+    lib = load()
+    n = len(packed.contracts)
+    strips = strips or [None] * n
+    kind = np.zeros(n, np.int32)
+    offset = np.zeros(n, np.int32)
+    length = np.zeros(n, np.int32)
+    levels = []
+    for i, strip in enumerate(strips):
+        if strip is not None:
+            kind[i], offset[i], length[i] = strip[0], len(levels), len(strip[1])
+            levels.extend(strip[1])
+    levels = np.array(levels + [0.0], np.float64)
+    lane_prices = np.zeros(n, np.float64)
+    strip_prices = np.zeros(len(levels), np.float64)
+    low, high = safe_log_returns(ctx.spot)
+    model = ctx.kgpu_model()
+    book = packed.struct()
+    I32, F64 = C.POINTER(C.c_int32), C.POINTER(C.c_double)
+    status = lib.kor_price_shared_group(C.byref(model), C.byref(book), C.byref(settings), low, high,
+                                        kind.ctypes.data_as(I32), offset.ctypes.data_as(I32),
+                                        length.ctypes.data_as(I32), levels.ctypes.data_as(F64),
+                                        len(levels) - 1, lane_prices.ctypes.data_as(F64),
+                                        strip_prices.ctypes.data_as(F64), threads)
+    if status != 0:
+        from kiyosi_gb300.errors import raise_for_status
+        raise_for_status(status, "oracle")
+    members = [None if strip is None else list(strip_prices[offset[i]:offset[i] + length[i]])
+               for i, strip in enumerate(strips)]
+    return list(lane_prices), members
 
 
 def pcg_normals(seed, block, first, count):

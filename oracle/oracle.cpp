@@ -6,6 +6,7 @@
 #include "oracle_core.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cstring>
 #include <limits>
@@ -857,6 +858,7 @@ static bool terminal_payoff(const kgpu_contract* c) {
 
 static int dimensions_of(const kgpu_contract* c, const Model& model) {
     if (terminal_payoff(c)) return 1;
+    if (c->dimensions > 0) return c->dimensions;
     return c->step_count * model.normals_per_step();
 }
 
@@ -905,6 +907,8 @@ static int price_contract(const Model& model, const Plan& p, const kgpu_settings
     if (paths < 1) return KGPU_INVALID_INPUT;
     bool sobol = settings->sampling == KGPU_SAMPLING_SOBOL;
     bool antithetic = settings->antithetic != 0;
+    if (c->dimensions < 0 || (c->dimensions > 0 && c->dimensions < c->step_count * model.normals_per_step()))
+        return KGPU_INVALID_INPUT;
     int dims = dimensions_of(c, model);
     // sobol::sequence rejects dimensions beyond the Joe-Kuo table (sobol.rs).
     if (sobol && (dims < 1 || dims > 21201)) return KGPU_INVALID_INPUT;
@@ -1003,6 +1007,303 @@ static int price_contract(const Model& model, const Plan& p, const kgpu_settings
     return KGPU_OK;
 }
 
+// --------------------------------------------------------------------------------------
+// Lanes of one shared daily grid on one path loop (engines/monte_carlo/autocallable/
+// portfolio.rs).  SharedEvents::new (903-1047) builds the interval plan from the union
+// of the lanes' cash and maturity dates; shared_payoffs (1275-1439) walks every lane
+// along one path; price_with_strips (1150-1258) turns the threshold-strip bucket sums
+// into prices.  Each lane is a contract of the book whose steps are a prefix of the
+// longest lane's grid; its own interval plan is not read here.
+// --------------------------------------------------------------------------------------
+
+// numerics::Sum: Neumaier-compensated addition.
+struct CompensatedSum {
+    double value = 0.0, correction = 0.0;
+    void add(double term) {
+        double next = value + term;
+        correction += std::fabs(value) >= std::fabs(term) ? (value - next) + term : (term - next) + value;
+        value = next;
+    }
+    double total() const { return value + correction; }
+    void merge(const CompensatedSum& other) {
+        add(other.value);
+        add(other.correction);
+    }
+};
+
+enum { kStripNone = 0, kStripKnockOut = 1, kStripKnockIn = 2 };
+
+struct SharedGroup {
+    const kgpu_book* book;
+    int lanes = 0;
+    const kgpu_step* steps = nullptr;  // the longest lane's grid
+    const uint8_t* flags = nullptr;
+    int step_count = 0;
+    struct Action {
+        int lane, event;  // event < 0: the lane's maturity
+    };
+    struct Interval {
+        int step, end;
+        double drift, diffusion;
+    };
+    std::vector<Action> actions;
+    std::vector<Interval> intervals;
+    std::vector<std::array<double, 2>> daily;
+    std::vector<std::pair<double, int>> barriers;  // live knock-in levels, ascending
+    const int32_t *kind, *offset, *length;
+    const double* levels;
+};
+
+struct LaneState {
+    double cash;
+    bool monitoring, knocked_in, terminated;
+    int next_threshold;
+};
+
+static void build_shared_group(SharedGroup& g, double safe_low, double safe_high) {
+    const kgpu_book* b = g.book;
+    int base = 0;
+    for (int l = 0; l < g.lanes; ++l)
+        if (b->contracts[l].step_count >= b->contracts[base].step_count) base = l;  // max_by_key keeps the last
+    const kgpu_contract& bc = b->contracts[base];
+    g.steps = b->steps + bc.step_offset;
+    g.flags = b->step_flags + bc.step_offset;
+    g.step_count = bc.step_count;
+    const int n = g.step_count;
+    std::vector<std::vector<SharedGroup::Action>> buckets(n);
+    for (int l = 0; l < g.lanes; ++l) {
+        const kgpu_contract& c = b->contracts[l];
+        if ((c.flags & KGPU_C_HAS_KNOCK_IN) && !(c.flags & KGPU_C_KNOCKED_IN)) g.barriers.push_back({c.knock_in, l});
+        int ev = 0;
+        for (int i = 0; i < c.step_count; ++i)
+            if (b->step_flags[c.step_offset + i] & KGPU_STEP_EVENT) buckets[i].push_back({l, ev++});
+        buckets[c.step_count - 1].push_back({l, -1});
+    }
+    std::vector<int> ends;
+    for (int i = 0; i < n; ++i) {
+        for (auto& a : buckets[i]) g.actions.push_back(a);
+        ends.push_back(int(g.actions.size()));
+    }
+    double excursion = 0.0;
+    for (int i = 0; i < n; ++i) excursion += std::fabs(g.steps[i].drift) + 20.0 * g.steps[i].diffusion;
+    const bool bridge = safe_low <= excursion && excursion <= safe_high && safe_low <= -excursion &&
+                        -excursion <= safe_high;
+    g.daily.assign(size_t(n), std::array<double, 2>{0.0, 0.0});
+    int first = 0, previous = 0;
+    for (int step = 0; step < n; ++step) {
+        const int end = ends[step];
+        if (end == previous && step + 1 < n) continue;
+        if (bridge && step - first >= 8) {
+            double drift = g.steps[step].drift, width = g.steps[step].diffusion;
+            double variance = width * width;
+            for (int i = step - 1; i >= first; --i) {
+                const double mean = g.steps[i].drift, w = g.steps[i].diffusion;
+                const double next = std::fma(w, w, variance);
+                g.daily[i] = {(w * w) / next, w * std::sqrt(variance / next)};
+                drift += mean;
+                variance = next;
+            }
+            const double diffusion = std::sqrt(variance);
+            bool usable = std::isnormal(diffusion) && std::isfinite(drift);
+            for (int i = first; i < step && usable; ++i) usable = g.daily[i][0] > 0.0 && g.daily[i][1] > 0.0;
+            if (usable) {
+                g.intervals.push_back({step, end, drift, diffusion});
+                first = step + 1;
+                previous = end;
+                continue;
+            }
+        }
+        for (int i = first; i <= step; ++i)
+            g.intervals.push_back({i, i == step ? end : previous, g.steps[i].drift, g.steps[i].diffusion});
+        first = step + 1;
+        previous = end;
+    }
+    std::stable_sort(g.barriers.begin(), g.barriers.end(),
+                     [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first < b.first; });
+}
+
+// One path of every lane; false when a lane's cash is not finite.
+static bool shared_path(const SharedGroup& g, PathNormals& n, std::vector<LaneState>& st,
+                        std::vector<CompensatedSum>& sums) {
+    const kgpu_book* b = g.book;
+    for (int l = 0; l < g.lanes; ++l) {
+        const kgpu_contract& c = b->contracts[l];
+        const bool knocked = c.flags & KGPU_C_KNOCKED_IN;
+        st[l] = {c.initial_cash, (c.flags & KGPU_C_HAS_KNOCK_IN) && !knocked, knocked, false, 0};
+    }
+    double lr = 0.0, minimum = std::numeric_limits<double>::infinity();
+    int first = 0, first_step = 0, remaining = g.lanes;
+    size_t cursor = 0;
+    bool ok = true;
+    auto strip_end = [&](const double* lv, int from, int len, double value) {
+        // partition_point(level <= value) over the ascending levels[from..len)
+        return int(std::upper_bound(lv + from, lv + len, value) - lv);
+    };
+    for (const auto& iv : g.intervals) {
+        const double target = lr + std::fma(iv.diffusion, n.normal(), iv.drift);
+        if (first_step < iv.step) {
+            while (cursor < g.barriers.size() && st[g.barriers[cursor].second].terminated) ++cursor;
+            const double floor =
+                cursor < g.barriers.size() ? g.barriers[cursor].first : std::numeric_limits<double>::infinity();
+            for (int i = first_step; i < iv.step; ++i) {
+                if (minimum < floor || floor == std::numeric_limits<double>::infinity()) {
+                    n.skip(iv.step - i);
+                    break;
+                }
+                const double z = n.normal();
+                lr += std::fma(g.daily[i][0], target - lr, g.daily[i][1] * z);
+                if (g.flags[i] & KGPU_STEP_KNOCK_IN) minimum = std::min(minimum, lr);
+            }
+        }
+        lr = target;
+        if (g.flags[iv.step] & KGPU_STEP_KNOCK_IN) minimum = std::min(minimum, lr);
+        for (int q = first; q < iv.end; ++q) {
+            const auto& a = g.actions[q];
+            LaneState& L = st[a.lane];
+            if (L.terminated) continue;
+            const kgpu_contract& c = b->contracts[a.lane];
+            const int kind = g.kind ? g.kind[a.lane] : kStripNone;
+            const double* lv = kind ? g.levels + g.offset[a.lane] : nullptr;
+            const int len = kind ? g.length[a.lane] : 0;
+            CompensatedSum* bucket = kind ? sums.data() + g.offset[a.lane] : nullptr;
+            bool terminated;
+            if (a.event >= 0) {
+                const kgpu_event& e = b->events[c.event_offset + a.event];
+                if (kind == kStripKnockOut) {
+                    const int crossed = strip_end(lv, L.next_threshold, len, lr);
+                    if (crossed > L.next_threshold) {
+                        const double cash = L.cash + e.payment[2];  // knocked out, coupon not due
+                        if (!std::isfinite(cash)) ok = false;
+                        bucket[L.next_threshold].add(cash);
+                        if (crossed < len) bucket[crossed].add(-cash);
+                        L.next_threshold = crossed;
+                    }
+                    terminated = crossed == len;
+                } else {
+                    const bool hit = e.has_knock_out && lr >= e.knock_out;
+                    L.cash += e.payment[int(lr >= e.coupon_barrier) | (int(hit) << 1)];
+                    if (!std::isfinite(L.cash)) ok = false;
+                    terminated = hit;
+                }
+            } else {
+                const double discount = g.steps[c.step_count - 1].discount;
+                const double floor = (c.flags & KGPU_C_EXPIRY_KNOCK_IN) ? std::min(minimum, lr) : minimum;
+                if (L.monitoring && floor < c.knock_in) {
+                    L.monitoring = false;
+                    L.knocked_in = true;
+                }
+                const double spot = spot_at(c.spot, lr);
+                const double cash = L.cash + autocallable_terminal(&c, spot, L.knocked_in) * discount;
+                if (!std::isfinite(cash)) ok = false;
+                if (kind == kStripKnockOut) {
+                    bucket[L.next_threshold].add(cash);
+                } else {
+                    if (kind == kStripKnockIn && !L.knocked_in) {
+                        const int start = strip_end(lv, 0, len, floor);
+                        if (start < len) {
+                            const double hit = L.cash + autocallable_terminal(&c, spot, true) * discount;
+                            if (!std::isfinite(hit - cash)) ok = false;
+                            bucket[start].add(hit - cash);
+                        }
+                    }
+                    L.cash = cash;
+                }
+                terminated = true;
+            }
+            if (terminated) {
+                L.terminated = true;
+                --remaining;
+            }
+        }
+        if (remaining == 0) return ok;
+        first = iv.end;
+        first_step = iv.step + 1;
+    }
+    return false;
+}
+
+static int price_shared_group(const Model& model, SharedGroup& g, const kgpu_settings* settings, int strip_total,
+                              double* lane_prices, double* strip_prices, int threads) {
+    const kgpu_book* b = g.book;
+    const int64_t paths = settings->path_count;
+    if (paths < 1 || g.lanes < 1) return KGPU_INVALID_INPUT;
+    const bool sobol = settings->sampling == KGPU_SAMPLING_SOBOL;
+    const bool antithetic = settings->antithetic != 0;
+    const int dims = g.step_count * model.normals_per_step();
+    if (sobol && dims > 21201) return KGPU_INVALID_INPUT;
+    const int64_t samples = antithetic ? (paths + 1) / 2 : paths;
+    const size_t blocks = size_t((samples + kBlockSize - 1) / kBlockSize);
+    std::unique_ptr<SobolSequence> seq;
+    if (sobol) seq.reset(new SobolSequence(dims, settings->seed));
+    struct Partial {
+        std::vector<Moments> moments;
+        std::vector<CompensatedSum> sums;
+    };
+    std::vector<Partial> partials(blocks);
+    std::atomic<bool> failed{false};
+    run_blocks(blocks, threads, [&](size_t blk) {
+        Partial r;
+        r.moments.assign(g.lanes, Moments());
+        r.sums.assign(size_t(strip_total), CompensatedSum());
+        std::vector<LaneState> st(g.lanes);
+        BlockDraws draws(settings->seed, blk, seq.get());
+        std::vector<double> buffer(dims);
+        bool ok = true;
+        const int64_t first = int64_t(blk) * kBlockSize;
+        const int64_t last = std::min<int64_t>(first + kBlockSize, samples);
+        for (int64_t sample = first; sample < last; ++sample) {
+            const bool paired = antithetic && sample < paths / 2;
+            auto record = [&]() {
+                for (int l = 0; l < g.lanes; ++l) r.moments[l].add(st[l].cash, false);
+            };
+            if (paired) {
+                for (int d = 0; d < dims; ++d) buffer[d] = draws.normal();
+                PathNormals pn{&draws, buffer.data()};
+                ok &= shared_path(g, pn, st, r.sums);
+                record();
+                PathNormals mn{&draws, buffer.data()};
+                mn.sign = -1.0;
+                ok &= shared_path(g, mn, st, r.sums);
+                record();
+            } else {
+                PathNormals pn{&draws, nullptr};
+                ok &= shared_path(g, pn, st, r.sums);
+                record();
+                pn.skip(dims - pn.used);
+            }
+            draws.next_path();
+        }
+        if (!ok) failed = true;
+        partials[blk] = std::move(r);
+    });
+    if (failed) return KGPU_COMPUTATION_FAILURE;
+    std::vector<Moments> total(g.lanes);
+    std::vector<CompensatedSum> adjustments(static_cast<size_t>(strip_total));
+    for (auto& r : partials) {
+        for (int k = 0; k < strip_total; ++k) adjustments[k].merge(r.sums[k]);
+        for (int l = 0; l < g.lanes; ++l) total[l].merge(r.moments[l], false);
+    }
+    for (int l = 0; l < g.lanes; ++l) {
+        lane_prices[l] = discounted_product(total[l].scale, total[l].mean, 0.0);
+        if (!std::isfinite(lane_prices[l])) return KGPU_COMPUTATION_FAILURE;
+    }
+    for (int l = 0; l < g.lanes; ++l) {
+        if (!g.kind || g.kind[l] == kStripNone) continue;
+        const double base = g.kind[l] == kStripKnockOut ? 0.0 : lane_prices[l];
+        CompensatedSum prefix;
+        for (int i = 0; i < g.length[l]; ++i) {
+            prefix.merge(adjustments[g.offset[l] + i]);
+            const double delta = prefix.total() / double(paths);
+            const double price = base + delta;
+            if (!std::isfinite(price) || (delta != 0.0 && std::fabs(price) < 1e-10 * (std::fabs(base) + std::fabs(delta))))
+                return KGPU_COMPUTATION_FAILURE;
+            strip_prices[g.offset[l] + i] = price;
+        }
+    }
+    (void)b;
+    return KGPU_OK;
+}
+
 }  // namespace kor
 
 using namespace kor;
@@ -1025,6 +1326,29 @@ int kor_price_book(const kgpu_model* model, const kgpu_book* book, const kgpu_se
         if (status != KGPU_OK) return status;
     }
     return KGPU_OK;
+}
+
+// The lanes of one shared daily grid (contracts of `book`), with optional threshold
+// strips: lane l with kind[l] != 0 represents the ascending log levels
+// levels[offset[l] .. offset[l] + length[l]), whose prices land in strip_prices at the
+// same positions.  safe_low / safe_high bound the log returns that keep the spot finite.
+int kor_price_shared_group(const kgpu_model* model, const kgpu_book* book, const kgpu_settings* settings,
+                           double safe_low, double safe_high, const int32_t* kind, const int32_t* offset,
+                           const int32_t* length, const double* levels, int strip_total, double* lane_prices,
+                           double* strip_prices, int threads) {
+    if (model->kind != KGPU_MODEL_BSM || book->contract_count < 1) return KGPU_INVALID_INPUT;
+    for (int l = 0; l < book->contract_count; ++l)
+        if (book->contracts[l].payoff != KGPU_PAYOFF_AUTOCALLABLE) return KGPU_INVALID_INPUT;
+    Model m(model);
+    SharedGroup g;
+    g.book = book;
+    g.lanes = book->contract_count;
+    g.kind = kind;
+    g.offset = offset;
+    g.length = length;
+    g.levels = levels;
+    build_shared_group(g, safe_low, safe_high);
+    return price_shared_group(m, g, settings, strip_total, lane_prices, strip_prices, threads);
 }
 
 // Raw PCG32 words of stream `stream` from word `first`.
