@@ -762,6 +762,102 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
     return KGPU_OK;
 }
 
+// KGPU_SCHEDULE_SHARED_GRID: the lanes of one shared daily grid on one path per sample
+// (portfolio.rs:1275-1439), path-major.
+template <class Real>
+kgpu_status run_shared(Call& k, const DevBook<Real>& db, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const kgpu_book& b = *k.book;
+    const kgpu_settings& s = k.s;
+    const int n = b.contract_count;
+    int base = 0;
+    for (int i = 0; i < n; ++i)
+        if (b.contracts[i].step_count >= b.contracts[base].step_count) base = i;
+    const kgpu_contract& bc = b.contracts[base];
+    const int steps = bc.step_count;
+    std::vector<char> ends(steps, 0);
+    for (int q = 0; q < bc.bridge_count; ++q) ends[b.intervals[bc.bridge_offset + q].end] = 1;
+    std::vector<int16_t> slot(steps, -1);
+    int slots = 0;
+    auto take = [&](int step) {
+        if (step < 0 || step >= steps || !ends[step]) return false;
+        if (slot[step] < 0) slot[step] = int16_t(slots++);
+        return slots < 32768;
+    };
+    for (int i = 0; i < n; ++i) {
+        const kgpu_contract& c = b.contracts[i];
+        if (c.payoff != KGPU_PAYOFF_AUTOCALLABLE || !(c.flags & KGPU_C_BRIDGE))
+            return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "lane %d: shared-grid lanes are bridged autocallables", i);
+        if (k.info[i].dims != k.info[base].dims || k.info[i].paths != k.info[base].paths)
+            return fail(ctx, KGPU_INVALID_INPUT, "lane %d: lanes share their sampling dimensions and path count", i);
+        bool prefix = c.bridge_count <= bc.bridge_count &&
+                      std::memcmp(b.steps + c.step_offset, b.steps + bc.step_offset,
+                                  sizeof(kgpu_step) * size_t(c.step_count)) == 0 &&
+                      std::memcmp(b.bridge_daily + c.step_offset, b.bridge_daily + bc.step_offset,
+                                  sizeof(kgpu_bridge_daily) * size_t(c.step_count)) == 0 &&
+                      std::memcmp(b.intervals + c.bridge_offset, b.intervals + bc.bridge_offset,
+                                  sizeof(kgpu_bridge_interval) * size_t(c.bridge_count)) == 0;
+        for (int q = 0; prefix && q < c.step_count; ++q)
+            prefix = ((b.step_flags[c.step_offset + q] ^ b.step_flags[bc.step_offset + q]) & KGPU_STEP_KNOCK_IN) == 0;
+        if (!prefix) return fail(ctx, KGPU_INVALID_INPUT, "lane %d: the grid is not a prefix of the longest lane's", i);
+        for (int e = 0; e < c.event_count; ++e)
+            if (!take(b.events[c.event_offset + e].step))
+                return fail(ctx, KGPU_INVALID_INPUT, "lane %d: event %d is not on an interval end", i, e);
+        if (!take(c.step_count - 1)) return fail(ctx, KGPU_INVALID_INPUT, "lane %d: maturity is not an interval end", i);
+    }
+    const size_t smem = shared_grid_smem_bytes(sizeof(Real), slots, steps, k.sobol);
+    if (smem > 227 * 1024)
+        return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "%d action dates exceed the shared-grid kernel's shared memory",
+                    slots);
+    const int64_t samples = k.info[base].samples;
+    const int ctas = int((samples + kSharedThreads - 1) / kSharedThreads);
+    kgpu_status st;
+    if ((st = upload(ctx, ctx->shared_slots, slot.data(), slot.size() * sizeof(int16_t)))) return st;
+    if (ctx->partials.ensure(size_t(n) * ctas * sizeof(double2)) || ctx->merged.ensure(size_t(n) * sizeof(double2)))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the shared-grid sums failed");
+    SharedArgs<Real> a;
+    a.book = db;
+    a.lanes = n;
+    a.base = base;
+    a.slot = static_cast<const int16_t*>(ctx->shared_slots.ptr);
+    a.slots = slots;
+    a.steps = steps;
+    a.dims = k.info[base].dims;
+    a.samples = samples;
+    a.seed = s.seed;
+    a.sobol = SobolTables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    if (k.sobol && (st = ensure_sobol(ctx, a.dims, s.seed, &a.sobol))) return st;
+    a.partials = static_cast<double2*>(ctx->partials.ptr);
+    a.ctas = ctas;
+    CUDA_TRY(ctx, path_kernel_begin(ctx));
+    cudaError_t launched;
+    if constexpr (std::is_same<Real, double>::value)
+        launched = launch_shared_grid_fp64(k.sobol, ctas, smem, ctx->stream, a);
+    else
+        launched = launch_shared_grid_fp32(k.sobol, ctas, smem, ctx->stream, a);
+    CUDA_TRY(ctx, launched);
+    CUDA_TRY(ctx, path_kernel_end(ctx));
+    CUDA_TRY(ctx, launch_shared_merge(a.partials, ctas, n, static_cast<double2*>(ctx->merged.ptr), ctx->stream));
+    launches += 2;
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    std::vector<double2> merged(n);
+    CUDA_TRY(ctx, cudaMemcpyAsync(merged.data(), ctx->merged.ptr, sizeof(double2) * n, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n; ++i) {
+        const kgpu_contract& c = b.contracts[i];
+        const double path_steps = double(k.info[i].paths) * c.step_count;
+        TilePartial t{merged[i].x, merged[i].y, double(samples), path_steps};
+        estimate_from_sums(c, s, k.info[i].paths, t, &k.out[i]);
+        k.out[i].path_steps = path_steps;
+        k.out[i].executed_steps = path_steps;
+        if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].sample_error))
+            return fail(ctx, KGPU_COMPUTATION_FAILURE,
+                        "Monte Carlo produced a non-finite parameter, path or result (lane %d)", i);
+    }
+    return KGPU_OK;
+}
+
 template <class Real>
 kgpu_status run_book(Call& k) {
     kgpu_context* ctx = k.ctx;
@@ -772,8 +868,9 @@ kgpu_status run_book(Call& k) {
     kgpu_status st = compile_book<Real>(k, &db);
     if (st) return st;
     int launches = std::is_same<Real, float>::value ? 2 : 1;
-    st = k.s.schedule == KGPU_SCHEDULE_PERSISTENT ? run_persistent<Real>(k, db, launches)
-                                                  : run_plain<Real>(k, db, launches);
+    st = k.s.schedule == KGPU_SCHEDULE_PERSISTENT    ? run_persistent<Real>(k, db, launches)
+         : k.s.schedule == KGPU_SCHEDULE_SHARED_GRID ? run_shared<Real>(k, db, launches)
+                                                     : run_plain<Real>(k, db, launches);
     float ms = 0;
     if (cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop) == cudaSuccess) ctx->last_kernel_ms = ms;
     if (st == KGPU_OK) ctx->last_path_kernel_ms = path_kernel_ms(ctx);
@@ -814,9 +911,14 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
         return fail(ctx, KGPU_INVALID_INPUT, "unknown model %d", model->kind);
     k.sobol = s.sampling == KGPU_SAMPLING_SOBOL;
     const bool persistent = s.schedule == KGPU_SCHEDULE_PERSISTENT;
+    if (s.schedule < KGPU_SCHEDULE_PLAIN || s.schedule > KGPU_SCHEDULE_SHARED_GRID)
+        return fail(ctx, KGPU_INVALID_INPUT, "unknown schedule %d", s.schedule);
     if (persistent && s.antithetic)
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
                     "the persistent schedule does not pair antithetic samples; use the plain schedule");
+    if (s.schedule == KGPU_SCHEDULE_SHARED_GRID && (s.antithetic || device_resident || model->kind != KGPU_MODEL_BSM))
+        return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
+                    "the shared-grid schedule takes host books under BSM without antithetic pairs");
     // Validate contracts (MonteCarloSettings::validate, monte_carlo.rs:197-220).
     k.info.resize(n);
     for (int i = 0; i < n; ++i) {

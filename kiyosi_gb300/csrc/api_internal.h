@@ -41,8 +41,8 @@ struct kgpu_context {
     std::string error;
     // book staging
     kgpu::DeviceBuffer contracts, steps, flags, events, intervals, daily, lv;
-    // plain schedule
-    kgpu::DeviceBuffer partials, merged;
+    // plain schedule (partials and merged sums also serve the shared-grid schedule)
+    kgpu::DeviceBuffer partials, merged, shared_slots;
     // persistent schedule
     kgpu::DeviceBuffer items, order, first_item, tiles, tile_out, queue, values, value_offset, chunks, executed;
     // plan in the kernel's precision (contract table always, arrays for FP32)
@@ -74,7 +74,7 @@ struct kgpu_context {
 
     std::vector<kgpu::DeviceBuffer*> buffers() {
         return {&contracts, &steps,     &flags,     &events,   &intervals, &daily,     &lv,
-                &partials,  &merged,    &items,     &order,    &first_item, &tiles,    &tile_out,
+                &partials,  &merged,    &shared_slots, &items,     &order,    &first_item, &tiles,    &tile_out,
                 &queue,     &values,    &value_offset, &chunks, &executed, &sobol_dirs, &sobol_shifts, &sobol_nibbles, &sobol_dirs32, &sobol_shifts32, &sobol_nibbles32, &sobol_high32, &ccontracts, &csteps,
                 &cevents,   &cintervals, &cdaily,      &cunits,     &cends,      &lsmc_store, &lsmc_cash, &lsmc_sums,
                 &lsmc_coef, &lsmc_misc, &mlp_params, &mlp_scratch, &stream_out};

@@ -1,6 +1,7 @@
 // Instantiation body shared by kernels_fp64.cu and kernels_fp32.cu; REAL and PRECISION
 // are defined by the including translation unit.
 #include "launch.h"
+#include "shared_grid.cuh"
 
 namespace kgpu {
 
@@ -144,5 +145,26 @@ cudaError_t KGPU_CAT(launch_sobol_points_, PRECISION)(const SobolTables& t, int 
                                                                       normals);
     return cudaGetLastError();
 }
+
+template <bool SOBOL>
+static cudaError_t shared_one(int ctas, size_t smem, cudaStream_t s, const SharedArgs<REAL>& a) {
+    auto k = shared_grid_kernel<REAL, SOBOL>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    k<<<ctas, kSharedThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t KGPU_CAT(launch_shared_grid_, PRECISION)(bool sobol, int ctas, size_t smem, cudaStream_t s,
+                                                     const SharedArgs<REAL>& a) {
+    return sobol ? shared_one<true>(ctas, smem, s, a) : shared_one<false>(ctas, smem, s, a);
+}
+
+#if !KGPU_FP32_UNIT
+cudaError_t launch_shared_merge(const double2* partials, int ctas, int lanes, double2* out, cudaStream_t s) {
+    shared_merge_kernel<<<lanes, 32, 0, s>>>(partials, ctas, lanes, out);
+    return cudaGetLastError();
+}
+#endif
 
 }  // namespace kgpu

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "shared_grid.cuh"
 
 namespace kgpu {
 
@@ -42,6 +43,13 @@ cudaError_t launch_compile_units_fp32(const kgpu_contract* contracts, int n,
 cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, EventT<float>* events,
                                        IntervalT<float>* intervals, DailyT<float>* daily,
                                        cudaStream_t s);
+
+// The lanes of one shared daily grid, path-major, and the merge of their CTA sums.
+cudaError_t launch_shared_grid_fp64(bool sobol, int ctas, size_t smem, cudaStream_t s,
+                                    const SharedArgs<double>& a);
+cudaError_t launch_shared_grid_fp32(bool sobol, int ctas, size_t smem, cudaStream_t s,
+                                    const SharedArgs<float>& a);
+cudaError_t launch_shared_merge(const double2* partials, int ctas, int lanes, double2* out, cudaStream_t s);
 
 // Raw streams (kgpu_pcg_words, kgpu_pcg_normals, kgpu_sobol_points).
 cudaError_t launch_pcg_normals_fp64(uint64_t seed, uint64_t block, uint64_t first, int64_t count,

@@ -1,0 +1,179 @@
+// The lanes of one shared daily grid, path-major (engines/monte_carlo/autocallable/
+// portfolio.rs:1275-1439).
+//
+// The reference walks one path per sample and lets every note of the group read it.
+// That is the GB300 shape too: a thread simulates its path once, then fans out over
+// every lane of the group.
+//
+// * Path phase. The path follows the base lane's interval plan: the interval end is
+//   drawn first, then the bridged days, exactly as the per-lane bridge kernel draws them.
+//   At each action date (a step where some lane pays or matures) the thread records, in
+//   shared memory, the log return and the running minimum over the monitored days. The
+//   layout is [date][thread], which is conflict-free.
+// * Lane phase. Every lane walks its cash events on those records and settles at its
+//   maturity. Knock-in is decided by the recorded minimum: the per-lane kernel stops
+//   drawing a lane's days once the lane has knocked in, and the values it does draw are
+//   the same, so the outcome is the same.
+// * Reduction. Each CTA writes the lanes' sums and sums of squares. The merge kernel adds
+//   the CTAs in a fixed order.
+//
+// Cost is paths x (grid steps + lane events), against paths x lanes x grid steps when
+// each lane re-simulates the path.
+#pragma once
+#include "kernels.cuh"
+
+namespace kgpu {
+
+constexpr int kSharedThreads = 128;  // paths per CTA
+constexpr int kSharedWarps = kSharedThreads / 32;
+
+template <class Real>
+struct SharedArgs {
+    DevBook<Real> book;   // the lanes (compiled contracts, steps, events, plan)
+    int lanes;
+    int base;             // the lane whose grid and interval plan drive the path
+    const int16_t* slot;  // [base steps]: the action-date record of each step, or -1
+    int slots;
+    int steps;            // base grid steps
+    int dims;             // sampling dimensions per path
+    int64_t samples;
+    uint64_t seed;
+    SobolTables sobol;
+    double2* partials;    // [lane][CTA]: (sum, sum of squares)
+    int ctas;
+};
+
+__host__ __device__ inline size_t shared_grid_smem_bytes(size_t real, int slots, int steps, bool sobol) {
+    size_t records = 2 * size_t(slots) * kSharedThreads * real;
+    size_t sums = size_t(32) * kSharedWarps * sizeof(double2);
+    size_t table = (size_t(steps) * sizeof(int16_t) + 15) / 16 * 16;
+    return records + sums + table + (sobol ? size_t(steps) * 8 : 0);
+}
+
+template <class Real, bool SOBOL>
+__global__ void __launch_bounds__(kSharedThreads) shared_grid_kernel(SharedArgs<Real> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real* lr = reinterpret_cast<Real*>(smem_raw);              // [slots][kSharedThreads]
+    Real* mn = lr + size_t(a.slots) * kSharedThreads;          // [slots][kSharedThreads]
+    double2* sums = reinterpret_cast<double2*>(mn + size_t(a.slots) * kSharedThreads);  // [32][warps]
+    int16_t* slot = reinterpret_cast<int16_t*>(sums + 32 * kSharedWarps);               // [steps]
+    uint64_t* high = reinterpret_cast<uint64_t*>(
+        reinterpret_cast<unsigned char*>(slot) + (size_t(a.steps) * sizeof(int16_t) + 15) / 16 * 16);
+    const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31;
+    for (int i = tid; i < a.steps; i += kSharedThreads) slot[i] = a.slot[i];
+    const int64_t sample = int64_t(blockIdx.x) * kSharedThreads + tid;
+    // A CTA's samples lie inside one reference block of 256 (kSharedThreads divides it).
+    if (SOBOL) sobol_high(a.sobol, uint64_t(int64_t(blockIdx.x) * kSharedThreads / kBlockSize), high, tid,
+                          kSharedThreads);
+    __syncthreads();
+    const bool active = sample < a.samples;
+    const ContractT<Real>& b = a.book.contracts[a.base];
+    const PlanPtrs<Real> p = plan_of(a.book, b);
+    if (active) {
+        // bridge_payoffs' draw order: interval end, then the interval's days.
+        auto walk = [&](auto& n) {
+            Real x = Real(0), minimum = xinf(Real());
+            int i = 0;
+            for (int k = 0; k < b.bridge_count; ++k) {
+                const IntervalT<Real> iv = p.intervals[k];
+                const Real target = x + xfma(iv.diffusion, n.normal(), iv.drift);
+                for (; i < iv.end; ++i) {
+                    const DailyT<Real> d = p.daily[i];
+                    x = x + xfma(d.weight, target - x, d.width * n.normal());
+                    if (p.flags[i] & KGPU_STEP_KNOCK_IN) minimum = x < minimum ? x : minimum;
+                }
+                x = target;
+                if (p.flags[iv.end] & KGPU_STEP_KNOCK_IN) minimum = x < minimum ? x : minimum;
+                i = iv.end + 1;
+                const int s = slot[iv.end];
+                if (s >= 0) {
+                    lr[size_t(s) * kSharedThreads + tid] = x;
+                    mn[size_t(s) * kSharedThreads + tid] = minimum;
+                }
+            }
+        };
+        if (SOBOL) {
+            SobolSource<Real> n{high, a.sobol.nibbles, a.dims, 0, 0, 0};
+            n.start(uint64_t(sample));
+            walk(n);
+        } else {
+            PcgSource<Real> n;
+            n.start(a.seed, uint64_t(sample), a.dims);
+            walk(n);
+        }
+    }
+    // Lane phase: each thread reads only its own column of the records.
+    const Real* my_lr = lr + tid;
+    const Real* my_mn = mn + tid;
+    for (int l = 0; l < a.lanes; ++l) {
+        Real v = Real(0);
+        if (active) {
+            const ContractT<Real>& c = a.book.contracts[l];
+            const EventT<Real>* ev = a.book.events ? a.book.events + c.event_offset : nullptr;
+            Real cash = c.initial_cash;
+            bool out = false;
+            for (int e = 0; e < c.event_count; ++e) {
+                const EventT<Real>& E = ev[e];
+                const Real y = my_lr[size_t(slot[E.step]) * kSharedThreads];
+                const bool hit = E.has_knock_out && y >= E.knock_out;
+                cash += E.payment[int(y >= E.coupon_barrier) | (int(hit) << 1)];
+                if (hit) {
+                    out = true;
+                    break;
+                }
+            }
+            if (!out) {
+                const size_t m = size_t(slot[c.step_count - 1]) * kSharedThreads;
+                const Real y = my_lr[m];
+                const bool has = (c.flags & KGPU_C_HAS_KNOCK_IN) != 0;
+                const bool ki = (c.flags & KGPU_C_KNOCKED_IN) || (has && my_mn[m] < c.knock_in) ||
+                                ((c.flags & KGPU_C_EXPIRY_KNOCK_IN) && has && y < c.knock_in);
+                cash += autocallable_terminal(c, spot_at(c.spot, y), ki) * c.final_discount;
+            }
+            v = cash;
+        }
+        // Warp sums in the kernel's precision, CTA sums in FP64.
+        Real q = v * v;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            v += __shfl_down_sync(0xffffffffu, v, off);
+            q += __shfl_down_sync(0xffffffffu, q, off);
+        }
+        if (lane_id == 0) sums[(l & 31) * kSharedWarps + warp] = make_double2(double(v), double(q));
+        if ((l & 31) == 31 || l == a.lanes - 1) {
+            __syncthreads();
+            const int first = l & ~31;
+            if (tid <= l - first) {
+                double2 t = sums[tid * kSharedWarps];
+#pragma unroll
+                for (int w = 1; w < kSharedWarps; ++w) {
+                    const double2 u = sums[tid * kSharedWarps + w];
+                    t.x += u.x;
+                    t.y += u.y;
+                }
+                a.partials[size_t(first + tid) * a.ctas + blockIdx.x] = t;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One warp per lane adds the CTAs' sums in a fixed order.
+static __global__ void shared_merge_kernel(const double2* partials, int ctas, int lanes, double2* out) {
+    const int l = blockIdx.x;
+    if (l >= lanes) return;
+    const double2* row = partials + size_t(l) * ctas;
+    double s = 0.0, q = 0.0;
+    for (int i = threadIdx.x; i < ctas; i += 32) {
+        s += row[i].x;
+        q += row[i].y;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, off);
+        q += __shfl_down_sync(0xffffffffu, q, off);
+    }
+    if (threadIdx.x == 0) out[l] = make_double2(s, q);
+}
+
+}  // namespace kgpu

@@ -82,8 +82,28 @@ def _new_contract(payoff: int, spot: float) -> np.ndarray:
     return c
 
 
+_GRID_CACHE: dict = {}
+
+
 def _grid_steps(ctx: PricingContext, times: List[float]):
-    """Per-step records of a grid ending at `times` (ascending, > 0)."""
+    """Per-step records of a grid ending at `times` (ascending, > 0).  Under BSM the
+    records depend only on the flat parameters and the dates, so books whose notes share
+    a grid build it once (the cached array is read-only)."""
+    model = ctx.model
+    if isinstance(model, BlackScholesMertonParameters):
+        key = (model.rate, model.dividend, model.volatility, tuple(times))
+        cached = _GRID_CACHE.get(key)
+        if cached is None:
+            if len(_GRID_CACHE) >= 256:
+                _GRID_CACHE.clear()
+            cached = _grid_steps_uncached(ctx, times)
+            cached.flags.writeable = False
+            _GRID_CACHE[key] = cached
+        return cached
+    return _grid_steps_uncached(ctx, times)
+
+
+def _grid_steps_uncached(ctx: PricingContext, times: List[float]):
     model = ctx.model
     n = len(times)
     steps = np.zeros(n, STEP_DTYPE)
@@ -601,23 +621,19 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
     times = sorted(set([o.time for o in events] + (list(note.knock_in_times) if daily else [])
                        + [note.expiry]))
     times = [t for t in times if t > 0.0]
-    daily_set = set(note.knock_in_times) if daily else set()
-    event_at = {o.time: o for o in events}
     steps = _grid_steps(ctx, times)
+    grid = np.array(times)
     flags = np.zeros(len(times), np.uint8)
+    if daily:
+        flags[np.isin(grid, np.array(note.knock_in_times))] |= abi.STEP_KNOCK_IN
+    # sum over steps of |drift| + 20 diffusion, added in step order
+    excursion = (float(np.cumsum(np.abs(steps["drift"]) + 20.0 * steps["diffusion"])[-1])
+                 if bsm else 0.0)
     ev = np.zeros(len(events), EVENT_DTYPE)
-    excursion = 0.0
-    k = 0
-    for i, t in enumerate(times):
-        if bsm:
-            excursion += abs(steps[i]["drift"]) + 20.0 * steps[i]["diffusion"]
-        if t in daily_set:
-            flags[i] |= abi.STEP_KNOCK_IN
-        o = event_at.get(t)
-        if o is not None:
-            flags[i] |= abi.STEP_EVENT
-            ev[k] = cash_event(note, o, spot, rate, i)
-            k += 1
+    position = np.searchsorted(grid, [o.time for o in events])
+    for k, (o, i) in enumerate(zip(events, position)):
+        flags[i] |= abi.STEP_EVENT
+        ev[k] = cash_event(note, o, spot, rate, int(i))
     c = _new_contract(abi.PAYOFF_AUTOCALLABLE, ctx.spot)
     flag = 0
     if note.knock_in_level is not None:

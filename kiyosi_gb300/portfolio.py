@@ -39,7 +39,7 @@ lane of the same launch. `threshold_strips` still describes them, for the oracle
 restatement of the strip sums.
 """
 import math
-from dataclasses import dataclass, field, replace
+from dataclasses import dataclass, field, fields, replace
 from fractions import Fraction
 from typing import Dict, List, Optional, Sequence, Tuple
 
@@ -107,15 +107,11 @@ def shared_lane(note: AutocallableNote, ctx: PricingContext, index: int) -> Opti
         return Lane(index, note, contract, template.steps, observe.astype(np.uint8),
                     [(int(e["step"]), tuple(e.tolist())) for e in template.events], False, False)
     maturity_on_grid = times[-1] == note.expiry
-    if not maturity_on_grid:
-        times.append(note.expiry)
-    steps = plans._grid_steps(ctx, times)
-    observe = np.array([abi.STEP_KNOCK_IN if t in monitored else 0 for t in times], np.uint8)
-    position = {t: i for i, t in enumerate(times)}
-    rate = ctx.model.rate
-    cash = [(position[o.time], plans.cash_event(note, o, ctx.spot, rate, position[o.time]))
-            for o in events]
-    return Lane(index, note, contract, steps, observe, cash, True, maturity_on_grid)
+    # With every event on a monitoring date or expiry, the scalar schedule (event dates,
+    # monitoring dates and expiry) is this grid, step for step.
+    observe = (template.flags & abi.STEP_KNOCK_IN).astype(np.uint8)
+    cash = [(int(e["step"]), tuple(e.tolist())) for e in template.events]
+    return Lane(index, note, contract, template.steps, observe, cash, True, maturity_on_grid)
 
 
 def _grid_key(lane: Lane):
@@ -248,9 +244,9 @@ def portfolio_coupon(note: AutocallableNote) -> float:
 def _without_coupon(note: AutocallableNote):
     """Every term but the portfolio coupon, with whether knock-in changes the payoff
     (portfolio_family_key and shares_portfolio_terms, autocallable.rs:1188-1300)."""
-    bare = (replace(note, period_coupon=0.0) if _is_phoenix(note)
-            else replace(note, maturity_coupon_rate=0.0))
-    return bare, note.knock_in_affects_payoff()
+    coupon = "period_coupon" if _is_phoenix(note) else "maturity_coupon_rate"
+    return (tuple(getattr(note, f.name) for f in fields(note) if f.name != coupon),
+            note.knock_in_affects_payoff())
 
 
 @dataclass
@@ -438,10 +434,14 @@ def plan_book(notes: Sequence[AutocallableNote], ctx: PricingContext, shared_gri
 
 def price_many(engine, notes: Sequence[AutocallableNote], ctx: PricingContext,
                shared_grid: bool) -> List[float]:
-    """Quotes of `notes` in input order, every sampled note in one launch."""
+    """Quotes of `notes` in input order.  Scalar quotes share one launch; each group's
+    lanes go to the engine's path-major schedule when it has one (one path per sample
+    settles every lane, kgpu's KGPU_SCHEDULE_SHARED_GRID), else into the same launch as
+    per-lane contracts (identical estimates, each lane re-walking the path)."""
     book = plan_book(notes, ctx, shared_grid)
     prices: Dict[int, float] = {}
     pending = list(range(len(book.groups)))
+    run_group = getattr(engine, "_run_group", None)
     first = True
     while first or pending:
         indices, batch = [], []
@@ -451,7 +451,13 @@ def price_many(engine, notes: Sequence[AutocallableNote], ctx: PricingContext,
                 batch.append(p)
         for g in pending:
             lanes = book.groups[g].simulated_lanes()
-            for lane, p in zip(lanes, lane_plans(lanes, ctx.spot)):
+            group_plans = lane_plans(lanes, ctx.spot)
+            estimates = run_group(ctx, group_plans) if run_group is not None else None
+            if estimates is not None:
+                for lane, e in zip(lanes, estimates):
+                    prices[lane.index] = e.price
+                continue
+            for lane, p in zip(lanes, group_plans):
                 indices.append(lane.index)
                 batch.append(p)
         if batch:

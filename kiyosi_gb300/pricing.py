@@ -23,7 +23,8 @@ PSEUDO_RANDOM = "pseudo_random"
 SOBOL = "sobol"
 _SAMPLING = {PSEUDO_RANDOM: abi.SAMPLING_PSEUDO_RANDOM, SOBOL: abi.SAMPLING_SOBOL}
 _PRECISION = {"fp64": abi.PRECISION_FP64, "fp32": abi.PRECISION_FP32}
-_SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT}
+_SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT,
+             "shared_grid": abi.SCHEDULE_SHARED_GRID}
 Z95 = 1.959963984540054
 
 
@@ -126,7 +127,15 @@ class _MonteCarloEngine:
                             schedule=_SCHEDULE[self.schedule], tile_paths=self.tile_paths,
                             seed=seed)
 
-    def _run(self, ctx: PricingContext, contract_plans, path_counts=None, cancel=None):
+    def _run_group(self, ctx: PricingContext, lane_plans):
+        """Prices the lanes of one shared daily grid with the path-major schedule (one
+        path per sample settles every lane); None when the engine pairs antithetic
+        samples, which that schedule does not."""
+        if self.antithetic:
+            return None
+        return self._run(ctx, lane_plans, schedule=abi.SCHEDULE_SHARED_GRID)
+
+    def _run(self, ctx: PricingContext, contract_plans, path_counts=None, cancel=None, schedule=None):
         """Prices plans (Known or ContractPlan) through kgpu_price_book."""
         seed = _resolve_seed(self.seed)
         results = [None] * len(contract_plans)
@@ -154,7 +163,9 @@ class _MonteCarloEngine:
             book = packed.struct()
             flag = None if cancel is None else C.byref(cancel)
             settings = self._settings(seed)
-            if self.tuning == "auto" and self.schedule == "persistent":
+            if schedule is not None:
+                settings.schedule = schedule
+            elif self.tuning == "auto" and self.schedule == "persistent":
                 from . import autotune
                 shape, _ = autotune.tune(native, ctx, packed, settings)
                 settings = autotune.apply(settings, shape)

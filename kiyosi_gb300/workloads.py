@@ -7,6 +7,8 @@ involved).  Tests build reduced-size versions with the same code.
 * heston_asian_c3() / heston_context(): Heston arithmetic-average Asian call, 252 steps.
 * lv_surface() / lv_book(): book of snowball/phoenix notes under local volatility.
 * heston_context() with an American put for least-squares Monte Carlo.
+* shared_grid_book() / c2_context(): a book of snowball and Phoenix notes on one daily
+  grid under BSM, priced with price_many on the shared grid.
 """
 import math
 
@@ -94,3 +96,38 @@ def european():
     """S0 = K = 100, r = 0.05, q = 0.02, sigma = 0.2, T = 1y (the reference's
     calibration inputs)."""
     return bsm(), EuropeanOption("call", 100.0, 1.0)
+
+
+def shared_grid_book(coupons=32, steps=504, years=2.0, months=24):
+    """A dealer book on one underlying and one daily grid: 128 term sets (snowball or
+    Phoenix; 6, 12, 18 or 24 monthly observations, each maturity a monitoring date;
+    knock-out 100/102/103/105%; knock-in 70/75/80/85%) with `coupons` coupons each,
+    from 5% to 25%.  A snowball's coupon is both its knock-out accrual and its maturity
+    coupon, so every snowball is simulated; Phoenix notes of one term set differ only in
+    their period coupon and form coupon families."""
+    dt = years / steps
+    per = steps // months
+    times = [dt * (i + 1) for i in range(steps)]
+    notes = []
+    for phoenix in (False, True):
+        for count in (6, 12, 18, 24):
+            dates = [times[per * (m + 1) - 1] for m in range(count)]
+            daily = times[:per * count]
+            for ko in (100.0, 102.0, 103.0, 105.0):
+                for ki in (70.0, 75.0, 80.0, 85.0):
+                    for j in range(coupons):
+                        coupon = 0.05 + 0.20 * j / max(coupons - 1, 1)
+                        if phoenix:
+                            obs = [Observation(t, ko, ki, 0.0) for t in dates]
+                            note = AutocallableNote(
+                                initial_spot=100.0, expiry=dates[-1], observations=obs,
+                                knock_in_level=ki, knock_in_times=daily, upper_strike=100.0,
+                                lower_strike=0.0, period_coupon=coupon / 12.0)
+                        else:
+                            obs = [Observation(t, ko, None, coupon) for t in dates]
+                            note = AutocallableNote(
+                                initial_spot=100.0, expiry=dates[-1], observations=obs,
+                                knock_in_level=ki, knock_in_times=daily, upper_strike=100.0,
+                                lower_strike=0.0, maturity_coupon_rate=coupon)
+                        notes.append(note)
+    return notes

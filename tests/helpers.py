@@ -12,7 +12,8 @@ from kiyosi_gb300.market import (BlackScholesMertonParameters, HestonParameters,
                                  LocalVolatilitySurface, PricingContext)
 
 PRECISION = {"fp64": abi.PRECISION_FP64, "fp32": abi.PRECISION_FP32}
-SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT}
+SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT,
+             "shared_grid": abi.SCHEDULE_SHARED_GRID}
 
 
 def settings(paths, seed, sobol=False, antithetic=False, precision="fp64", schedule="plain",

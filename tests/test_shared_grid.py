@@ -243,14 +243,51 @@ def test_gpu_lanes_match_group_loop(native, sampling):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("sobol", [False, True])
+def test_gpu_path_major_schedule_matches_lanes(native, sobol):
+    """KGPU_SCHEDULE_SHARED_GRID (one path per sample settles every lane) against the
+    per-lane plain schedule and the oracle's loop: FP64 to rounding, FP32 within half a
+    sample error."""
+    from kiyosi_gb300 import abi
+    from kiyosi_gb300.errors import KiyosiError
+    ctx = _ctx()
+    notes = ([snowball(c) for c in (0.02, 0.08, -0.01)] + [snowball(knock_in=85.0),
+             snowball(knock_out=(103.0,) * 3), phoenix(), phoenix(0.03),
+             snowball(dates=[_DATES[0], _DATES[1]], knock_out=(110.0, 108.0))] * 5)
+    lanes = [portfolio.shared_lane(n, ctx, i) for i, n in enumerate(notes)]
+    packed = pack(portfolio.lane_plans(lanes, ctx.spot))
+    paths = 1 << 14 if sobol else (1 << 14) + 77  # a ragged last CTA for pseudo-random
+    plain = gpu_price(native, ctx, packed, settings(paths, 13, sobol=sobol))
+    fast = gpu_price(native, ctx, packed, settings(paths, 13, sobol=sobol, schedule="shared_grid"))
+    loop, _ = loader.price_shared_group(ctx, packed, settings(paths, 13, sobol=sobol))
+    for f, p, r in zip(fast, plain, loop):
+        assert abs(f.price - p.price) <= 1e-12 * max(1.0, abs(p.price)), (f.price, p.price)
+        assert abs(f.price - r) <= 1e-11 * max(1.0, abs(r)), (f.price, r)
+        assert abs(f.sample_error - p.sample_error) <= 1e-6 * p.sample_error
+    fast32 = gpu_price(native, ctx, packed, settings(paths, 13, sobol=sobol, precision="fp32",
+                                                      schedule="shared_grid"))
+    for f, p in zip(fast32, plain):
+        assert abs(f.price - p.price) <= 0.5 * max(p.sample_error, 1e-4), (f.price, p.price)
+    with pytest.raises(KiyosiError):
+        gpu_price(native, ctx, packed, settings(paths, 13, antithetic=True, schedule="shared_grid"))
+    # lanes of two different grids are refused
+    other = portfolio.shared_lane(snowball(dates=[_DATES[0], _year(datetime.date(2025, 2, 10))],
+                                           knock_out=(110.0, 108.0)), ctx, 0)
+    bad = pack(portfolio.lane_plans([lanes[0]], ctx.spot) + portfolio.lane_plans([other], ctx.spot))
+    with pytest.raises(KiyosiError):
+        gpu_price(native, ctx, bad, settings(1024, 1, schedule="shared_grid"))
+
+
+@pytest.mark.gpu
 def test_gpu_engine_shared_grid_book(native):
     from kiyosi_gb300.pricing import MonteCarloAutocallableEngine
     ctx = _ctx()
     notes = [snowball(c) for c in (0.02, 0.08, -0.01, 0.02, 0.04)] + [
         snowball(knock_out=(k,) * 3) for k in (103.0, 106.0, 101.0)] + [phoenix(), phoenix(0.05)]
-    for schedule in ("plain", "persistent"):
-        engine = MonteCarloAutocallableEngine(path_count=1 << 14, seed=21, schedule=schedule)
+    for antithetic in (False, True):  # path-major schedule, then per-lane contracts
+        engine = MonteCarloAutocallableEngine(path_count=1 << 14, seed=21, antithetic=antithetic)
         got = engine.price_many_on_shared_grid(notes, ctx)
-        expected = portfolio.price_many(OracleBookEngine(1 << 14, 21), notes, ctx, True)
+        expected = portfolio.price_many(OracleBookEngine(1 << 14, 21, antithetic=antithetic),
+                                        notes, ctx, True)
         for g, r in zip(got, expected):
-            assert abs(g - r) <= 1e-11 * max(1.0, abs(r)), (schedule, g, r)
+            assert abs(g - r) <= 1e-11 * max(1.0, abs(r)), (antithetic, g, r)
