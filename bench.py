@@ -511,6 +511,113 @@ def run_workload(args, name):
     print(json.dumps(line), flush=True)
 
 
+def run_shared_grid(args):
+    """price_many on a shared daily grid (autocallable/portfolio.rs): a 4096-note book of
+    snowball and Phoenix notes on one 504-step daily grid under BSM, 2^16 PCG32 paths.
+    The group's lanes go through the path-major schedule: one thread per path walks the
+    grid once and settles every lane from its per-date records.  Beside it:
+    * the per-lane layout (each lane re-walks the path; FP32 persistent);
+    * FP64 parity;
+    * the whole engine call from host notes;
+    * the reference's multi-lane CPU algorithm (coupon families and threshold strips,
+      restated in the FP64 oracle) on a bounded sample of paths."""
+    from kiyosi_gb300 import _native, abi, plans, portfolio, workloads
+    from kiyosi_gb300.pricing import MonteCarloAutocallableEngine
+    from oracle import loader
+    native = _native.context(0)
+    ctx = workloads.c2_context()
+    notes = workloads.shared_grid_book()
+    paths, seed = 1 << 16, 42
+    t0 = time.perf_counter()
+    book = portfolio.plan_book(notes, ctx, True)
+    lanes = [lane for g in book.groups for lane in g.simulated_lanes()]
+    builder = plans.BookBuilder()
+    for p in portfolio.lane_plans(lanes, ctx.spot):
+        builder.add(p)
+    packed = builder.build()
+    plan_s = time.perf_counter() - t0
+    assert len(book.groups) == 1 and not book.scalar
+
+    def cfg(precision, schedule):
+        return abi.Settings(path_count=paths, sampling=abi.SAMPLING_PSEUDO_RANDOM, antithetic=0,
+                            precision=precision, schedule=schedule, seed=seed, **TUNING)
+
+    fast32 = cfg(abi.PRECISION_FP32, abi.SCHEDULE_SHARED_GRID)
+    for _ in range(args.warmup):
+        _host_pricing(native, ctx, packed, fast32)
+    kernel, path, walls, launches = [], [], [], 0
+    with Clocks() as clocks:
+        for _ in range(args.steps):
+            est32, k, pk, w = _host_pricing(native, ctx, packed, fast32)
+            kernel.append(k)
+            path.append(pk)
+            walls.append(w)
+            launches += native.last_launches
+    ms = statistics.median(kernel)
+    est64, k64, _, _ = _host_pricing(native, ctx, packed, cfg(abi.PRECISION_FP64, abi.SCHEDULE_SHARED_GRID))
+    # the first 64 lanes on the per-lane FP64 plain schedule
+    first = type(packed)(packed.contracts[:64].copy(), packed.steps, packed.flags, packed.events,
+                         packed.intervals, packed.daily)
+    lanes64, _, _, _ = _host_pricing(native, ctx, first, cfg(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN))
+    per_lane = [_host_pricing(native, ctx, packed, cfg(abi.PRECISION_FP32, abi.SCHEDULE_PERSISTENT))[1]
+                for _ in range(2)]
+    worst_fp64 = max(abs(a.price - b.price) / max(abs(b.price), 1.0) for a, b in zip(est64, lanes64))
+    worst_se = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(est32, est64))
+    # The whole engine call from host notes (planning, staging, launch, results).
+    engine = MonteCarloAutocallableEngine(path_count=paths, seed=seed, precision="fp32")
+    engine.price_many_on_shared_grid(notes, ctx)
+    e2e = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        engine.price_many_on_shared_grid(notes, ctx)
+        e2e.append(time.perf_counter() - t0)
+    # CPU: the reference's multi-lane loop with its threshold strips, all 2^16 paths.
+    order, strips = portfolio.threshold_strips(lanes, ctx.spot)
+    cpu_book = plans.BookBuilder()
+    for p in portfolio.lane_plans([lanes[i] for i in order], ctx.spot):
+        cpu_book.add(p)
+    cpu_paths = paths
+    threads = os.cpu_count() or 1
+    s_cpu = abi.Settings(path_count=cpu_paths, sampling=abi.SAMPLING_PSEUDO_RANDOM, antithetic=0,
+                         precision=abi.PRECISION_FP64, schedule=abi.SCHEDULE_PLAIN, seed=seed)
+    t0 = time.perf_counter()
+    loader.price_shared_group(ctx, cpu_book.build(), s_cpu,
+                              [None if st is None else (st[0], st[1]) for st in strips], threads=threads)
+    cpu_s = (time.perf_counter() - t0) * (paths / cpu_paths)
+    lane_path_steps = sum(e.path_steps for e in est32)
+    line = {
+        "metric": "notes priced per second (price_many on a shared daily grid)",
+        "value": len(notes) / (ms / 1e3), "unit": "notes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded draws; benchmark contract parameters)",
+        "config": {"workload": "book of 4096 snowball/Phoenix notes on one 504-step daily grid, BSM, "
+                               "2^16 PCG32 paths, coupon families interpolated",
+                   "notes": len(notes), "simulated_lanes": len(lanes), "group_steps": int(packed.contracts["step_count"].max()),
+                   "precision": "fp32", "schedule": "shared_grid (path-major)",
+                   "l2": "per-path records live in shared memory (no flush)"},
+        "e2e": {"value": len(notes) / statistics.median(e2e), "unit": "notes/s",
+                "h2d_bytes_per_step": int(packed.steps.nbytes + packed.flags.nbytes + packed.events.nbytes
+                                          + packed.contracts.nbytes + packed.intervals.nbytes
+                                          + (packed.daily.nbytes if packed.daily is not None else 0)),
+                "d2h_bytes_per_step": int(len(lanes) * C.sizeof(abi.Estimate)),
+                "includes": "host planning of the book (Python), staging, launch, results"},
+        "host_planning_s": plan_s,
+        "gpu_launches": launches, "clocks": clocks.summary(),
+        "path_kernel_ms": statistics.median(path),
+        "lane_equivalent_path_steps_per_s": lane_path_steps / (ms / 1e3),
+        "per_lane_layout": {"ms": statistics.median(per_lane), "schedule": "persistent fp32, each lane re-walks the path",
+                            "speedup_path_major": statistics.median(per_lane) / ms},
+        "fp64_path_major_ms": k64,
+        "parity": {"fp64_path_major_vs_fp64_lanes_max_rel": worst_fp64, "lanes_checked": 64,
+                   "fp32_vs_fp64_max_in_se": worst_se},
+        "cpu_baseline": {"value": len(notes) / cpu_s, "unit": "notes/s", "cores": threads, "kind": "port",
+                         "sample": "the reference's multi-lane path loop with coupon families and threshold "
+                                   f"strips (FP64 oracle), {cpu_paths} of {paths} paths"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_lsmc(args):
     """American put under Heston, 50 exercise dates x 5 Euler substeps, judged by the
     Heston ADI price.  Two comparisons of the polynomial LSMC (the reference's method)
@@ -628,15 +735,19 @@ def main():
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")
     ap.add_argument("--refill", type=int, default=0, help="units between lane refills (0 = 16)")
     ap.add_argument("--workload", default="snowball",
-                    choices=["snowball", "european", "heston-asian", "lv-book", "lsmc", "all"],
+                    choices=["snowball", "european", "heston-asian", "lv-book", "lsmc", "shared-grid",
+                             "all"],
                     help="benchmark configuration (default: the snowball headline)")
     args = ap.parse_args()
     TUNING.update(tile_paths=args.tile, ctas_per_sm=args.ctas_per_sm, refill=args.refill)
     if args.workload != "snowball" and args.impl == "ours" and not args.kernel_only:
-        names = ["european", "heston-asian", "lv-book", "lsmc"] if args.workload == "all" else [args.workload]
+        names = (["european", "heston-asian", "lv-book", "shared-grid", "lsmc"] if args.workload == "all"
+                 else [args.workload])
         for name in names:
             if name == "lsmc":
                 run_lsmc(args)
+            elif name == "shared-grid":
+                run_shared_grid(args)
             else:
                 run_workload(args, name)
         return

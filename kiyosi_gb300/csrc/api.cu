@@ -763,12 +763,17 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
 }
 
 // KGPU_SCHEDULE_SHARED_GRID: the lanes of one shared daily grid on one path per sample
-// (portfolio.rs:1275-1439), path-major.
-template <class Real>
-kgpu_status run_shared(Call& k, const DevBook<Real>& db, int& launches) {
+// (portfolio.rs:1275-1439), path-major.  plan_shared checks the lanes on the host (before
+// the call's timed region) and numbers the action dates; run_shared launches.
+struct SharedPlan {
+    int base = 0;
+    int slots = 0;
+    std::vector<int16_t> slot;
+};
+
+kgpu_status plan_shared(Call& k, SharedPlan* plan) {
     kgpu_context* ctx = k.ctx;
     const kgpu_book& b = *k.book;
-    const kgpu_settings& s = k.s;
     const int n = b.contract_count;
     int base = 0;
     for (int i = 0; i < n; ++i)
@@ -805,6 +810,21 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, int& launches) {
                 return fail(ctx, KGPU_INVALID_INPUT, "lane %d: event %d is not on an interval end", i, e);
         if (!take(c.step_count - 1)) return fail(ctx, KGPU_INVALID_INPUT, "lane %d: maturity is not an interval end", i);
     }
+    plan->base = base;
+    plan->slots = slots;
+    plan->slot = std::move(slot);
+    return KGPU_OK;
+}
+
+template <class Real>
+kgpu_status run_shared(Call& k, const DevBook<Real>& db, const SharedPlan& plan, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const kgpu_book& b = *k.book;
+    const kgpu_settings& s = k.s;
+    const int n = b.contract_count;
+    const int base = plan.base, slots = plan.slots;
+    const std::vector<int16_t>& slot = plan.slot;
+    const int steps = b.contracts[base].step_count;
     const size_t smem = shared_grid_smem_bytes(sizeof(Real), slots, steps, k.sobol);
     if (smem > 227 * 1024)
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "%d action dates exceed the shared-grid kernel's shared memory",
@@ -830,11 +850,18 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, int& launches) {
     a.partials = static_cast<double2*>(ctx->partials.ptr);
     a.ctas = ctas;
     CUDA_TRY(ctx, path_kernel_begin(ctx));
+    // Lane chunks: enough CTAs for about four waves of resident CTAs, each chunk at
+    // least 16 lanes.
+    const int resident = (std::is_same<Real, double>::value ? shared_grid_occupancy_fp64(k.sobol, smem)
+                                                            : shared_grid_occupancy_fp32(k.sobol, smem)) *
+                         ctx->sm_count;
+    const int chunks = int(std::max<int64_t>(
+        1, std::min<int64_t>({(n + 15) / 16, (4LL * resident + ctas - 1) / ctas, int64_t(65535)})));
     cudaError_t launched;
     if constexpr (std::is_same<Real, double>::value)
-        launched = launch_shared_grid_fp64(k.sobol, ctas, smem, ctx->stream, a);
+        launched = launch_shared_grid_fp64(k.sobol, ctas, chunks, smem, ctx->stream, a);
     else
-        launched = launch_shared_grid_fp32(k.sobol, ctas, smem, ctx->stream, a);
+        launched = launch_shared_grid_fp32(k.sobol, ctas, chunks, smem, ctx->stream, a);
     CUDA_TRY(ctx, launched);
     CUDA_TRY(ctx, path_kernel_end(ctx));
     CUDA_TRY(ctx, launch_shared_merge(a.partials, ctas, n, static_cast<double2*>(ctx->merged.ptr), ctx->stream));
@@ -861,6 +888,11 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, int& launches) {
 template <class Real>
 kgpu_status run_book(Call& k) {
     kgpu_context* ctx = k.ctx;
+    SharedPlan shared;
+    if (k.s.schedule == KGPU_SCHEDULE_SHARED_GRID) {
+        kgpu_status planned = plan_shared(k, &shared);
+        if (planned) return planned;
+    }
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     ctx->path_events_used = 0;
     ctx->last_path_kernel_ms = 0.0;
@@ -869,7 +901,7 @@ kgpu_status run_book(Call& k) {
     if (st) return st;
     int launches = std::is_same<Real, float>::value ? 2 : 1;
     st = k.s.schedule == KGPU_SCHEDULE_PERSISTENT    ? run_persistent<Real>(k, db, launches)
-         : k.s.schedule == KGPU_SCHEDULE_SHARED_GRID ? run_shared<Real>(k, db, launches)
+         : k.s.schedule == KGPU_SCHEDULE_SHARED_GRID ? run_shared<Real>(k, db, shared, launches)
                                                      : run_plain<Real>(k, db, launches);
     float ms = 0;
     if (cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop) == cudaSuccess) ctx->last_kernel_ms = ms;

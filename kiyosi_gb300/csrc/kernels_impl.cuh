@@ -147,17 +147,25 @@ cudaError_t KGPU_CAT(launch_sobol_points_, PRECISION)(const SobolTables& t, int 
 }
 
 template <bool SOBOL>
-static cudaError_t shared_one(int ctas, size_t smem, cudaStream_t s, const SharedArgs<REAL>& a) {
+static cudaError_t shared_one(int ctas, int chunks, size_t smem, cudaStream_t s, const SharedArgs<REAL>& a) {
     auto k = shared_grid_kernel<REAL, SOBOL>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
-    k<<<ctas, kSharedThreads, smem, s>>>(a);
+    k<<<dim3(unsigned(ctas), unsigned(chunks)), kSharedThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t KGPU_CAT(launch_shared_grid_, PRECISION)(bool sobol, int ctas, size_t smem, cudaStream_t s,
-                                                     const SharedArgs<REAL>& a) {
-    return sobol ? shared_one<true>(ctas, smem, s, a) : shared_one<false>(ctas, smem, s, a);
+cudaError_t KGPU_CAT(launch_shared_grid_, PRECISION)(bool sobol, int ctas, int chunks, size_t smem,
+                                                     cudaStream_t s, const SharedArgs<REAL>& a) {
+    return sobol ? shared_one<true>(ctas, chunks, smem, s, a) : shared_one<false>(ctas, chunks, smem, s, a);
+}
+
+int KGPU_CAT(shared_grid_occupancy_, PRECISION)(bool sobol, size_t smem) {
+    auto k = sobol ? shared_grid_kernel<REAL, true> : shared_grid_kernel<REAL, false>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kSharedThreads, smem) != cudaSuccess) return 1;
+    return n > 0 ? n : 1;
 }
 
 #if !KGPU_FP32_UNIT

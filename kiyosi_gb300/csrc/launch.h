@@ -45,10 +45,13 @@ cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, Ev
                                        cudaStream_t s);
 
 // The lanes of one shared daily grid, path-major, and the merge of their CTA sums.
-cudaError_t launch_shared_grid_fp64(bool sobol, int ctas, size_t smem, cudaStream_t s,
+// `ctas` path tiles x `chunks` lane chunks.
+cudaError_t launch_shared_grid_fp64(bool sobol, int ctas, int chunks, size_t smem, cudaStream_t s,
                                     const SharedArgs<double>& a);
-cudaError_t launch_shared_grid_fp32(bool sobol, int ctas, size_t smem, cudaStream_t s,
+cudaError_t launch_shared_grid_fp32(bool sobol, int ctas, int chunks, size_t smem, cudaStream_t s,
                                     const SharedArgs<float>& a);
+int shared_grid_occupancy_fp64(bool sobol, size_t smem);
+int shared_grid_occupancy_fp32(bool sobol, size_t smem);
 cudaError_t launch_shared_merge(const double2* partials, int ctas, int lanes, double2* out, cudaStream_t s);
 
 // Raw streams (kgpu_pcg_words, kgpu_pcg_normals, kgpu_sobol_points).

@@ -16,6 +16,9 @@
 //   the same, so the outcome is the same.
 // * Reduction. Each CTA writes the lanes' sums and sums of squares. The merge kernel adds
 //   the CTAs in a fixed order.
+// * Grid. CTAs are (path tile) x (lane chunk): every chunk re-walks its tile's paths,
+//   which is cheap next to the lanes, so that enough warps are resident to hide the
+//   latency of the lane walk.
 //
 // Cost is paths x (grid steps + lane events), against paths x lanes x grid steps when
 // each lane re-simulates the path.
@@ -102,27 +105,33 @@ __global__ void __launch_bounds__(kSharedThreads) shared_grid_kernel(SharedArgs<
             walk(n);
         }
     }
-    // Lane phase: each thread reads only its own column of the records.
+    // Lane phase over this CTA's chunk of lanes (blockIdx.y); each thread reads only its
+    // own column of the records.
     const Real* my_lr = lr + tid;
     const Real* my_mn = mn + tid;
-    for (int l = 0; l < a.lanes; ++l) {
+    const int per_chunk = (a.lanes + int(gridDim.y) - 1) / int(gridDim.y);
+    const int l_begin = int(blockIdx.y) * per_chunk;
+    const int l_end = min(a.lanes, l_begin + per_chunk);
+    for (int l = l_begin; l < l_end; ++l) {
         Real v = Real(0);
         if (active) {
             const ContractT<Real>& c = a.book.contracts[l];
             const EventT<Real>* ev = a.book.events ? a.book.events + c.event_offset : nullptr;
             Real cash = c.initial_cash;
-            bool out = false;
+            // A warp walks a lane's events until its last path knocks out, so the walk
+            // runs to the end with the knocked-out paths masked: the loads of successive
+            // events are independent and overlap.
+            bool live = true;
+#pragma unroll 4
             for (int e = 0; e < c.event_count; ++e) {
                 const EventT<Real>& E = ev[e];
                 const Real y = my_lr[size_t(slot[E.step]) * kSharedThreads];
                 const bool hit = E.has_knock_out && y >= E.knock_out;
-                cash += E.payment[int(y >= E.coupon_barrier) | (int(hit) << 1)];
-                if (hit) {
-                    out = true;
-                    break;
-                }
+                const Real pay = E.payment[int(y >= E.coupon_barrier) | (int(hit) << 1)];
+                if (live) cash += pay;
+                live = live && !hit;
             }
-            if (!out) {
+            if (live) {
                 const size_t m = size_t(slot[c.step_count - 1]) * kSharedThreads;
                 const Real y = my_lr[m];
                 const bool has = (c.flags & KGPU_C_HAS_KNOCK_IN) != 0;
@@ -139,10 +148,11 @@ __global__ void __launch_bounds__(kSharedThreads) shared_grid_kernel(SharedArgs<
             v += __shfl_down_sync(0xffffffffu, v, off);
             q += __shfl_down_sync(0xffffffffu, q, off);
         }
-        if (lane_id == 0) sums[(l & 31) * kSharedWarps + warp] = make_double2(double(v), double(q));
-        if ((l & 31) == 31 || l == a.lanes - 1) {
+        const int j = l - l_begin;
+        if (lane_id == 0) sums[(j & 31) * kSharedWarps + warp] = make_double2(double(v), double(q));
+        if ((j & 31) == 31 || l == l_end - 1) {
             __syncthreads();
-            const int first = l & ~31;
+            const int first = l - (j & 31);
             if (tid <= l - first) {
                 double2 t = sums[tid * kSharedWarps];
 #pragma unroll

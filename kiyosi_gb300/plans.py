@@ -582,6 +582,39 @@ def asian(option: AsianOption, ctx: PricingContext, step_count: Optional[int] = 
     return ContractPlan(c, _grid_steps(ctx, times), flags)
 
 
+_EVENT_GRID_CACHE: dict = {}
+
+
+def _event_grid(ctx: PricingContext, event_times, knock_in_times, expiry):
+    """future_event_times (instruments/autocallable/pricing.rs:70-106): the merged grid
+    of event dates, daily knock-in dates (None when not monitored) and expiry, with its
+    step records, knock-in flags and excursion (the sum over steps of |drift| + 20
+    diffusion, added in step order).  Notes of one schedule share the result."""
+    model = ctx.model
+    bsm = isinstance(model, BlackScholesMertonParameters)
+    key = (type(model), model.rate, model.dividend, getattr(model, "volatility", None), event_times,
+           knock_in_times, expiry) if bsm else None
+    hit = _EVENT_GRID_CACHE.get(key) if key is not None else None
+    if hit is not None:
+        return hit
+    times = sorted(set(list(event_times) + (list(knock_in_times) if knock_in_times is not None else [])
+                       + [expiry]))
+    times = [t for t in times if t > 0.0]
+    steps = _grid_steps(ctx, times)
+    flags = np.zeros(len(times), np.uint8)
+    if knock_in_times is not None:
+        flags[np.isin(np.array(times), np.array(knock_in_times))] |= abi.STEP_KNOCK_IN
+    excursion = (float(np.cumsum(np.abs(steps["drift"]) + 20.0 * steps["diffusion"])[-1])
+                 if bsm else 0.0)
+    out = (times, steps, flags, excursion)
+    if key is not None:
+        if len(_EVENT_GRID_CACHE) >= 256:
+            _EVENT_GRID_CACHE.clear()
+        flags.flags.writeable = False
+        _EVENT_GRID_CACHE[key] = out
+    return out
+
+
 def cash_event(note: AutocallableNote, o, spot: float, rate: float, step: int):
     """CashEvent::new and discounted_payment (autocallable.rs:532-562): one observation's
     log-space knock-out and coupon thresholds and its four discounted payments, indexed
@@ -616,19 +649,12 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
     expiry_knock_in = note.knock_in_level is not None and (
         note.knock_in_times is None or (len(note.knock_in_times) > 0
                                         and note.knock_in_times[-1] == note.expiry))
-    # future_event_times (instruments/autocallable/pricing.rs:70-106)
     events = [o for o in note.observations if o.time > 0.0]
-    times = sorted(set([o.time for o in events] + (list(note.knock_in_times) if daily else [])
-                       + [note.expiry]))
-    times = [t for t in times if t > 0.0]
-    steps = _grid_steps(ctx, times)
+    times, steps, ki_flags, excursion = _event_grid(ctx, tuple(o.time for o in events),
+                                                    note.knock_in_times if daily else None,
+                                                    note.expiry)
     grid = np.array(times)
-    flags = np.zeros(len(times), np.uint8)
-    if daily:
-        flags[np.isin(grid, np.array(note.knock_in_times))] |= abi.STEP_KNOCK_IN
-    # sum over steps of |drift| + 20 diffusion, added in step order
-    excursion = (float(np.cumsum(np.abs(steps["drift"]) + 20.0 * steps["diffusion"])[-1])
-                 if bsm else 0.0)
+    flags = ki_flags.copy()
     ev = np.zeros(len(events), EVENT_DTYPE)
     position = np.searchsorted(grid, [o.time for o in events])
     for k, (o, i) in enumerate(zip(events, position)):
