@@ -378,6 +378,23 @@ def run_kernel_only(args):
                           "wall_ms": out.wall_ms, "path_store_ms": out.path_store_ms,
                           "regression_ms": out.regression_ms, "launches": native.last_launches}))
         return
+    if args.kernel_only == "shared-grid":
+        # the shared-grid book's lanes on the path-major FP32 schedule
+        from kiyosi_gb300 import plans, portfolio, workloads
+        ctx = workloads.c2_context()
+        book_plan = portfolio.plan_book(workloads.shared_grid_book(), ctx, True)
+        lanes = [lane for g in book_plan.groups for lane in g.simulated_lanes()]
+        builder = plans.BookBuilder()
+        for p in portfolio.lane_plans(lanes, ctx.spot):
+            builder.add(p)
+        packed = builder.build()
+        s = abi.Settings(path_count=args.paths, sampling=abi.SAMPLING_PSEUDO_RANDOM, antithetic=0,
+                         precision=abi.PRECISION_FP32, schedule=abi.SCHEDULE_SHARED_GRID, seed=42)
+        for _ in range(args.warmup + args.steps):
+            est, k, pk, _ = _host_pricing(native, ctx, packed, s)
+        print(json.dumps({"arm": args.kernel_only, "paths": args.paths, "lanes": len(lanes),
+                          "first_price": est[0].price, "kernel_ms": k, "path_kernel_ms": pk}))
+        return
     ctx, packed = packed_plan()
     model = ctx.kgpu_model()
     book = packed.struct()
@@ -729,7 +746,7 @@ def main():
                     help="LSMC network: in-the-money samples trained on per date (0: all)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the kernel's default launch shape instead of the autotuner's")
-    ap.add_argument("--kernel-only", choices=["fp32", "fp64", "lsmc-poly", "lsmc-mlp"],
+    ap.add_argument("--kernel-only", choices=["fp32", "fp64", "lsmc-poly", "lsmc-mlp", "shared-grid"],
                     help="run only the device-resident pricing of one arm (for profilers)")
     ap.add_argument("--tile", type=int, default=0, help="persistent tile paths (0 = default)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")

@@ -626,12 +626,20 @@ def cash_event(note: AutocallableNote, o, spot: float, rate: float, step: int):
     period_coupon = note.period_coupon if o.coupon_barrier_level is not None else 0.0
     redemption = note.knock_out_payment(o) if has_ko else 0.0
     log_discount = -rate * o.time
+    # discounted_product(1, amount, log_discount), with the discount factor taken once
+    discount = math.exp(log_discount) if log_discount < 709.0 else math.inf
+    plain = math.isfinite(discount) and discount >= 2.2250738585072014e-308
     payments = []
     for outcome in range(4):
         coupon_due, knocked_out = outcome & 1, outcome >> 1
         coupon = period_coupon if coupon_due else 0.0
         amount = redemption + coupon if knocked_out else coupon
-        payments.append(discounted_product(1.0, amount, log_discount))
+        if amount == 0.0:
+            payments.append(0.0)
+        elif plain and math.isfinite(amount) and abs(amount) >= 2.2250738585072014e-308:
+            payments.append(amount * discount)
+        else:
+            payments.append(discounted_product(1.0, amount, log_discount))
     return (ko, barrier, tuple(payments), int(has_ko), step)
 
 
