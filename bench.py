@@ -486,6 +486,7 @@ def run_workload(args, name):
     # FP64 plain, one launch per contract: the whole book, or its first 128 notes for the
     # local-volatility book (the FP64 path would take minutes on all 4096).
     fp64_n = min(len(est32), 128)
+    _host_pricing(native, ctx, _first(packed, min(fp64_n, 2)), s64)  # loads the FP64 kernels
     est64, k64, _, _ = _host_pricing(native, ctx, _first(packed, fp64_n), s64)
     fp64_path_steps = sum(e.path_steps for e in est64)
     worst = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(est32, est64))
