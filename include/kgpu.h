@@ -64,7 +64,7 @@ enum { KGPU_PRECISION_FP64 = 0, KGPU_PRECISION_FP32 = 1 };
  * the longest lane's, with equal sampling dimensions and path counts).  One thread per
  * path walks the longest lane's plan once and settles every lane on it; the estimates
  * equal those of the plain schedule up to the order of the sums.  Pseudo-random or
- * Sobol, no antithetic pairs, host-resident books only. */
+ * Sobol, with or without antithetic pairs; host-resident books only. */
 enum { KGPU_SCHEDULE_PLAIN = 0, KGPU_SCHEDULE_PERSISTENT = 1, KGPU_SCHEDULE_SHARED_GRID = 2 };
 
 /* MonteCarloSettings (monte_carlo.rs:86-105) plus the GPU controls. */

@@ -825,7 +825,7 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, const SharedPlan& plan,
     const int base = plan.base, slots = plan.slots;
     const std::vector<int16_t>& slot = plan.slot;
     const int steps = b.contracts[base].step_count;
-    const size_t smem = shared_grid_smem_bytes(sizeof(Real), slots, steps, k.sobol);
+    const size_t smem = shared_grid_smem_bytes(sizeof(Real), slots, steps, k.sobol, s.antithetic != 0);
     if (smem > 227 * 1024)
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "%d action dates exceed the shared-grid kernel's shared memory",
                     slots);
@@ -833,7 +833,7 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, const SharedPlan& plan,
     const int ctas = int((samples + kSharedThreads - 1) / kSharedThreads);
     kgpu_status st;
     if ((st = upload(ctx, ctx->shared_slots, slot.data(), slot.size() * sizeof(int16_t)))) return st;
-    if (ctx->partials.ensure(size_t(n) * ctas * sizeof(double2)) || ctx->merged.ensure(size_t(n) * sizeof(double2)))
+    if (ctx->partials.ensure(size_t(n) * ctas * 3 * sizeof(double)) || ctx->merged.ensure(size_t(n) * 3 * sizeof(double)))
         return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the shared-grid sums failed");
     SharedArgs<Real> a;
     a.book = db;
@@ -844,10 +844,12 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, const SharedPlan& plan,
     a.steps = steps;
     a.dims = k.info[base].dims;
     a.samples = samples;
+    a.paths = k.info[base].paths;
+    a.antithetic = s.antithetic != 0;
     a.seed = s.seed;
     a.sobol = SobolTables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
     if (k.sobol && (st = ensure_sobol(ctx, a.dims, s.seed, &a.sobol))) return st;
-    a.partials = static_cast<double2*>(ctx->partials.ptr);
+    a.partials = static_cast<double*>(ctx->partials.ptr);
     a.ctas = ctas;
     CUDA_TRY(ctx, path_kernel_begin(ctx));
     // Lane chunks: enough CTAs for about four waves of resident CTAs, each chunk at
@@ -864,18 +866,37 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, const SharedPlan& plan,
         launched = launch_shared_grid_fp32(k.sobol, ctas, chunks, smem, ctx->stream, a);
     CUDA_TRY(ctx, launched);
     CUDA_TRY(ctx, path_kernel_end(ctx));
-    CUDA_TRY(ctx, launch_shared_merge(a.partials, ctas, n, static_cast<double2*>(ctx->merged.ptr), ctx->stream));
+    CUDA_TRY(ctx, launch_shared_merge(a.partials, ctas, n, static_cast<double*>(ctx->merged.ptr), ctx->stream));
     launches += 2;
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
-    std::vector<double2> merged(n);
-    CUDA_TRY(ctx, cudaMemcpyAsync(merged.data(), ctx->merged.ptr, sizeof(double2) * n, cudaMemcpyDeviceToHost,
+    std::vector<double> merged(size_t(n) * 3);
+    CUDA_TRY(ctx, cudaMemcpyAsync(merged.data(), ctx->merged.ptr, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
                                   ctx->stream));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < n; ++i) {
         const kgpu_contract& c = b.contracts[i];
-        const double path_steps = double(k.info[i].paths) * c.step_count;
-        TilePartial t{merged[i].x, merged[i].y, double(samples), path_steps};
-        estimate_from_sums(c, s, k.info[i].paths, t, &k.out[i]);
+        const int64_t paths = k.info[i].paths;
+        const double path_steps = double(paths) * c.step_count;
+        const double sum = merged[3 * i], sumsq = merged[3 * i + 1], pairsq = merged[3 * i + 2];
+        TilePartial t{sum, sumsq, double(paths), path_steps};
+        estimate_from_sums(c, s, paths, t, &k.out[i]);
+        if (s.antithetic && !k.sobol) {
+            // sampling_standard_error over the pair means (monte_carlo.rs:1435-1452).
+            kgpu_estimate& e = k.out[i];
+            e.standard_error = 0.0;
+            const double pairs = double(paths / 2);
+            if (paths % 2 != 0) {
+                e.uncertainty_status = KGPU_UNCERTAINTY_INCOMPLETE_ANTITHETIC_PAIR;
+            } else if (pairs < 2) {
+                e.uncertainty_status = KGPU_UNCERTAINTY_INSUFFICIENT_OBSERVATIONS;
+            } else {
+                const double mean = 0.5 * sum / pairs;
+                const double var = std::max(0.0, (pairsq - 0.5 * sum * mean) / (pairs - 1.0));
+                e.standard_error = std::sqrt(var / pairs);
+                e.uncertainty_status = e.standard_error == 0.0 ? KGPU_UNCERTAINTY_ZERO_OBSERVED_VARIANCE
+                                                               : KGPU_UNCERTAINTY_AVAILABLE;
+            }
+        }
         k.out[i].path_steps = path_steps;
         k.out[i].executed_steps = path_steps;
         if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].sample_error))
@@ -948,9 +969,8 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
     if (persistent && s.antithetic)
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
                     "the persistent schedule does not pair antithetic samples; use the plain schedule");
-    if (s.schedule == KGPU_SCHEDULE_SHARED_GRID && (s.antithetic || device_resident || model->kind != KGPU_MODEL_BSM))
-        return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
-                    "the shared-grid schedule takes host books under BSM without antithetic pairs");
+    if (s.schedule == KGPU_SCHEDULE_SHARED_GRID && (device_resident || model->kind != KGPU_MODEL_BSM))
+        return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "the shared-grid schedule takes host books under BSM");
     // Validate contracts (MonteCarloSettings::validate, monte_carlo.rs:197-220).
     k.info.resize(n);
     for (int i = 0; i < n; ++i) {

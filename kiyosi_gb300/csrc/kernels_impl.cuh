@@ -146,9 +146,9 @@ cudaError_t KGPU_CAT(launch_sobol_points_, PRECISION)(const SobolTables& t, int 
     return cudaGetLastError();
 }
 
-template <bool SOBOL>
+template <bool SOBOL, bool PAIRS>
 static cudaError_t shared_one(int ctas, int chunks, size_t smem, cudaStream_t s, const SharedArgs<REAL>& a) {
-    auto k = shared_grid_kernel<REAL, SOBOL>;
+    auto k = shared_grid_kernel<REAL, SOBOL, PAIRS>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     k<<<dim3(unsigned(ctas), unsigned(chunks)), kSharedThreads, smem, s>>>(a);
@@ -157,11 +157,13 @@ static cudaError_t shared_one(int ctas, int chunks, size_t smem, cudaStream_t s,
 
 cudaError_t KGPU_CAT(launch_shared_grid_, PRECISION)(bool sobol, int ctas, int chunks, size_t smem,
                                                      cudaStream_t s, const SharedArgs<REAL>& a) {
-    return sobol ? shared_one<true>(ctas, chunks, smem, s, a) : shared_one<false>(ctas, chunks, smem, s, a);
+    if (a.antithetic)
+        return sobol ? shared_one<true, true>(ctas, chunks, smem, s, a) : shared_one<false, true>(ctas, chunks, smem, s, a);
+    return sobol ? shared_one<true, false>(ctas, chunks, smem, s, a) : shared_one<false, false>(ctas, chunks, smem, s, a);
 }
 
 int KGPU_CAT(shared_grid_occupancy_, PRECISION)(bool sobol, size_t smem) {
-    auto k = sobol ? shared_grid_kernel<REAL, true> : shared_grid_kernel<REAL, false>;
+    auto k = sobol ? shared_grid_kernel<REAL, true, false> : shared_grid_kernel<REAL, false, false>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return 1;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kSharedThreads, smem) != cudaSuccess) return 1;
@@ -169,7 +171,7 @@ int KGPU_CAT(shared_grid_occupancy_, PRECISION)(bool sobol, size_t smem) {
 }
 
 #if !KGPU_FP32_UNIT
-cudaError_t launch_shared_merge(const double2* partials, int ctas, int lanes, double2* out, cudaStream_t s) {
+cudaError_t launch_shared_merge(const double* partials, int ctas, int lanes, double* out, cudaStream_t s) {
     shared_merge_kernel<<<lanes, 32, 0, s>>>(partials, ctas, lanes, out);
     return cudaGetLastError();
 }

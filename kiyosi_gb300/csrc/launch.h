@@ -52,7 +52,7 @@ cudaError_t launch_shared_grid_fp32(bool sobol, int ctas, int chunks, size_t sme
                                     const SharedArgs<float>& a);
 int shared_grid_occupancy_fp64(bool sobol, size_t smem);
 int shared_grid_occupancy_fp32(bool sobol, size_t smem);
-cudaError_t launch_shared_merge(const double2* partials, int ctas, int lanes, double2* out, cudaStream_t s);
+cudaError_t launch_shared_merge(const double* partials, int ctas, int lanes, double* out, cudaStream_t s);
 
 // Raw streams (kgpu_pcg_words, kgpu_pcg_normals, kgpu_sobol_points).
 cudaError_t launch_pcg_normals_fp64(uint64_t seed, uint64_t block, uint64_t first, int64_t count,

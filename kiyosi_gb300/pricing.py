@@ -129,10 +129,7 @@ class _MonteCarloEngine:
 
     def _run_group(self, ctx: PricingContext, lane_plans):
         """Prices the lanes of one shared daily grid with the path-major schedule (one
-        path per sample settles every lane); None when the engine pairs antithetic
-        samples, which that schedule does not."""
-        if self.antithetic:
-            return None
+        path per sample settles every lane)."""
         return self._run(ctx, lane_plans, schedule=abi.SCHEDULE_SHARED_GRID)
 
     def _run(self, ctx: PricingContext, contract_plans, path_counts=None, cancel=None, schedule=None):

@@ -246,8 +246,8 @@ def test_gpu_lanes_match_group_loop(native, sampling):
 @pytest.mark.parametrize("sobol", [False, True])
 def test_gpu_path_major_schedule_matches_lanes(native, sobol):
     """KGPU_SCHEDULE_SHARED_GRID (one path per sample settles every lane) against the
-    per-lane plain schedule and the oracle's loop: FP64 to rounding, FP32 within half a
-    sample error."""
+    per-lane plain schedule and the oracle's loop: FP64 to rounding, with and without
+    antithetic pairs; FP32 within half a sample error."""
     from kiyosi_gb300 import abi
     from kiyosi_gb300.errors import KiyosiError
     ctx = _ctx()
@@ -268,8 +268,15 @@ def test_gpu_path_major_schedule_matches_lanes(native, sobol):
                                                       schedule="shared_grid"))
     for f, p in zip(fast32, plain):
         assert abs(f.price - p.price) <= 0.5 * max(p.sample_error, 1e-4), (f.price, p.price)
-    with pytest.raises(KiyosiError):
-        gpu_price(native, ctx, packed, settings(paths, 13, antithetic=True, schedule="shared_grid"))
+    # antithetic pairs: both partners walked by one thread
+    pairs_fast = gpu_price(native, ctx, packed, settings(paths, 13, sobol=sobol, antithetic=True,
+                                                          schedule="shared_grid"))
+    pairs_plain = gpu_price(native, ctx, packed, settings(paths, 13, sobol=sobol, antithetic=True))
+    for f, p in zip(pairs_fast, pairs_plain):
+        assert abs(f.price - p.price) <= 1e-12 * max(1.0, abs(p.price)), (f.price, p.price)
+        assert f.uncertainty_status == p.uncertainty_status
+        assert abs(f.standard_error - p.standard_error) <= 1e-6 * max(p.standard_error, 1e-300)
+        assert abs(f.sample_error - p.sample_error) <= 1e-6 * p.sample_error
     # lanes of two different grids are refused
     other = portfolio.shared_lane(snowball(dates=[_DATES[0], _year(datetime.date(2025, 2, 10))],
                                            knock_out=(110.0, 108.0)), ctx, 0)
@@ -284,7 +291,7 @@ def test_gpu_engine_shared_grid_book(native):
     ctx = _ctx()
     notes = [snowball(c) for c in (0.02, 0.08, -0.01, 0.02, 0.04)] + [
         snowball(knock_out=(k,) * 3) for k in (103.0, 106.0, 101.0)] + [phoenix(), phoenix(0.05)]
-    for antithetic in (False, True):  # path-major schedule, then per-lane contracts
+    for antithetic in (False, True):  # path-major schedule, single paths and pairs
         engine = MonteCarloAutocallableEngine(path_count=1 << 14, seed=21, antithetic=antithetic)
         got = engine.price_many_on_shared_grid(notes, ctx)
         expected = portfolio.price_many(OracleBookEngine(1 << 14, 21, antithetic=antithetic),
