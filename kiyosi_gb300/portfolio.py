@@ -206,7 +206,8 @@ def lane_plans(lanes: Sequence[Lane], spot: float) -> List[plans.ContractPlan]:
     out = []
     for lane in lanes:
         m = lane.maturity
-        if not (same_daily_grid(base, lane) or len(lane.steps) == len(base.steps)) or any(
+        # the lane's grid and monitoring flags are the longest grid's first m + 1 steps
+        if lane.observe.tobytes() != base.observe[:m + 1].tobytes() or any(
                 lane.steps[f].tobytes() != base.steps[f][:m + 1].tobytes()
                 for f in ("drift", "diffusion", "discount")):
             raise InvalidInputError("the lanes do not share one daily grid")
