@@ -615,10 +615,28 @@ def _event_grid(ctx: PricingContext, event_times, knock_in_times, expiry):
     return out
 
 
+_CASH_EVENT_CACHE: dict = {}
+
+
 def cash_event(note: AutocallableNote, o, spot: float, rate: float, step: int):
     """CashEvent::new and discounted_payment (autocallable.rs:532-562): one observation's
     log-space knock-out and coupon thresholds and its four discounted payments, indexed
-    coupon_due | knocked_out << 1, as an EVENT_DTYPE record at grid step `step`."""
+    coupon_due | knocked_out << 1, as an EVENT_DTYPE record at grid step `step`.  Notes
+    of a book that share an observation and the terms its payments read share the
+    record."""
+    period_coupon = note.period_coupon if o.coupon_barrier_level is not None else 0.0
+    key = (o, period_coupon, note.principal, note.rebate_rate, note.annual_rebate_rate,
+           note.effective_time, spot, rate)
+    record = _CASH_EVENT_CACHE.get(key)
+    if record is None:
+        if len(_CASH_EVENT_CACHE) >= 65536:
+            _CASH_EVENT_CACHE.clear()
+        record = _cash_event(note, o, spot, rate)
+        _CASH_EVENT_CACHE[key] = record
+    return record + (step,)
+
+
+def _cash_event(note: AutocallableNote, o, spot: float, rate: float):
     has_ko = o.knock_out_level is not None
     ko = log_ratio(o.knock_out_level, spot) if has_ko else 0.0
     barrier = log_ratio(o.coupon_barrier_level if o.coupon_barrier_level is not None
@@ -640,7 +658,7 @@ def cash_event(note: AutocallableNote, o, spot: float, rate: float, step: int):
             payments.append(amount * discount)
         else:
             payments.append(discounted_product(1.0, amount, log_discount))
-    return (ko, barrier, tuple(payments), int(has_ko), step)
+    return (ko, barrier, tuple(payments), int(has_ko))
 
 
 def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool = True):
