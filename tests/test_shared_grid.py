@@ -216,9 +216,18 @@ def test_shared_grid_quote_near_scalar_quote():
 
 
 def test_batch_size_limit():
+    """autocallable_batches_reject_an_excessive_contract_count
+    (autocallable_monte_carlo.rs:10-27), with and without the shared grid."""
+    from kiyosi_gb300.pricing import MonteCarloAutocallableEngine
     note = snowball()
     with pytest.raises(InvalidInputError, match="1,048,576"):
         portfolio.plan_book([note] * ((1 << 20) + 1), _ctx(), True)
+    engine = MonteCarloAutocallableEngine(path_count=1024, seed=1)
+    for shared in (False, True):
+        with pytest.raises(InvalidInputError, match="1,048,576"):
+            engine.price_many([note] * ((1 << 20) + 1), _ctx(), shared_grid=shared)
+    with pytest.raises(InvalidInputError):
+        engine.price_many([note, note], _ctx(), path_counts=[1024, 2048], shared_grid=True)
 
 
 @pytest.mark.gpu
