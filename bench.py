@@ -27,6 +27,7 @@ import statistics
 import subprocess
 import sys
 import threading
+import tempfile
 import time
 
 import numpy as np
@@ -39,7 +40,7 @@ STEPS = 504
 SEED = 42
 # Warp instructions the FP32 persistent kernel issues per executed path position on
 # this workload, from one ncu capture (smsp__inst_executed.sum 403,176,851 over the
-# 41,683,020 positions of a 2^19-path pricing; profiles/persistent_kernel_snowball.md).
+# 41,683,020 positions of a 2^19-path pricing of this workload).
 # The kernel is neither HBM- nor tensor-bound, so its roofline is the SM issue rate
 # (4 warp-instructions per cycle per SM).
 WARP_INST_PER_EXECUTED_STEP = 403176851 / 41683020
@@ -123,8 +124,8 @@ class Clocks:
         self.device = device
 
     def __enter__(self):
-        self.path = os.path.join(ROOT, "gpurun_out", f"bench_clocks{self.device}.csv")
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        fd, self.path = tempfile.mkstemp(prefix=f"kiyosi_clocks{self.device}_", suffix=".csv")
+        os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device),
                                           f"--query-gpu={self.QUERY}",
@@ -139,8 +140,11 @@ class Clocks:
         if self.proc:
             self.proc.terminate()
             self.proc.wait()
+        self.summary()
 
     def summary(self):
+        if getattr(self, "_summary", None) is not None:
+            return self._summary
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         try:
@@ -155,8 +159,14 @@ class Clocks:
                         reasons.add(name)
         except OSError:
             pass
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        self._summary = {"sm_mhz": statistics.median(sm) if sm else None,
+                         "sm_max_mhz": mx or None, "reasons": sorted(reasons),
+                         "samples": len(sm)}
+        return self._summary
 
 
 class Ranks:

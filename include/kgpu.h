@@ -49,9 +49,11 @@ typedef enum kgpu_status {
 /* MonteCarloSampling (monte_carlo.rs:71-80). */
 enum { KGPU_SAMPLING_PSEUDO_RANDOM = 0, KGPU_SAMPLING_SOBOL = 1 };
 
-/* Arithmetic of the path kernels.  FP64 follows the reference's arithmetic step for step;
- * FP32 steps paths in single precision with compensated per-thread payoff sums and
- * FP64 cross-block reductions. */
+/* Arithmetic of the path kernels.  FP64 follows the reference's arithmetic step for step.
+ * FP32 steps paths in single precision; each path's payoff is widened to FP64 before any
+ * addition, and every sum (per block, across blocks) is an FP64 sum in a fixed order.
+ * An FP64 sum of FP32 payoffs carries less rounding than a compensated FP32 running sum
+ * would, so no per-thread FP32 accumulator exists. */
 enum { KGPU_PRECISION_FP64 = 0, KGPU_PRECISION_FP32 = 1 };
 
 /* Launch schedule.  PLAIN: one contract per launch, one thread per sample, the
@@ -432,9 +434,13 @@ kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double s
  * All pointers of `device_book`, including `contracts`, are device pointers; `model`,
  * `settings` and `out` are host memory.  The call runs the FP64 plain schedule
  * (results equal kgpu_price_book's for the same plan and settings) on `stream` (a
- * cudaStream_t; NULL for the default stream) and returns when the estimate is in `out`.
- * Limits: BSM or Heston models, pseudo-random sampling, at most 4,194,304 samples per
- * call.  Its scratch is one fixed 1.7 MB array in device memory that every GPU loading
+ * cudaStream_t; NULL for the default stream), synchronises `stream` and returns when the
+ * estimate is in `out`.  Before any launch it checks the contract as kgpu_price_book
+ * checks a host book: step, event and bridge ranges, the event steps against the event
+ * records and the order of the bridge intervals (read back through fixed host stack
+ * buffers).  Limits: BSM or Heston models, pseudo-random sampling, settings asking for
+ * KGPU_PRECISION_FP64 and KGPU_SCHEDULE_PLAIN (others are KGPU_UNSUPPORTED_OPERATION),
+ * at most 4,194,304 samples per call.  Its scratch is one fixed 1.7 MB array in device memory that every GPU loading
  * this library holds until process exit; the first call on a device looks up the
  * array's device address (make that first call before any stream capture).  Every call
  * shares the array, so calls that overlap on the GPU -- on different streams or from

@@ -567,26 +567,6 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Kahan-compensated running sum in the kernel's precision.
-template <class Real>
-struct Compensated {
-    Real sum, carry;
-    __device__ __forceinline__ void add(Real x) {
-        Real y = x - carry;
-        Real t = sum + y;
-        carry = (t - sum) - y;
-        sum = t;
-    }
-    __device__ __forceinline__ double value() const { return double(sum) - double(carry); }
-};
-
-// Persistent schedule.  Warps pull (contract, tile) items from a device queue and keep
-// two items in flight: a lane whose path has finished starts the next unstarted sample
-// of the older item, else of the newer one, so lanes never wait for an item to drain
-// while work is queued (early knock-out and bridge skipping make path lengths very
-// uneven).  Each finished path writes its payoff to values[value_offset[contract] +
-// sample]; reduce_values_kernel then sums them in a fixed order, so results do not
-// depend on which warp ran which path.
 // Persistent schedule.  Warps pull (contract, tile) items from a device queue and hand
 // the item's samples to lanes one at a time: lanes run kRefill path units in lockstep,
 // then every lane whose path has finished takes the next unstarted sample -- of the

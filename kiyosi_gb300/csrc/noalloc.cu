@@ -61,6 +61,47 @@ kgpu_status scratch_address(NoAllocScratch** out) {
     return KGPU_OK;
 }
 
+// The plan checks kgpu_price_book makes on host books, made here on the device book
+// through fixed host stack buffers: every event step of an autocallable has an event
+// record (the kernel reads one record per event step), and bridge intervals end in
+// ascending order with the last one on the final step.
+kgpu_status check_device_plan(const kgpu_book& book, const kgpu_contract& c, cudaStream_t st) {
+    constexpr int kChunk = 4096;
+    if (c.payoff == KGPU_PAYOFF_AUTOCALLABLE) {
+        uint8_t flags[kChunk];
+        int events = 0;
+        for (int q = 0; q < c.step_count; q += kChunk) {
+            const int n = c.step_count - q < kChunk ? c.step_count - q : kChunk;
+            if (cudaMemcpyAsync(flags, book.step_flags + c.step_offset + q, size_t(n), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)
+                return noalloc_fail(KGPU_DEVICE_ERROR, "cannot read the step flags");
+            for (int k = 0; k < n; ++k) events += (flags[k] & KGPU_STEP_EVENT) != 0;
+        }
+        if (events != c.event_count) return noalloc_fail(KGPU_INVALID_INPUT, "event steps and event records differ");
+    }
+    if (c.flags & KGPU_C_BRIDGE) {
+        constexpr int kIntervals = kChunk / int(sizeof(kgpu_bridge_interval)) + 1;
+        kgpu_bridge_interval intervals[kIntervals];
+        int previous = -1;
+        for (int q = 0; q < c.bridge_count; q += kIntervals) {
+            const int n = c.bridge_count - q < kIntervals ? c.bridge_count - q : kIntervals;
+            if (cudaMemcpyAsync(intervals, book.intervals + c.bridge_offset + q, sizeof(kgpu_bridge_interval) * n,
+                                cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)
+                return noalloc_fail(KGPU_DEVICE_ERROR, "cannot read the bridge intervals");
+            for (int k = 0; k < n; ++k) {
+                if (intervals[k].end <= previous || intervals[k].end >= c.step_count)
+                    return noalloc_fail(KGPU_INVALID_INPUT, "bridge intervals end out of order");
+                previous = intervals[k].end;
+            }
+        }
+        if (previous != c.step_count - 1)
+            return noalloc_fail(KGPU_INVALID_INPUT, "the last bridge interval must end the grid");
+    }
+    return KGPU_OK;
+}
+
 }  // namespace
 
 extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book* device_book,
@@ -69,11 +110,22 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
     kgpu::set_thread_error("");
     if (!model || !device_book || !settings || !out)
         return noalloc_fail(KGPU_INVALID_INPUT, "null argument");
+    if (model->kind < KGPU_MODEL_BSM || model->kind > KGPU_MODEL_LOCAL_VOL)
+        return noalloc_fail(KGPU_INVALID_INPUT, "unknown model");
     if (model->kind != KGPU_MODEL_BSM && model->kind != KGPU_MODEL_HESTON)
         return noalloc_fail(KGPU_UNSUPPORTED_OPERATION, "the no-allocation entry point prices BSM and Heston");
+    if (settings->sampling != KGPU_SAMPLING_PSEUDO_RANDOM && settings->sampling != KGPU_SAMPLING_SOBOL)
+        return noalloc_fail(KGPU_INVALID_INPUT, "unknown sampling");
     if (settings->sampling != KGPU_SAMPLING_PSEUDO_RANDOM)
         return noalloc_fail(KGPU_UNSUPPORTED_OPERATION, "the no-allocation entry point samples pseudo-random paths");
-    if (contract < 0 || contract >= device_book->contract_count)
+    if (settings->precision != KGPU_PRECISION_FP64 && settings->precision != KGPU_PRECISION_FP32)
+        return noalloc_fail(KGPU_INVALID_INPUT, "unknown precision");
+    if (settings->schedule < KGPU_SCHEDULE_PLAIN || settings->schedule > KGPU_SCHEDULE_SHARED_GRID)
+        return noalloc_fail(KGPU_INVALID_INPUT, "unknown schedule");
+    if (settings->precision != KGPU_PRECISION_FP64 || settings->schedule != KGPU_SCHEDULE_PLAIN)
+        return noalloc_fail(KGPU_UNSUPPORTED_OPERATION,
+                            "the no-allocation entry point runs the FP64 plain schedule only");
+    if (contract < 0 || contract >= device_book->contract_count || !device_book->contracts)
         return noalloc_fail(KGPU_INVALID_INPUT, "contract index out of range");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // The contract record, read from device memory into this stack frame.
@@ -91,6 +143,24 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
         return noalloc_fail(KGPU_INVALID_INPUT, "a bridge plan needs BSM");
     if (c.step_count < 1 || c.step_offset < 0 || c.step_offset + c.step_count > device_book->step_total)
         return noalloc_fail(KGPU_INVALID_INPUT, "steps out of range");
+    if (!device_book->steps || !device_book->step_flags)
+        return noalloc_fail(KGPU_INVALID_INPUT, "steps missing");
+    if (c.event_count < 0 || c.event_offset < 0 || c.event_offset + c.event_count > device_book->event_total)
+        return noalloc_fail(KGPU_INVALID_INPUT, "events out of range");
+    if (c.event_count > 0 && !device_book->events)
+        return noalloc_fail(KGPU_INVALID_INPUT, "events missing");
+    if ((c.flags & KGPU_C_BRIDGE) &&
+        (!device_book->bridge_daily || !device_book->intervals || c.bridge_count < 1 || c.bridge_offset < 0 ||
+         c.bridge_offset + c.bridge_count > device_book->interval_total))
+        return noalloc_fail(KGPU_INVALID_INPUT, "invalid bridge plan");
+    if (c.payoff == KGPU_PAYOFF_AUTOCALLABLE || (c.flags & KGPU_C_BRIDGE)) {
+        const kgpu_status plan = check_device_plan(*device_book, c, st);
+        if (plan != KGPU_OK) return plan;
+    }
+    const bool terminal = c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL;
+    const int step_dims = c.step_count * (model->kind == KGPU_MODEL_HESTON ? 2 : 1);
+    if (c.dimensions < 0 || (c.dimensions > 0 && (terminal || c.dimensions < step_dims)))
+        return noalloc_fail(KGPU_INVALID_INPUT, "dimensions must cover every step's normals");
     const int64_t samples = settings->antithetic ? (paths + 1) / 2 : paths;
     const int64_t blocks = (samples + 255) / 256;
     if (blocks > kNoAllocMaxBlocks)
@@ -115,12 +185,7 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
     a.book.units = nullptr;
     a.book.ends = nullptr;
     a.contract = 0;
-    const int step_dims = c.step_count * (model->kind == KGPU_MODEL_HESTON ? 2 : 1);
-    if (c.dimensions < 0 || (c.dimensions > 0 && c.dimensions < step_dims))
-        return noalloc_fail(KGPU_INVALID_INPUT, "dimensions must cover every step's normals");
-    a.dims = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1
-             : c.dimensions > 0                                                    ? c.dimensions
-                                                                                   : step_dims;
+    a.dims = terminal ? 1 : c.dimensions > 0 ? c.dimensions : step_dims;
     a.paths = paths;
     a.samples = samples;
     a.seed = settings->seed;
@@ -143,7 +208,7 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
     kgpu_settings s = *settings;
     s.sampling = KGPU_SAMPLING_PSEUDO_RANDOM;
     kgpu::estimate_from_moments(c, s, paths, merged, out);
-    const int grid = (c.payoff == KGPU_PAYOFF_EUROPEAN || c.payoff == KGPU_PAYOFF_DIGITAL) ? 1 : c.step_count;
+    const int grid = terminal ? 1 : c.step_count;
     out->path_steps = double(paths) * grid;
     out->executed_steps = merged.executed;
     if (!(out->price == out->price) || out->price - out->price != 0.0)
