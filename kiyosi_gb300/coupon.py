@@ -139,14 +139,18 @@ def _solve(engine, option, ctx, observed: float, s: ImpliedCouponSettings, minim
             raise ComputationFailureError("non-finite coupon residual")
         return r
 
+    def plan_of(note, ctx):
+        build = getattr(engine, "_plan", None)
+        return build(note, ctx) if build is not None else plans.autocallable(note, ctx)
+
     def scalar_price(note):
-        return checked(engine._run(ctx, [plans.autocallable(note, ctx)])[0].price)
+        return checked(engine._run(ctx, [plan_of(note, ctx)])[0].price)
 
     lo, hi = lower_bound, s.upper_bound
     lower_note, upper_note = with_coupon(option, lo), with_coupon(option, hi)
     original_lo, original_hi = lo, hi
     # price_coupon_bounds: both bound notes on shared paths, one launch.
-    bounds = engine._run(ctx, [plans.autocallable(lower_note, ctx), plans.autocallable(upper_note, ctx)])
+    bounds = engine._run(ctx, [plan_of(lower_note, ctx), plan_of(upper_note, ctx)])
     lower, upper = checked(bounds[0].price), checked(bounds[1].price)
     curve = (s.price_tolerance >= 1e-10 * max(abs(observed), 1.0)
              and lower_note.knock_in_affects_payoff() == upper_note.knock_in_affects_payoff()
@@ -165,7 +169,7 @@ def _solve(engine, option, ctx, observed: float, s: ImpliedCouponSettings, minim
     def price(coupon):
         note = with_coupon(option, coupon)
         if curve and note.knock_in_affects_payoff() == affected:
-            plan = plans.autocallable(note, ctx)
+            plan = plan_of(note, ctx)
             if isinstance(plan, plans.Known):
                 return checked(plan.value)
             span = original_hi - original_lo

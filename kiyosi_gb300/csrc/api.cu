@@ -290,6 +290,43 @@ bool terminal_payoff(const kgpu_contract& c) {
            c.payoff == KGPU_PAYOFF_AVERAGE_GEOMETRIC || c.payoff == KGPU_PAYOFF_DOUBLE_BARRIER;
 }
 
+// FP32 plans are converted from the FP64 plan field by field.  A finite nonzero value
+// below 2^-100 or above 2^120 in magnitude would underflow, or leave no headroom for
+// the products the kernels form, in single precision (a diffusion of 1e-200, a daily
+// quantity of 1e200); such plans are priced in FP64 or not at all.
+bool fp32_value(double v) {
+    const double a = std::fabs(v);
+    return v == 0.0 || !std::isfinite(v) || (a >= 0x1p-100 && a <= 0x1p120);
+}
+
+// Whether FP32 kernels can carry contract c of a host book (every double field of the
+// contract, its steps, events, bridge records and the model).
+bool fp32_representable(const kgpu_model* m, const kgpu_book* b, const kgpu_contract& c) {
+    const double* first = &c.strike;
+    const double* last = &c.greek_log_weight;
+    for (const double* v = first; v <= last; ++v)
+        if (!fp32_value(*v)) return false;
+    for (double v : {m->spot, m->rate, m->dividend, m->volatility, m->v0, m->kappa, m->theta, m->xi, m->rho})
+        if (!fp32_value(v)) return false;
+    for (int64_t q = c.step_offset; q < c.step_offset + c.step_count; ++q) {
+        const kgpu_step& st = b->steps[q];
+        if (!fp32_value(st.drift) || !fp32_value(st.diffusion) || !fp32_value(st.discount)) return false;
+        if (b->bridge_daily && (c.flags & KGPU_C_BRIDGE) &&
+            (!fp32_value(b->bridge_daily[q].weight) || !fp32_value(b->bridge_daily[q].width)))
+            return false;
+    }
+    for (int q = c.event_offset; q < c.event_offset + c.event_count; ++q) {
+        const kgpu_event& e = b->events[q];
+        if (!fp32_value(e.knock_out) || !fp32_value(e.coupon_barrier)) return false;
+        for (double v : e.payment)
+            if (!fp32_value(v)) return false;
+    }
+    if (c.flags & KGPU_C_BRIDGE)
+        for (int q = c.bridge_offset; q < c.bridge_offset + c.bridge_count; ++q)
+            if (!fp32_value(b->intervals[q].drift) || !fp32_value(b->intervals[q].diffusion)) return false;
+    return true;
+}
+
 int dims_of(const kgpu_contract& c, const kgpu_model* m) {
     if (terminal_payoff(c)) return 1;
     if (c.dimensions > 0) return c.dimensions;
@@ -1028,6 +1065,11 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
                 return fail(ctx, KGPU_INVALID_INPUT, "contract %d: %d event steps but %d events", i, events,
                             c.event_count);
         }
+        if (s.precision == KGPU_PRECISION_FP32 && !device_resident && !fp32_representable(model, book, c))
+            return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
+                        "contract %d: FP32 cannot carry this plan (a nonzero value below 2^-100 or above "
+                        "2^120 in magnitude); price it in FP64",
+                        i);
         k.info[i].dims = dims_of(c, model);
         k.info[i].paths = paths;
         k.info[i].samples = s.antithetic ? (paths + 1) / 2 : paths;

@@ -21,13 +21,13 @@ def _sign(option_type: str) -> float:
     return 1.0 if option_type == CALL else -1.0
 
 
-def _times(values: Sequence[float], expiry: float, name: str) -> List[float]:
+def _times(values: Sequence[float], expiry: float, name: str, start: float = 0.0) -> List[float]:
     out = [float(v) for v in values]
     if any(not math.isfinite(v) for v in out):
         raise InvalidInputError(f"{name} must be finite")
     if any(b <= a for a, b in zip(out, out[1:])):
         raise InvalidInputError(f"{name} must be strictly increasing")
-    if out and (out[0] < 0.0 or out[-1] > expiry):
+    if out and (out[0] < start or out[-1] > expiry):
         raise InvalidInputError(f"{name} must lie within the contract's life")
     return out
 
@@ -218,6 +218,9 @@ class Observation:
     coupon_rate: float = 0.0
 
 
+BARRIER_STATES = (None, "no_event", "knocked_in", "knocked_out")
+
+
 @dataclass(frozen=True)
 class AutocallableNote:
     """Snowball, binary/ternary snowball or Phoenix note (instruments/autocallable.rs).
@@ -227,6 +230,13 @@ class AutocallableNote:
     or a fixed annual coupon.  Without knock-in the note pays principal + rebate +
     maturity_coupon_rate x accrual.  Phoenix notes pay `period_coupon` at each coupon
     observation whose barrier is met.
+
+    Times are year fractions after the valuation instant, so a seasoned note has a
+    negative `effective_time` and may list observation and monitoring times at or before
+    zero; `expiry` 0 values the note at expiry.  `barrier_state` is the note's history
+    strictly before valuation (AutocallableBarrierState: None when unknown, 'no_event',
+    'knocked_in', 'knocked_out'); a note with past observations or past daily monitoring
+    needs it (AutocallableNote::prior, instruments/autocallable.rs:1320-1369).
     """
     initial_spot: float
     expiry: float
@@ -242,17 +252,29 @@ class AutocallableNote:
     rebate_rate: float = 0.0
     annual_rebate_rate: float = 0.0
     effective_time: float = 0.0
-    knocked_in: bool = False
+    barrier_state: Optional[str] = None
 
     def __post_init__(self):
+        if not (math.isfinite(self.effective_time) and math.isfinite(self.expiry)):
+            raise InvalidInputError("effective and expiry times must be finite")
+        if self.effective_time > 0.0 or self.expiry < 0.0:
+            # validate_life (instruments/monitoring.rs:470-481)
+            raise InvalidInputError("valuation outside contract life")
+        if self.effective_time > self.expiry:
+            raise InvalidInputError("the effective time must not follow expiry")
+        if self.barrier_state not in BARRIER_STATES:
+            raise InvalidInputError(f"barrier_state must be one of {BARRIER_STATES}")
+        if self.barrier_state == "knocked_in" and self.knock_in_level is None:
+            raise InvalidInputError("knock-in state requires a knock-in barrier")
         obs = tuple(self.observations)
         object.__setattr__(self, "observations", obs)
-        _times([o.time for o in obs], self.expiry, "observations")
+        _times([o.time for o in obs], self.expiry, "observations", self.effective_time)
         if self.knock_in_times is not None:
             object.__setattr__(self, "knock_in_times",
-                               tuple(_times(self.knock_in_times, self.expiry, "knock_in_times")))
-        if not (self.initial_spot > 0.0 and self.expiry > 0.0):
-            raise InvalidInputError("initial spot and expiry must be positive")
+                               tuple(_times(self.knock_in_times, self.expiry, "knock_in_times",
+                                            self.effective_time)))
+        if not self.initial_spot > 0.0:
+            raise InvalidInputError("initial spot must be positive")
         if self.upper_strike == 0.0:
             object.__setattr__(self, "upper_strike", self.initial_spot)
         if self.lower_strike > self.upper_strike:
@@ -278,6 +300,35 @@ class AutocallableNote:
         else:
             coupon = self.maturity_coupon_rate
         return base + coupon * (self.expiry - self.effective_time)
+
+    @property
+    def knocked_in(self) -> bool:
+        """Knocked in before valuation (the recorded history)."""
+        return self.barrier_state == "knocked_in"
+
+    @property
+    def daily_knock_in(self) -> bool:
+        """Knock-in monitored on every listed date (KnockInObservation::EveryTradingDay)
+        rather than at expiry only."""
+        return self.knock_in_level is not None and self.knock_in_times is not None
+
+    def observes_knock_in(self, time: float) -> bool:
+        """AutocallableNote::observes_knock_in (instruments/autocallable.rs:1075-1080)."""
+        if self.knock_in_level is None:
+            return False
+        if self.knock_in_times is not None:
+            return time in self.knock_in_times
+        return time == self.expiry
+
+    def below_knock_in(self, spot: float) -> bool:
+        """Terms::below_knock_in (instruments/autocallable.rs:1652-1654): strict."""
+        return self.knock_in_level is not None and spot < self.knock_in_level
+
+    def observation_coupon(self, obs: Optional["Observation"], spot: float) -> float:
+        """AutocallableNote::observation_coupon (instruments/autocallable.rs:1164-1174)."""
+        if obs is not None and obs.coupon_barrier_level is not None and spot >= obs.coupon_barrier_level:
+            return self.period_coupon
+        return 0.0
 
     def knock_in_affects_payoff(self) -> bool:
         """instruments/autocallable.rs:1323-1332."""
@@ -325,7 +376,8 @@ class Accumulator:
     knock_out_times: Sequence[float]
     daily_quantity: float = 1.0
     acceleration: float = 2.0
-    quantity: float = 0.0
+    quantity: float = 0.0           # accumulated before valuation
+    knock_out_settled: bool = False  # knocked out and settled before valuation
 
     def __post_init__(self):
         _sign(self.option_type)
@@ -337,3 +389,16 @@ class Accumulator:
     @property
     def sign(self) -> float:
         return _sign(self.option_type)
+
+    def purchase(self, spot: float) -> float:
+        """Accumulator::purchase (instruments/accumulator.rs:486-499): the daily quantity,
+        times the acceleration when the spot is below (call) or above (put) the strike."""
+        distance = spot - self.strike
+        accelerated = distance < 0.0 if self.option_type == CALL else distance > 0.0
+        return self.daily_quantity * self.acceleration if accelerated else self.daily_quantity
+
+    def unit_payoff(self, spot: float) -> float:
+        return spot - self.strike if self.option_type == CALL else self.strike - spot
+
+    def is_knock_out(self, spot: float) -> bool:
+        return spot >= self.knock_out_level if self.option_type == CALL else spot <= self.knock_out_level

@@ -39,6 +39,41 @@ class Known:
     value: float
 
 
+def _fp32_ok(values) -> bool:
+    a = np.abs(np.asarray(values, dtype=np.float64).ravel())
+    ok = (a == 0.0) | ~np.isfinite(a) | ((a >= 2.0 ** -100) & (a <= 2.0 ** 120))
+    return bool(ok.all())
+
+
+def fp32_representable(plan, ctx: PricingContext) -> bool:
+    """Whether FP32 kernels can carry `plan`: every finite nonzero value of the plan and
+    the model lies within [2^-100, 2^120] in magnitude (the rule kgpu_price_book
+    applies before an FP32 launch; a diffusion of 1e-200 or a daily quantity of 1e200
+    is priced in FP64)."""
+    if not isinstance(plan, ContractPlan):
+        return True
+    c = plan.contract[0]
+    first = list(CONTRACT_DTYPE.names).index("strike")
+    last = list(CONTRACT_DTYPE.names).index("greek_log_weight")
+    if not _fp32_ok([c[n] for n in CONTRACT_DTYPE.names[first:last + 1]]):
+        return False
+    m = ctx.kgpu_model()
+    if not _fp32_ok([m.spot, m.rate, m.dividend, m.volatility, m.v0, m.kappa, m.theta, m.xi, m.rho]):
+        return False
+    st = plan.steps
+    if not (_fp32_ok(st["drift"]) and _fp32_ok(st["diffusion"]) and _fp32_ok(st["discount"])):
+        return False
+    if len(plan.events) and not (_fp32_ok(plan.events["knock_out"]) and _fp32_ok(plan.events["coupon_barrier"])
+                                 and _fp32_ok(plan.events["payment"])):
+        return False
+    if c["flags"] & abi.C_BRIDGE:
+        if not (_fp32_ok(plan.intervals["drift"]) and _fp32_ok(plan.intervals["diffusion"])):
+            return False
+        if plan.daily is not None and not (_fp32_ok(plan.daily["weight"]) and _fp32_ok(plan.daily["width"])):
+            return False
+    return True
+
+
 @dataclass
 class ContractPlan:
     contract: np.ndarray                 # one CONTRACT_DTYPE record
@@ -585,21 +620,45 @@ def asian(option: AsianOption, ctx: PricingContext, step_count: Optional[int] = 
 _EVENT_GRID_CACHE: dict = {}
 
 
-def _event_grid(ctx: PricingContext, event_times, knock_in_times, expiry):
+def refine_grid(times: List[float], time_steps: Optional[int]) -> List[float]:
+    """Adds path steps between the dates of a grid (ascending, > 0) so that no step is
+    much longer than times[-1] / time_steps: each interval between consecutive dates
+    (from valuation) is cut into max(round(length / dt_max), 1) equal steps.  This is
+    the rule of QuantLib's TimeGrid(mandatory times, steps), so a path discretised here
+    visits the same times as QuantLib's path generators.  Exact BSM stepping does not
+    need it; Euler schemes (local volatility, Heston) use it to bound the time step."""
+    if not time_steps or not times:
+        return list(times)
+    if int(time_steps) < 1:
+        raise InvalidInputError("time_steps must be positive")
+    dt_max = times[-1] / int(time_steps)
+    out = []
+    begin = 0.0
+    for end in times:
+        n = max(int(math.floor((end - begin) / dt_max + 0.5)), 1)
+        dt = (end - begin) / n
+        out.extend(begin + k * dt for k in range(1, n))
+        out.append(end)
+        begin = end
+    return out
+
+
+def _event_grid(ctx: PricingContext, event_times, knock_in_times, expiry, time_steps=None):
     """future_event_times (instruments/autocallable/pricing.rs:70-106): the merged grid
     of event dates, daily knock-in dates (None when not monitored) and expiry, with its
     step records, knock-in flags and excursion (the sum over steps of |drift| + 20
-    diffusion, added in step order).  Notes of one schedule share the result."""
+    diffusion, added in step order).  `time_steps` refines the grid (refine_grid).
+    Notes of one schedule share the result."""
     model = ctx.model
     bsm = isinstance(model, BlackScholesMertonParameters)
     key = (type(model), model.rate, model.dividend, getattr(model, "volatility", None), event_times,
-           knock_in_times, expiry) if bsm else None
+           knock_in_times, expiry, time_steps) if bsm else None
     hit = _EVENT_GRID_CACHE.get(key) if key is not None else None
     if hit is not None:
         return hit
     times = sorted(set(list(event_times) + (list(knock_in_times) if knock_in_times is not None else [])
                        + [expiry]))
-    times = [t for t in times if t > 0.0]
+    times = refine_grid([t for t in times if t > 0.0], time_steps)
     steps = _grid_steps(ctx, times)
     flags = np.zeros(len(times), np.uint8)
     if knock_in_times is not None:
@@ -661,16 +720,142 @@ def _cash_event(note: AutocallableNote, o, spot: float, rate: float):
     return (ko, barrier, tuple(payments), int(has_ko))
 
 
-def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool = True):
-    """prepare_sample_on_grid (autocallable.rs:293-430) for a note valued before its first
-    observation: merged event and daily knock-in grid, log-space thresholds, discounted
-    cash events, and the Brownian-bridge plan when the reference would use one."""
+@dataclass(frozen=True)
+class AutocallableInitial:
+    """pricing::Initial (instruments/autocallable/pricing.rs:7-11): the knock-in state at
+    valuation, a settlement that makes sampling unnecessary, and the coupon fixed at the
+    valuation instant."""
+    knocked_in: bool
+    settlement: Optional[float]
+    coupon: float
+
+
+def _current_observation(note: AutocallableNote):
+    """AutocallableNote::event_at(valuation) (instruments/autocallable.rs:1045-1051)."""
+    for o in note.observations:
+        if o.time == 0.0:
+            return o
+    return None
+
+
+def autocallable_prior(note: AutocallableNote) -> bool:
+    """AutocallableNote::prior (instruments/autocallable.rs:1320-1369): checks the
+    recorded history against the schedule before valuation and returns whether the note
+    knocked in before valuation."""
+    ko = [o.time for o in note.observations if o.knock_out_level is not None]
+    first_out = ko[0] if ko else (note.observations[0].time if note.observations else None)
+    had_out = first_out is not None and first_out < 0.0
+    had_in = (note.daily_knock_in and note.effective_time < 0.0
+              and any(note.effective_time <= t < 0.0 for t in note.knock_in_times))
+    state = note.barrier_state
+    if state is None and (had_out or had_in):
+        from .errors import MissingHistoryError
+        raise MissingHistoryError("prior autocallable state is required")
+    if state == "knocked_out" and not had_out:
+        raise InvalidInputError("knock-out predates observations")
+    if state == "knocked_in" and not had_in:
+        raise InvalidInputError("knock-in predates monitoring")
+    return state == "knocked_in"
+
+
+def autocallable_expiry_payment(note: AutocallableNote, spot: float, knocked_in: bool, record) -> float:
+    """pricing::expiry_payment (instruments/autocallable/pricing.rs:51-69)."""
+    coupon = note.observation_coupon(record, spot)
+    if record is not None and record.knock_out_level is not None and spot >= record.knock_out_level:
+        return coupon + note.knock_out_payment(record)
+    ki = knocked_in or (note.observes_knock_in(note.expiry) and note.below_knock_in(spot))
+    return coupon + note.terminal(spot, ki)
+
+
+def autocallable_initial(note: AutocallableNote, spot: float) -> AutocallableInitial:
+    """pricing::initial (instruments/autocallable/pricing.rs:12-49) at the valuation
+    instant (time 0): a knocked-out note settles at 0; a daily-monitored note whose
+    valuation is a monitoring date knocks in when the spot is below the level (strict);
+    an observation at valuation fixes its coupon, and settles the note when it knocks
+    out (inclusive) or when valuation is expiry."""
+    if note.barrier_state == "knocked_out":
+        return AutocallableInitial(False, 0.0, 0.0)
+    knocked_in = note.barrier_state == "knocked_in"
+    if note.daily_knock_in and 0.0 in note.knock_in_times:
+        knocked_in |= note.below_knock_in(spot)
+    current = _current_observation(note)
+    coupon = note.observation_coupon(current, spot)
+    if note.expiry == 0.0:
+        settlement = autocallable_expiry_payment(note, spot, knocked_in, current)
+    elif (current is not None and current.knock_out_level is not None
+          and spot >= current.knock_out_level):
+        settlement = note.knock_out_payment(current) + coupon
+    else:
+        settlement = None
+    return AutocallableInitial(knocked_in, settlement, coupon)
+
+
+def _is_normal_float(x: float) -> bool:
+    return math.isfinite(x) and abs(x) >= 2.2250738585072014e-308
+
+
+def autocallable_fixed_value(note: AutocallableNote, ctx: PricingContext, knocked_in: bool):
+    """pricing::fixed_value_at (instruments/autocallable/pricing.rs:137-193) at
+    valuation: the note's value when no remaining path can change it (an exact
+    comparison of terms and discounted payments), else None."""
+    if note.daily_knock_in:
+        pending = note.expiry > 0.0 and any(0.0 < t <= note.expiry for t in note.knock_in_times)
+    else:
+        pending = note.knock_in_level is not None and note.expiry > 0.0
+    if knocked_in or pending:
+        if note.fixed_knock_in_coupon is None and note.knock_in_level is not None:
+            if note.lower_strike != note.upper_strike or (not knocked_in and note.maturity_coupon_rate != 0.0):
+                return None
+        elif not knocked_in and note.knock_in_affects_payoff():
+            return None
+    rate = ctx.rate
+
+    def discount(t):
+        return math.exp(-rate * t)
+    value = note.terminal(ctx.spot, knocked_in) * discount(note.expiry)
+    if not math.isfinite(value):
+        return None
+    coupons = 0.0
+    for o in reversed(note.observations):
+        if not o.time > 0.0:
+            break
+        d = discount(o.time)
+        if not _is_normal_float(d) or (o.knock_out_level is not None
+                                       and note.knock_out_payment(o) * d != value + coupons):
+            return None
+        if o.coupon_barrier_level is not None:
+            if note.period_coupon != 0.0 and o.coupon_barrier_level != 0.0:
+                return None
+            coupons += note.period_coupon * d
+            if not math.isfinite(coupons):
+                return None
+    return value + coupons if _is_normal_float(discount(note.expiry)) else None
+
+
+def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool = True,
+                 time_steps: Optional[int] = None):
+    """prepare_sample_on_grid (autocallable.rs:293-430): the history check and
+    `pricing::initial` at valuation (a settled or path-independent note is Known), then
+    the merged event and daily knock-in grid of the future dates, log-space thresholds,
+    discounted cash events, the coupon fixed at valuation as initial cash, and the
+    Brownian-bridge plan when the reference would use one.  `time_steps` adds path
+    steps between the dates (refine_grid) for Euler schemes."""
     model = ctx.model
     spot = ctx.spot
     rate, dividend = model.rate, model.dividend
     bsm = isinstance(model, BlackScholesMertonParameters)
-    knocked_in = bool(note.knocked_in)
-    daily = (note.knock_in_times is not None and not knocked_in and note.knock_in_affects_payoff())
+    autocallable_prior(note)
+    state = autocallable_initial(note, spot)
+    value = state.settlement
+    if value is None:
+        fixed = autocallable_fixed_value(note, ctx, state.knocked_in)
+        value = None if fixed is None else fixed + state.coupon
+    if value is not None:
+        if not math.isfinite(value):
+            raise ComputationFailureError("Monte Carlo produced a non-finite parameter, path or result")
+        return Known(value)
+    knocked_in = state.knocked_in
+    daily = note.daily_knock_in and not knocked_in and note.knock_in_affects_payoff()
     knock_in = log_ratio(note.knock_in_level, spot) if note.knock_in_level is not None else 0.0
     expiry_knock_in = note.knock_in_level is not None and (
         note.knock_in_times is None or (len(note.knock_in_times) > 0
@@ -678,7 +863,7 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
     events = [o for o in note.observations if o.time > 0.0]
     times, steps, ki_flags, excursion = _event_grid(ctx, tuple(o.time for o in events),
                                                     note.knock_in_times if daily else None,
-                                                    note.expiry)
+                                                    note.expiry, time_steps)
     grid = np.array(times)
     flags = ki_flags.copy()
     ev = np.zeros(len(events), EVENT_DTYPE)
@@ -699,7 +884,7 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
     c["step_count"] = len(times)
     c["event_count"] = len(events)
     c["knock_in"] = knock_in
-    c["initial_cash"] = 0.0
+    c["initial_cash"] = state.coupon
     c["terminal_base"] = note.principal + note.rebate_payment(note.expiry)
     c["terminal_plain"] = note.terminal(0.0, False)
     c["terminal_fixed"] = note.terminal(0.0, True) if note.fixed_knock_in_coupon is not None else 0.0
@@ -753,12 +938,50 @@ def _bridge_plan(times, steps, flags, model):
     return np.array(intervals, INTERVAL_DTYPE), daily
 
 
-def accumulator(option: Accumulator, ctx: PricingContext):
-    """MonteCarloAccumulatorEngine::sample (accumulator.rs:91-160) without fixed purchase
-    events: steps on the union of accumulation and knock-out dates."""
+def _accrues(option: Accumulator) -> bool:
+    """Accumulator::accrues (instruments/accumulator.rs:456-470)."""
+    if option.knock_out_settled or option.daily_quantity == 0.0 or option.expiry <= 0.0:
+        return False
+    ko = set(option.knock_out_times)
+    return any(t > 0.0 and (option.acceleration != 0.0 or not option.is_knock_out(option.strike)
+                            or t not in ko) for t in option.accumulation_times)
+
+
+def accumulator_initial(option: Accumulator, ctx: PricingContext):
+    """Accumulator::initial_with_accrual (instruments/accumulator.rs:528-567) at the
+    valuation instant (time 0): (quantity held, settlement or None).  A knock-out
+    observed now settles the held quantity; an accumulation date now adds its purchase
+    at the current spot; a note that can no longer accrue, or is at expiry, settles."""
     spot = ctx.spot
+    if option.knock_out_settled:
+        return 0.0, 0.0
+    quantity = option.quantity
+    if 0.0 in option.knock_out_times and option.is_knock_out(spot):
+        return quantity, quantity * option.unit_payoff(spot)
+    if 0.0 in option.accumulation_times:
+        quantity += option.purchase(spot)
+    accrues = _accrues(option)
+    if quantity == 0.0 and not accrues:
+        return quantity, 0.0
+    if option.expiry == 0.0 or (not accrues and ctx.rate == 0.0 and ctx.dividend == 0.0):
+        return quantity, quantity * option.unit_payoff(spot)
+    return quantity, None
+
+
+def accumulator(option: Accumulator, ctx: PricingContext, time_steps: Optional[int] = None):
+    """MonteCarloAccumulatorEngine::sample (accumulator.rs:91-160) without fixed purchase
+    events: steps on the union of accumulation and knock-out dates, refined by
+    `time_steps` (refine_grid) for Euler schemes."""
+    spot = ctx.spot
+    quantity, settlement = accumulator_initial(option, ctx)
+    if settlement is not None:
+        if not math.isfinite(settlement):
+            raise ComputationFailureError("Monte Carlo produced a non-finite parameter, path or result")
+        return Known(settlement)
+    if not math.isfinite(quantity):
+        raise ComputationFailureError("Monte Carlo produced a non-finite parameter, path or result")
     times = sorted(set(option.accumulation_times) | set(option.knock_out_times))
-    times = [t for t in times if t > 0.0]
+    times = refine_grid([t for t in times if t > 0.0], time_steps)
     if not times:
         raise InvalidInputError("an accumulator needs a future observation")
     acc = set(option.accumulation_times)
@@ -775,7 +998,7 @@ def accumulator(option: Accumulator, ctx: PricingContext):
     c["step_count"] = len(times)
     c["knock_out"] = log_ratio(option.knock_out_level, spot)
     c["log_strike"] = log_ratio(option.strike, spot)
-    c["quantity"] = option.quantity
+    c["quantity"] = quantity
     c["daily_quantity"] = option.daily_quantity
     c["acceleration"] = option.acceleration
     c["final_discount"] = math.exp(-ctx.rate * times[-1])

@@ -79,10 +79,11 @@ class Lane:
         return len(self.steps) - 1
 
 
-def _daily(note: AutocallableNote) -> bool:
-    """prepare_sample_on_grid's `daily` (autocallable.rs:335)."""
-    return (note.knock_in_times is not None and not note.knocked_in
-            and note.knock_in_affects_payoff())
+def _daily(note: AutocallableNote, spot: float) -> bool:
+    """prepare_sample_on_grid's `daily` (autocallable.rs:335), with the knock-in state
+    at valuation (pricing::initial)."""
+    return (note.daily_knock_in and note.knock_in_affects_payoff()
+            and not plans.autocallable_initial(note, spot).knocked_in)
 
 
 def shared_lane(note: AutocallableNote, ctx: PricingContext, index: int) -> Optional[Lane]:
@@ -92,9 +93,11 @@ def shared_lane(note: AutocallableNote, ctx: PricingContext, index: int) -> Opti
     expiry when expiry is not one of them. A cash event off those dates keeps the
     ordinary schedule. That schedule still shares a grid when it monitors knock-in
     (PathPlan::shared_daily_grid, portfolio.rs:868-870)."""
-    if not (_daily(note) and isinstance(ctx.model, BlackScholesMertonParameters)):
+    if not (_daily(note, ctx.spot) and isinstance(ctx.model, BlackScholesMertonParameters)):
         return None
     template = plans.autocallable(note, ctx, allow_bridge=False)
+    if isinstance(template, plans.Known):
+        return None
     contract = template.contract.copy()
     times = [t for t in note.knock_in_times if t > 0.0]
     monitored = set(times)

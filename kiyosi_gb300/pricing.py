@@ -152,24 +152,48 @@ class _MonteCarloEngine:
                 builder.add(p)
                 index.append(i)
                 counts.append(path_counts[i] if path_counts is not None else 0)
-        if index:
-            packed = builder.build(counts)
-            native = context(self.device)
-            out = (abi.Estimate * len(index))()
-            model = ctx.kgpu_model()
+        if not index:
+            return results
+        settings = self._settings(seed)
+        if schedule is not None:
+            settings.schedule = schedule
+        # FP32 kernels cannot carry every plan (plans.fp32_representable): those
+        # contracts are priced by the FP64 kernels in a second launch.
+        wide = []
+        if settings.precision == abi.PRECISION_FP32:
+            wide = [j for j, i in enumerate(index)
+                    if not plans.fp32_representable(contract_plans[i], ctx)]
+        narrow = set(wide)
+        parts = [(settings, [j for j in range(len(index)) if j not in narrow])]
+        if wide:
+            fp64 = abi.Settings.from_buffer_copy(settings)
+            fp64.precision = abi.PRECISION_FP64
+            parts.append((fp64, wide))
+        native = context(self.device)
+        model = ctx.kgpu_model()
+        flag = None if cancel is None else C.byref(cancel)
+        for part_settings, members in parts:
+            if not members:
+                continue
+            if len(parts) == 1:
+                packed = builder.build(counts)
+            else:
+                sub = plans.BookBuilder()
+                for j in members:
+                    sub.add(builder.plans[j])
+                packed = sub.build([counts[j] for j in members])
+            out = (abi.Estimate * len(members))()
             book = packed.struct()
-            flag = None if cancel is None else C.byref(cancel)
-            settings = self._settings(seed)
-            if schedule is not None:
-                settings.schedule = schedule
-            elif self.tuning == "auto" and self.schedule == "persistent":
+            if (schedule is None and self.tuning == "auto" and self.schedule == "persistent"
+                    and part_settings.precision == settings.precision):
                 from . import autotune
-                shape, _ = autotune.tune(native, ctx, packed, settings)
-                settings = autotune.apply(settings, shape)
+                shape, _ = autotune.tune(native, ctx, packed, part_settings)
+                part_settings = autotune.apply(part_settings, shape)
             native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book),
-                                                    C.byref(settings), out, flag))
-            for j, i in enumerate(index):
-                results[i] = MonteCarloEstimate.from_native(out[j])
+                                                    C.byref(part_settings), out, flag))
+            for k, j in enumerate(members):
+                i = index[j]
+                results[i] = MonteCarloEstimate.from_native(out[k])
                 addend = getattr(contract_plans[i], "addend", None)
                 if addend is not None:
                     results[i] = replace(results[i], price=results[i].price + addend(ctx))
@@ -332,14 +356,31 @@ class MonteCarloAsianEngine(_MonteCarloEngine):
         return [prices[float(k)] for k in strikes]
 
 
-class MonteCarloAutocallableEngine(_MonteCarloEngine):
+class _TimeStepsMixin:
+    """`time_steps` (added keyword, default None): refines each contract's date grid so
+    that no path step is much longer than its life / time_steps (plans.refine_grid,
+    QuantLib's TimeGrid rule).  BSM steps are exact and need none; the Euler schemes of
+    local volatility and Heston use it to bound the discretisation error."""
+
+    def _init_time_steps(self, time_steps):
+        if time_steps is not None and int(time_steps) < 1:
+            raise InvalidInputError("time_steps must be positive")
+        self.time_steps = None if time_steps is None else int(time_steps)
+
+
+class MonteCarloAutocallableEngine(_MonteCarloEngine, _TimeStepsMixin):
     """Snowball / Phoenix notes (autocallable.rs), singly or as a batched book."""
+    _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + ("time_steps",)
+
+    def __init__(self, *, time_steps: Optional[int] = None, **kw):
+        super().__init__(**kw)
+        self._init_time_steps(time_steps)
 
     def _plan(self, note: AutocallableNote, ctx: PricingContext):
-        return plans.autocallable(note, ctx)
+        return plans.autocallable(note, ctx, time_steps=self.time_steps)
 
     def price_with_statistics(self, note: AutocallableNote, ctx: PricingContext):
-        return self._run(ctx, [plans.autocallable(note, ctx)])[0]
+        return self._run(ctx, [self._plan(note, ctx)])[0]
 
     def price_with_greeks(self, note: AutocallableNote, ctx: PricingContext, request, shifts=None):
         """Numerical Greeks with a pinned seed (autocallable.rs:174-283: the reference
@@ -369,15 +410,21 @@ class MonteCarloAutocallableEngine(_MonteCarloEngine):
         return self.price_many(notes, ctx, shared_grid=True)
 
     def price_many_with_statistics(self, notes, ctx: PricingContext, path_counts=None):
-        return self._run(ctx, [plans.autocallable(n, ctx) for n in notes], path_counts)
+        return self._run(ctx, [self._plan(n, ctx) for n in notes], path_counts)
 
 
-class MonteCarloAccumulatorEngine(_MonteCarloEngine):
+class MonteCarloAccumulatorEngine(_MonteCarloEngine, _TimeStepsMixin):
+    _STATE_FIELDS = _MonteCarloEngine._STATE_FIELDS + ("time_steps",)
+
+    def __init__(self, *, time_steps: Optional[int] = None, **kw):
+        super().__init__(**kw)
+        self._init_time_steps(time_steps)
+
     def _plan(self, option: Accumulator, ctx: PricingContext):
-        return plans.accumulator(option, ctx)
+        return plans.accumulator(option, ctx, time_steps=self.time_steps)
 
     def price_with_statistics(self, option: Accumulator, ctx: PricingContext):
-        return self._run(ctx, [plans.accumulator(option, ctx)])[0]
+        return self._run(ctx, [self._plan(option, ctx)])[0]
 
     def price_with_greeks(self, option: Accumulator, ctx: PricingContext, request, shifts=None):
         from .greeks import numerical_greeks

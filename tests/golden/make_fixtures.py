@@ -4,8 +4,9 @@ calibration records (benchmarks/quantlib/calibration/*.json, produced by the kiy
 
 Run in a checkout that has the reference mounted:
     python tests/golden/make_fixtures.py /path/to/kiyosi
-Writes european_calibration.json, barrier_calibration.json, american_calibration.json
-and known_answers.json here.
+Writes european_calibration.json, barrier_calibration.json, american_calibration.json,
+known_answers.json and local_volatility_structured.json (from the reference's QuantLib
+local-volatility fixture, python/tests/quantlib_reference/) here.
 """
 import ast
 import json
@@ -89,8 +90,18 @@ def main(root):
                               "inputs": prov.get("inputs") if isinstance(prov, dict) else None}
     json.dump({"source": "benchmarks/quantlib/references/*.json", "values": known},
               open(os.path.join(HERE, "known_answers.json"), "w"), indent=1)
+    # QuantLib local-volatility paths of the structured notes (the reference's Python test
+    # fixture; prices with antithetic-pair standard errors and the time-refinement bias).
+    lv = json.load(open(os.path.join(root, "python", "tests", "quantlib_reference",
+                                     "local_volatility_structured.json")))
+    keep = {k: lv["reference"][k] for k in ("quantlib_version", "pairs", "substeps_per_day",
+                                             "time_steps", "seed", "spot", "results")}
+    json.dump({"source": "python/tests/quantlib_reference/local_volatility_structured.json "
+                         "(generator local_volatility_paths.py)",
+               "reference": keep, "time_refinement": lv["time_refinement"][-1]},
+              open(os.path.join(HERE, "local_volatility_structured.json"), "w"), indent=1)
     print(len(rows), "European rows,", len(brows), "barrier rows,", len(arows), "American rows,",
-          len(known), "known answers")
+          len(known), "known answers,", len(keep["results"]), "local-volatility notes")
 
 
 if __name__ == "__main__":

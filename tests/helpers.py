@@ -72,3 +72,32 @@ def gpu_lsmc(native, ctx, strike, sign, expiry, s, fresh_seed=None):
                                             C.byref(s), s.seed if fresh_seed is None else fresh_seed,
                                             C.byref(out)))
     return out
+
+
+FP64_REL = 1e-12
+HALF_SE = 0.5
+
+
+def compare_gpu_oracle(native, ctx, packed, s, rel=FP64_REL, fp32_also=True):
+    """GPU prices of `packed` against the FP64 oracle on the same random numbers: FP64
+    (plain schedule) within `rel` relative with equal standard errors and statuses, and
+    FP32 (plain and persistent schedules) within half a sample standard error."""
+    from oracle import loader
+    ref = loader.price_book(ctx, packed, s)
+    got = gpu_price(native, ctx, packed, s)
+    for r, g in zip(ref, got):
+        assert abs(g.price - r.price) <= rel * max(1.0, abs(r.price)), (g.price, r.price)
+        assert g.uncertainty_status == r.uncertainty_status
+        if r.uncertainty_status == 0:
+            assert abs(g.standard_error - r.standard_error) <= 1e-9 * r.standard_error
+    if fp32_also:
+        for schedule in ("plain", "persistent"):
+            if schedule == "persistent" and s.antithetic:
+                continue
+            s32 = settings(s.path_count, s.seed, sobol=bool(s.sampling), precision="fp32",
+                           schedule=schedule, antithetic=bool(s.antithetic))
+            got32 = gpu_price(native, ctx, packed, s32)
+            for r, g in zip(ref, got32):
+                se = max(r.sample_error, 1e-12)
+                assert abs(g.price - r.price) <= HALF_SE * se, (schedule, g.price, r.price, se)
+    return ref, got
