@@ -493,24 +493,42 @@ def run_workload(args, name):
             walls.append(w)
             launches += native.last_launches
     path_steps = sum(e.path_steps for e in est32)
-    # FP64 plain, one launch per contract: the whole book, or its first 128 notes for the
-    # local-volatility book (the FP64 path would take minutes on all 4096).
+    # FP64 plain, one launch per contract (the speed comparator): the whole book, or its
+    # first 128 notes for the local-volatility book (one launch per note would take
+    # minutes on all 4096).
     fp64_n = min(len(est32), 128)
     _host_pricing(native, ctx, _first(packed, min(fp64_n, 2)), s64)  # loads the FP64 kernels
     est64, k64, _, _ = _host_pricing(native, ctx, _first(packed, fp64_n), s64)
     fp64_path_steps = sum(e.path_steps for e in est64)
-    worst = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(est32, est64))
-    # CPU oracle on a bounded sample: the first contracts at up to 2^13 paths.
-    sample_n = min(len(est32), 16)
-    sub = _first(packed, sample_n)
-    sub.contracts["path_count"] = np.minimum(np.where(sub.contracts["path_count"] > 0,
-                                                      sub.contracts["path_count"], paths[0]), 1 << 13)
-    s_cpu = abi.Settings(path_count=min(paths[0], 1 << 13), sampling=sampling, antithetic=0,
-                         precision=abi.PRECISION_FP64, schedule=abi.SCHEDULE_PLAIN, seed=seed)
+    # Parity over every contract at full size: FP32 against FP64 on the same random
+    # numbers, the FP64 side on the persistent schedule (one launch for the book).
+    s64_all = abi.Settings.from_buffer_copy(s64)
+    s64_all.schedule = abi.SCHEDULE_PERSISTENT
+    est64_all = _host_pricing(native, ctx, packed, s64_all)[0]
+    worst = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(est32, est64_all))
+    # Against the CPU oracle: every contract, at full size (C1, C3) or with each note's
+    # paths capped at 2^12 (the local-volatility book), GPU FP64 and FP32 on the same
+    # random numbers as the oracle.
+    cap = 1 << 12 if name == "lv-book" else None
+    sub = _first(packed, len(est32))
+    if cap:
+        sub.contracts["path_count"] = np.minimum(np.where(sub.contracts["path_count"] > 0,
+                                                          sub.contracts["path_count"], paths[0]), cap)
+    s_cpu = abi.Settings.from_buffer_copy(s64)
+    if cap:
+        s_cpu.path_count = min(paths[0], cap)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     cpu = loader.price_book(ctx, sub, s_cpu, threads=threads)
     cpu_s = time.perf_counter() - t0
+    s64_sub = abi.Settings.from_buffer_copy(s_cpu)
+    s64_sub.schedule = abi.SCHEDULE_PERSISTENT
+    g64 = _host_pricing(native, ctx, sub, s64_sub)[0]
+    s32_sub = abi.Settings.from_buffer_copy(s32)
+    s32_sub.path_count = s_cpu.path_count
+    g32 = _host_pricing(native, ctx, sub, s32_sub)[0]
+    oracle_fp64_rel = max(abs(a.price - b.price) / max(abs(b.price), 1.0) for a, b in zip(g64, cpu))
+    oracle_fp32_se = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(g32, cpu))
     ms = statistics.median(kernel)
     line = {
         "metric": "path-steps/s (FP32 batched vs FP64 plain) at <=0.5 SE",
@@ -530,11 +548,20 @@ def run_workload(args, name):
         "fp64_plain": {"value": fp64_path_steps / (k64 / 1e3), "unit": "path-steps/s",
                        "ms": k64, "contracts": fp64_n,
                        "speedup_fp32_persistent": (path_steps / (ms / 1e3)) / (fp64_path_steps / (k64 / 1e3))},
-        "parity": {"max_fp32_vs_fp64_in_se": worst, "contracts": fp64_n},
+        "parity": {"contracts": len(est32),
+                   "max_fp32_vs_fp64_in_se": worst,
+                   "fp64_schedule": "persistent (one launch, every contract, full paths)",
+                   "oracle": {"paths": f"each note capped at {cap}" if cap else "full",
+                              "max_err_in_se": oracle_fp32_se,
+                              "max_fp64_gpu_rel_err": oracle_fp64_rel,
+                              "note": "GPU FP32 (persistent) and FP64 against the FP64 CPU oracle "
+                                      "on the same random numbers, every contract"}},
         "executed_steps_per_path_step": sum(e.executed_steps for e in est32) / path_steps,
+        "executed_path_steps_per_s": sum(e.executed_steps for e in est32) / (ms / 1e3),
         "cpu_baseline": {"value": sum(e.path_steps for e in cpu) / cpu_s,
                          "unit": "path-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample_n} contracts at up to 2^13 paths, FP64 oracle"},
+                         "sample": (f"all {len(est32)} contracts at up to {cap} paths" if cap else
+                                    "the full workload") + ", FP64 oracle"},
     }
     print(json.dumps(line), flush=True)
 
@@ -684,6 +711,28 @@ def run_lsmc(args):
 
     poly = price(abi.BASIS_POLY3, 20)
     poly64 = price(abi.BASIS_POLY3, 20, precision=abi.PRECISION_FP64)
+    # The configuration at full size on the FP64 CPU oracle (same random numbers):
+    # 2^20 paths x 50 dates x 5 substeps, polynomial basis, fresh-path pass included.
+    s_or = abi.LsmcSettings(path_count=1 << 20, exercise_dates=50, substeps=5, basis=abi.BASIS_POLY3,
+                            sampling=0, precision=abi.PRECISION_FP64, mlp_epochs=5, mlp_batch=8192,
+                            mlp_hidden=64, mlp_samples=0, mlp_learning_rate=1e-3, seed=42, mlp_seed=7)
+    oracle = abi.LsmcResult()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    st = loader.load().kor_lsmc_price(C.byref(model), 100.0, -1.0, 1.0, C.byref(s_or), 43,
+                                      C.byref(oracle), threads)
+    oracle_s = time.perf_counter() - t0
+    assert st == 0, st
+    oracle_parity = {
+        "paths": 1 << 20, "dates": 50, "substeps": 5, "basis": "poly3",
+        "oracle_price": oracle.price, "oracle_out_of_sample": oracle.out_of_sample,
+        "fp64_gpu_rel_err": abs(poly64["price"] - oracle.price) / oracle.price,
+        "fp64_gpu_out_of_sample_rel_err": abs(poly64["out_of_sample"] - oracle.out_of_sample) / oracle.out_of_sample,
+        "fp32_err_in_se": abs(poly["price"] - oracle.price) / oracle.standard_error,
+        "fp32_out_of_sample_err_in_se": abs(poly["out_of_sample"] - oracle.out_of_sample) / oracle.out_of_sample_error,
+        "max_err_in_se": max(abs(poly["price"] - oracle.price) / oracle.standard_error,
+                             abs(poly["out_of_sample"] - oracle.out_of_sample) / oracle.out_of_sample_error),
+        "oracle_cpu_s": oracle_s, "oracle_threads": threads}
     mlp = price(abi.BASIS_MLP, 20)
     mlp_eq = price(abi.BASIS_MLP, 22, samples=131072)
     polys = [price(abi.BASIS_POLY3, k) for k in range(21, 27)]
@@ -699,6 +748,7 @@ def run_lsmc(args):
                                "epochs/date, batch 8192", "fresh_paths_seed": 43},
         "adi": {"price": adi, "grid": "400 x 100 x 400 (MCS, Ikonen-Toivanen)", "cpu_s": adi_s},
         "at_2^20_paths": {"poly3_fp32": poly, "poly3_fp64": poly64, "poly3_plus_network": mlp},
+        "parity": {"oracle": oracle_parity},
         "at_equal_wall_time": {"poly3_plus_network": mlp_eq, "poly3": equal},
         "poly3_by_paths": polys,
     }

@@ -106,6 +106,24 @@ def test_local_vol_book(native):
     _compare(native, ctx, packed, settings(256, 7), rel=1e-10)
 
 
+def test_local_vol_book_every_contract(native):
+    """The benchmark's whole 4096-note local-volatility book (every maturity, level and
+    coupon it draws) with each note's paths capped at 2^10: GPU FP64 on both schedules
+    within 1e-10 of the oracle, FP32 persistent within half a standard error, all on the
+    same random numbers."""
+    notes, paths = lv_book(4096)
+    ctx = PricingContext(lv_surface(), 100.0)
+    packed = pack([plans.autocallable(n, ctx) for n in notes], [min(p, 1 << 10) for p in paths])
+    ref = loader.price_book(ctx, packed, settings(1 << 10, 7))
+    for schedule in ("plain", "persistent"):
+        got = gpu_price(native, ctx, packed, settings(1 << 10, 7, schedule=schedule))
+        worst = max(abs(g.price - r.price) / max(1.0, abs(r.price)) for g, r in zip(got, ref))
+        assert worst <= 1e-10, (schedule, worst)
+    got32 = gpu_price(native, ctx, packed, settings(1 << 10, 7, precision="fp32", schedule="persistent"))
+    worst = max(abs(g.price - r.price) / max(r.sample_error, 1e-12) for g, r in zip(got32, ref))
+    assert worst <= HALF_SE, worst
+
+
 def test_accumulator_and_digital(native):
     ctx = bsm(0.03, 0.01, 0.3)
     dt = 1.0 / 252
