@@ -410,6 +410,8 @@ def run_kernel_only(args):
     book = packed.struct()
     s = (settings(abi.PRECISION_FP32, abi.SCHEDULE_PERSISTENT, args.paths)
          if args.kernel_only == "fp32" else
+         settings(abi.PRECISION_FP32, abi.SCHEDULE_LANE_REFILL, args.paths)
+         if args.kernel_only == "fp32-lanes" else
          settings(abi.PRECISION_FP64, abi.SCHEDULE_PLAIN, args.paths))
     out = (abi.Estimate * 1)()
     for _ in range(args.warmup + args.steps):
@@ -807,7 +809,7 @@ def main():
                     help="LSMC network: in-the-money samples trained on per date (0: all)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the kernel's default launch shape instead of the autotuner's")
-    ap.add_argument("--kernel-only", choices=["fp32", "fp64", "lsmc-poly", "lsmc-mlp", "shared-grid"],
+    ap.add_argument("--kernel-only", choices=["fp32", "fp32-lanes", "fp64", "lsmc-poly", "lsmc-mlp", "shared-grid"],
                     help="run only the device-resident pricing of one arm (for profilers)")
     ap.add_argument("--tile", type=int, default=0, help="persistent tile paths (0 = default)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")

@@ -58,16 +58,28 @@ enum { KGPU_PRECISION_FP64 = 0, KGPU_PRECISION_FP32 = 1 };
 
 /* Launch schedule.  PLAIN: one contract per launch, one thread per sample, the
  * reference's 256-sample blocks as CUDA blocks, sequential scaled-Welford moments per
- * block merged in block order.  PERSISTENT: one launch for the whole book; warps pull
- * (contract, tile) work items from a device queue and refill finished lanes with the
- * next path of the tile. */
+ * block merged in block order.  PERSISTENT: the whole book at once.  A book whose every
+ * contract is a Brownian-bridged autocallable (KGPU_C_BRIDGE, BSM) runs phase-major in
+ * FP32: one launch per bridge interval advances every path still monitoring knock-in by
+ * one interval, the lanes of a warp on the same grid positions, survivors compacted into
+ * the next interval's list; knocked-in paths are completed by one final launch.  Other
+ * books (and FP64) run the lane-refill kernel: warps pull (contract, tile) work items
+ * from a device queue and refill finished lanes with the next path of the tile.
+ * LANE_REFILL: the lane-refill kernel for every book.  Both persistent kernels store each
+ * path's payoff and sum the payoffs in a fixed order, so their estimates are identical
+ * for a book both can run. */
 /* KGPU_SCHEDULE_SHARED_GRID: the book's contracts are the lanes of one shared daily grid
  * (bridged autocallables whose steps, bridge intervals and bridge weights are prefixes of
  * the longest lane's, with equal sampling dimensions and path counts).  One thread per
  * path walks the longest lane's plan once and settles every lane on it; the estimates
  * equal those of the plain schedule up to the order of the sums.  Pseudo-random or
  * Sobol, with or without antithetic pairs; host-resident books only. */
-enum { KGPU_SCHEDULE_PLAIN = 0, KGPU_SCHEDULE_PERSISTENT = 1, KGPU_SCHEDULE_SHARED_GRID = 2 };
+enum {
+    KGPU_SCHEDULE_PLAIN = 0,
+    KGPU_SCHEDULE_PERSISTENT = 1,
+    KGPU_SCHEDULE_SHARED_GRID = 2,
+    KGPU_SCHEDULE_LANE_REFILL = 3
+};
 
 /* MonteCarloSettings (monte_carlo.rs:86-105) plus the GPU controls. */
 typedef struct kgpu_settings {

@@ -22,6 +22,7 @@ PRECISION_FP32 = 1
 SCHEDULE_PLAIN = 0
 SCHEDULE_PERSISTENT = 1
 SCHEDULE_SHARED_GRID = 2
+SCHEDULE_LANE_REFILL = 3
 
 MODEL_BSM = 0
 MODEL_HESTON = 1

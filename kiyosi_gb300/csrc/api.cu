@@ -621,6 +621,81 @@ bool extended_payoffs(const kgpu_book& b) {
     return false;
 }
 
+// Per-path value slots of every contract, the reduction chunks over them and the
+// per-contract counters of simulated positions, staged for a persistent or phased launch.
+template <class Real>
+kgpu_status stage_values(Call& k, int* chunk_count) {
+    kgpu_context* ctx = k.ctx;
+    const int n = k.raw.contract_count;
+    std::vector<int64_t> value_offset(n + 1, 0);
+    for (int i = 0; i < n; ++i) value_offset[i + 1] = value_offset[i] + k.info[i].samples;
+    // Reduction chunks of each contract's per-path values.
+    const int64_t chunk = 4096;
+    std::vector<int4> chunks;
+    std::vector<int> first_chunk(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        first_chunk[i] = int(chunks.size());
+        for (int64_t b = 0; b < k.info[i].samples; b += chunk)
+            chunks.push_back(make_int4(i, int(b), int(std::min<int64_t>(chunk, k.info[i].samples - b)), 0));
+    }
+    first_chunk[n] = int(chunks.size());
+    kgpu_status st;
+    if ((st = upload(ctx, ctx->value_offset, value_offset.data(), value_offset.size() * sizeof(int64_t))) ||
+        (st = upload(ctx, ctx->chunks, chunks.data(), chunks.size() * sizeof(int4))) ||
+        (st = upload(ctx, ctx->first_item, first_chunk.data(), first_chunk.size() * sizeof(int))))
+        return st;
+    if (ctx->values.ensure(size_t(value_offset[n]) * sizeof(Real)) ||
+        ctx->tiles.ensure(chunks.size() * sizeof(TilePartial)) || ctx->tile_out.ensure(size_t(n) * sizeof(TilePartial)) ||
+        ctx->executed.ensure(size_t(n) * sizeof(unsigned long long)) || ctx->queue.ensure(sizeof(int) * 4))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of path values failed");
+    CUDA_TRY(ctx, cudaMemsetAsync(static_cast<int*>(ctx->queue.ptr) + 1, 0, sizeof(int), ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(ctx->executed.ptr, 0, size_t(n) * sizeof(unsigned long long), ctx->stream));
+    *chunk_count = int(chunks.size());
+    return KGPU_OK;
+}
+
+// Sums the per-path values in a fixed order, reads the sums, the simulated positions and
+// the cancellation state back, and forms the estimates.
+template <class Real>
+kgpu_status finish_values(Call& k, int chunk_count, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const kgpu_settings& s = k.s;
+    const int n = k.raw.contract_count;
+    reduce_values_kernel<Real><<<chunk_count, 256, 0, ctx->stream>>>(
+        static_cast<const Real*>(ctx->values.ptr), static_cast<const int4*>(ctx->chunks.ptr),
+        static_cast<const int64_t*>(ctx->value_offset.ptr), static_cast<TilePartial*>(ctx->tiles.ptr));
+    CUDA_TRY(ctx, cudaGetLastError());
+    reduce_tiles_kernel<<<n, 256, 0, ctx->stream>>>(static_cast<const TilePartial*>(ctx->tiles.ptr),
+                                                     static_cast<const int*>(ctx->first_item.ptr),
+                                                     static_cast<TilePartial*>(ctx->tile_out.ptr));
+    CUDA_TRY(ctx, cudaGetLastError());
+    launches += 2;
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
+    std::vector<TilePartial> sums(n);
+    std::vector<unsigned long long> executed(n);
+    int aborted = 0;
+    CUDA_TRY(ctx, cudaMemcpyAsync(sums.data(), ctx->tile_out.ptr, sizeof(TilePartial) * n, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpyAsync(executed.data(), ctx->executed.ptr, sizeof(unsigned long long) * n,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpyAsync(&aborted, static_cast<int*>(ctx->queue.ptr) + 1, sizeof(int),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (aborted) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
+    for (int i = 0; i < n; ++i) {
+        const kgpu_contract& c = k.book->contracts[i];
+        sums[i].executed = double(executed[i]);
+        estimate_from_sums(c, s, k.info[i].paths, sums[i], &k.out[i]);
+        int grid = terminal_payoff(c) ? 1 : c.step_count;
+        k.out[i].path_steps = double(k.info[i].paths) * grid;
+        k.out[i].executed_steps = sums[i].executed;
+        if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].standard_error))
+            return fail(ctx, KGPU_COMPUTATION_FAILURE,
+                        "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
+    }
+    return KGPU_OK;
+}
+
 template <class Real>
 kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
     const bool ext = extended_payoffs(*k.book);
@@ -661,36 +736,16 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
     // Work items grouped by contract, in contract order.  Sobol tiles are one reference
     // block (they share the block's high gray-code bits).
     std::vector<int4> items;
-    std::vector<int64_t> value_offset(n + 1, 0);
     for (int i = 0; i < n; ++i) {
         int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision);
         for (int64_t b = 0; b < k.info[i].samples; b += tile)
             items.push_back(make_int4(i, int(b), int(std::min<int64_t>(tile, k.info[i].samples - b)), k.info[i].dims));
-        value_offset[i + 1] = value_offset[i] + k.info[i].samples;
     }
-    // Reduction chunks of each contract's per-path values.
-    const int64_t chunk = 4096;
-    std::vector<int4> chunks;
-    std::vector<int> first_chunk(n + 1, 0);
-    for (int i = 0; i < n; ++i) {
-        first_chunk[i] = int(chunks.size());
-        for (int64_t b = 0; b < k.info[i].samples; b += chunk)
-            chunks.push_back(make_int4(i, int(b), int(std::min<int64_t>(chunk, k.info[i].samples - b)), 0));
-    }
-    first_chunk[n] = int(chunks.size());
     const int item_count = int(items.size());
     kgpu_status st;
-    if ((st = upload(ctx, ctx->items, items.data(), items.size() * sizeof(int4))) ||
-        (st = upload(ctx, ctx->value_offset, value_offset.data(), value_offset.size() * sizeof(int64_t))) ||
-        (st = upload(ctx, ctx->chunks, chunks.data(), chunks.size() * sizeof(int4))) ||
-        (st = upload(ctx, ctx->first_item, first_chunk.data(), first_chunk.size() * sizeof(int))))
-        return st;
-    if (ctx->values.ensure(size_t(value_offset[n]) * sizeof(Real)) ||
-        ctx->tiles.ensure(chunks.size() * sizeof(TilePartial)) || ctx->tile_out.ensure(size_t(n) * sizeof(TilePartial)) ||
-        ctx->executed.ensure(size_t(n) * sizeof(unsigned long long)) || ctx->queue.ensure(sizeof(int) * 4))
-        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of path values failed");
-    CUDA_TRY(ctx, cudaMemsetAsync(static_cast<int*>(ctx->queue.ptr) + 1, 0, sizeof(int), ctx->stream));
-    CUDA_TRY(ctx, cudaMemsetAsync(ctx->executed.ptr, 0, size_t(n) * sizeof(unsigned long long), ctx->stream));
+    if ((st = upload(ctx, ctx->items, items.data(), items.size() * sizeof(int4)))) return st;
+    int chunk_count = 0;
+    if ((st = stage_values<Real>(k, &chunk_count))) return st;
     CancelWatcher watcher(k.cancel, ctx->cancel_host);
     std::vector<int> order;
     std::vector<int> first_item(n + 1, 0);
@@ -764,39 +819,126 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
         // `order` is reused by the next group: wait for this launch's upload to be consumed.
         if (group_dims.size() > 1) CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     }
-    reduce_values_kernel<Real><<<int(chunks.size()), 256, 0, ctx->stream>>>(
-        static_cast<const Real*>(ctx->values.ptr), static_cast<const int4*>(ctx->chunks.ptr),
-        static_cast<const int64_t*>(ctx->value_offset.ptr), static_cast<TilePartial*>(ctx->tiles.ptr));
-    CUDA_TRY(ctx, cudaGetLastError());
-    reduce_tiles_kernel<<<n, 256, 0, ctx->stream>>>(static_cast<const TilePartial*>(ctx->tiles.ptr),
-                                                     static_cast<const int*>(ctx->first_item.ptr),
-                                                     static_cast<TilePartial*>(ctx->tile_out.ptr));
-    CUDA_TRY(ctx, cudaGetLastError());
-    launches += 2;
-    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
-    std::vector<TilePartial> sums(n);
-    std::vector<unsigned long long> executed(n);
-    int aborted = 0;
-    CUDA_TRY(ctx, cudaMemcpyAsync(sums.data(), ctx->tile_out.ptr, sizeof(TilePartial) * n, cudaMemcpyDeviceToHost,
-                                  ctx->stream));
-    CUDA_TRY(ctx, cudaMemcpyAsync(executed.data(), ctx->executed.ptr, sizeof(unsigned long long) * n,
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    CUDA_TRY(ctx, cudaMemcpyAsync(&aborted, static_cast<int*>(ctx->queue.ptr) + 1, sizeof(int),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
-    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (aborted) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
-    for (int i = 0; i < n; ++i) {
-        const kgpu_contract& c = k.book->contracts[i];
-        sums[i].executed = double(executed[i]);
-        estimate_from_sums(c, s, k.info[i].paths, sums[i], &k.out[i]);
-        int grid = terminal_payoff(c) ? 1 : c.step_count;
-        k.out[i].path_steps = double(k.info[i].paths) * grid;
-        k.out[i].executed_steps = sums[i].executed;
-        if (!std::isfinite(k.out[i].price) || !std::isfinite(k.out[i].standard_error))
-            return fail(ctx, KGPU_COMPUTATION_FAILURE,
-                        "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
+    return finish_values<Real>(k, chunk_count, launches);
+}
+
+// Phase-major schedule (phased.cuh) of books whose every contract is a bridged
+// autocallable: FP32, BSM, the persistent schedule, one Sobol dimension count.
+bool phased_eligible(const Call& k) {
+    if (k.s.precision != KGPU_PRECISION_FP32 || k.s.schedule != KGPU_SCHEDULE_PERSISTENT ||
+        k.model->kind != KGPU_MODEL_BSM || k.s.antithetic)
+        return false;
+    const kgpu_book& b = *k.book;
+    if (b.contract_count >= (1 << (32 - kPhaseTagShift))) return false;
+    int64_t total = 0;
+    for (int i = 0; i < b.contract_count; ++i) {
+        const kgpu_contract& c = b.contracts[i];
+        if (c.payoff != KGPU_PAYOFF_AUTOCALLABLE || !(c.flags & KGPU_C_BRIDGE) || c.bridge_count < 1 ||
+            c.bridge_count >= kPhaseMaxIntervals)
+            return false;
+        if (k.sobol && k.info[i].dims != k.info[0].dims) return false;
+        total += k.info[i].samples;
     }
-    return KGPU_OK;
+    // Two generations of the monitoring list and the knocked-in pool.
+    const int64_t entry = k.sobol ? 16 : 32;
+    return total < (int64_t(1) << 31) && total * entry * 3 <= (int64_t(16) << 30);
+}
+
+template <class Real, bool SOBOL>
+kgpu_status run_phased_impl(Call& k, DevBook<Real> db, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const kgpu_settings& s = k.s;
+    const int n = k.raw.contract_count;
+    using Entry = PhaseEntry<Real, SOBOL>;
+    if (ctx->cunits.ensure(size_t(k.raw.step_total) * sizeof(UnitT<Real>)) ||
+        ctx->cends.ensure(size_t(k.raw.step_total) * sizeof(EndT<Real>)))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of bridge units failed");
+    CUDA_TRY(ctx, PrecisionOps<Real>::units(k.raw.contracts, n, k.raw.intervals, k.raw.daily, k.raw.flags, k.raw.events,
+                                            static_cast<UnitT<Real>*>(ctx->cunits.ptr),
+                                            static_cast<EndT<Real>*>(ctx->cends.ptr), ctx->stream));
+    db.units = static_cast<const UnitT<Real>*>(ctx->cunits.ptr);
+    db.ends = static_cast<const EndT<Real>*>(ctx->cends.ptr);
+    launches += 1;
+    kgpu_status st;
+    int chunk_count = 0;
+    if ((st = stage_values<Real>(k, &chunk_count))) return st;
+    int64_t total = 0;
+    int phases = 0;
+    std::vector<int> dims(n);
+    for (int i = 0; i < n; ++i) {
+        total += k.info[i].samples;
+        phases = std::max(phases, k.book->contracts[i].bridge_count);
+        dims[i] = k.info[i].dims;
+    }
+    if ((st = upload(ctx, ctx->phase_dims, dims.data(), dims.size() * sizeof(int)))) return st;
+    // Monitoring-list sizes of every generation, the knocked-in pool size, the
+    // completion flag.
+    const size_t count_bytes = (size_t(phases + 1) + 2) * sizeof(int);
+    if (ctx->phase_lists.ensure(3 * size_t(total) * sizeof(Entry) + 16) || ctx->phase_counts.ensure(count_bytes))
+        return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the phase lists failed");
+    CUDA_TRY(ctx, cudaMemsetAsync(ctx->phase_counts.ptr, 0, count_bytes, ctx->stream));
+    PhaseArgs<Real, SOBOL> a;
+    a.book = db;
+    a.contract_count = n;
+    a.total = total;
+    a.value_offset = static_cast<const int64_t*>(ctx->value_offset.ptr);
+    a.dims = static_cast<const int*>(ctx->phase_dims.ptr);
+    a.values = static_cast<Real*>(ctx->values.ptr);
+    a.executed = static_cast<unsigned long long*>(ctx->executed.ptr);
+    a.seed = s.seed;
+    a.sobol = SobolTables{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    a.high_t = nullptr;
+    a.high_blocks = 0;
+    if (SOBOL) {
+        if ((st = ensure_sobol(ctx, k.info[0].dims, s.seed, &a.sobol))) return st;
+        int64_t blocks = 1;
+        for (int i = 0; i < n; ++i) blocks = std::max<int64_t>(blocks, (k.info[i].samples + 255) / 256);
+        if (ctx->sobol_high32.ensure(size_t(blocks) * k.info[0].dims * 4))
+            return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the Sobol high table failed");
+        CUDA_TRY(ctx, launch_sobol_high_t(a.sobol, int(blocks), static_cast<uint32_t*>(ctx->sobol_high32.ptr),
+                                          ctx->stream));
+        a.high_t = static_cast<const uint32_t*>(ctx->sobol_high32.ptr);
+        a.high_blocks = int(blocks);
+        launches += 1;
+    }
+    a.cancel = k.cancel ? ctx->cancel_dev : nullptr;
+    a.aborted = static_cast<int*>(ctx->queue.ptr) + 1;
+    const int per_sm = phased_occupancy_fp32(SOBOL);
+    const int64_t warps_needed = (total + 31) / 32;
+    const int grid = int(std::max<int64_t>(1, std::min<int64_t>(int64_t(ctx->sm_count) * per_sm,
+                                                                (warps_needed + kWarps - 1) / kWarps)));
+    Entry* lists = static_cast<Entry*>(ctx->phase_lists.ptr);
+    int* counts = static_cast<int*>(ctx->phase_counts.ptr);
+    a.knocked = lists + 2 * size_t(total);
+    a.knocked_count = counts + phases + 1;
+    a.finished = counts + phases + 2;
+    // Monitoring paths that fit in one wave of resident lanes run to completion in one
+    // launch.
+    a.complete_below = int64_t(ctx->sm_count) * per_sm * kThreads;
+    CancelWatcher watcher(k.cancel, ctx->cancel_host);
+    CUDA_TRY(ctx, path_kernel_begin(ctx));
+    for (int p = 0; p <= phases; ++p) {
+        // Phase p reads monitoring list (p % 2) and writes list ((p + 1) % 2); the last
+        // launch drains the knocked-in pool.
+        a.drain = p == phases;
+        a.phase = a.drain ? 0 : p;
+        a.in_monitoring = lists + size_t(p % 2) * total;
+        a.in_count = counts + p;
+        a.out_monitoring = lists + size_t((p + 1) % 2) * total;
+        a.out_count = counts + std::min(p + 1, phases);
+        CUDA_TRY(ctx, launch_phased_fp32(grid, ctx->stream, a));
+        launches += 1;
+    }
+    CUDA_TRY(ctx, path_kernel_end(ctx));
+    return finish_values<Real>(k, chunk_count, launches);
+}
+
+template <class Real>
+kgpu_status run_phased(Call& k, DevBook<Real> db, int& launches) {
+    if constexpr (std::is_same<Real, float>::value)
+        return k.sobol ? run_phased_impl<Real, true>(k, db, launches) : run_phased_impl<Real, false>(k, db, launches);
+    else
+        return fail(k.ctx, KGPU_UNSUPPORTED_OPERATION, "the phase-major schedule runs in FP32");
 }
 
 // KGPU_SCHEDULE_SHARED_GRID: the lanes of one shared daily grid on one path per sample
@@ -958,7 +1100,9 @@ kgpu_status run_book(Call& k) {
     kgpu_status st = compile_book<Real>(k, &db);
     if (st) return st;
     int launches = std::is_same<Real, float>::value ? 2 : 1;
-    st = k.s.schedule == KGPU_SCHEDULE_PERSISTENT    ? run_persistent<Real>(k, db, launches)
+    st = k.s.schedule == KGPU_SCHEDULE_PERSISTENT    ? (phased_eligible(k) ? run_phased<Real>(k, db, launches)
+                                                                           : run_persistent<Real>(k, db, launches))
+         : k.s.schedule == KGPU_SCHEDULE_LANE_REFILL ? run_persistent<Real>(k, db, launches)
          : k.s.schedule == KGPU_SCHEDULE_SHARED_GRID ? run_shared<Real>(k, db, shared, launches)
                                                      : run_plain<Real>(k, db, launches);
     float ms = 0;
@@ -1000,8 +1144,8 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
     if (model->kind < KGPU_MODEL_BSM || model->kind > KGPU_MODEL_LOCAL_VOL)
         return fail(ctx, KGPU_INVALID_INPUT, "unknown model %d", model->kind);
     k.sobol = s.sampling == KGPU_SAMPLING_SOBOL;
-    const bool persistent = s.schedule == KGPU_SCHEDULE_PERSISTENT;
-    if (s.schedule < KGPU_SCHEDULE_PLAIN || s.schedule > KGPU_SCHEDULE_SHARED_GRID)
+    const bool persistent = s.schedule == KGPU_SCHEDULE_PERSISTENT || s.schedule == KGPU_SCHEDULE_LANE_REFILL;
+    if (s.schedule < KGPU_SCHEDULE_PLAIN || s.schedule > KGPU_SCHEDULE_LANE_REFILL)
         return fail(ctx, KGPU_INVALID_INPUT, "unknown schedule %d", s.schedule);
     if (persistent && s.antithetic)
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION,

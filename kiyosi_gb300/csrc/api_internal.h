@@ -45,6 +45,9 @@ struct kgpu_context {
     kgpu::DeviceBuffer partials, merged, shared_slots;
     // persistent schedule
     kgpu::DeviceBuffer items, order, first_item, tiles, tile_out, queue, values, value_offset, chunks, executed;
+    // phase-major schedule: two generations of the monitoring list and the knocked-in
+    // pool, the list sizes and completion flag, per-contract sampling dimensions
+    kgpu::DeviceBuffer phase_lists, phase_counts, phase_dims;
     // plan in the kernel's precision (contract table always, arrays for FP32)
     kgpu::DeviceBuffer ccontracts, csteps, cevents, cintervals, cdaily, cunits, cends;
     // Sobol sequence cache (one sequence per (seed, dims))
@@ -75,7 +78,7 @@ struct kgpu_context {
     std::vector<kgpu::DeviceBuffer*> buffers() {
         return {&contracts, &steps,     &flags,     &events,   &intervals, &daily,     &lv,
                 &partials,  &merged,    &shared_slots, &items,     &order,    &first_item, &tiles,    &tile_out,
-                &queue,     &values,    &value_offset, &chunks, &executed, &sobol_dirs, &sobol_shifts, &sobol_nibbles, &sobol_dirs32, &sobol_shifts32, &sobol_nibbles32, &sobol_high32, &ccontracts, &csteps,
+                &queue,     &values,    &value_offset, &chunks, &executed, &phase_lists, &phase_counts, &phase_dims, &sobol_dirs, &sobol_shifts, &sobol_nibbles, &sobol_dirs32, &sobol_shifts32, &sobol_nibbles32, &sobol_high32, &ccontracts, &csteps,
                 &cevents,   &cintervals, &cdaily,      &cunits,     &cends,      &lsmc_store, &lsmc_cash, &lsmc_sums,
                 &lsmc_coef, &lsmc_misc, &mlp_params, &mlp_scratch, &stream_out};
     }

@@ -1,6 +1,7 @@
 // Instantiation body shared by kernels_fp64.cu and kernels_fp32.cu; REAL and PRECISION
 // are defined by the including translation unit.
 #include "launch.h"
+#include "phased.cuh"
 #include "shared_grid.cuh"
 
 namespace kgpu {
@@ -122,6 +123,34 @@ static __global__ void sobol_points_kernel(SobolTables t, int dim, uint64_t firs
 }
 
 #if KGPU_FP32_UNIT
+template <bool SOBOL>
+static cudaError_t phased_one(int blocks, cudaStream_t s, const PhaseArgs<float, SOBOL>& a) {
+    phased_kernel<float, SOBOL><<<blocks, kThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, true>& a) {
+    return phased_one<true>(blocks, s, a);
+}
+
+cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, false>& a) {
+    return phased_one<false>(blocks, s, a);
+}
+
+int phased_occupancy_fp32(bool sobol) {
+    int n = 0;
+    const cudaError_t e = sobol ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phased_kernel<float, true>, kThreads, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phased_kernel<float, false>, kThreads, 0);
+    return e == cudaSuccess && n > 0 ? n : 1;
+}
+
+cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s) {
+    const int64_t total = int64_t(blocks) * t.dims;
+    if (total <= 0) return cudaSuccess;
+    sobol_high_table_t_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(t, blocks, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, EventT<float>* events,
                                        IntervalT<float>* intervals, DailyT<float>* daily,
                                        cudaStream_t s) {

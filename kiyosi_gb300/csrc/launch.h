@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "phased.cuh"
 #include "shared_grid.cuh"
 
 namespace kgpu {
@@ -43,6 +44,13 @@ cudaError_t launch_compile_units_fp32(const kgpu_contract* contracts, int n,
 cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, EventT<float>* events,
                                        IntervalT<float>* intervals, DailyT<float>* daily,
                                        cudaStream_t s);
+
+// Phase-major schedule of bridged autocallable books (FP32): one launch per bridge
+// interval and a final drain launch; the dimension-major Sobol high table it reads.
+cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, true>& a);
+cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, false>& a);
+int phased_occupancy_fp32(bool sobol);
+cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s);
 
 // The lanes of one shared daily grid, path-major, and the merge of their CTA sums.
 // `ctas` path tiles x `chunks` lane chunks.

@@ -120,7 +120,7 @@ extern "C" kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, cons
         return noalloc_fail(KGPU_UNSUPPORTED_OPERATION, "the no-allocation entry point samples pseudo-random paths");
     if (settings->precision != KGPU_PRECISION_FP64 && settings->precision != KGPU_PRECISION_FP32)
         return noalloc_fail(KGPU_INVALID_INPUT, "unknown precision");
-    if (settings->schedule < KGPU_SCHEDULE_PLAIN || settings->schedule > KGPU_SCHEDULE_SHARED_GRID)
+    if (settings->schedule < KGPU_SCHEDULE_PLAIN || settings->schedule > KGPU_SCHEDULE_LANE_REFILL)
         return noalloc_fail(KGPU_INVALID_INPUT, "unknown schedule");
     if (settings->precision != KGPU_PRECISION_FP64 || settings->schedule != KGPU_SCHEDULE_PLAIN)
         return noalloc_fail(KGPU_UNSUPPORTED_OPERATION,

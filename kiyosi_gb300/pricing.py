@@ -24,7 +24,7 @@ SOBOL = "sobol"
 _SAMPLING = {PSEUDO_RANDOM: abi.SAMPLING_PSEUDO_RANDOM, SOBOL: abi.SAMPLING_SOBOL}
 _PRECISION = {"fp64": abi.PRECISION_FP64, "fp32": abi.PRECISION_FP32}
 _SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT,
-             "shared_grid": abi.SCHEDULE_SHARED_GRID}
+             "shared_grid": abi.SCHEDULE_SHARED_GRID, "lane_refill": abi.SCHEDULE_LANE_REFILL}
 Z95 = 1.959963984540054
 
 

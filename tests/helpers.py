@@ -13,7 +13,7 @@ from kiyosi_gb300.market import (BlackScholesMertonParameters, HestonParameters,
 
 PRECISION = {"fp64": abi.PRECISION_FP64, "fp32": abi.PRECISION_FP32}
 SCHEDULE = {"plain": abi.SCHEDULE_PLAIN, "persistent": abi.SCHEDULE_PERSISTENT,
-             "shared_grid": abi.SCHEDULE_SHARED_GRID}
+             "shared_grid": abi.SCHEDULE_SHARED_GRID, "lane_refill": abi.SCHEDULE_LANE_REFILL}
 
 
 def settings(paths, seed, sobol=False, antithetic=False, precision="fp64", schedule="plain",
