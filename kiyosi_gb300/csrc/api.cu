@@ -406,6 +406,7 @@ static kgpu_status ensure_sobol(kgpu_context* ctx, int dims, uint64_t seed, Sobo
         CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
         ctx->sobol_dims = dims;
         ctx->sobol_seed = seed;
+        ctx->sobol_high_t_blocks = 0;
     }
     t->directions = static_cast<const uint64_t*>(ctx->sobol_dirs.ptr);
     t->shifts = static_cast<const uint64_t*>(ctx->sobol_shifts.ptr);
@@ -629,8 +630,8 @@ kgpu_status stage_values(Call& k, int* chunk_count) {
     const int n = k.raw.contract_count;
     std::vector<int64_t> value_offset(n + 1, 0);
     for (int i = 0; i < n; ++i) value_offset[i + 1] = value_offset[i] + k.info[i].samples;
-    // Reduction chunks of each contract's per-path values.
-    const int64_t chunk = 4096;
+    // Reduction chunks of each contract's per-path values (four per thread of a CTA).
+    const int64_t chunk = 1024;
     std::vector<int4> chunks;
     std::vector<int> first_chunk(n + 1, 0);
     for (int i = 0; i < n; ++i) {
@@ -871,14 +872,15 @@ kgpu_status run_phased_impl(Call& k, DevBook<Real> db, int& launches) {
         dims[i] = k.info[i].dims;
     }
     if ((st = upload(ctx, ctx->phase_dims, dims.data(), dims.size() * sizeof(int)))) return st;
-    // Monitoring-list sizes of every generation, the knocked-in pool size, the
-    // completion flag.
-    const size_t count_bytes = (size_t(phases + 1) + 2) * sizeof(int);
+    // Monitoring-list sizes of every generation, the knocked-in pool size and the grid
+    // barrier's words.
+    const size_t count_bytes = (size_t(phases + 1) + 4) * sizeof(int);
     if (ctx->phase_lists.ensure(3 * size_t(total) * sizeof(Entry) + 16) || ctx->phase_counts.ensure(count_bytes))
         return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the phase lists failed");
     CUDA_TRY(ctx, cudaMemsetAsync(ctx->phase_counts.ptr, 0, count_bytes, ctx->stream));
     PhaseArgs<Real, SOBOL> a;
     a.book = db;
+    a.phases = phases;
     a.contract_count = n;
     a.total = total;
     a.value_offset = static_cast<const int64_t*>(ctx->value_offset.ptr);
@@ -893,44 +895,44 @@ kgpu_status run_phased_impl(Call& k, DevBook<Real> db, int& launches) {
         if ((st = ensure_sobol(ctx, k.info[0].dims, s.seed, &a.sobol))) return st;
         int64_t blocks = 1;
         for (int i = 0; i < n; ++i) blocks = std::max<int64_t>(blocks, (k.info[i].samples + 255) / 256);
-        if (ctx->sobol_high32.ensure(size_t(blocks) * k.info[0].dims * 4))
-            return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the Sobol high table failed");
-        CUDA_TRY(ctx, launch_sobol_high_t(a.sobol, int(blocks), static_cast<uint32_t*>(ctx->sobol_high32.ptr),
-                                          ctx->stream));
-        a.high_t = static_cast<const uint32_t*>(ctx->sobol_high32.ptr);
-        a.high_blocks = int(blocks);
-        launches += 1;
+        // Like the sequence's other tables, the high table depends on the seed and the
+        // dimension count only: it is kept for later calls and rebuilt when they need
+        // more blocks or another sequence.
+        if (ctx->sobol_high_t_blocks < blocks) {
+            if (ctx->sobol_high_t.ensure(size_t(blocks) * k.info[0].dims * 4))
+                return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of the Sobol high table failed");
+            CUDA_TRY(ctx, launch_sobol_high_t(a.sobol, int(blocks), static_cast<uint32_t*>(ctx->sobol_high_t.ptr),
+                                              ctx->stream));
+            ctx->sobol_high_t_blocks = blocks;
+            launches += 1;
+        }
+        a.high_t = static_cast<const uint32_t*>(ctx->sobol_high_t.ptr);
+        a.high_blocks = int(ctx->sobol_high_t_blocks);
     }
     a.cancel = k.cancel ? ctx->cancel_dev : nullptr;
     a.aborted = static_cast<int*>(ctx->queue.ptr) + 1;
-    const int per_sm = phased_occupancy_fp32(SOBOL);
-    const int64_t warps_needed = (total + 31) / 32;
-    const int grid = int(std::max<int64_t>(1, std::min<int64_t>(int64_t(ctx->sm_count) * per_sm,
-                                                                (warps_needed + kWarps - 1) / kWarps)));
     Entry* lists = static_cast<Entry*>(ctx->phase_lists.ptr);
-    int* counts = static_cast<int*>(ctx->phase_counts.ptr);
+    a.lists = lists;
     a.knocked = lists + 2 * size_t(total);
-    a.knocked_count = counts + phases + 1;
-    a.finished = counts + phases + 2;
-    // Monitoring paths that fit in one wave of resident lanes run to completion in one
-    // launch.
-    a.complete_below = int64_t(ctx->sm_count) * per_sm * kThreads;
+    a.counts = static_cast<int*>(ctx->phase_counts.ptr);
+    // Every CTA of the cooperative launch is resident at once; monitoring paths that fit
+    // in that wave of lanes are completed CTA by CTA.
+    const int per_sm = phased_occupancy_fp32(SOBOL);
+    const int grid = std::max(1, ctx->sm_count * per_sm);
+    a.complete_below = int64_t(grid) * kThreads;
     CancelWatcher watcher(k.cancel, ctx->cancel_host);
     CUDA_TRY(ctx, path_kernel_begin(ctx));
-    for (int p = 0; p <= phases; ++p) {
-        // Phase p reads monitoring list (p % 2) and writes list ((p + 1) % 2); the last
-        // launch drains the knocked-in pool.
-        a.drain = p == phases;
-        a.phase = a.drain ? 0 : p;
-        a.in_monitoring = lists + size_t(p % 2) * total;
-        a.in_count = counts + p;
-        a.out_monitoring = lists + size_t((p + 1) % 2) * total;
-        a.out_count = counts + std::min(p + 1, phases);
-        CUDA_TRY(ctx, launch_phased_fp32(grid, ctx->stream, a));
-        launches += 1;
-    }
+    CUDA_TRY(ctx, launch_phased_fp32(grid, ctx->stream, a));
+    launches += 1;
+    int failed = 0;
+    CUDA_TRY(ctx, cudaMemcpyAsync(&failed, static_cast<int*>(ctx->phase_counts.ptr) + phases + 4, sizeof(int),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_TRY(ctx, path_kernel_end(ctx));
-    return finish_values<Real>(k, chunk_count, launches);
+    kgpu_status done = finish_values<Real>(k, chunk_count, launches);
+    // `failed` arrived with finish_values' synchronisation.
+    if (done == KGPU_OK && failed)
+        return fail(ctx, KGPU_DEVICE_ERROR, "the phase-major kernel's grid barrier timed out");
+    return done;
 }
 
 template <class Real>

@@ -48,6 +48,10 @@ struct kgpu_context {
     // phase-major schedule: two generations of the monitoring list and the knocked-in
     // pool, the list sizes and completion flag, per-contract sampling dimensions
     kgpu::DeviceBuffer phase_lists, phase_counts, phase_dims;
+    // the dimension-major Sobol high table of the cached sequence, for `sobol_high_t_blocks`
+    // reference blocks (0: not built since the sequence was last rebuilt)
+    kgpu::DeviceBuffer sobol_high_t;
+    int64_t sobol_high_t_blocks = 0;
     // plan in the kernel's precision (contract table always, arrays for FP32)
     kgpu::DeviceBuffer ccontracts, csteps, cevents, cintervals, cdaily, cunits, cends;
     // Sobol sequence cache (one sequence per (seed, dims))
@@ -78,7 +82,7 @@ struct kgpu_context {
     std::vector<kgpu::DeviceBuffer*> buffers() {
         return {&contracts, &steps,     &flags,     &events,   &intervals, &daily,     &lv,
                 &partials,  &merged,    &shared_slots, &items,     &order,    &first_item, &tiles,    &tile_out,
-                &queue,     &values,    &value_offset, &chunks, &executed, &phase_lists, &phase_counts, &phase_dims, &sobol_dirs, &sobol_shifts, &sobol_nibbles, &sobol_dirs32, &sobol_shifts32, &sobol_nibbles32, &sobol_high32, &ccontracts, &csteps,
+                &queue,     &values,    &value_offset, &chunks, &executed, &phase_lists, &phase_counts, &phase_dims, &sobol_high_t, &sobol_dirs, &sobol_shifts, &sobol_nibbles, &sobol_dirs32, &sobol_shifts32, &sobol_nibbles32, &sobol_high32, &ccontracts, &csteps,
                 &cevents,   &cintervals, &cdaily,      &cunits,     &cends,      &lsmc_store, &lsmc_cash, &lsmc_sums,
                 &lsmc_coef, &lsmc_misc, &mlp_params, &mlp_scratch, &stream_out};
     }

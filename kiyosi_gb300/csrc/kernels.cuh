@@ -185,48 +185,104 @@ static __global__ void compile_arrays_fp32_kernel(RawBook b, StepT<float>* steps
     }
 }
 
-// Per-position bridge units of every bridged contract: one CTA per contract walks its
-// intervals; the positions of an interval are written in parallel.
+// Per-position bridge units of every bridged contract, one CTA per contract.  The CTA
+// stages the contract's interval ends and the running count of cash events at them in
+// shared memory (up to kUnitsStaged intervals; longer plans are walked interval by
+// interval), then every thread fills positions, finding its interval by bisection.
+constexpr int kUnitsStaged = 2048;
+
 template <class Real>
-__global__ void compile_units_kernel(const kgpu_contract* contracts, const kgpu_bridge_interval* intervals,
-                                     const kgpu_bridge_daily* daily, const uint8_t* flags,
-                                     const kgpu_event* events, UnitT<Real>* units, EndT<Real>* ends) {
+__global__ void __launch_bounds__(256) compile_units_kernel(const kgpu_contract* contracts,
+                                                            const kgpu_bridge_interval* intervals,
+                                                            const kgpu_bridge_daily* daily, const uint8_t* flags,
+                                                            const kgpu_event* events, UnitT<Real>* units,
+                                                            EndT<Real>* ends) {
+    __shared__ int end_of[kUnitsStaged];
+    __shared__ int event_before[kUnitsStaged];  // cash events at interval ends before interval k
+    __shared__ int warp_total[8];
     const kgpu_contract c = contracts[blockIdx.x];
     if (!(c.flags & KGPU_C_BRIDGE)) return;
-    int start = 0;
-    int ev = c.event_offset;
-    for (int k = 0; k < c.bridge_count; ++k) {
+    auto unit_at = [&](int q, int k, int start, int ev) {
         const kgpu_bridge_interval iv = intervals[c.bridge_offset + k];
         const int fl = flags[c.step_offset + iv.end];
         const bool event = (fl & KGPU_STEP_EVENT) != 0;
-        const kgpu_event e = event ? events[ev] : kgpu_event{};
-        for (int q = start + int(threadIdx.x); q <= iv.end; q += blockDim.x) {
-            UnitT<Real> u;
-            if (q == start) {
-                u.a = Real(iv.diffusion);
-                u.b = Real(iv.drift);
-                u.flags = kUnitBegin;
-            } else {
-                const kgpu_bridge_daily d = daily[c.step_offset + q - 1];
-                u.a = Real(d.width);
-                u.b = Real(d.weight);
-                u.flags = 0;
-            }
-            u.end = iv.end;
-            u.flags |= fl << 8;
-            if (q == iv.end) u.flags |= kUnitLast;
-            if (event && e.has_knock_out) u.flags |= kUnitKnockOut;
-            units[c.step_offset + q] = u;
-            EndT<Real> o{};
-            if (q == iv.end && event) {
+        UnitT<Real> u;
+        if (q == start) {
+            u.a = Real(iv.diffusion);
+            u.b = Real(iv.drift);
+            u.flags = kUnitBegin;
+        } else {
+            const kgpu_bridge_daily d = daily[c.step_offset + q - 1];
+            u.a = Real(d.width);
+            u.b = Real(d.weight);
+            u.flags = 0;
+        }
+        u.end = iv.end;
+        u.flags |= fl << 8;
+        if (q == iv.end) u.flags |= kUnitLast;
+        EndT<Real> o{};
+        if (event) {
+            const kgpu_event e = events[ev];
+            if (e.has_knock_out) u.flags |= kUnitKnockOut;
+            if (q == iv.end) {
                 o.knock_out = Real(e.knock_out);
                 o.coupon_barrier = Real(e.coupon_barrier);
                 for (int j = 0; j < 4; ++j) o.payment[j] = Real(e.payment[j]);
             }
-            ends[c.step_offset + q] = o;
         }
-        ev += event ? 1 : 0;
-        start = iv.end + 1;
+        units[c.step_offset + q] = u;
+        ends[c.step_offset + q] = o;
+    };
+    const int n = c.bridge_count;
+    if (n > kUnitsStaged) {
+        // Long plans: interval by interval, positions of an interval in parallel.
+        int start = 0, ev = c.event_offset;
+        for (int k = 0; k < n; ++k) {
+            const int e = intervals[c.bridge_offset + k].end;
+            for (int q = start + int(threadIdx.x); q <= e; q += blockDim.x) unit_at(q, k, start, ev);
+            ev += (flags[c.step_offset + e] & KGPU_STEP_EVENT) ? 1 : 0;
+            start = e + 1;
+        }
+        return;
+    }
+    // Interval ends and an exclusive scan of the event flags at them (8 per thread).
+    constexpr int kPer = kUnitsStaged / 256;
+    int local[kPer];
+    int sum = 0;
+    for (int j = 0; j < kPer; ++j) {
+        const int k = int(threadIdx.x) * kPer + j;
+        int is_event = 0;
+        if (k < n) {
+            const int e = intervals[c.bridge_offset + k].end;
+            end_of[k] = e;
+            is_event = (flags[c.step_offset + e] & KGPU_STEP_EVENT) ? 1 : 0;
+        }
+        local[j] = sum;
+        sum += is_event;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inclusive = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inclusive, o);
+        if (lane >= o) inclusive += v;
+    }
+    if (lane == 31) warp_total[warp] = inclusive;
+    __syncthreads();
+    int base = inclusive - sum;
+    for (int w = 0; w < warp; ++w) base += warp_total[w];
+    for (int j = 0; j < kPer; ++j) {
+        const int k = int(threadIdx.x) * kPer + j;
+        if (k < n) event_before[k] = base + local[j];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < c.step_count; q += blockDim.x) {
+        int lo = 0, hi = n - 1;  // first interval whose end is >= q
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (end_of[mid] >= q) hi = mid; else lo = mid + 1;
+        }
+        const int start = lo == 0 ? 0 : end_of[lo - 1] + 1;
+        unit_at(q, lo, start, c.event_offset + event_before[lo]);
     }
 }
 

@@ -89,7 +89,7 @@ cudaError_t KGPU_CAT(launch_compile_units_, PRECISION)(const kgpu_contract* cont
                                                        const kgpu_bridge_daily* daily, const uint8_t* flags,
                                                        const kgpu_event* events, UnitT<REAL>* units,
                                                        EndT<REAL>* ends, cudaStream_t s) {
-    compile_units_kernel<REAL><<<n, 128, 0, s>>>(contracts, intervals, daily, flags, events, units, ends);
+    compile_units_kernel<REAL><<<n, 256, 0, s>>>(contracts, intervals, daily, flags, events, units, ends);
     return cudaGetLastError();
 }
 
@@ -123,10 +123,14 @@ static __global__ void sobol_points_kernel(SobolTables t, int dim, uint64_t firs
 }
 
 #if KGPU_FP32_UNIT
+// A cooperative launch: every CTA is resident at once (the kernel's grid barrier needs
+// it); the runtime refuses a grid larger than the device can hold.
 template <bool SOBOL>
 static cudaError_t phased_one(int blocks, cudaStream_t s, const PhaseArgs<float, SOBOL>& a) {
-    phased_kernel<float, SOBOL><<<blocks, kThreads, 0, s>>>(a);
-    return cudaGetLastError();
+    PhaseArgs<float, SOBOL> args = a;
+    void* params[] = {&args};
+    return cudaLaunchCooperativeKernel((const void*)phased_kernel<float, SOBOL>, dim3(blocks), dim3(kThreads), params,
+                                       0, s);
 }
 
 cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, true>& a) {
@@ -145,9 +149,8 @@ int phased_occupancy_fp32(bool sobol) {
 }
 
 cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s) {
-    const int64_t total = int64_t(blocks) * t.dims;
-    if (total <= 0) return cudaSuccess;
-    sobol_high_table_t_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(t, blocks, out);
+    if (blocks <= 0 || t.dims <= 0) return cudaSuccess;
+    sobol_high_table_t_kernel<<<dim3(unsigned((blocks + 255) / 256), unsigned(t.dims)), 256, 0, s>>>(t, blocks, out);
     return cudaGetLastError();
 }
 

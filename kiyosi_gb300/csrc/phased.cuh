@@ -9,18 +9,20 @@
 // runs 504 daily positions while the average path runs 80, the last paths of each lane
 // leave most lanes idle.
 //
-// Here launch k advances every path still monitoring knock-in by exactly one interval.
-// A warp takes 32 paths of one list, so its lanes walk the same grid positions: unit
-// records, cash events and Sobol direction rows are broadcast reads and the loop over
-// days is uniform.  Paths that finish write their payoff to
-// values[value_offset[contract] + sample]; monitoring survivors are appended to the list
-// of launch k + 1, one atomic per warp.  A knocked-in path draws only one normal per
-// interval (its daily steps no longer matter), so it leaves the phase lists for a pool
-// that one drain launch, after the last phase, runs to completion.  Once the monitoring
-// paths fit in one wave of resident lanes, a launch runs them to completion as well and
-// the remaining phase launches return at once.  The lists carry all the state a path
-// holds between intervals, so the per-path payoffs are the lane-refill kernel's to the
-// bit: the same arithmetic in the same order on the same normals.
+// Here the book advances interval by interval.  While many paths still monitor
+// knock-in, each interval is a grid-wide step: a warp takes 32 paths of the current
+// monitoring list, so its lanes walk the same grid positions (unit records, cash events
+// and Sobol direction rows are broadcast reads; the loop over days is uniform).  Paths
+// that finish write their payoff to values[value_offset[contract] + sample]; monitoring
+// survivors are appended to the next interval's list, one atomic per warp.  A
+// knocked-in path draws one normal per interval (its daily steps no longer matter), so
+// it leaves for a pool completed at the end.  Once the monitoring paths fit in one wave
+// of resident lanes, each CTA runs a batch of them to completion, compacting the live
+// paths after every interval so its warps stay full; the knocked-in pool is completed
+// the same way.  The whole schedule is one cooperative launch with a grid barrier
+// between the steps.  The lists carry all the state a path holds between intervals, so
+// the per-path payoffs are the lane-refill kernel's to the bit: the same arithmetic in
+// the same order on the same normals.
 #pragma once
 #include "kernels.cuh"
 
@@ -56,18 +58,16 @@ struct __align__(16) PhaseEntry<Real, false> {
 template <class Real, bool SOBOL>
 struct PhaseArgs {
     DevBook<Real> book;
-    int phase;
+    int phases;                     // intervals of the longest contract
     int contract_count;
-    int64_t total;                  // phase 0: every sample of every contract
+    int64_t total;                  // every sample of every contract
     const int64_t* value_offset;    // [contract_count + 1]
     const int* dims;                // per contract: normals per sample (PCG positions)
-    const PhaseEntry<Real, SOBOL>* in_monitoring;  // paths still monitoring knock-in
-    const int* in_count;            // their number (phase > 0)
-    PhaseEntry<Real, SOBOL>* out_monitoring;
-    int* out_count;
+    PhaseEntry<Real, SOBOL>* lists;    // two generations of the monitoring list, total each
     PhaseEntry<Real, SOBOL>* knocked;  // knocked-in paths, each with its next interval
-    int* knocked_count;
-    int drain;                      // this launch runs the knocked-in pool to completion
+    int* counts;                    // [phases + 1] monitoring-list sizes, then the knocked-in
+                                    // pool size, the barrier's arrivals and generation, and
+                                    // the barrier failure flag
     Real* values;
     unsigned long long* executed;   // per contract: positions simulated
     uint64_t seed;
@@ -76,8 +76,7 @@ struct PhaseArgs {
     int high_blocks;
     const volatile int* cancel;     // host-mapped cancellation word (may be null)
     int* aborted;
-    int* finished;                  // phase + 1 of the launch that completed the monitoring paths
-    int64_t complete_below;         // monitoring paths at or below which a launch completes them
+    int64_t complete_below;         // monitoring paths at or below which the CTAs complete them
 };
 
 // One path's state within a launch.
@@ -201,113 +200,226 @@ __device__ __forceinline__ PhaseEntry<Real, SOBOL> phase_entry(const PhaseLane<R
     return e;
 }
 
-// Launch `phase` advances the paths still monitoring knock-in by one interval; the
-// drain launch (after the last phase) runs the knocked-in pool to completion.
+// Loads path `idx` of a list (or, in the first interval, sample `idx` of the book) into
+// a lane; returns the interval it runs next.
 template <class Real, bool SOBOL>
-__global__ void __launch_bounds__(kThreads, 4) phased_kernel(PhaseArgs<Real, SOBOL> a) {
-    using Entry = PhaseEntry<Real, SOBOL>;
+__device__ __forceinline__ int phase_load(const PhaseArgs<Real, SOBOL>& a, const PhaseEntry<Real, SOBOL>* list,
+                                          int64_t idx, PhaseLane<Real>& L, PcgSource<Real>& pn) {
+    if (!list) {
+        int lo = 0, hi = a.contract_count;  // contract with value_offset[c] <= idx
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (a.value_offset[mid] <= idx) lo = mid; else hi = mid;
+        }
+        L.contract = lo;
+        L.sample = uint32_t(idx - a.value_offset[lo]);
+        const ContractT<Real>& c0 = a.book.contracts[lo];
+        L.knocked_in = (c0.flags & KGPU_C_KNOCKED_IN) != 0;
+        L.monitoring = !L.knocked_in && (c0.flags & KGPU_C_HAS_KNOCK_IN);
+        L.lr = Real(0);
+        L.cash = c0.initial_cash;
+        if (!SOBOL) pn.start(a.seed, L.sample, a.dims[lo]);
+        return 0;
+    }
+    const PhaseEntry<Real, SOBOL> e = list[idx];
+    L.sample = e.sample;
+    L.contract = int(e.tag >> kPhaseTagShift);
+    L.monitoring = (e.tag & kPhaseMonitoring) != 0;
+    L.knocked_in = (e.tag & kPhaseKnockedIn) != 0;
+    L.lr = e.lr;
+    L.cash = e.cash;
+    if constexpr (!SOBOL) {
+        pn.g.state = e.state;
+        pn.g.inc = ((uint64_t(L.sample) / kBlockSize) << 1) | 1;
+        pn.spare = e.spare;
+        pn.has_spare = e.has_spare != 0;
+    }
+    return int((e.tag >> kPhaseIntervalShift) & (kPhaseMaxIntervals - 1));
+}
+
+// Adds the positions a warp's lanes simulated to their contracts' counters.
+__device__ __forceinline__ void phase_count(unsigned long long* counters, int contract, int executed, int lane) {
     constexpr unsigned kFull = 0xffffffffu;
-    // An earlier launch completed every monitoring path (`finished` holds its phase + 1).
-    const int done = *(volatile int*)a.finished;
-    if (!a.drain && done != 0 && done - 1 < a.phase) return;
-    if (*(volatile int*)a.aborted) return;
-    if (a.cancel && blockIdx.x == 0 && threadIdx.x == 0 && *a.cancel) atomicExch(a.aborted, 1);
-    const int lane = threadIdx.x & 31;
+    const int lead = __shfl_sync(kFull, contract, 0);
+    if (__all_sync(kFull, contract == lead || executed == 0)) {
+        const unsigned total = __reduce_add_sync(kFull, unsigned(executed));
+        if (lane == 0 && total) atomicAdd(counters + lead, (unsigned long long)total);
+    } else if (executed) {
+        atomicAdd(counters + contract, (unsigned long long)executed);
+    }
+}
+
+// Appends the flagged lanes of a warp to a list, one atomic per warp.
+template <class Entry>
+__device__ __forceinline__ void phase_append(Entry* list, int* count, bool keep, const Entry& e, int lane,
+                                             unsigned below) {
+    const unsigned b = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if (lane == 0 && b) base = atomicAdd(count, __popc(b));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) list[base + __popc(b & below)] = e;
+}
+
+// Grid-wide barrier of the cooperative launch.  The wait is bounded: after about two
+// seconds it records a failure and returns false, and the kernel stops.
+constexpr long long kPhaseBarrierCycles = 4000000000LL;
+
+__device__ __forceinline__ bool phase_grid_sync(int* arrive, volatile int* generation, int* failed) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int g = *generation;
+        __threadfence();
+        if (atomicAdd(arrive, 1) == int(gridDim.x) - 1) {
+            atomicExch(arrive, 0);
+            __threadfence();
+            atomicAdd((int*)generation, 1);
+        } else {
+            const long long t0 = clock64();
+            while (*generation == g) {
+                if (clock64() - t0 > kPhaseBarrierCycles) {
+                    atomicExch(failed, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = *(volatile int*)failed == 0;
+    }
+    __syncthreads();
+    return ok != 0;  // the same answer for every thread of the CTA
+}
+
+// Runs paths of a list to completion, a CTA batch of kThreads paths at a time.  After
+// every interval the batch's live paths are compacted to the front of the CTA through
+// shared memory, so its warps stay full while the batch thins out.  Completing the
+// monitoring list (drain false), a path that knocks in moves to the knocked-in pool.
+template <class Real, bool SOBOL>
+__device__ void phase_complete(const PhaseArgs<Real, SOBOL>& a, const PhaseEntry<Real, SOBOL>* list, int64_t count,
+                               int first_phase, bool drain, PhaseEntry<Real, SOBOL>* pool, int* warp_live) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned below = lanemask_lt();
-    const int64_t count = a.drain ? int64_t(*a.knocked_count) : a.phase == 0 ? a.total : int64_t(*a.in_count);
-    // Few monitoring paths left: run them to completion in this launch, so the last
-    // intervals pay no launch or list handoff.
-    const bool complete = a.drain || count <= a.complete_below;
-    if (!a.drain && complete && blockIdx.x == 0 && threadIdx.x == 0) *(volatile int*)a.finished = a.phase + 1;
-    const int64_t chunks = (count + 31) / 32;
-    const int64_t warps = int64_t(gridDim.x) * kWarps;
-    for (int64_t ch = (int64_t(blockIdx.x) * kThreads + threadIdx.x) / 32; ch < chunks; ch += warps) {
-        const int64_t idx = ch * 32 + lane;
-        // The path's state at the start of its next interval.
+    int* knocked_count = a.counts + a.phases + 1;
+    for (int64_t base = int64_t(blockIdx.x) * kThreads; base < count; base += int64_t(gridDim.x) * kThreads) {
         PhaseLane<Real> L;
-        L.valid = idx < count;
+        PcgSource<Real> pn;
+        L.valid = base + threadIdx.x < count;
         L.sample = 0;
         L.contract = 0;
         L.monitoring = L.knocked_in = false;
         L.lr = L.cash = Real(0);
-        int phase = a.phase;
-        PcgSource<Real> pn;
+        int phase = first_phase;
         if (L.valid) {
-            if (!a.drain && a.phase == 0) {
-                int lo = 0, hi = a.contract_count;  // contract with value_offset[c] <= idx
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (a.value_offset[mid] <= idx) lo = mid; else hi = mid;
-                }
-                L.contract = lo;
-                L.sample = uint32_t(idx - a.value_offset[lo]);
-                const ContractT<Real>& c0 = a.book.contracts[lo];
-                L.knocked_in = (c0.flags & KGPU_C_KNOCKED_IN) != 0;
-                L.monitoring = !L.knocked_in && (c0.flags & KGPU_C_HAS_KNOCK_IN);
-                L.cash = c0.initial_cash;
-                if (!SOBOL) pn.start(a.seed, L.sample, a.dims[lo]);
-            } else {
-                const Entry e = a.drain ? a.knocked[idx] : a.in_monitoring[idx];
-                L.sample = e.sample;
-                L.contract = int(e.tag >> kPhaseTagShift);
-                L.monitoring = (e.tag & kPhaseMonitoring) != 0;
-                L.knocked_in = (e.tag & kPhaseKnockedIn) != 0;
-                phase = int((e.tag >> kPhaseIntervalShift) & (kPhaseMaxIntervals - 1));
-                L.lr = e.lr;
-                L.cash = e.cash;
-                if constexpr (!SOBOL) {
-                    pn.g.state = e.state;
-                    pn.g.inc = ((uint64_t(L.sample) / kBlockSize) << 1) | 1;
-                    pn.spare = e.spare;
-                    pn.has_spare = e.has_spare != 0;
-                }
-            }
+            const int p = phase_load<Real, SOBOL>(a, list, base + threadIdx.x, L, pn);
+            if (list) phase = p;
         }
-        int executed = 0;
-        bool finished = phase_interval<Real, SOBOL>(a, phase, L, pn, executed);
-        if (complete) {
-            while (__any_sync(kFull, L.valid && !finished)) {
-                L.valid = L.valid && !finished;
-                ++phase;
+        bool alive = L.valid;
+        for (;;) {
+            // Compact the live paths to the front of the CTA.
+            const unsigned b = __ballot_sync(kFull, alive);
+            if (lane == 0) warp_live[warp] = __popc(b);
+            __syncthreads();
+            int offset = 0, live = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                offset += w < warp ? warp_live[w] : 0;
+                live += warp_live[w];
+            }
+            if (live == 0) break;
+            if (alive) pool[offset + __popc(b & below)] = phase_entry<Real, SOBOL>(L, phase, pn);
+            __syncthreads();
+            L.valid = int(threadIdx.x) < live;
+            if (L.valid) phase = phase_load<Real, SOBOL>(a, pool, threadIdx.x, L, pn);
+            __syncthreads();
+            bool finished = false;
+            int executed = 0;
+            if (warp * 32 < live) {
                 finished = phase_interval<Real, SOBOL>(a, phase, L, pn, executed);
+                phase_count(a.executed, L.contract, executed, lane);
+                alive = L.valid && !finished;
+                ++phase;
+                if (!drain) {
+                    const bool to_pool = alive && !L.monitoring;
+                    phase_append(a.knocked, knocked_count, to_pool, phase_entry<Real, SOBOL>(L, phase, pn), lane,
+                                 below);
+                    alive = alive && !to_pool;
+                }
+            } else {
+                alive = false;
             }
         }
-        // Positions simulated, summed per contract.
-        const int lead = __shfl_sync(kFull, L.contract, 0);
-        if (__all_sync(kFull, L.contract == lead)) {
-            const unsigned total = __reduce_add_sync(kFull, unsigned(executed));
-            if (lane == 0 && total) atomicAdd(a.executed + lead, (unsigned long long)total);
-        } else if (executed) {
-            atomicAdd(a.executed + L.contract, (unsigned long long)executed);
-        }
-        if (complete) continue;
-        // Survivors: monitoring paths to the next phase's list, knocked-in paths to the
-        // pool the drain launch completes.
-        const bool keep = L.valid && !finished;
-        const bool keep_m = keep && L.monitoring, keep_k = keep && !L.monitoring;
-        const unsigned bm = __ballot_sync(kFull, keep_m), bk = __ballot_sync(kFull, keep_k);
-        int base_m = 0, base_k = 0;
-        if (lane == 0) {
-            if (bm) base_m = atomicAdd(a.out_count, __popc(bm));
-            if (bk) base_k = atomicAdd(a.knocked_count, __popc(bk));
-        }
-        base_m = __shfl_sync(kFull, base_m, 0);
-        base_k = __shfl_sync(kFull, base_k, 0);
-        if (keep_m) a.out_monitoring[base_m + __popc(bm & below)] = phase_entry<Real, SOBOL>(L, phase + 1, pn);
-        if (keep_k) a.knocked[base_k + __popc(bk & below)] = phase_entry<Real, SOBOL>(L, phase + 1, pn);
     }
 }
 
-// The high part of every reference block, dimension-major: out[d * blocks + b].
+// One cooperative launch prices the book.  While more paths monitor knock-in than fill
+// one wave of resident lanes, every interval is a grid-wide step: each warp advances 32
+// paths of the current monitoring list by one interval, appends the survivors to the
+// next list (knocked-in ones to the pool), and a grid barrier ends the step.  Then the
+// CTAs complete the remaining monitoring paths, and after one more barrier the
+// knocked-in pool.
+template <class Real, bool SOBOL>
+__global__ void __launch_bounds__(kThreads, 4) phased_kernel(PhaseArgs<Real, SOBOL> a) {
+    using Entry = PhaseEntry<Real, SOBOL>;
+    __shared__ Entry pool[kThreads];
+    __shared__ int warp_live[kWarps];
+    const int lane = threadIdx.x & 31;
+    const unsigned below = lanemask_lt();
+    int* knocked_count = a.counts + a.phases + 1;
+    int* arrive = a.counts + a.phases + 2;
+    volatile int* generation = a.counts + a.phases + 3;
+    int* failed = a.counts + a.phases + 4;
+    int phase = 0;
+    int64_t count = a.total;
+    const int64_t warps = int64_t(gridDim.x) * kWarps;
+    while (count > a.complete_below && phase < a.phases) {
+        if (a.cancel && blockIdx.x == 0 && threadIdx.x == 0 && *a.cancel) atomicExch(a.aborted, 1);
+        const Entry* in = phase == 0 ? nullptr : a.lists + size_t(phase % 2) * a.total;
+        Entry* out = a.lists + size_t((phase + 1) % 2) * a.total;
+        int* out_count = a.counts + phase + 1;
+        const int64_t chunks = (count + 31) / 32;
+        for (int64_t ch = (int64_t(blockIdx.x) * kThreads + threadIdx.x) / 32; ch < chunks; ch += warps) {
+            const int64_t idx = ch * 32 + lane;
+            PhaseLane<Real> L;
+            PcgSource<Real> pn;
+            L.valid = idx < count;
+            L.sample = 0;
+            L.contract = 0;
+            L.monitoring = L.knocked_in = false;
+            L.lr = L.cash = Real(0);
+            if (L.valid) phase_load<Real, SOBOL>(a, in, idx, L, pn);
+            int executed = 0;
+            const bool finished = phase_interval<Real, SOBOL>(a, phase, L, pn, executed);
+            phase_count(a.executed, L.contract, executed, lane);
+            // Survivors: monitoring paths to the next list, knocked-in paths to the pool.
+            const bool keep = L.valid && !finished;
+            const Entry e = phase_entry<Real, SOBOL>(L, phase + 1, pn);
+            phase_append(out, out_count, keep && L.monitoring, e, lane, below);
+            phase_append(a.knocked, knocked_count, keep && !L.monitoring, e, lane, below);
+        }
+        // The cancellation word is read before the barrier, so after it every thread
+        // sees the same value.
+        if (!phase_grid_sync(arrive, generation, failed) || *(volatile int*)a.aborted) return;
+        ++phase;
+        count = *(volatile int*)(a.counts + phase);
+    }
+    phase_complete<Real, SOBOL>(a, phase == 0 ? nullptr : a.lists + size_t(phase % 2) * a.total, count, phase,
+                                false, pool, warp_live);
+    if (!phase_grid_sync(arrive, generation, failed)) return;
+    phase_complete<Real, SOBOL>(a, a.knocked, *(volatile int*)knocked_count, 0, true, pool, warp_live);
+}
+
+// The high part of every reference block, dimension-major: out[d * blocks + b] is the
+// shift of dimension d XOR the directions of the gray-code bits >= 8 of block b's first
+// point (those bits are the gray code of b).  Grid: (block tiles, dimensions).
 static __global__ void sobol_high_table_t_kernel(SobolTables t, int blocks, uint32_t* out) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= int64_t(blocks) * t.dims) return;
-    const int d = int(i / blocks), b = int(i % blocks);
-    const uint64_t first = uint64_t(b) * kBlockSize;
-    uint64_t g = (first ^ (first >> 1)) >> 8;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (b >= blocks) return;
+    uint32_t g = uint32_t(b) ^ (uint32_t(b) >> 1);
     uint32_t x = t.shifts32[d];
-    for (; g; g &= g - 1) x ^= t.directions32[size_t(__ffsll(g) - 1 + 8) * t.dims + d];
-    out[i] = x;
+    for (; g; g &= g - 1) x ^= t.directions32[size_t(__ffs(g) - 1 + 8) * t.dims + d];
+    out[size_t(d) * blocks + b] = x;
 }
 
 }  // namespace kgpu
