@@ -481,6 +481,14 @@ int32_t kgpu_context_last_launches(const kgpu_context* ctx);
  * kernel launches, without plan compilation and reductions), summed over launches. */
 double kgpu_context_last_path_kernel_ms(const kgpu_context* ctx);
 
+/* Throughput of the device's pipes, measured on `ctx`'s device (no counterpart in the
+ * reference: the denominators of the benchmark's op-model roofline).  rates[0..4], in
+ * thread operations per second: FP32 fused multiply-add, its packed two-lane form
+ * (counted in FMAs), 32-bit logic (LOP3), the multi-function unit's base-2 logarithm,
+ * and 32-bit loads that hit L1; entries past the fifth are set to 0.  Runs about a
+ * millisecond of kernels on the context's stream. */
+kgpu_status kgpu_pipe_rates(kgpu_context* ctx, double* rates, int32_t count);
+
 /* Library identification. */
 int32_t kgpu_abi_version(void);
 int32_t kgpu_device_count(void);

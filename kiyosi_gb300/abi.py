@@ -180,7 +180,7 @@ EXPORTED_SYMBOLS = (
     "kgpu_price_book", "kgpu_price_book_device", "kgpu_pcg_normals", "kgpu_pcg_words",
     "kgpu_sobol_points", "kgpu_lsmc_price", "kgpu_context_last_kernel_ms",
     "kgpu_context_last_path_kernel_ms",
-    "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count",
+    "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count", "kgpu_pipe_rates",
     "kgpu_price_contract_noalloc", "kgpu_mlp_gradients",
 )
 MLP_PARAMS = 4481
@@ -228,4 +228,6 @@ def declare(lib):
     lib.kgpu_abi_version.restype = _I
     lib.kgpu_device_count.argtypes = []
     lib.kgpu_device_count.restype = _I
+    lib.kgpu_pipe_rates.argtypes = [V, C.POINTER(_D), _I]
+    lib.kgpu_pipe_rates.restype = _I
     return lib

@@ -24,6 +24,7 @@ UNITS = {
     "lsmc.cu": [],
     "mlp.cu": [],
     "noalloc.cu": [],
+    "pipes.cu": [],
 }
 HEADERS = ["device_rng.cuh", "path_engine.cuh", "kernels.cuh", "kernels_impl.cuh", "launch.h",
            "api_internal.h", "joe_kuo_6_21201.inc", "shared_grid.cuh", "lsmc_common.cuh", "tcgen05.cuh", "phased.cuh"]

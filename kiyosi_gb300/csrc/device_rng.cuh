@@ -223,6 +223,35 @@ __device__ __forceinline__ float normal_from_tail(float t, bool upper) {
     return upper ? z : -z;
 }
 
+// Two quantiles at once: normal_from_tail's central-piece operations in their packed
+// FP32x2 forms (each lane of FFMA2 / FMUL2 / FADD2 is the IEEE single-precision
+// operation, so each result equals normal_from_tail's); an element that needs the tail
+// piece (w >= 5, and `need`) is evaluated by normal_from_tail itself.
+__device__ __forceinline__ float2 normal_from_tail_pair(float2 t, bool upper0, bool upper1, bool need0,
+                                                        bool need1) {
+    const float2 x = __ffma2_rn(make_float2(-2.0f, -2.0f), t, make_float2(1.0f, 1.0f));
+    const float2 rest = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-t.x, -t.y));
+    const float2 prod = __fmul2_rn(__fmul2_rn(make_float2(4.0f, 4.0f), t), rest);
+    const float2 w = make_float2(-__logf(prod.x), -__logf(prod.y));
+    const float2 v1 = __fadd2_rn(w, make_float2(-2.5f, -2.5f));
+    auto c = [](float k) { return make_float2(k, k); };
+    float2 p = c(3.194503809e-08f);
+    p = __ffma2_rn(p, v1, c(3.488168990e-07f));
+    p = __ffma2_rn(p, v1, c(-3.563068968e-06f));
+    p = __ffma2_rn(p, v1, c(-4.445640587e-06f));
+    p = __ffma2_rn(p, v1, c(2.187011429e-04f));
+    p = __ffma2_rn(p, v1, c(-1.253577486e-03f));
+    p = __ffma2_rn(p, v1, c(-4.177785603e-03f));
+    p = __ffma2_rn(p, v1, c(2.466406437e-01f));
+    p = __ffma2_rn(p, v1, c(1.501409427e+00f));
+    float2 z = __fmul2_rn(__fmul2_rn(c(1.41421356237309505f), x), p);
+    z.x = upper0 ? z.x : -z.x;
+    z.y = upper1 ? z.y : -z.y;
+    if (need0 && w.x >= 5.0f) z.x = normal_from_tail(t.x, upper0);
+    if (need1 && w.y >= 5.0f) z.y = normal_from_tail(t.y, upper1);
+    return z;
+}
+
 // Lower-tail probability from the top 32 bits k32 of the 52-bit tail integer: the
 // unknown low 20 bits are taken at their midpoint.
 __device__ __forceinline__ float normal_from_tail32(uint32_t k32, bool upper) {

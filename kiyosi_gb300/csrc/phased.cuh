@@ -100,6 +100,21 @@ __device__ __forceinline__ float phase_sobol_from_word(const SobolTables& t, uin
     return normal_from_tail32(k, upper);
 }
 
+// The normals of two Sobol words of dimensions d and d + 1 (phase_sobol_from_word for
+// both, the central quantile piece evaluated as a packed pair).  An element not `need`ed
+// may hold any word; it is neither rebuilt nor sent to the tail piece.
+__device__ __forceinline__ float2 phase_sobol_pair(const SobolTables& t, uint32_t v0, uint32_t v1, bool need0,
+                                                   bool need1, uint64_t gray, int d) {
+    const bool up0 = (v0 >> 31) != 0, up1 = (v1 >> 31) != 0;
+    const uint32_t k0 = up0 ? ~v0 : v0, k1 = up1 ? ~v1 : v1;
+    const float2 tail = __ffma2_rn(make_float2(__uint2float_rn(k0), __uint2float_rn(k1)), make_float2(0x1p-32f, 0x1p-32f),
+                                   make_float2(0x1p-33f, 0x1p-33f));
+    float2 z = normal_from_tail_pair(tail, up0, up1, need0 && k0 >= (1u << 12), need1 && k1 >= (1u << 12));
+    if (need0 && k0 < (1u << 12)) z.x = phase_sobol_from_word(t, v0, gray, d);
+    if (need1 && k1 < (1u << 12)) z.y = phase_sobol_from_word(t, v1, gray, d + 1);
+    return z;
+}
+
 // Advances the lanes of a warp by one bridge interval (`phase`, per lane) of their
 // contracts, position by position as bridge_unit_step (path_engine.cuh) does.  Returns
 // whether the lane's path finished; its payoff is then stored.
@@ -137,17 +152,58 @@ __device__ __forceinline__ bool phase_interval(const PhaseArgs<Real, SOBOL>& a, 
     }
     // Daily bridge steps of the monitoring paths, until knock-in is decided.  `next`:
     // the lane's next undrawn position (PCG stream position).
+    // Two positions per iteration: their normals are drawn together (a packed quantile
+    // pair for Sobol), then the two bridge steps run in order; a path that decides
+    // knock-in at the first leaves the second unused.
     bool walking = L.valid && L.monitoring;
     int next = start + 1;
-    for (int q = start + 1; __any_sync(kFull, walking && q <= end); ++q) {
-        if (walking && q <= end) {
-            const UnitT<Real> u = units[q];
-            const Real z = normal_at(q);
-            const Real daily = lr + xfma(u.b, target - lr, u.a * z);
+    const UnitT<Real>* up = units + start + 1;
+    size_t hi = size_t(start + 1) * a.high_blocks + block;  // Sobol: high table and nibble rows
+    size_t ri = size_t(start + 1) * 32;
+    const size_t hstep = size_t(2) * a.high_blocks;
+    for (int q = start + 1; __any_sync(kFull, walking && q <= end); q += 2, up += 2, hi += hstep, ri += 64) {
+        const bool s0 = walking && q <= end;
+        const bool s1 = walking && q + 1 <= end;
+        UnitT<Real> u0q{}, u1q{};
+        Real z0 = Real(0), z1 = Real(0);
+        if constexpr (SOBOL) {
+            uint32_t w0 = 0, w1 = 0;
+            const uint32_t* row = a.sobol.nibbles32 + ri;
+            if (s0) {
+                u0q = up[0];
+                w0 = __ldg(a.high_t + hi) ^ __ldg(row + glo) ^ __ldg(row + ghi);
+            }
+            if (s1) {
+                u1q = up[1];
+                w1 = __ldg(a.high_t + hi + a.high_blocks) ^ __ldg(row + 32 + glo) ^ __ldg(row + 32 + ghi);
+            }
+            const float2 z = phase_sobol_pair(a.sobol, w0, w1, s0, s1, gray, q);
+            z0 = z.x;
+            z1 = z.y;
+        } else {
+            if (s0) {
+                u0q = up[0];
+                z0 = pn.normal();
+                next = q + 1;
+            }
+            if (s1) {
+                u1q = up[1];
+                z1 = pn.normal();
+                next = q + 2;
+            }
+        }
+        if (s0) {
+            const Real daily = lr + xfma(u0q.b, target - lr, u0q.a * z0);
             lr = daily;
             minimum = daily < minimum ? daily : minimum;
             executed += 1;
-            next = q + 1;
+            walking = !(minimum < level);
+        }
+        if (s1 && walking) {
+            const Real daily = lr + xfma(u1q.b, target - lr, u1q.a * z1);
+            lr = daily;
+            minimum = daily < minimum ? daily : minimum;
+            executed += 1;
             walking = !(minimum < level);
         }
     }

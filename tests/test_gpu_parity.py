@@ -155,6 +155,44 @@ def test_cancel_flag_interrupts(native):
                                                 schedule="persistent"), cancel=flag)
 
 
+@pytest.mark.parametrize("workload", ["heston_asian", "snowball"])
+def test_cancel_during_a_pricing(native, workload):
+    """Cancellation while the kernel runs (cancellation.rs:33-100): a host thread sets
+    the caller's word about a quarter into a long FP32 pricing -- the Heston Asian
+    option at 2^22 paths on the lane-refill kernel, which reads the word at every work
+    item, or the snowball at 2^24 Sobol paths on the phase-major kernel, which reads it
+    at every interval step.  The call raises InterruptedError and returns no estimate;
+    the next call on the same context prices normally."""
+    import threading
+    import time
+    if workload == "heston_asian":
+        ctx = heston_context()
+        packed = pack([plans.asian(heston_asian_c3(), ctx)])
+        s = settings(1 << 22, 42, precision="fp32", schedule="persistent")
+    else:
+        ctx = c2_context()
+        packed = pack([plans.autocallable(snowball_c2(), ctx)])
+        s = settings(1 << 24, 42, sobol=True, precision="fp32", schedule="persistent")
+    reference = gpu_price(native, ctx, packed, s)[0]
+    t0 = time.perf_counter()
+    gpu_price(native, ctx, packed, s)
+    full = time.perf_counter() - t0
+    flag = C.c_int32(0)
+
+    def cancel():
+        time.sleep(0.25 * full)
+        flag.value = 1
+    thread = threading.Thread(target=cancel)
+    thread.start()
+    t0 = time.perf_counter()
+    with pytest.raises(InterruptedError):
+        gpu_price(native, ctx, packed, s, cancel=flag)
+    thread.join()
+    assert time.perf_counter() - t0 < 5.0
+    after = gpu_price(native, ctx, packed, s)[0]
+    assert after.price == reference.price and after.executed_steps == reference.executed_steps
+
+
 def test_invalid_inputs_are_rejected(native):
     from kiyosi_gb300.errors import InvalidInputError, UnsupportedOperationError
     ctx = bsm()
