@@ -485,7 +485,8 @@ double kgpu_context_last_path_kernel_ms(const kgpu_context* ctx);
  * reference: the denominators of the benchmark's op-model roofline).  rates[0..4], in
  * thread operations per second: FP32 fused multiply-add, its packed two-lane form
  * (counted in FMAs), 32-bit logic (LOP3), the multi-function unit's base-2 logarithm,
- * and 32-bit loads that hit L1; entries past the fifth are set to 0.  Runs about a
+ * and 32-bit loads that hit L1 with every lane of a warp at one address; entries past
+ * the fifth are set to 0.  Runs about a
  * millisecond of kernels on the context's stream. */
 kgpu_status kgpu_pipe_rates(kgpu_context* ctx, double* rates, int32_t count);
 

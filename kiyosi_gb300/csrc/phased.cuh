@@ -152,60 +152,61 @@ __device__ __forceinline__ bool phase_interval(const PhaseArgs<Real, SOBOL>& a, 
     }
     // Daily bridge steps of the monitoring paths, until knock-in is decided.  `next`:
     // the lane's next undrawn position (PCG stream position).
-    // Two positions per iteration: their normals are drawn together (a packed quantile
-    // pair for Sobol), then the two bridge steps run in order; a path that decides
-    // knock-in at the first leaves the second unused.
+    // Four positions per iteration: their normals are drawn together (two packed
+    // quantile pairs for Sobol), then the bridge steps run in order; a path that decides
+    // knock-in early leaves the later ones unused.
     bool walking = L.valid && L.monitoring;
     int next = start + 1;
     const UnitT<Real>* up = units + start + 1;
     size_t hi = size_t(start + 1) * a.high_blocks + block;  // Sobol: high table and nibble rows
     size_t ri = size_t(start + 1) * 32;
-    const size_t hstep = size_t(2) * a.high_blocks;
-    for (int q = start + 1; __any_sync(kFull, walking && q <= end); q += 2, up += 2, hi += hstep, ri += 64) {
-        const bool s0 = walking && q <= end;
-        const bool s1 = walking && q + 1 <= end;
-        UnitT<Real> u0q{}, u1q{};
-        Real z0 = Real(0), z1 = Real(0);
+    const size_t hstep = size_t(4) * a.high_blocks;
+    for (int q = start + 1; __any_sync(kFull, walking && q <= end); q += 4, up += 4, hi += hstep, ri += 128) {
+        bool s[4];
+        UnitT<Real> u[4];
+        Real z[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            s[j] = walking && q + j <= end;
+            u[j] = UnitT<Real>{};
+            z[j] = Real(0);
+        }
         if constexpr (SOBOL) {
-            uint32_t w0 = 0, w1 = 0;
             const uint32_t* row = a.sobol.nibbles32 + ri;
-            if (s0) {
-                u0q = up[0];
-                w0 = __ldg(a.high_t + hi) ^ __ldg(row + glo) ^ __ldg(row + ghi);
+            uint32_t w[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                w[j] = 0;
+                if (s[j]) {
+                    u[j] = up[j];
+                    w[j] = __ldg(a.high_t + hi + size_t(j) * a.high_blocks) ^ __ldg(row + 32 * j + glo) ^
+                           __ldg(row + 32 * j + ghi);
+                }
             }
-            if (s1) {
-                u1q = up[1];
-                w1 = __ldg(a.high_t + hi + a.high_blocks) ^ __ldg(row + 32 + glo) ^ __ldg(row + 32 + ghi);
-            }
-            const float2 z = phase_sobol_pair(a.sobol, w0, w1, s0, s1, gray, q);
-            z0 = z.x;
-            z1 = z.y;
+            const float2 za = phase_sobol_pair(a.sobol, w[0], w[1], s[0], s[1], gray, q);
+            const float2 zb = phase_sobol_pair(a.sobol, w[2], w[3], s[2], s[3], gray, q + 2);
+            z[0] = za.x;
+            z[1] = za.y;
+            z[2] = zb.x;
+            z[3] = zb.y;
         } else {
-            if (s0) {
-                u0q = up[0];
-                z0 = pn.normal();
-                next = q + 1;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (s[j]) {
+                    u[j] = up[j];
+                    z[j] = pn.normal();
+                    next = q + j + 1;
+                }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (s[j] && walking) {
+                const Real daily = lr + xfma(u[j].b, target - lr, u[j].a * z[j]);
+                lr = daily;
+                minimum = daily < minimum ? daily : minimum;
+                executed += 1;
+                walking = !(minimum < level);
             }
-            if (s1) {
-                u1q = up[1];
-                z1 = pn.normal();
-                next = q + 2;
-            }
-        }
-        if (s0) {
-            const Real daily = lr + xfma(u0q.b, target - lr, u0q.a * z0);
-            lr = daily;
-            minimum = daily < minimum ? daily : minimum;
-            executed += 1;
-            walking = !(minimum < level);
-        }
-        if (s1 && walking) {
-            const Real daily = lr + xfma(u1q.b, target - lr, u1q.a * z1);
-            lr = daily;
-            minimum = daily < minimum ? daily : minimum;
-            executed += 1;
-            walking = !(minimum < level);
-        }
     }
     // PCG: the interval's normals not drawn (knock-in decided, or not monitored) are
     // skipped, as SkippingPath::skip does; Sobol draws are positional.

@@ -60,11 +60,12 @@ __global__ void __launch_bounds__(kBlock) lg2_kernel(float* sink) {
     if (s == 1234.5f) sink[threadIdx.x] = s;
 }
 
-// 32-bit loads that hit L1: each thread walks a 4 KiB table with a dependent index, as
+// 32-bit loads that hit L1, every lane of a warp at the same address (the path kernels'
+// table reads are broadcasts): each warp walks a 4 KiB table with a dependent index, as
 // kChains independent walks.
 __global__ void __launch_bounds__(kBlock) load_kernel(const unsigned* table, unsigned* sink) {
     unsigned x[kChains];
-    for (int c = 0; c < kChains; ++c) x[c] = (threadIdx.x + 37u * c) & 1023u;
+    for (int c = 0; c < kChains; ++c) x[c] = ((threadIdx.x >> 5) * 61u + 37u * c) & 1023u;
     for (int i = 0; i < kIterations; ++i)
 #pragma unroll
         for (int c = 0; c < kChains; ++c) x[c] = __ldg(table + x[c]);
@@ -113,8 +114,8 @@ extern "C" kgpu_status kgpu_pipe_rates(kgpu_context* ctx, double* rates, int32_t
         const double per = which == 1 ? 2.0 : 1.0;  // FFMA2: two lanes of FMA per operation
         return best > 0.f ? ops * per / (double(best) * 1e-3) : 0.0;
     };
-    // rates[0] FFMA, [1] FFMA2 (FMAs), [2] LOP3, [3] MUFU lg2, [4] L1-hit loads; thread
-    // operations per second.
+    // rates[0] FFMA, [1] FFMA2 (FMAs), [2] LOP3, [3] MUFU lg2, [4] L1-hit broadcast
+    // loads; thread operations per second.
     for (int i = 0; i < count && i < 5; ++i) rates[i] = timed(i);
     for (int i = 5; i < count; ++i) rates[i] = 0.0;
     cudaEventDestroy(start);
