@@ -38,14 +38,15 @@ sys.path.insert(0, ROOT)
 PATHS = 1 << 20
 STEPS = 504
 SEED = 42
-# Warp instructions the FP32 persistent kernel issues per executed path position on
-# this workload, from one ncu capture (smsp__inst_executed.sum 403,176,851 over the
-# 41,683,020 positions of a 2^19-path pricing of this workload).
-# The kernel is neither HBM- nor tensor-bound, so its roofline is the SM issue rate
-# (4 warp-instructions per cycle per SM).
-WARP_INST_PER_EXECUTED_STEP = 403176851 / 41683020
-# DRAM bytes per path of the same capture (5.07 MB read, 512 B written, at 2^19 paths).
-DRAM_BYTES_PER_PATH = (5.069568e6 + 512) / (1 << 19)
+# The phase-major kernel on this workload, from one ncu capture of a 2^19-path pricing
+# (41,683,020 executed path positions): warp instructions issued and DRAM bytes moved
+# per launch.  The kernel is neither HBM- nor tensor-bound; its roofline is the op model
+# of kiyosi_gb300/roofline_ops.json against the measured pipe rates, with the SM issue
+# rate (4 warp-instructions per cycle per SM) beside it.
+PHASED_WARP_INST = 146560264
+PHASED_POSITIONS = 41683020
+PHASED_DRAM_BYTES = 4308224
+PHASED_CAPTURE_PATHS = 1 << 19
 
 
 def snowball():
@@ -300,18 +301,13 @@ def run_ours(args):
     cpu1_rate = (1 << 18) * STEPS / (time.perf_counter() - t0)
     se = ref.sample_error
     executed = est32.executed_steps
-    issue = None
     kernel_s = sum(path_ms) / len(path_ms) / 1e3
-    if WARP_INST_PER_EXECUTED_STEP and clock["sm_mhz"] and kernel_s > 0:
-        achieved = WARP_INST_PER_EXECUTED_STEP * executed / kernel_s
-        peak = 4.0 * native_sm_count(native) * clock["sm_mhz"] * 1e6
-        issue = {"bound": "issue", "achieved": achieved / 1e9, "peak": peak / 1e9,
-                 "unit": "Gwarp-inst/s", "frac": achieved / peak,
-                 "traffic": DRAM_BYTES_PER_PATH * PATHS,
-                 "kernel": "persistent_kernel<float, BSM, Sobol>",
-                 "kernel_ms": kernel_s * 1e3,
-                 "note": "peak = 4 warp-instructions/cycle x SMs x median SM clock sampled "
-                         "during the timed region; traffic = DRAM bytes per launch (ncu)"}
+    roofline = op_roofline(native, executed, kernel_s, clock)
+    # The lane-refill kernel on the same book (one pricing, flushed L2), for comparison.
+    lanes = settings(abi.PRECISION_FP32, abi.SCHEDULE_LANE_REFILL)
+    device_call(lanes)
+    cuda.flush_l2()
+    lane_est, _, _, lane_ms = device_call(lanes)
     line = {
         "metric": "path-steps/s (FP32 batched vs FP64 plain) at <=0.5 SE",
         "value": value,
@@ -337,7 +333,10 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
         "clocks": clock,
-        "roofline": issue,
+        "roofline": roofline,
+        "executed_path_steps_per_s": executed * args.steps / (total_ms / 1e3) * ranks.world,
+        "lane_refill": {"path_kernel_ms": lane_ms, "identical_estimate": lane_est.price == est32.price,
+                        "note": "the same book on the lane-refill persistent kernel"},
         "fp64_plain": {"value": fp64_rate, "unit": "path-steps/s",
                        "speedup_fp32_persistent": value / fp64_rate,
                        "price": est64.price},
@@ -356,6 +355,38 @@ def run_ours(args):
         line["config"]["parallelism"] = f"replicas x{ranks.world} (one full pricing per GPU)"
     print(json.dumps(line))
     ranks.close()
+
+
+def op_roofline(native, executed, kernel_s, clock):
+    """The path kernel against its op model: algorithmic operations per executed position
+    by pipe (kiyosi_gb300/roofline_ops.json) over the pipe rates measured on this device
+    (kgpu_pipe_rates); the bound is the pipe that allows the fewest positions per second.
+    Beside it, the issued warp instructions against the SM issue rate."""
+    from kiyosi_gb300 import abi
+    model = json.load(open(os.path.join(ROOT, "kiyosi_gb300", "roofline_ops.json")))
+    ops = model["per_executed_position"]
+    r = (C.c_double * 5)()
+    native.check(native.lib.kgpu_pipe_rates(native.handle, r, 5))
+    rates = {"fp32": max(r[0], r[1]), "logic": r[2], "mufu": r[3], "l1_loads": r[4]}
+    ceilings = {pipe: rates[pipe] / ops[pipe] for pipe in ops}
+    bound = min(ceilings, key=ceilings.get)
+    achieved = ops[bound] * executed / kernel_s
+    sms = native_sm_count(native)
+    issue_peak = 4.0 * sms * (clock["sm_mhz"] or 2070.0) * 1e6
+    issued = PHASED_WARP_INST / PHASED_POSITIONS * executed / kernel_s
+    return {"bound": bound, "achieved": achieved / 1e9, "peak": rates[bound] / 1e9,
+            "unit": "Gop/s", "frac": achieved / rates[bound],
+            "traffic": PHASED_DRAM_BYTES * PATHS / PHASED_CAPTURE_PATHS,
+            "kernel": "phased_kernel<float, Sobol> (one cooperative launch)",
+            "kernel_ms": kernel_s * 1e3,
+            "positions_per_s": executed / kernel_s,
+            "position_ceiling_per_s": ceilings[bound],
+            "ops_per_position": ops, "pipe_rates_gops": {k: v / 1e9 for k, v in rates.items()},
+            "issue": {"warp_inst_per_position": PHASED_WARP_INST / PHASED_POSITIONS,
+                      "achieved_gwarp_inst_s": issued / 1e9, "peak_gwarp_inst_s": issue_peak / 1e9,
+                      "frac": issued / issue_peak},
+            "note": "peak = the bound pipe's rate measured by kgpu_pipe_rates in this run; "
+                    "traffic = DRAM bytes per launch (ncu, 2^19-path capture scaled by paths)"}
 
 
 def native_sm_count(native):
