@@ -709,10 +709,11 @@ def run_shared_grid(args):
 def run_lsmc(args):
     """American put under Heston, 50 exercise dates x 5 Euler substeps, judged by the
     Heston ADI price.  Two comparisons of the polynomial LSMC (the reference's method)
-    with the polynomial plus the fitted network: at the configuration's 2^20 paths
-    (network: 5 epochs per date over every in-the-money path, batch 8192), and at equal
-    wall time (network at 2^22 paths training on 131,072 samples per date, against the
-    polynomial at the path count whose wall time is closest)."""
+    with the polynomial plus the fitted network and with the network alone (no
+    polynomial): at the configuration's 2^20 paths (network: 5 epochs per date over every
+    in-the-money path, batch 8192), and at equal wall time (networks at 2^22 paths
+    training on 131,072 samples per date, against the polynomial at the path count whose
+    wall time is closest).  Also the trainer's time per Adam step."""
     from kiyosi_gb300 import _native, abi, workloads
     from oracle import loader
     native = _native.context(0)
@@ -767,9 +768,25 @@ def run_lsmc(args):
                              abs(poly["out_of_sample"] - oracle.out_of_sample) / oracle.out_of_sample_error),
         "oracle_cpu_s": oracle_s, "oracle_threads": threads}
     mlp = price(abi.BASIS_MLP, 20)
+    alone = price(abi.BASIS_MLP_STANDALONE, 20)
     mlp_eq = price(abi.BASIS_MLP, 22, samples=131072)
+    alone_eq = price(abi.BASIS_MLP_STANDALONE, 22, samples=131072)
     polys = [price(abi.BASIS_POLY3, k) for k in range(21, 27)]
     equal = min(polys, key=lambda r: abs(r["wall_ms"] - mlp_eq["wall_ms"]))
+    # The trainer alone: Adam steps of batch 8192 over 65,536 samples, one launch.
+    rng = np.random.default_rng(5)
+    tsamples = rng.normal(size=(65536, 4)).astype(np.float32)
+    tsamples[:, 3] = np.abs(tsamples[:, 3]) * 0.1
+    tparams = (rng.uniform(-0.3, 0.3, abi.MLP_PARAMS)).astype(np.float32)
+    fp = C.POINTER(C.c_float)
+    trainer = {}
+    for steps in (8, 1008):
+        q = tparams.copy()
+        t0 = time.perf_counter()
+        native.check(native.lib.kgpu_mlp_train(native.handle, q.ctypes.data_as(fp), tsamples.ctypes.data_as(fp),
+                                               len(tsamples), 8192, steps, 1e-3))
+        trainer[steps] = time.perf_counter() - t0
+    us_per_step = (trainer[1008] - trainer[8]) / 1000 * 1e6
     line = {
         "metric": "LSMC |price - ADI| at equal wall time: polynomial + fitted network vs polynomial",
         "value": abs(mlp_eq["error_vs_adi"]), "unit": "price units",
@@ -780,9 +797,12 @@ def run_lsmc(args):
                                "substeps; network 3-64-64-1 on the polynomial's residual, 5 "
                                "epochs/date, batch 8192", "fresh_paths_seed": 43},
         "adi": {"price": adi, "grid": "400 x 100 x 400 (MCS, Ikonen-Toivanen)", "cpu_s": adi_s},
-        "at_2^20_paths": {"poly3_fp32": poly, "poly3_fp64": poly64, "poly3_plus_network": mlp},
+        "at_2^20_paths": {"poly3_fp32": poly, "poly3_fp64": poly64, "poly3_plus_network": mlp,
+                          "network_alone": alone},
         "parity": {"oracle": oracle_parity},
-        "at_equal_wall_time": {"poly3_plus_network": mlp_eq, "poly3": equal},
+        "at_equal_wall_time": {"poly3_plus_network": mlp_eq, "network_alone": alone_eq, "poly3": equal},
+        "trainer": {"us_per_adam_step": us_per_step, "batch": 8192, "network": "3-64-64-1",
+                    "timing": "host clock around kgpu_mlp_train, 1008 minus 8 steps"},
         "poly3_by_paths": polys,
     }
     print(json.dumps(line), flush=True)

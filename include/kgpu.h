@@ -400,7 +400,11 @@ kgpu_status kgpu_sobol_points(kgpu_context* ctx, uint64_t seed, int32_t dimensio
 /* ---------------------------------------------------------------------------------
  * American exercise by least-squares Monte Carlo (american.rs:955-1455).
  * --------------------------------------------------------------------------------- */
-enum { KGPU_BASIS_QUADRATIC = 0, KGPU_BASIS_POLY3 = 1, KGPU_BASIS_MLP = 2 };
+/* MLP: the polynomial basis plus a 3 -> 64 -> 64 -> 1 network fitted to what the
+ * polynomial leaves unexplained.  MLP_STANDALONE: the network alone is the continuation
+ * value, fitted to the in-the-money paths' discounted cash flows on the raw features
+ * (log moneyness, variance, time). */
+enum { KGPU_BASIS_QUADRATIC = 0, KGPU_BASIS_POLY3 = 1, KGPU_BASIS_MLP = 2, KGPU_BASIS_MLP_STANDALONE = 3 };
 
 typedef struct kgpu_lsmc_settings {
     int32_t path_count;
@@ -471,6 +475,15 @@ kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book
 #define KGPU_MLP_PARAMS 4481
 kgpu_status kgpu_mlp_gradients(kgpu_context* ctx, const float* params, const float* samples, int32_t count,
                                float* grads, double* loss);
+
+/* `steps` Adam steps (Kingma and Ba; beta1 0.9, beta2 0.999, eps 1e-8, zero initial
+ * moments) of the same tensor-core training kernel on `samples` (count x 4 floats, as for
+ * kgpu_mlp_gradients), minibatch b being samples [b * batch, ...) cycled in order;
+ * `params` (KGPU_MLP_PARAMS floats) is updated in place.  No counterpart in the
+ * reference: exposed so the optimiser can be checked against a CPU restatement.  batch
+ * <= 8192. */
+kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const float* samples, int32_t count, int32_t batch,
+                           int32_t steps, double learning_rate);
 
 /* Instrumentation of the last call on `ctx`: device time from the first to the last
  * kernel of the call (CUDA events on the context's stream) and the number of kernel

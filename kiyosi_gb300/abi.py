@@ -73,6 +73,7 @@ UNCERTAINTY_NAMES = {
 BASIS_QUADRATIC = 0
 BASIS_POLY3 = 1
 BASIS_MLP = 2
+BASIS_MLP_STANDALONE = 3
 
 _D = C.c_double
 _I = C.c_int32
@@ -181,7 +182,7 @@ EXPORTED_SYMBOLS = (
     "kgpu_sobol_points", "kgpu_lsmc_price", "kgpu_context_last_kernel_ms",
     "kgpu_context_last_path_kernel_ms",
     "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count", "kgpu_pipe_rates",
-    "kgpu_price_contract_noalloc", "kgpu_mlp_gradients",
+    "kgpu_price_contract_noalloc", "kgpu_mlp_gradients", "kgpu_mlp_train",
 )
 MLP_PARAMS = 4481
 
@@ -228,6 +229,8 @@ def declare(lib):
     lib.kgpu_abi_version.restype = _I
     lib.kgpu_device_count.argtypes = []
     lib.kgpu_device_count.restype = _I
+    lib.kgpu_mlp_train.argtypes = [V, C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _I, _I, _D]
+    lib.kgpu_mlp_train.restype = _I
     lib.kgpu_pipe_rates.argtypes = [V, C.POINTER(_D), _I]
     lib.kgpu_pipe_rates.restype = _I
     return lib

@@ -429,7 +429,9 @@ extern "C" kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* mode
         return KGPU_UNSUPPORTED_OPERATION;
     }
     const bool heston = model->kind == KGPU_MODEL_HESTON;
-    if (settings->basis == KGPU_BASIS_MLP) {
+    if (settings->basis < KGPU_BASIS_QUADRATIC || settings->basis > KGPU_BASIS_MLP_STANDALONE)
+        return bad("unknown basis");
+    if (settings->basis == KGPU_BASIS_MLP || settings->basis == KGPU_BASIS_MLP_STANDALONE) {
         return kgpu_lsmc_mlp(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
     }
     if ((settings->basis == KGPU_BASIS_QUADRATIC) == heston)

@@ -1049,6 +1049,7 @@ cudaError_t train_step(cudaStream_t st, float* params, float* m, float* v, Adam&
 template <bool TWO>
 kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
                     const kgpu_lsmc_settings* s, uint64_t fresh_seed, kgpu_lsmc_result* out) {
+    const bool standalone = s->basis == KGPU_BASIS_MLP_STANDALONE;
     const LsmcParams<float> p = make_lsmc_params<float>(model, strike, sign, expiry, s);
     const size_t n = size_t(p.paths), d = size_t(p.dates);
     const int batch = s->mlp_batch > 0 ? s->mlp_batch : 8192;
@@ -1168,16 +1169,21 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
         mlp_discount_kernel<<<pblocks, 256, 0, st>>>(cash, p.paths, p.discount);
         ++launches;
         // The polynomial fit of this date (lsmc_solve: block-ordered merge, pivoted FP64
-        // elimination with degree fallback), then the residual samples.
-        mlp_poly_sums_kernel<TWO><<<sblocks, kLsmcThreads, 0, st>>>(p, date, a, b, cash, poly_partials);
-        reduce_partials_kernel<<<sum_count(TWO ? 10 : 3), 32, 0, st>>>(poly_partials, sblocks, poly_reduced);
-        lsmc_solve<TWO><<<1, kSolveThreads, 0, st>>>(poly_reduced, 1, p.max_degree, coefs + size_t(date) * kMaxTerms,
-                                           have + date, poly_failed);
+        // elimination with degree fallback), then the residual samples.  The standalone
+        // network fits no polynomial: `have` stays 0, so the targets are the discounted
+        // cash flows themselves and the network alone is the continuation value.
+        if (!standalone) {
+            mlp_poly_sums_kernel<TWO><<<sblocks, kLsmcThreads, 0, st>>>(p, date, a, b, cash, poly_partials);
+            reduce_partials_kernel<<<sum_count(TWO ? 10 : 3), 32, 0, st>>>(poly_partials, sblocks, poly_reduced);
+            lsmc_solve<TWO><<<1, kSolveThreads, 0, st>>>(poly_reduced, 1, p.max_degree,
+                                                         coefs + size_t(date) * kMaxTerms, have + date, poly_failed);
+            launches += 3;
+        }
         mlp_count_kernel<TWO><<<pblocks, 256, 0, st>>>(p, date, a, b, cash, coefs, have, stats);
         mlp_scan_kernel<<<1, kScanThreads, 0, st>>>(stats, pblocks, counts, total, norms + date);
         mlp_scatter_kernel<TWO><<<pblocks, 256, 0, st>>>(p, f, date, a, b, cash, coefs, have, counts, norms + date,
                                                         samples, sample_path);
-        launches += 6;
+        launches += 3;
         MLP_TRY(cudaGetLastError());
         int itm = 0;
         MLP_TRY(cudaMemcpyAsync(&itm, total, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1316,7 +1322,8 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
 }  // namespace
 }  // namespace kgpu
 
-// LSMC with the continuation network (called by kgpu_lsmc_price for KGPU_BASIS_MLP).
+// LSMC with the continuation network (called by kgpu_lsmc_price for KGPU_BASIS_MLP and
+// KGPU_BASIS_MLP_STANDALONE).
 kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
                           const kgpu_lsmc_settings* settings, uint64_t fresh_seed, kgpu_lsmc_result* out) {
     if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
@@ -1327,6 +1334,66 @@ kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model* model, double str
     return model->kind == KGPU_MODEL_HESTON
                ? kgpu::mlp_run<true>(ctx, model, strike, sign, expiry, settings, fresh_seed, out)
                : kgpu::mlp_run<false>(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
+}
+
+extern "C" kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const float* samples, int32_t count,
+                                      int32_t batch, int32_t steps, double learning_rate) {
+    using namespace kgpu;
+    if (!ctx || !params || !samples || count < 1 || batch < 1 || steps < 1 || !(learning_rate > 0.0))
+        return KGPU_INVALID_INPUT;
+    if (batch > 64 * kRows) {
+        ctx->error = "the training batch is at most 8192 samples";
+        return KGPU_INVALID_INPUT;
+    }
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->error.clear();
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
+    if (!configure_train_kernel()) {
+        ctx->error = "cannot configure the training kernel's shared memory";
+        return KGPU_DEVICE_ERROR;
+    }
+    const int blocks = (std::min(batch, count) + kRows - 1) / kRows;
+    if (!cooperative_fits(ctx->device, blocks)) {
+        ctx->error = "the training kernel's CTAs do not fit the device at once";
+        return KGPU_UNSUPPORTED_OPERATION;
+    }
+    // Parameters, Adam moments, gradient partials ([parameter][CTA]), W2 tiles, the
+    // samples, the error word and the grid barrier.
+    const size_t floats = size_t(3) * kStride + size_t(blocks) * kStride + 2 * kHidden * kHidden;
+    const size_t bytes = floats * 4 + size_t(count) * 16 + 64;
+    if (ctx->mlp_scratch.ensure(bytes)) return KGPU_DEVICE_ERROR;
+    float* dparams = static_cast<float*>(ctx->mlp_scratch.ptr);
+    float* dm = dparams + kStride;
+    float* dv = dm + kStride;
+    float* dpartials = dv + kStride;
+    __nv_bfloat16* w2_tiles = reinterpret_cast<__nv_bfloat16*>(dpartials + size_t(blocks) * kStride);
+    float4* dsamples = reinterpret_cast<float4*>(w2_tiles + 2 * kHidden * kHidden);
+    int* derror = reinterpret_cast<int*>(dsamples + count);
+    GridBarrier* barrier = reinterpret_cast<GridBarrier*>(derror + 2);
+    cudaStream_t st = ctx->stream;
+    if (cudaMemcpyAsync(dsamples, samples, size_t(count) * 16, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(dparams, params, size_t(kParams) * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(dm, 0, size_t(2) * kStride * 4, st) != cudaSuccess ||
+        cudaMemsetAsync(derror, 0, 8 + sizeof(GridBarrier), st) != cudaSuccess)
+        return KGPU_DEVICE_ERROR;
+    Adam adam;
+    TrainArgs ta{dparams, w2_tiles, dm, dv, dsamples, dpartials, barrier, derror, count, batch, steps,
+                 0, float(learning_rate), adam.beta1, adam.beta2, adam.eps};
+    void* args[] = {&ta};
+    int failed = 0;
+    if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel), dim3(blocks), dim3(kThreadsTrain),
+                                    args, kTrainSmemBytes, st) != cudaSuccess ||
+        cudaMemcpyAsync(params, dparams, size_t(kParams) * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&failed, derror, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        ctx->error = "training kernel failed";
+        return KGPU_DEVICE_ERROR;
+    }
+    if (failed) {
+        ctx->error = "a tensor-core wait or grid barrier gave up in the training kernel";
+        return KGPU_DEVICE_ERROR;
+    }
+    return KGPU_OK;
 }
 
 extern "C" kgpu_status kgpu_mlp_gradients(kgpu_context* ctx, const float* params, const float* samples, int32_t count,

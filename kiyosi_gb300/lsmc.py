@@ -12,7 +12,8 @@ from ._native import context
 from .errors import InvalidInputError
 from .market import BlackScholesMertonParameters, HestonParameters
 
-_BASIS = {"quadratic": abi.BASIS_QUADRATIC, "poly3": abi.BASIS_POLY3, "mlp": abi.BASIS_MLP}
+_BASIS = {"quadratic": abi.BASIS_QUADRATIC, "poly3": abi.BASIS_POLY3, "mlp": abi.BASIS_MLP,
+          "mlp_standalone": abi.BASIS_MLP_STANDALONE}
 
 
 def lsmc_settings(engine, model, basis=None, substeps=None, fresh_seed=None, seed=None):

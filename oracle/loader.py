@@ -160,3 +160,29 @@ def mlp_gradients(params, samples, bf16_operands=True):
                                  samples.ctypes.data_as(C.POINTER(C.c_float)), len(samples),
                                  int(bf16_operands), grads.ctypes.data_as(C.POINTER(C.c_double)))
     return loss, grads
+
+
+def mlp_adam(params, samples, batch, steps, learning_rate, beta1=0.9, beta2=0.999, eps=1e-8):
+    """`steps` Adam steps (Kingma and Ba, zero initial moments) on the LSMC continuation
+    network, minibatch b being samples [b * batch, ...) cycled in order, with the
+    gradients of mlp_gradients (the tensor-core kernel's BF16 operand rounding) and the
+    moments, bias corrections and update in float32 as the training kernel keeps them.
+    Returns the parameters after the last step."""
+    p = np.array(params, np.float32)
+    x = np.ascontiguousarray(samples, np.float32)
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    per_epoch = (len(x) + batch - 1) // batch
+    b1, b2, e, lr = np.float32(beta1), np.float32(beta2), np.float32(eps), np.float32(learning_rate)
+    one = np.float32(1.0)
+    for step in range(steps):
+        first = (step % per_epoch) * batch
+        _, g = mlp_gradients(p, x[first:first + batch])
+        g = g.astype(np.float32)
+        m = b1 * m + (one - b1) * g
+        v = b2 * v + (one - b2) * g * g
+        t = np.float32(step + 1)
+        bias1 = one - np.float32(b1 ** t)
+        bias2 = one - np.float32(b2 ** t)
+        p = (p - lr * (m / bias1) / (np.sqrt(v / bias2) + e)).astype(np.float32)
+    return p

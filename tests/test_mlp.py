@@ -68,6 +68,45 @@ def test_tensor_core_gradients_match_oracle(native, count):
         assert err <= 1e-3 * scale + 1e-9, (name, err, scale)
 
 
+def test_oracle_adam_first_step_and_descent():
+    """The first Adam step moves every parameter with a nonzero gradient by the learning
+    rate against the gradient's sign; a few hundred steps reduce the loss."""
+    p, x = _params(), _samples(512)
+    lr = 1e-3
+    _, g = loader.mlp_gradients(p, x)
+    one = loader.mlp_adam(p, x, 512, 1, lr)
+    moved = np.abs(g) > 1e-4
+    assert np.allclose((one - p)[moved], -lr * np.sign(g[moved]), rtol=1e-3, atol=1e-7)
+    before, _ = loader.mlp_gradients(p, x)
+    after, _ = loader.mlp_gradients(loader.mlp_adam(p, x, 128, 200, lr), x)
+    assert after < 0.5 * before, (after, before)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("count,batch,steps", [(1000, 1000, 1), (3000, 1024, 12)])
+def test_tensor_core_adam_matches_oracle(native, count, batch, steps):
+    """kgpu_mlp_train (the cooperative tensor-core trainer: gradients, partial sums and
+    Adam in one launch) against the oracle's float32 Adam on the oracle's gradients.  One
+    step moves each parameter by the learning rate against the gradient's sign, so the
+    parameters agree to rounding wherever the gradient is not negligible; over twelve
+    steps the ratio m / sqrt(v) amplifies the 1e-3 relative gradient differences only for
+    parameters whose gradient sits near zero, so 99% of the parameters agree to 2% of one
+    step and all of them to one step per step."""
+    lr = 1e-3
+    p, x = _params(), _samples(count)
+    got = p.copy()
+    native.check(native.lib.kgpu_mlp_train(
+        native.handle, got.ctypes.data_as(C.POINTER(C.c_float)), x.ctypes.data_as(C.POINTER(C.c_float)),
+        count, batch, steps, lr))
+    ref = loader.mlp_adam(p, x, batch, steps, lr)
+    diff = np.abs(got - ref)
+    assert np.max(diff) <= lr * steps, np.max(diff)
+    assert np.quantile(diff, 0.99) <= 0.02 * lr, np.quantile(diff, 0.99)
+    ref_loss, _ = loader.mlp_gradients(ref, x)
+    got_loss, _ = loader.mlp_gradients(got, x)
+    assert abs(got_loss - ref_loss) <= 1e-3 * ref_loss, (got_loss, ref_loss)
+
+
 def _heston():
     return PricingContext(HestonParameters(0.03, 0.0, 0.04, 2.0, 0.04, 0.5, -0.7), 100.0)
 
@@ -103,3 +142,21 @@ def test_network_improves_the_polynomial_exercise_policy(native):
     s.mlp_epochs, s.mlp_batch, s.mlp_learning_rate, s.mlp_seed = 5, 8192, 1e-3, 7
     mlp = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, s, fresh_seed=43)
     assert mlp.out_of_sample > poly.out_of_sample, (mlp.out_of_sample, poly.out_of_sample)
+
+
+@pytest.mark.gpu
+def test_standalone_network_prices_the_american_put(native, oracle):
+    """The network alone (no polynomial, targets the discounted cash flows themselves) as
+    the continuation estimate: deterministic, and its in-sample price and out-of-sample
+    lower bound sit near the ADI price like the residual network's."""
+    ctx = _heston()
+    model = ctx.kgpu_model()
+    adi = oracle.kor_heston_adi_american(C.byref(model), 100.0, -1.0, 1.0, 200, 50, 200, 1)
+    s = lsmc_settings(1 << 16, 10, 42, abi.BASIS_MLP_STANDALONE, precision="fp32", substeps=2)
+    s.mlp_epochs, s.mlp_batch, s.mlp_learning_rate, s.mlp_seed = 5, 4096, 1e-3, 7
+    a = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, s, fresh_seed=43)
+    b = gpu_lsmc(native, ctx, 100.0, -1.0, 1.0, s, fresh_seed=43)
+    assert a.price == b.price and a.out_of_sample == b.out_of_sample
+    assert a.out_of_sample - 4 * a.out_of_sample_error < adi + 0.05
+    assert abs(a.price - adi) < 0.25, (a.price, adi)
+    assert abs(a.out_of_sample - adi) < 0.25, (a.out_of_sample, adi)
