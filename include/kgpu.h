@@ -441,6 +441,19 @@ kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double s
                             double sign, double expiry, const kgpu_lsmc_settings* settings,
                             uint64_t fresh_seed, kgpu_lsmc_result* out);
 
+/* Prices the same American option in `count` (1..16) Black-Scholes-Merton scenarios --
+ * the bumped contexts of the option's numerical Greeks -- with the quadratic basis, on
+ * one set of paths: the scenarios share the seed's normals and the stored Brownian
+ * coordinates, and each runs its own regression.  out[y] equals what kgpu_lsmc_price
+ * returns for models[y] with the same settings, bit for bit.  Replaces the grouped
+ * scenario pricing of MonteCarloVanillaEngine::greek_prices / american_spots
+ * (crates/kiyosi/src/engines/monte_carlo/american.rs:820-946), which batches up to nine
+ * contexts of one valuation date.  KGPU_UNSUPPORTED_OPERATION for Heston or local-vol
+ * scenarios and for the other bases. */
+kgpu_status kgpu_lsmc_price_scenarios(kgpu_context* ctx, const kgpu_model* models, int32_t count, double strike,
+                                      double sign, double expiry, const kgpu_lsmc_settings* settings,
+                                      uint64_t fresh_seed, kgpu_lsmc_result* out);
+
 /* Prices contract `contract` of `device_book` without allocating device memory, for
  * callers that cannot call cudaMalloc (a host that reserves its device-memory budget up
  * front and hands out slices itself, a plugin inside such a host, or a latency-critical

@@ -182,7 +182,7 @@ EXPORTED_SYMBOLS = (
     "kgpu_sobol_points", "kgpu_lsmc_price", "kgpu_context_last_kernel_ms",
     "kgpu_context_last_path_kernel_ms",
     "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count", "kgpu_pipe_rates",
-    "kgpu_price_contract_noalloc", "kgpu_mlp_gradients", "kgpu_mlp_train",
+    "kgpu_price_contract_noalloc", "kgpu_mlp_gradients", "kgpu_mlp_train", "kgpu_lsmc_price_scenarios",
 )
 MLP_PARAMS = 4481
 
@@ -213,6 +213,9 @@ def declare(lib):
     lib.kgpu_lsmc_price.argtypes = [V, _P(Model), _D, _D, _D, _P(LsmcSettings), C.c_uint64,
                                     _P(LsmcResult)]
     lib.kgpu_lsmc_price.restype = _I
+    lib.kgpu_lsmc_price_scenarios.argtypes = [V, _P(Model), _I, _D, _D, _D, _P(LsmcSettings), C.c_uint64,
+                                              _P(LsmcResult)]
+    lib.kgpu_lsmc_price_scenarios.restype = _I
     lib.kgpu_context_last_kernel_ms.argtypes = [V]
     lib.kgpu_context_last_kernel_ms.restype = C.c_double
     lib.kgpu_context_last_path_kernel_ms.argtypes = [V]

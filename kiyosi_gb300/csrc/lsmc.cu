@@ -36,9 +36,9 @@ namespace {
 
 // One exercise date of the backward induction (american.rs:1347-1417).
 template <class Real, bool TWO>
-__global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p, int date, const double* coef_next,
-                                                              const int* have_next, const Real* a, const Real* b,
-                                                              Real* cash, double* partials) {
+__device__ __forceinline__ void backward_body(const LsmcParams<Real>& p, int date, const double* coef_next,
+                                              const int* have_next, const Real* a, const Real* b, Real* cash,
+                                              double* partials) {
     constexpr int T = TWO ? 10 : 3;
     constexpr int S = sum_count(T);
     Real acc[S];
@@ -98,11 +98,32 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p
     block_sums<Real, S>(acc, partials);
 }
 
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_backward(LsmcParams<Real> p, int date, const double* coef_next,
+                                                              const int* have_next, const Real* a, const Real* b,
+                                                              Real* cash, double* partials) {
+    backward_body<Real, TWO>(p, date, coef_next, have_next, a, b, cash, partials);
+}
+
+// One date of a BSM scenario batch: CTA row y is scenario y, with its cash
+// ([scenario][path]), coefficients ([scenario][date][term]), flags ([scenario][date]) and
+// partials ([scenario][sum][block]); the store is shared.
+template <class Real>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_backward_batch(const __grid_constant__ LsmcBatch<Real> batch,
+                                                                    int date, const double* coef_next,
+                                                                    const int* have_next, const Real* a, Real* cash,
+                                                                    double* partials) {
+    const int y = blockIdx.y;
+    const LsmcParams<Real> p = batch.p[y];
+    backward_body<Real, false>(p, date, coef_next ? coef_next + size_t(y) * p.dates * kMaxTerms : nullptr,
+                               have_next ? have_next + size_t(y) * p.dates : nullptr, a, nullptr,
+                               cash + size_t(y) * p.paths, partials + size_t(y) * sum_count(3) * gridDim.x);
+}
+
 // Date-0 decision and the mean of the cash (FP64 block partials: sum, sum of squares).
 template <class Real, bool TWO>
-__global__ void __launch_bounds__(kLsmcThreads) lsmc_final(LsmcParams<Real> p, const double* coef0, const int* have0,
-                                                           const Real* a, const Real* b, const Real* cash,
-                                                           double* partials) {
+__device__ __forceinline__ void final_body(const LsmcParams<Real>& p, const double* coef0, const int* have0,
+                                           const Real* a, const Real* b, const Real* cash, double* partials) {
     constexpr int T = TWO ? 10 : 3;
     Real cn[T];
     const bool decide = *have0;
@@ -142,6 +163,23 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_final(LsmcParams<Real> p, c
     }
 }
 
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_final(LsmcParams<Real> p, const double* coef0, const int* have0,
+                                                           const Real* a, const Real* b, const Real* cash,
+                                                           double* partials) {
+    final_body<Real, TWO>(p, coef0, have0, a, b, cash, partials);
+}
+
+template <class Real>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_final_batch(const __grid_constant__ LsmcBatch<Real> batch,
+                                                                 const double* coefs, const int* have, const Real* a,
+                                                                 const Real* cash, double* partials) {
+    const int y = blockIdx.y;
+    const LsmcParams<Real> p = batch.p[y];
+    final_body<Real, false>(p, coefs + size_t(y) * p.dates * kMaxTerms, have + size_t(y) * p.dates, a, nullptr,
+                            cash + size_t(y) * p.paths, partials + size_t(y) * 2 * gridDim.x);
+}
+
 // Lower bound on fresh paths: the fitted policy applied forward (american.rs:574-637).
 // The fitted FP64 coefficients in the path store's precision, for the forward pass.
 template <class Real>
@@ -151,9 +189,8 @@ __global__ void coef_table_kernel(const double* coefs, Real* table, int n) {
 }
 
 template <class Real, bool TWO>
-__global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound(LsmcParams<Real> p, uint64_t seed,
-                                                                 const Real* table, const int* have,
-                                                                 double* partials) {
+__device__ __forceinline__ void lower_bound_body(const LsmcParams<Real>& p, uint64_t seed, const Real* table,
+                                                 const int* have, double* partials) {
     constexpr int T = TWO ? 10 : 3;
     const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
     const Real inv_k = Real(1) / p.strike;
@@ -213,39 +250,62 @@ __global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound(LsmcParams<Real
     }
 }
 
+template <class Real, bool TWO>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound(LsmcParams<Real> p, uint64_t seed,
+                                                                 const Real* table, const int* have,
+                                                                 double* partials) {
+    lower_bound_body<Real, TWO>(p, seed, table, have, partials);
+}
+
+template <class Real>
+__global__ void __launch_bounds__(kLsmcThreads) lsmc_lower_bound_batch(const __grid_constant__ LsmcBatch<Real> batch,
+                                                                       uint64_t seed, const Real* table,
+                                                                       const int* have, double* partials) {
+    const int y = blockIdx.y;
+    const LsmcParams<Real> p = batch.p[y];
+    lower_bound_body<Real, false>(p, seed, table + size_t(y) * p.dates * kMaxTerms, have + size_t(y) * p.dates,
+                                  partials + size_t(y) * 2 * gridDim.x);
+}
+
 }  // namespace
 
-// Runs one LSMC pricing in precision Real; all device buffers come from the context.
+// Runs one LSMC pricing in precision Real, or a batch of `count` BSM scenarios that share
+// the path store (one result each, equal to the scalar pricing of that scenario); all
+// device buffers come from the context.
 template <class Real>
-static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double strike, double sign,
+static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* models, int count, double strike, double sign,
                             double expiry, const kgpu_lsmc_settings* s, uint64_t fresh_seed, kgpu_lsmc_result* out) {
+    const kgpu_model* model = models;
     const bool two = model->kind == KGPU_MODEL_HESTON;
-    const LsmcParams<Real> p = make_lsmc_params<Real>(model, strike, sign, expiry, s);
+    const bool batch = count > 1;
+    LsmcBatch<Real> pb{};
+    for (int y = 0; y < count; ++y) pb.p[y] = make_lsmc_params<Real>(models + y, strike, sign, expiry, s);
+    const LsmcParams<Real>& p = pb.p[0];
     const int S = sum_count(p.terms);
-    const size_t n = size_t(p.paths), d = size_t(p.dates);
+    const size_t n = size_t(p.paths), d = size_t(p.dates), ns = size_t(count);
     const int blocks = std::min<int>(ctx->sm_count * 4, int((n + kLsmcThreads - 1) / kLsmcThreads));
-    if (ctx->lsmc_store.ensure(n * d * sizeof(Real) * (two ? 2 : 1)) || ctx->lsmc_cash.ensure(n * sizeof(Real)) ||
-        ctx->lsmc_sums.ensure((size_t(blocks) + 1) * kMaxSums * sizeof(double)) ||
-        ctx->lsmc_coef.ensure(d * kMaxTerms * (sizeof(double) + sizeof(Real)) + d * sizeof(int) + 64) ||
-        ctx->lsmc_misc.ensure(size_t(blocks) * 2 * sizeof(double) + 16))
+    if (ctx->lsmc_store.ensure(n * d * sizeof(Real) * (two ? 2 : 1)) || ctx->lsmc_cash.ensure(ns * n * sizeof(Real)) ||
+        ctx->lsmc_sums.ensure(ns * (size_t(blocks) + 1) * kMaxSums * sizeof(double)) ||
+        ctx->lsmc_coef.ensure(ns * d * kMaxTerms * (sizeof(double) + sizeof(Real)) + ns * d * sizeof(int) + 64) ||
+        ctx->lsmc_misc.ensure(ns * size_t(blocks) * 2 * sizeof(double) + 16))
         return KGPU_DEVICE_ERROR;
     Real* a = static_cast<Real*>(ctx->lsmc_store.ptr);
     Real* b = two ? a + n * d : nullptr;
     Real* cash = static_cast<Real*>(ctx->lsmc_cash.ptr);
     double* coefs = static_cast<double*>(ctx->lsmc_coef.ptr);
-    int* have = reinterpret_cast<int*>(coefs + d * kMaxTerms);
-    int* failed = have + d;
+    int* have = reinterpret_cast<int*>(coefs + ns * d * kMaxTerms);
+    int* failed = have + ns * d;
     // Converted coefficients after `failed`, aligned to 16 bytes.
     Real* table = reinterpret_cast<Real*>(
         (reinterpret_cast<uintptr_t>(failed + 1) + 15) & ~uintptr_t(15));
     double* partials = static_cast<double*>(ctx->lsmc_sums.ptr);
-    double* reduced = partials + size_t(blocks) * kMaxSums;  // one partial per sum
+    double* reduced = partials + ns * size_t(blocks) * kMaxSums;  // one partial per sum and scenario
     double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
     cudaStream_t st = ctx->stream;
     const bool lower = fresh_seed != s->seed;
     double* lp = nullptr;
     if (lower) {
-        if (ctx->mlp_scratch.ensure(size_t(blocks) * 2 * sizeof(double))) return KGPU_DEVICE_ERROR;
+        if (ctx->mlp_scratch.ensure(ns * size_t(blocks) * 2 * sizeof(double))) return KGPU_DEVICE_ERROR;
         lp = static_cast<double*>(ctx->mlp_scratch.ptr);
     }
     for (cudaEvent_t& e : ctx->lsmc_events)
@@ -256,8 +316,10 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     // The whole launch sequence: captured once per problem into a CUDA graph and replayed.
     auto enqueue = [&]() {
         launches = 0;
-        cudaMemsetAsync(coefs, 0, d * kMaxTerms * sizeof(double) + d * sizeof(int) + sizeof(int), st);
-        if (two)
+        cudaMemsetAsync(coefs, 0, ns * d * kMaxTerms * sizeof(double) + ns * d * sizeof(int) + sizeof(int), st);
+        if (batch)
+            lsmc_forward_batch<Real><<<unsigned((n + 255) / 256), 256, 0, st>>>(pb, count, s->seed, a, cash);
+        else if (two)
             lsmc_forward<Real, true><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
         else
             lsmc_forward<Real, false><<<unsigned((n + 255) / 256), 256, 0, st>>>(p, s->seed, a, b, cash);
@@ -266,7 +328,14 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
         for (int date = p.dates - 2; date >= 0; --date) {
             const double* cnext = date + 1 <= p.dates - 2 ? coefs + size_t(date + 1) * kMaxTerms : nullptr;
             const int* hnext = date + 1 <= p.dates - 2 ? have + date + 1 : nullptr;
-            if (two) {
+            if (batch) {
+                lsmc_backward_batch<Real><<<dim3(blocks, count), kLsmcThreads, 0, st>>>(pb, date, cnext, hnext, a, cash,
+                                                                                       partials);
+                reduce_partials_kernel<<<dim3(S, count), 32, 0, st>>>(partials, blocks, reduced);
+                lsmc_solve<false><<<count, kSolveThreads, 0, st>>>(reduced, 1, p.max_degree,
+                                                                   coefs + size_t(date) * kMaxTerms, have + date,
+                                                                   failed, int(d) * kMaxTerms, int(d));
+            } else if (two) {
                 lsmc_backward<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, date, cnext, hnext, a, b, cash, partials);
                 reduce_partials_kernel<<<S, 32, 0, st>>>(partials, blocks, reduced);
                 lsmc_solve<true><<<1, kSolveThreads, 0, st>>>(reduced, 1, p.max_degree, coefs + size_t(date) * kMaxTerms,
@@ -280,16 +349,21 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
             }
             launches += 3;
         }
-        if (two)
+        if (batch)
+            lsmc_final_batch<Real><<<dim3(blocks, count), kLsmcThreads, 0, st>>>(pb, coefs, have, a, cash, finals);
+        else if (two)
             lsmc_final<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
         else
             lsmc_final<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, coefs, have, a, b, cash, finals);
         ++launches;
         cudaEventRecordWithFlags(e2, st, cudaEventRecordExternal);
         if (lower) {
-            const int terms = int(d) * kMaxTerms;
+            const int terms = count * int(d) * kMaxTerms;
             coef_table_kernel<Real><<<(terms + 255) / 256, 256, 0, st>>>(coefs, table, terms);
-            if (two)
+            if (batch)
+                lsmc_lower_bound_batch<Real><<<dim3(blocks, count), kLsmcThreads, 0, st>>>(pb, fresh_seed, table,
+                                                                                          have, lp);
+            else if (two)
                 lsmc_lower_bound<Real, true><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, table, have, lp);
             else
                 lsmc_lower_bound<Real, false><<<blocks, kLsmcThreads, 0, st>>>(p, fresh_seed, table, have, lp);
@@ -297,15 +371,16 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
         }
     };
     // Key of the captured sequence: every argument its launches bake in.
-    std::vector<unsigned char> key(sizeof(p) + 64);
+    std::vector<unsigned char> key;
     {
-        unsigned char* k = key.data();
-        std::memcpy(k, &p, sizeof(p));
         const void* ptrs[] = {a, b, cash, coefs, partials, finals, lp};
-        std::memcpy(k + sizeof(p), ptrs, sizeof(ptrs));
-        const uint64_t tail[] = {s->seed, fresh_seed, uint64_t(blocks) | (uint64_t(sizeof(Real)) << 32)};
-        key.resize(sizeof(p) + sizeof(ptrs) + sizeof(tail));
-        std::memcpy(key.data() + sizeof(p) + sizeof(ptrs), tail, sizeof(tail));
+        const uint64_t tail[] = {s->seed, fresh_seed, uint64_t(blocks) | (uint64_t(sizeof(Real)) << 32),
+                                 uint64_t(count)};
+        key.resize(sizeof(LsmcParams<Real>) * ns + sizeof(ptrs) + sizeof(tail));
+        unsigned char* k = key.data();
+        std::memcpy(k, pb.p, sizeof(LsmcParams<Real>) * ns);
+        std::memcpy(k + sizeof(LsmcParams<Real>) * ns, ptrs, sizeof(ptrs));
+        std::memcpy(k + sizeof(LsmcParams<Real>) * ns + sizeof(ptrs), tail, sizeof(tail));
     }
     if (!(ctx->lsmc_exec && ctx->lsmc_key == key)) {
         cudaGraph_t graph = nullptr;
@@ -327,7 +402,7 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
         ctx->lsmc_key = ctx->lsmc_exec ? key : std::vector<unsigned char>();
     } else {
         // Replaying: count the launches the sequence holds.
-        launches = 2 * (p.dates - 1) + 2 + (lower ? 1 : 0);
+        launches = 3 * (p.dates - 1) + 2 + (lower ? 2 : 0);
     }
     cudaGetLastError();  // a refused capture or update leaves nothing behind
     cudaEventRecord(e0, st);
@@ -342,10 +417,10 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     cudaEventRecord(e3, st);
     std::vector<double> lower_partials;
     if (lower) {
-        lower_partials.resize(size_t(blocks) * 2);
+        lower_partials.resize(ns * size_t(blocks) * 2);
         cudaMemcpyAsync(lower_partials.data(), lp, lower_partials.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     }
-    std::vector<double> fin(size_t(blocks) * 2);
+    std::vector<double> fin(ns * size_t(blocks) * 2);
     int fail_flag = 0;
     cudaMemcpyAsync(fin.data(), finals, fin.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&fail_flag, failed, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -368,36 +443,42 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
     }
     ctx->last_launches = launches;
     ctx->last_kernel_ms = ms_total;
-    double s0 = 0.0, s1 = 0.0;
-    for (int blk = 0; blk < blocks; ++blk) {
-        s0 += fin[2 * blk];
-        s1 += fin[2 * blk + 1];
-    }
-    const double disc0 = std::exp(-model->rate * (expiry / s->exercise_dates));
-    const double mean = s0 / double(n);
-    const double var = n > 1 ? std::max(0.0, (s1 - s0 * mean) / double(n - 1)) : 0.0;
-    const double immediate = std::max(0.0, sign * (model->spot - strike));
-    out->price = std::max(immediate, mean * disc0);
-    out->standard_error = std::sqrt(var / double(n)) * disc0;
-    out->out_of_sample = std::nan("");
-    out->out_of_sample_error = std::nan("");
-    if (lower) {
-        double l0 = 0.0, l1 = 0.0;
+    for (int y = 0; y < count; ++y) {
+        const kgpu_model* m = models + y;
+        const double* fy = fin.data() + size_t(y) * blocks * 2;
+        double s0 = 0.0, s1 = 0.0;
         for (int blk = 0; blk < blocks; ++blk) {
-            l0 += lower_partials[2 * blk];
-            l1 += lower_partials[2 * blk + 1];
+            s0 += fy[2 * blk];
+            s1 += fy[2 * blk + 1];
         }
-        const double lm = l0 / double(n);
-        const double lv = n > 1 ? std::max(0.0, (l1 - l0 * lm) / double(n - 1)) : 0.0;
-        out->out_of_sample = std::max(immediate, lm);
-        out->out_of_sample_error = std::sqrt(lv / double(n));
-    }
-    out->wall_ms = ms_total;
-    out->path_store_ms = ms_store;
-    out->regression_ms = ms_regress;
-    if (!std::isfinite(out->price)) {
-        ctx->error = "Monte Carlo produced a non-finite parameter, path or result";
-        return KGPU_COMPUTATION_FAILURE;
+        const double disc0 = std::exp(-m->rate * (expiry / s->exercise_dates));
+        const double mean = s0 / double(n);
+        const double var = n > 1 ? std::max(0.0, (s1 - s0 * mean) / double(n - 1)) : 0.0;
+        const double immediate = std::max(0.0, sign * (m->spot - strike));
+        kgpu_lsmc_result& o = out[y];
+        o.price = std::max(immediate, mean * disc0);
+        o.standard_error = std::sqrt(var / double(n)) * disc0;
+        o.out_of_sample = std::nan("");
+        o.out_of_sample_error = std::nan("");
+        if (lower) {
+            const double* ly = lower_partials.data() + size_t(y) * blocks * 2;
+            double l0 = 0.0, l1 = 0.0;
+            for (int blk = 0; blk < blocks; ++blk) {
+                l0 += ly[2 * blk];
+                l1 += ly[2 * blk + 1];
+            }
+            const double lm = l0 / double(n);
+            const double lv = n > 1 ? std::max(0.0, (l1 - l0 * lm) / double(n - 1)) : 0.0;
+            o.out_of_sample = std::max(immediate, lm);
+            o.out_of_sample_error = std::sqrt(lv / double(n));
+        }
+        o.wall_ms = ms_total;
+        o.path_store_ms = ms_store;
+        o.regression_ms = ms_regress;
+        if (!std::isfinite(o.price)) {
+            ctx->error = "Monte Carlo produced a non-finite parameter, path or result";
+            return KGPU_COMPUTATION_FAILURE;
+        }
     }
     return KGPU_OK;
 }
@@ -407,12 +488,9 @@ static kgpu_status lsmc_run(kgpu_context* ctx, const kgpu_model* model, double s
 kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
                           const kgpu_lsmc_settings* settings, uint64_t fresh_seed, kgpu_lsmc_result* out);
 
-extern "C" kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double strike, double sign,
-                                       double expiry, const kgpu_lsmc_settings* settings, uint64_t fresh_seed,
-                                       kgpu_lsmc_result* out) {
-    if (!ctx || !model || !settings || !out) return KGPU_INVALID_INPUT;
-    std::lock_guard<std::mutex> lock(ctx->mu);
-    ctx->error.clear();
+// Checks shared by the scalar and the scenario entry points.
+static kgpu_status lsmc_check(kgpu_context* ctx, const kgpu_model* model, double strike, double sign, double expiry,
+                              const kgpu_lsmc_settings* settings) {
     auto bad = [&](const char* msg) {
         ctx->error = msg;
         return KGPU_INVALID_INPUT;
@@ -428,16 +506,55 @@ extern "C" kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* mode
         ctx->error = "GPU LSMC supports BSM and Heston";
         return KGPU_UNSUPPORTED_OPERATION;
     }
-    const bool heston = model->kind == KGPU_MODEL_HESTON;
     if (settings->basis < KGPU_BASIS_QUADRATIC || settings->basis > KGPU_BASIS_MLP_STANDALONE)
         return bad("unknown basis");
+    const bool heston = model->kind == KGPU_MODEL_HESTON;
+    if (settings->basis != KGPU_BASIS_MLP && settings->basis != KGPU_BASIS_MLP_STANDALONE &&
+        (settings->basis == KGPU_BASIS_QUADRATIC) == heston)
+        return bad("the quadratic basis prices BSM, the cubic (S/K, v) basis Heston");
+    return KGPU_OK;
+}
+
+extern "C" kgpu_status kgpu_lsmc_price(kgpu_context* ctx, const kgpu_model* model, double strike, double sign,
+                                       double expiry, const kgpu_lsmc_settings* settings, uint64_t fresh_seed,
+                                       kgpu_lsmc_result* out) {
+    if (!ctx || !model || !settings || !out) return KGPU_INVALID_INPUT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->error.clear();
+    if (const kgpu_status st = lsmc_check(ctx, model, strike, sign, expiry, settings)) return st;
     if (settings->basis == KGPU_BASIS_MLP || settings->basis == KGPU_BASIS_MLP_STANDALONE) {
         return kgpu_lsmc_mlp(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
     }
-    if ((settings->basis == KGPU_BASIS_QUADRATIC) == heston)
-        return bad("the quadratic basis prices BSM, the cubic (S/K, v) basis Heston");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
     return settings->precision == KGPU_PRECISION_FP64
-               ? kgpu::lsmc_run<double>(ctx, model, strike, sign, expiry, settings, fresh_seed, out)
-               : kgpu::lsmc_run<float>(ctx, model, strike, sign, expiry, settings, fresh_seed, out);
+               ? kgpu::lsmc_run<double>(ctx, model, 1, strike, sign, expiry, settings, fresh_seed, out)
+               : kgpu::lsmc_run<float>(ctx, model, 1, strike, sign, expiry, settings, fresh_seed, out);
+}
+
+extern "C" kgpu_status kgpu_lsmc_price_scenarios(kgpu_context* ctx, const kgpu_model* models, int32_t count,
+                                                 double strike, double sign, double expiry,
+                                                 const kgpu_lsmc_settings* settings, uint64_t fresh_seed,
+                                                 kgpu_lsmc_result* out) {
+    if (!ctx || !models || !settings || !out) return KGPU_INVALID_INPUT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->error.clear();
+    if (count < 1 || count > kgpu::kMaxLsmcScenarios) {
+        ctx->error = "an LSMC scenario batch holds 1 to 16 scenarios";
+        return KGPU_INVALID_INPUT;
+    }
+    for (int y = 0; y < count; ++y) {
+        if (const kgpu_status st = lsmc_check(ctx, models + y, strike, sign, expiry, settings)) return st;
+        if (models[y].kind != KGPU_MODEL_BSM) {
+            ctx->error = "LSMC scenario batches price Black-Scholes-Merton scenarios";
+            return KGPU_UNSUPPORTED_OPERATION;
+        }
+    }
+    if (settings->basis != KGPU_BASIS_QUADRATIC) {
+        ctx->error = "LSMC scenario batches use the quadratic basis";
+        return KGPU_UNSUPPORTED_OPERATION;
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return KGPU_DEVICE_ERROR;
+    return settings->precision == KGPU_PRECISION_FP64
+               ? kgpu::lsmc_run<double>(ctx, models, count, strike, sign, expiry, settings, fresh_seed, out)
+               : kgpu::lsmc_run<float>(ctx, models, count, strike, sign, expiry, settings, fresh_seed, out);
 }

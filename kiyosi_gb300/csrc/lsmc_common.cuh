@@ -63,6 +63,15 @@ LsmcParams<Real> make_lsmc_params(const kgpu_model* model, double strike, double
     return p;
 }
 
+// Scenarios of one batched pricing (bumped BSM contexts sharing the random numbers) and
+// their parameters, passed by value to the batch kernels; blockIdx.y selects one.
+constexpr int kMaxLsmcScenarios = 16;
+
+template <class Real>
+struct LsmcBatch {
+    LsmcParams<Real> p[kMaxLsmcScenarios];
+};
+
 constexpr int kLsmcThreads = 128;
 constexpr int kMaxTerms = 10;
 constexpr int kMaxSums = kMaxTerms * (kMaxTerms + 1) / 2 + kMaxTerms;  // upper triangle + rhs
@@ -138,8 +147,11 @@ __device__ __forceinline__ void block_sums(const Real (&acc)[S], double* partial
 // stride over the partials in a fixed order and a fixed shuffle tree adds the lanes.
 // The solve then reads one partial per sum, so these sums are its inputs bit for bit,
 // while the FP64 additions are spread over many SMs (one SM's FP64 pipe is slow).
+// A grid with blockIdx.y > 0 reduces scenario y's sums ([S][blocks] partials each).
 __global__ void __launch_bounds__(32) reduce_partials_kernel(const double* partials, int blocks, double* sums) {
     const int j = blockIdx.x, lane = threadIdx.x;
+    partials += size_t(blockIdx.y) * gridDim.x * blocks;
+    sums += size_t(blockIdx.y) * gridDim.x;
     double v = 0.0;
     for (int base = lane; base < blocks; base += 8 * 32) {
         double chunk[8];
@@ -163,11 +175,16 @@ __global__ void __launch_bounds__(32) reduce_partials_kernel(const double* parti
 // count); 512 threads leave the elimination its 128 registers.
 constexpr int kSolveThreads = 512;
 
+// A grid of several CTAs solves one system per scenario: CTA y reads its partials at
+// y S blocks and writes its coefficients at y coef_stride, its flag at y have_stride.
 template <bool TWO>
 __global__ void __launch_bounds__(kSolveThreads) lsmc_solve(const double* partials, int blocks, int max_degree, double* coef, int* have,
-                           int* failed) {
+                           int* failed, int coef_stride = 0, int have_stride = 0) {
     constexpr int T = TWO ? 10 : 3;
     constexpr int S = sum_count(T);
+    partials += size_t(blockIdx.x) * S * blocks;
+    coef += size_t(blockIdx.x) * coef_stride;
+    have += size_t(blockIdx.x) * have_stride;
     __shared__ double sums[S];
     // Each warp owns the sums j = warp + 16 q.  Lanes stride over the block partials of
     // a sum in a fixed order, then a fixed shuffle tree adds the lanes (deterministic).
@@ -323,6 +340,29 @@ __global__ void __launch_bounds__(256) lsmc_forward(LsmcParams<Real> p, uint64_t
         a[size_t(k) * p.paths + i] = x;
     }
     cash[i] = intrinsic(p, spot_at_date<Real, TWO>(p, p.dates - 1, x));
+}
+
+// Forward pass of a BSM scenario batch: the store holds the cumulative Brownian
+// coordinate, which every scenario shares (its spot, rate, dividend and volatility enter
+// only through spot_at_date), so it is written once; each scenario gets its own terminal
+// cash ([scenario][path]).  The draws and the store are those of lsmc_forward.
+template <class Real>
+__global__ void __launch_bounds__(256) lsmc_forward_batch(const __grid_constant__ LsmcBatch<Real> batch, int count,
+                                                          uint64_t seed, Real* a, Real* cash) {
+    const LsmcParams<Real>& p0 = batch.p[0];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p0.paths) return;
+    PcgSource<Real> n;
+    n.start(seed, uint64_t(i), p0.dates);
+    Real x = Real(0);
+    for (int k = 0; k < p0.dates; ++k) {
+        x += n.normal();
+        a[size_t(k) * p0.paths + i] = x;
+    }
+    for (int y = 0; y < count; ++y) {
+        const LsmcParams<Real> p = batch.p[y];
+        cash[size_t(y) * p.paths + i] = intrinsic(p, spot_at_date<Real, false>(p, p.dates - 1, x));
+    }
 }
 
 }  // namespace

@@ -6,6 +6,7 @@ reference): `step_count` exercise intervals, the quadratic basis under BSM, the 
 """
 import ctypes as C
 import math
+from dataclasses import replace
 
 from . import abi
 from ._native import context
@@ -38,9 +39,28 @@ def lsmc_settings(engine, model, basis=None, substeps=None, fresh_seed=None, see
     return s
 
 
-def price_american(engine, option, ctx, fresh_seed=None):
+def _no_early_exercise(option, model) -> bool:
+    """A call under BSM with no dividend yield and a nonnegative rate is never exercised
+    early: its American price is the European one (american.rs:1047-1070)."""
+    return (option.sign > 0.0 and isinstance(model, BlackScholesMertonParameters)
+            and model.dividend <= 0.0 and model.rate >= 0.0)
+
+
+def _european_shortcut(engine, option, ctx, seed):
+    """The American price of a call that is never exercised early: the engine's European
+    price of the same terms with the same seed, floored at the immediate payoff."""
+    from .instruments import EuropeanOption
+    est = engine.replace(seed=seed).price_with_statistics(EuropeanOption(option.option_type, option.strike, option.expiry), ctx)
+    immediate = max(option.sign * (ctx.spot - option.strike), 0.0)
+    return replace(est, price=max(immediate, est.price))
+
+
+def price_american(engine, option, ctx, fresh_seed=None, shortcut=True):
     """MonteCarloEstimate of an American option (the in-sample LSMC price).  With
-    `fresh_seed`, the out-of-sample lower bound is returned as well."""
+    `fresh_seed`, the out-of-sample lower bound is returned as well.  `shortcut` prices
+    calls that are never exercised early as European options, as the reference's
+    scalar price does; the rate Greeks of a call whose stencil crosses that boundary
+    keep the exercise-grid estimator on both sides (american.rs:1606-1656)."""
     from .pricing import MonteCarloEstimate, _resolve_seed
     if engine.sampling != "pseudo_random":
         raise InvalidInputError("GPU LSMC samples pseudo-random paths")
@@ -53,6 +73,8 @@ def price_american(engine, option, ctx, fresh_seed=None):
         return MonteCarloEstimate(max(option.sign * (ctx.spot - option.strike), 0.0), None,
                                   "insufficient_observations", None)
     seed = _resolve_seed(engine.seed)
+    if shortcut and fresh_seed is None and _no_early_exercise(option, model):
+        return _european_shortcut(engine, option, ctx, seed)
     s = lsmc_settings(engine, model, seed=seed)
     native = context(engine.device)
     out = abi.LsmcResult()
@@ -76,3 +98,96 @@ def price_american_out_of_sample(engine, option, ctx, fresh_seed):
     engine's paths, applied forward to fresh paths drawn with `fresh_seed`."""
     est, (lower, lower_se) = price_american(engine, option, ctx, fresh_seed=fresh_seed)
     return lower, lower_se
+
+
+# Default spot bump of the American Greeks: 8% of spot (american.rs:555-557).
+AMERICAN_SPOT_SHIFT = 0.08
+
+
+def price_american_scenarios(engine, option, contexts, seed, shortcut=True):
+    """Prices of one American option in BSM `contexts` with one seed: the LSMC
+    scenarios go through kgpu_lsmc_price_scenarios, 16 per call, sharing the paths
+    (each equals its scalar kgpu_lsmc_price bit for bit); calls that are never exercised
+    early are priced as European options when `shortcut` is set."""
+    out = [None] * len(contexts)
+    lsmc = []
+    for i, c in enumerate(contexts):
+        if shortcut and _no_early_exercise(option, c.model):
+            out[i] = _european_shortcut(engine, option, c, seed).price
+        else:
+            lsmc.append(i)
+    if lsmc:
+        s = lsmc_settings(engine, contexts[lsmc[0]].model, seed=seed)
+        native = context(engine.device)
+        for first in range(0, len(lsmc), 16):
+            chunk = lsmc[first:first + 16]
+            models = (abi.Model * len(chunk))(*[contexts[i].kgpu_model() for i in chunk])
+            results = (abi.LsmcResult * len(chunk))()
+            native.check(native.lib.kgpu_lsmc_price_scenarios(
+                native.handle, models, len(chunk), option.strike, option.sign, option.expiry, C.byref(s),
+                seed, results))
+            for i, r in zip(chunk, results):
+                out[i] = r.price
+    return out
+
+
+def american_greeks(engine, option, ctx, request, shifts=None):
+    """Numerical Greeks of an American option under BSM (price_with_greeks_with_settings,
+    american.rs:1487-1687): the reference's stencils and formulas with its 8%-of-spot
+    default spot bump, every bumped context priced on the same seed and paths in
+    batched LSMC scenario calls (greek_prices / american_spots, american.rs:820-946).
+    For a call, rho and dividend rho whose rate stencil crosses the no-early-exercise
+    boundary use the exercise-grid estimator on both sides (american.rs:1606-1656).
+    Time Greeks report `unsupported`, as for the other engines."""
+    from . import greeks as G
+    from .errors import ComputationFailureError, UnsupportedOperationError
+    from .pricing import _resolve_seed
+    request = G._check_request(request)
+    shifts = shifts or G.NumericalShiftSettings()
+    shifts.validate()
+    model = ctx.model
+    if not isinstance(model, BlackScholesMertonParameters):
+        raise UnsupportedOperationError("numerical Greeks need Black-Scholes-Merton parameters")
+    if option.expiry > 0.0 and shifts.spot_shift is None:
+        shifts = G.NumericalShiftSettings(AMERICAN_SPOT_SHIFT * ctx.spot, shifts.volatility_shift,
+                                          shifts.rate_shift)
+    seed = _resolve_seed(engine.seed)
+    discontinuity = G.vanilla_discontinuity(option, ctx)
+    base = (ctx.spot, model.volatility, model.rate, model.dividend)
+    needed = [base]
+
+    def record(key):
+        if key not in needed:
+            needed.append(key)
+        return 0.0
+
+    G._stencils(ctx, option.expiry, request, shifts, discontinuity, record, 0.0)
+    if option.expiry == 0.0:
+        prices = [max(option.sign * (k[0] - option.strike), 0.0) for k in needed]
+    else:
+        prices = price_american_scenarios(engine, option, [G.scenario_context(k) for k in needed], seed)
+    table = dict(zip(needed, prices))
+    result = G._stencils(ctx, option.expiry, request, shifts, discontinuity, table.__getitem__, table[base])
+    if option.expiry > 0.0 and option.sign > 0.0:
+        spot, vol, rate, dividend = base
+        for greek, value, can_switch in (("rho", rate, dividend <= 0.0), ("dividend_rho", dividend, rate >= 0.0)):
+            if greek not in request or not can_switch:
+                continue
+            h = G.symmetric_shift(value, shifts.rate_shift)
+            if not (h > 0.0 and math.isfinite(2.0 * h)):
+                continue
+            lo, hi = value - h, value + h
+            crosses = (lo < 0.0 <= hi) if greek == "rho" else (lo <= 0.0 < hi)
+            if not crosses:
+                continue
+            keys = ([(spot, vol, hi, dividend), (spot, vol, lo, dividend)] if greek == "rho"
+                    else [(spot, vol, rate, hi), (spot, vol, rate, lo)])
+            up, down = price_american_scenarios(engine, option, [G.scenario_context(k) for k in keys], seed,
+                                                shortcut=False)
+            result.greeks[greek] = (up - down) / (2.0 * h)
+            result.status.pop(greek, None)
+    for g, value in result.greeks.items():
+        if not math.isfinite(value):
+            raise ComputationFailureError(f"non-finite {g}")
+    result.seed = seed
+    return result

@@ -261,11 +261,13 @@ class MonteCarloVanillaEngine(_MonteCarloEngine):
         return self._run(ctx, [self._plan(option, ctx)])[0]
 
     def price_with_greeks(self, option, ctx: PricingContext, request, shifts=None):
-        """European Greeks by bump-and-reprice with a pinned seed, every scenario in one
-        launch (monte_carlo.rs:1334-1409, european_greek_prices).  American options are
-        not supported."""
+        """Greeks by bump-and-reprice with a pinned seed: European options with every
+        scenario in one launch (monte_carlo.rs:1334-1409, european_greek_prices),
+        American options with the bumped contexts in batched LSMC scenario calls
+        (american.rs:820-946, 1487-1687)."""
         if isinstance(option, AmericanOption):
-            raise UnsupportedOperationError("American Monte Carlo Greeks are not built")
+            from .lsmc import american_greeks
+            return american_greeks(self, option, ctx, request, shifts)
         from .greeks import numerical_greeks
         return numerical_greeks(self, option, ctx, request, shifts)
 
