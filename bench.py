@@ -780,13 +780,15 @@ def run_lsmc(args):
     tparams = (rng.uniform(-0.3, 0.3, abi.MLP_PARAMS)).astype(np.float32)
     fp = C.POINTER(C.c_float)
     trainer = {}
-    for steps in (8, 1008):
-        q = tparams.copy()
-        t0 = time.perf_counter()
-        native.check(native.lib.kgpu_mlp_train(native.handle, q.ctypes.data_as(fp), tsamples.ctypes.data_as(fp),
-                                               len(tsamples), 8192, steps, 1e-3))
-        trainer[steps] = time.perf_counter() - t0
-    us_per_step = (trainer[1008] - trainer[8]) / 1000 * 1e6
+    for kind in (abi.TRAINER_CLUSTER, abi.TRAINER_GRID):
+        for steps in (8, 1008):
+            q = tparams.copy()
+            t0 = time.perf_counter()
+            native.check(native.lib.kgpu_mlp_train(native.handle, q.ctypes.data_as(fp),
+                                                   tsamples.ctypes.data_as(fp), len(tsamples), 8192, steps,
+                                                   1e-3, kind))
+            trainer[kind, steps] = time.perf_counter() - t0
+    us_per_step = {k: (trainer[k, 1008] - trainer[k, 8]) / 1000 * 1e6 for k in (abi.TRAINER_CLUSTER, abi.TRAINER_GRID)}
     line = {
         "metric": "LSMC |price - ADI| at equal wall time: polynomial + fitted network vs polynomial",
         "value": abs(mlp_eq["error_vs_adi"]), "unit": "price units",
@@ -801,7 +803,9 @@ def run_lsmc(args):
                           "network_alone": alone},
         "parity": {"oracle": oracle_parity},
         "at_equal_wall_time": {"poly3_plus_network": mlp_eq, "network_alone": alone_eq, "poly3": equal},
-        "trainer": {"us_per_adam_step": us_per_step, "batch": 8192, "network": "3-64-64-1",
+        "trainer": {"us_per_adam_step": us_per_step[abi.TRAINER_CLUSTER],
+                    "us_per_adam_step_grid_barrier_trainer": us_per_step[abi.TRAINER_GRID],
+                    "batch": 8192, "network": "3-64-64-1",
                     "timing": "host clock around kgpu_mlp_train, 1008 minus 8 steps"},
         "poly3_by_paths": polys,
     }

@@ -489,14 +489,20 @@ kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book
 kgpu_status kgpu_mlp_gradients(kgpu_context* ctx, const float* params, const float* samples, int32_t count,
                                float* grads, double* loss);
 
+/* Trainers of the continuation network: 8-CTA thread-block clusters that keep the
+ * network, the Adam state and the gradient sums on chip (what the network LSMC uses
+ * where the device can co-schedule them), or one cooperative launch with two grid
+ * barriers per step (the fallback). */
+enum { KGPU_TRAINER_CLUSTER = 0, KGPU_TRAINER_GRID = 1 };
+
 /* `steps` Adam steps (Kingma and Ba; beta1 0.9, beta2 0.999, eps 1e-8, zero initial
- * moments) of the same tensor-core training kernel on `samples` (count x 4 floats, as for
+ * moments) of the tensor-core trainer `trainer` on `samples` (count x 4 floats, as for
  * kgpu_mlp_gradients), minibatch b being samples [b * batch, ...) cycled in order;
  * `params` (KGPU_MLP_PARAMS floats) is updated in place.  No counterpart in the
  * reference: exposed so the optimiser can be checked against a CPU restatement.  batch
- * <= 8192. */
+ * <= 8192; KGPU_UNSUPPORTED_OPERATION when the device cannot run that trainer. */
 kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const float* samples, int32_t count, int32_t batch,
-                           int32_t steps, double learning_rate);
+                           int32_t steps, double learning_rate, int32_t trainer);
 
 /* Instrumentation of the last call on `ctx`: device time from the first to the last
  * kernel of the call (CUDA events on the context's stream) and the number of kernel

@@ -74,6 +74,8 @@ BASIS_QUADRATIC = 0
 BASIS_POLY3 = 1
 BASIS_MLP = 2
 BASIS_MLP_STANDALONE = 3
+TRAINER_CLUSTER = 0
+TRAINER_GRID = 1
 
 _D = C.c_double
 _I = C.c_int32
@@ -232,7 +234,7 @@ def declare(lib):
     lib.kgpu_abi_version.restype = _I
     lib.kgpu_device_count.argtypes = []
     lib.kgpu_device_count.restype = _I
-    lib.kgpu_mlp_train.argtypes = [V, C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _I, _I, _D]
+    lib.kgpu_mlp_train.argtypes = [V, C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _I, _I, _D, _I]
     lib.kgpu_mlp_train.restype = _I
     lib.kgpu_pipe_rates.argtypes = [V, C.POINTER(_D), _I]
     lib.kgpu_pipe_rates.restype = _I

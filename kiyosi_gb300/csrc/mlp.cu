@@ -12,11 +12,11 @@
 // place of the polynomial.
 //
 // Training runs on the fifth-generation tensor cores: one CTA holds 128 samples; the
-// 64 x 64 layer's forward product, the backward product through it and its weight
-// gradient are tcgen05 MMAs (BF16 operands in shared memory, FP32 accumulators in
-// tensor memory); the 3 -> 64 and 64 -> 1 layers, the activations and the reductions run
-// on the CUDA cores in FP32.  Per-CTA gradient partials are summed in a fixed order by
-// the Adam kernel, so training is deterministic.
+// 64 x 64 layer's forward product, the backward product through it and every gradient's
+// sum over the samples (W2 and b2; W1 and b1; w3) are tcgen05 MMAs (BF16 operands in
+// shared memory, FP32 accumulators in tensor memory); the 3 -> 64 and 64 -> 1 layers'
+// forward values and the activations run on the CUDA cores in FP32.  Per-CTA gradient
+// partials are summed in a fixed order before Adam, so training is deterministic.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -32,6 +32,8 @@
 #include "lsmc_common.cuh"
 #include "tcgen05.cuh"
 
+#include <cooperative_groups.h>
+
 namespace kgpu {
 namespace {
 
@@ -44,18 +46,34 @@ constexpr int kParams = 4481;
 constexpr int kStride = 4484;  // per-CTA partial: kParams gradients, then the loss sum; also the
                                // 16-byte-aligned stride of every parameter-sized region
 constexpr int kLossSlot = 4481;
-constexpr uint32_t kTmemColumns = 256;  // [0,64) Z2, [64,128) dH1, [128,192) dW2
+// Tensor memory: [0,64) Z2, [64,128) dH1, [128,208) dW2 and db2, [256,272) the small
+// gradients (dW1, db1 in lanes 0..63; dW3 in lanes 64..127).
+constexpr uint32_t kTmemColumns = 512;
+constexpr uint32_t kColZ2 = 0, kColDH1 = 64, kColDW2 = 128, kColSmall = 256;
+constexpr int kH1Rows = kHidden + 16;  // H1^T, a row of ones (db2) and 15 zero rows: N = 80
 
+// Every sum over a tile's rows is a tensor-core product with the rows as K:
+//   [dW2 | db2]  = dZ2^T (outputs, padded to M = 128) . [H1 | 1]       (N = 80)
+//   [dW1 | db1]  = dZ1^T . [x0 x1 x2 1]   and   dW3 = relu(Z2)^T . dout,
+// the last two as one product: A stacks dZ1^T (units 0..63) on relu(Z2)^T (64..127), B
+// holds the rows' x0, x1, x2, 1 and dout (N = 16).  BF16 operands, FP32 sums.
 struct __align__(1024) TrainSmem {
     __nv_bfloat16 h1[kRows * kHidden];       // A of the forward product: rows x inputs
-    __nv_bfloat16 h1t[kHidden * kRows];      // B of the weight gradient: inputs x rows
+    __nv_bfloat16 h1t[kH1Rows * kRows];      // B of [dW2 | db2]: inputs, ones, zeros x rows
     __nv_bfloat16 dz2[kRows * kHidden];      // A of the backward product: rows x outputs
-    __nv_bfloat16 dz2t[kRows * kRows];       // A of the weight gradient: outputs (64 + 64 zero) x rows
+    __nv_bfloat16 dz2t[kRows * kRows];       // A of [dW2 | db2]: outputs (64 + 64 zero) x rows
+    __nv_bfloat16 gt[kRows * kRows];         // A of the small gradients: dZ1^T, relu(Z2)^T x rows
+    __nv_bfloat16 xe[16 * kRows];            // B of the small gradients: x0, x1, x2, 1, dout, zeros x rows
     __nv_bfloat16 w2f[kHidden * kHidden];    // B forward: outputs x inputs
     __nv_bfloat16 w2b[kHidden * kHidden];    // B backward: inputs x outputs
-    float w1[3 * kHidden], b1[kHidden], b2[kHidden], w3[kHidden];
-    float red[8][128];   // per-warp partial sums of half_sum
-    float tot[2][128];   // per-half totals of half_sum
+    float4 l1[kHidden];  // layer 1 of unit j: W1[j][0..2], b1[j] (one 16-byte load)
+    float b2[kHidden], w3[kHidden];
+    float b3;
+    // The clustered trainer's gradient sums of this CTA and its published parameters,
+    // both in slot order (see slot_of).
+    alignas(16) float acc[kStride];
+    alignas(16) float pub[kStride];
+    float red[16];       // per-warp sums of db3 and of the squared residuals
     float xch[256];      // output halves exchanged between the two threads of a row
     uint64_t bar;
     uint32_t tmem;
@@ -66,28 +84,9 @@ constexpr size_t kTrainSmemBytes = sizeof(TrainSmem) + 1024;
 
 __device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-// Sums N values across the warp: on return v[0 .. N/32) hold the warp totals of indices
-// (N/32) * lane + i.
-template <int N>
-__device__ __forceinline__ void warp_transpose_sum(float* v, int lane) {
-    int n = N;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        const bool upper = (lane & o) != 0;
-        n >>= 1;
-#pragma unroll
-        for (int i = 0; i < N / 2; ++i) {
-            if (i < n) {
-                const float send = upper ? v[i] : v[i + n];
-                const float keep = upper ? v[i + n] : v[i];
-                v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-            }
-        }
-    }
-}
-
-// Prepares a training CTA: tensor memory, the completion barrier and the zero rows of
-// the weight-gradient operand (rows 64..127 of dz2t stay zero across steps).
+// Prepares a training CTA: tensor memory, the completion barrier and the constant rows
+// of the gradient operands (rows 64..127 of dz2t, rows 64..79 of h1t, rows 5..15 of xe;
+// they stay unchanged across steps).
 __device__ __forceinline__ void train_setup(TrainSmem& s) {
     const int t = threadIdx.x;
     if ((t >> 5) == 0) {
@@ -98,8 +97,13 @@ __device__ __forceinline__ void train_setup(TrainSmem& s) {
         tc::mbar_init(&s.bar, 1);
         s.failed = 0;
     }
-    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f);
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f), one = __float2bfloat16_rn(1.0f);
     for (int i = t; i < kHidden * kRows; i += kThreadsTrain) s.dz2t[kHidden * kRows + i] = zero;
+    for (int i = t; i < 16 * kRows; i += kThreadsTrain) {
+        const int r = kHidden + i / kRows, c = i % kRows;
+        s.h1t[tc::kmajor(r, c, kRows)] = r == kHidden ? one : zero;
+        if (i / kRows >= 5) s.xe[tc::kmajor(i / kRows, c, kRows)] = zero;
+    }
 }
 
 __device__ __forceinline__ void train_release(TrainSmem& s) {
@@ -108,22 +112,22 @@ __device__ __forceinline__ void train_release(TrainSmem& s) {
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(s.tmem, kTmemColumns);
 }
 
-// Reduces, over the CTA's 128 rows, per-thread vectors of N values that belong to the
-// thread's column half: on return red[h][k] (h = half, k < N) holds the total of index k.
-// Threads t and t + 128 own the same row; the two halves are reduced separately.
-template <int N>
-__device__ __forceinline__ void half_sum(TrainSmem& s, float* v) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    warp_transpose_sum<N>(v, lane);
-#pragma unroll
-    for (int i = 0; i < N / 32; ++i) s.red[warp][(N / 32) * lane + i] = v[i];
-    __syncthreads();
-    for (int q = threadIdx.x; q < 2 * N; q += kThreadsTrain) {
-        const int h = q / N, k = q % N, w0 = 4 * h;
-        s.tot[h][k] = ((s.red[w0][k] + s.red[w0 + 1][k]) + s.red[w0 + 2][k]) + s.red[w0 + 3][k];
-    }
-    __syncthreads();
+// Slot order of the clustered trainer's gradient sums and parameters: W2 transposed
+// (slot in * 64 + o for W2[o][in]; a warp's 32 output units are 32 consecutive slots),
+// then W1, b1, b2, w3, b3 (slots 4096..4480), the loss (4481) and two unused slots.
+__host__ __device__ constexpr int slot_of(int param) {
+    return param >= kPW2 && param < kPB2 ? ((param - kPW2) & 63) * kHidden + ((param - kPW2) >> 6)
+           : param < kPW2               ? kHidden * kHidden + param
+                                        : kHidden * kHidden + kPW2 + (param - kPB2);
 }
+__host__ __device__ constexpr int param_of_slot(int slot) {
+    return slot < kHidden * kHidden ? kPW2 + (slot & 63) * kHidden + (slot >> 6)
+           : slot < kHidden * kHidden + kPW2 ? slot - kHidden * kHidden
+           : slot < kHidden * kHidden + kPW2 + (kParams - kPB2) ? kPB2 + slot - kHidden * kHidden - kPW2
+                                                                 : -1;
+}
+static_assert(slot_of(kPB3) == 4480 && param_of_slot(4480) == kPB3 && param_of_slot(slot_of(kPW2 + 70)) == kPW2 + 70,
+              "slot order");
 
 // One batch's gradient partial of this CTA: it covers samples
 // [first + 128 blockIdx.x, first + 128 blockIdx.x + 128) of the batch [first, first + count)
@@ -133,20 +137,28 @@ __device__ __forceinline__ void half_sum(TrainSmem& s, float* v) {
 // same tensor-memory lanes, one column half each.  `phase` is the completion barrier's
 // next parity (two completions per step).  Returns false, on every thread, when a
 // tensor-core wait gave up.
+template <bool kLocal>
 __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const uint4* __restrict__ w2_tiles,
                           const float4* __restrict__ samples, int first, int count, float inv_count,
                           float* __restrict__ partial, int pstride, uint32_t& phase) {
     const int t = threadIdx.x, warp = t >> 5;
     const int row = t & (kRows - 1), half = t >> 7, j0 = 32 * half;
+    // A gradient value: to the partial (parameter order, stride pstride), or with kLocal
+    // to this CTA's sums in shared memory (slot order).
+    auto put = [&](int param, float value) {
+        if (kLocal) s.acc[slot_of(param)] = value;
+        else partial[size_t(param) * pstride] = value;
+    };
+    if (!kLocal) {
     // Parameters are read past L1 (ld.global.cg): the persistent trainer rewrites them
     // from other SMs between steps.
-    for (int i = t; i < 3 * kHidden; i += kThreadsTrain) s.w1[i] = __ldcg(params + kPW1 + i);
     if (t < kHidden) {
-        s.b1[t] = __ldcg(params + kPB1 + t);
+        s.l1[t] = make_float4(__ldcg(params + kPW1 + 3 * t), __ldcg(params + kPW1 + 3 * t + 1),
+                              __ldcg(params + kPW1 + 3 * t + 2), __ldcg(params + kPB1 + t));
         s.b2[t] = __ldcg(params + kPB2 + t);
         s.w3[t] = __ldcg(params + kPW3 + t);
     }
-    const float b3 = __ldcg(params + kPB3);
+    s.b3 = __ldcg(params + kPB3);
     if (w2_tiles) {
         // Both BF16 operand tiles of W2, already in shared-memory order (16 KB).
         uint4* dst = reinterpret_cast<uint4*>(s.w2f);  // w2f and w2b are contiguous
@@ -159,6 +171,7 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
             s.w2b[tc::kmajor(in, o, kHidden)] = w;
         }
     }
+    }  // the clustered trainer keeps the network in shared memory
     const int local = blockIdx.x * kRows + row;
     const bool valid = local < count;
     const float4 x = valid ? samples[first + local] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -173,12 +186,20 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             const int j = j0 + 8 * g + u;
-            const float z = fmaf(s.w1[3 * j], x.x, fmaf(s.w1[3 * j + 1], x.y, fmaf(s.w1[3 * j + 2], x.z, s.b1[j])));
+            const float4 w = s.l1[j];
+            const float z = fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, w.w)));
             if (z > 0.f) mask1 |= 1u << (8 * g + u);
             pack[u] = __float2bfloat16_rn(valid && z > 0.f ? z : 0.f);
             s.h1t[tc::kmajor(j, row, kRows)] = pack[u];
         }
         *reinterpret_cast<uint4*>(&s.h1[tc::kmajor(row, j0 + 8 * g, kHidden)]) = *reinterpret_cast<const uint4*>(pack);
+    }
+    // The row's inputs of the small gradients (zero past the batch).
+    if (half == 0) {
+        s.xe[tc::kmajor(0, row, kRows)] = __float2bfloat16_rn(x.x);
+        s.xe[tc::kmajor(1, row, kRows)] = __float2bfloat16_rn(x.y);
+        s.xe[tc::kmajor(2, row, kRows)] = __float2bfloat16_rn(x.z);
+        s.xe[tc::kmajor(3, row, kRows)] = __float2bfloat16_rn(valid ? 1.0f : 0.0f);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -189,8 +210,8 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
     if (t == 0) {
         const uint32_t a0 = tc::smem_u32(s.h1), b0 = tc::smem_u32(s.w2f);
         for (int k = 0; k < kHidden / 16; ++k)
-            tc::mma_bf16(tmem, tc::smem_desc(a0 + 256 * k, 128, kHidden * 16), tc::smem_desc(b0 + 256 * k, 128, kHidden * 16),
-                         idesc, k > 0);
+            tc::mma_bf16(tmem + kColZ2, tc::smem_desc(a0 + 256 * k, 128, kHidden * 16),
+                         tc::smem_desc(b0 + 256 * k, 128, kHidden * 16), idesc, k > 0);
         tc::mma_commit(&s.bar);
     }
     bool ok = tc::mbar_wait(&s.bar, phase);
@@ -200,7 +221,7 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
     // Z2 of this row's 32 units (TMEM lane = row).
     const uint32_t lane_base = uint32_t((warp & 3) * 32) << 16;
     float z2[32];
-    tc::tmem_load32(tmem + lane_base + j0, z2);
+    tc::tmem_load32(tmem + lane_base + kColZ2 + j0, z2);
     float out = 0.f;
 #pragma unroll
     for (int u = 0; u < 32; ++u) {
@@ -210,11 +231,10 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
     // The output needs both halves: exchange through shared memory.
     s.xch[t] = out;
     __syncthreads();
-    out = (b3 + s.xch[row]) + s.xch[row + kRows];
+    out = (s.b3 + s.xch[row]) + s.xch[row + kRows];
     const float res = valid ? out - x.w : 0.f;
     const float dout = 2.f * res * inv_count;
-    // dW3 and db2 contributions of this row (64 values), and dZ2 in both operand layouts.
-    float v[64];
+    // dZ2 in both operand layouts, relu(Z2)^T, and dout.
 #pragma unroll
     for (int g = 0; g < 4; ++g) {
         __align__(16) __nv_bfloat16 pack[8];
@@ -222,35 +242,28 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
         for (int u = 0; u < 8; ++u) {
             const int k = 8 * g + u, j = j0 + k;
             const bool on = z2[k] > 0.f;
-            const float gz = on ? dout * s.w3[j] : 0.f;
-            v[k] = dout * (on ? z2[k] : 0.f);
-            v[32 + k] = gz;
-            pack[u] = __float2bfloat16_rn(gz);
+            pack[u] = __float2bfloat16_rn(on ? dout * s.w3[j] : 0.f);
             s.dz2t[tc::kmajor(j, row, kRows)] = pack[u];
+            s.gt[tc::kmajor(kHidden + j, row, kRows)] = __float2bfloat16_rn(on ? z2[k] : 0.f);
         }
         *reinterpret_cast<uint4*>(&s.dz2[tc::kmajor(row, j0 + 8 * g, kHidden)]) = *reinterpret_cast<const uint4*>(pack);
     }
+    if (half == 0) s.xe[tc::kmajor(4, row, kRows)] = __float2bfloat16_rn(dout);
     tc::fence_async_smem();
     tc::fence_before_sync();
-    half_sum<64>(s, v);  // contains __syncthreads
+    __syncthreads();
     tc::fence_after_sync();
     if (t == 0) {
         const uint32_t ad = tc::smem_u32(s.dz2), bw = tc::smem_u32(s.w2b);
         for (int k = 0; k < kHidden / 16; ++k)
-            tc::mma_bf16(tmem + 64, tc::smem_desc(ad + 256 * k, 128, kHidden * 16),
+            tc::mma_bf16(tmem + kColDH1, tc::smem_desc(ad + 256 * k, 128, kHidden * 16),
                          tc::smem_desc(bw + 256 * k, 128, kHidden * 16), idesc, k > 0);
         const uint32_t at = tc::smem_u32(s.dz2t), bh = tc::smem_u32(s.h1t);
+        const uint32_t idesc80 = tc::idesc_bf16(kRows, kH1Rows);
         for (int k = 0; k < kRows / 16; ++k)
-            tc::mma_bf16(tmem + 128, tc::smem_desc(at + 256 * k, 128, kRows * 16),
-                         tc::smem_desc(bh + 256 * k, 128, kRows * 16), idesc, k > 0);
+            tc::mma_bf16(tmem + kColDW2, tc::smem_desc(at + 256 * k, 128, kRows * 16),
+                         tc::smem_desc(bh + 256 * k, 128, kRows * 16), idesc80, k > 0);
         tc::mma_commit(&s.bar);
-    }
-    float* part = partial;
-    if (t < 2 * kHidden) {
-        // totals: [h][0..31] dW3 of units 32 h + k, [h][32..63] db2
-        const int h = t >> 6, k = t & 63;
-        const int unit = 32 * h + (k & 31);
-        part[size_t((k < 32 ? kPW3 : kPB2) + unit) * pstride] = s.tot[h][k];
     }
     // db3 and the loss: half 0 holds one copy of every row.
     float d3 = half == 0 ? dout : 0.f, l2 = half == 0 ? res * res : 0.f;
@@ -259,50 +272,79 @@ __device__ bool grad_step(TrainSmem& s, const float* __restrict__ params, const 
         l2 += __shfl_xor_sync(0xffffffffu, l2, o);
     }
     if ((t & 31) == 0 && half == 0) {
-        s.red[0][64 + warp] = d3;
-        s.red[0][96 + warp] = l2;
-    }
-    __syncthreads();
-    if (t == 0) {
-        part[size_t(kPB3) * pstride] = ((s.red[0][64] + s.red[0][65]) + s.red[0][66]) + s.red[0][67];
-        part[size_t(kLossSlot) * pstride] = ((s.red[0][96] + s.red[0][97]) + s.red[0][98]) + s.red[0][99];
+        s.red[warp] = d3;
+        s.red[8 + warp] = l2;
     }
     ok = tc::mbar_wait(&s.bar, phase);
     phase ^= 1u;
     if (__syncthreads_or(!ok)) return false;
     tc::fence_after_sync();
-    // dH1 -> dZ1 -> dW1, db1: 4 x 32 values per thread.
-    float dh1[32];
-    tc::tmem_load32(tmem + lane_base + 64 + j0, dh1);
-    float w[128];
+    if (t == 0) {
+        put(kPB3, ((s.red[0] + s.red[1]) + s.red[2]) + s.red[3]);
+        if (kLocal) s.acc[kLossSlot] = ((s.red[8] + s.red[9]) + s.red[10]) + s.red[11];
+        else partial[size_t(kLossSlot) * pstride] = ((s.red[8] + s.red[9]) + s.red[10]) + s.red[11];
+    }
+    // dZ1^T (rows 0..63 of the small gradients' A operand).
+    {
+        float dh1[32];
+        tc::tmem_load32(tmem + lane_base + kColDH1 + j0, dh1);
 #pragma unroll
-    for (int k = 0; k < 32; ++k) {
-        const float g = ((mask1 >> k) & 1u) ? dh1[k] : 0.f;
-        w[k] = g * x.x;
-        w[32 + k] = g * x.y;
-        w[64 + k] = g * x.z;
-        w[96 + k] = g;
+        for (int k = 0; k < 32; ++k)
+            s.gt[tc::kmajor(j0 + k, row, kRows)] = __float2bfloat16_rn(((mask1 >> k) & 1u) ? dh1[k] : 0.f);
     }
-    half_sum<128>(s, w);
-    for (int q = t; q < 256; q += kThreadsTrain) {
-        // totals: [h][c * 32 + k]: c = 0..2 column c of W1 (row-major [64][3]), c = 3 b1
-        const int h = q >> 7, k = q & 127, c = k >> 5, unit = 32 * h + (k & 31);
-        const int idx = c < 3 ? kPW1 + 3 * unit + c : kPB1 + unit;
-        part[size_t(idx) * pstride] = s.tot[h][k];
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (t == 0) {
+        const uint32_t ag = tc::smem_u32(s.gt), bx = tc::smem_u32(s.xe);
+        const uint32_t idesc16 = tc::idesc_bf16(kRows, 16);
+        for (int k = 0; k < kRows / 16; ++k)
+            tc::mma_bf16(tmem + kColSmall, tc::smem_desc(ag + 256 * k, 128, kRows * 16),
+                         tc::smem_desc(bx + 256 * k, 128, kRows * 16), idesc16, k > 0);
+        tc::mma_commit(&s.bar);
     }
-    // dW2: TMEM lanes 0..63 hold rows = output units; warps 0, 1 (inputs 0..31) and 4, 5
-    // (inputs 32..63) read them.
+    // dW2 and db2 while the tensor cores run: TMEM lanes 0..63 hold rows = output units;
+    // warps 0, 1 (inputs 0..31, and db2) and 4, 5 (inputs 32..63) read them.
     if ((warp & 3) < 2) {
-        float g2[32];
-        tc::tmem_load32(tmem + lane_base + 128 + j0, g2);
         const int unit = row;  // output unit
-        if (pstride == 1) {
-            float4* dst = reinterpret_cast<float4*>(part + kPW2 + unit * kHidden + j0);
+        float g2[32];
+        tc::tmem_load32(tmem + lane_base + kColDW2 + j0, g2);
+        if (kLocal) {
+            // Slot (j0 + q) * 64 + unit: consecutive lanes, consecutive words.
+#pragma unroll
+            for (int q = 0; q < 32; ++q) s.acc[(j0 + q) * kHidden + unit] = g2[q];
+        } else if (pstride == 1) {
+            float4* dst = reinterpret_cast<float4*>(partial + kPW2 + unit * kHidden + j0);
 #pragma unroll
             for (int q = 0; q < 8; ++q) dst[q] = make_float4(g2[4 * q], g2[4 * q + 1], g2[4 * q + 2], g2[4 * q + 3]);
         } else {
 #pragma unroll
-            for (int q = 0; q < 32; ++q) part[size_t(kPW2 + unit * kHidden + j0 + q) * pstride] = g2[q];
+            for (int q = 0; q < 32; ++q) partial[size_t(kPW2 + unit * kHidden + j0 + q) * pstride] = g2[q];
+        }
+        if (half == 0) {
+            float b[4];
+            tc::tmem_load4(tmem + lane_base + kColDW2 + kHidden, b);
+            put(kPB2 + unit, b[0]);
+        }
+    }
+    ok = tc::mbar_wait(&s.bar, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) return false;
+    tc::fence_after_sync();
+    if (warp < 4) {
+        float gv[4];
+        if (warp < 2) {
+            // dW1 (columns 0..2) and db1 (column 3) of units 0..63.
+            tc::tmem_load4(tmem + lane_base + kColSmall, gv);
+            const int unit = 32 * warp + (t & 31);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) put(kPW1 + 3 * unit + c, gv[c]);
+            put(kPB1 + unit, gv[3]);
+        } else {
+            // dW3 (column 4) of units 0..63, in lanes 64..127.
+            tc::tmem_load4(tmem + lane_base + kColSmall + 4, gv);
+            put(kPW3 + 32 * (warp - 2) + (t & 31), gv[0]);
         }
     }
     return true;
@@ -317,7 +359,7 @@ __global__ void __launch_bounds__(kThreadsTrain, 1) mlp_grad_kernel(const float*
     TrainSmem& s = *reinterpret_cast<TrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     train_setup(s);
     uint32_t phase = 0;
-    if (!grad_step(s, params, nullptr, samples, first, count, inv_count, partials + size_t(blockIdx.x) * kStride, 1,
+    if (!grad_step<false>(s, params, nullptr, samples, first, count, inv_count, partials + size_t(blockIdx.x) * kStride, 1,
                    phase) &&
         threadIdx.x == 0)
         atomicExch(error, 1);
@@ -414,7 +456,7 @@ __global__ void __launch_bounds__(kThreadsTrain, 1) mlp_train_kernel(TrainArgs a
     for (int step = 0; ok && step < a.steps; ++step) {
         const int first = (step % per_epoch) * a.batch;
         const int count = min(a.batch, a.itm - first);
-        if (!grad_step(s, a.params, reinterpret_cast<const uint4*>(a.w2_tiles), a.samples, first, count,
+        if (!grad_step<false>(s, a.params, reinterpret_cast<const uint4*>(a.w2_tiles), a.samples, first, count,
                        1.0f / float(count), a.partials + blockIdx.x, int(ctas), phase)) {
             if (threadIdx.x == 0) atomicExch(a.error, 1);
             break;
@@ -468,6 +510,225 @@ __global__ void __launch_bounds__(kThreadsTrain, 1) mlp_train_kernel(TrainArgs a
         __threadfence();
         ok = grid_barrier(a.barrier, ctas, a.error);
     }
+    train_release(s);
+}
+
+// ---------------------------------------------------------------------------------
+// The clustered trainer: the cooperative trainer's 64 CTAs (one 128-sample tile each)
+// as 8 thread-block clusters of 8, with the network, the Adam state and the gradient
+// sums kept on chip.  Each step:
+//   1. every CTA computes its tile's gradient sums into shared memory (slot order);
+//   2. cluster barrier; CTA r of a cluster adds the sums of its slice of the slots over
+//      the cluster's CTAs in rank order (distributed shared memory) and publishes the
+//      cluster's slice to global memory with a flag (step number, release);
+//   3. it waits (bounded) for the same slice's flags of the other clusters, adds the
+//      8 cluster sums in cluster order and applies Adam to the slice: every cluster
+//      computes the same update, and each slot's value and moments stay in the
+//      registers of its owning thread;
+//   4. cluster barrier; every CTA pulls the whole updated network from the 8 owners
+//      of its cluster (16-byte distributed-shared-memory loads) into its copy.
+// So a step has two cluster barriers and one point-to-point exchange per slice, no
+// grid barrier, and no global traffic but the samples and the 8 x 4484 slice sums.
+// The slice sums are double-buffered by step parity: a cluster can run at most one
+// step ahead of the slowest, which has read the older buffer by then.
+// Every CTA runs the same steps and barriers whatever happens: a tensor-core wait or a
+// flag wait that gives up stops the dependent work and raises the error flag.
+constexpr int kClusterCtas = 8;
+constexpr int kSliceSlots = ((kStride + kClusterCtas - 1) / kClusterCtas + 3) & ~3;  // 564
+
+struct ClusterTrainArgs {
+    float* params;    // parameter order; read at the start, written at the end
+    float* m;
+    float* v;
+    const float4* samples;
+    float* exchange;  // [2][clusters][kStride] cluster sums of each slice
+    int* flags;       // [clusters][kClusterCtas]: last step whose slice sums are published
+    int* error;
+    int itm, batch, steps, first_step;
+    float lr, beta1, beta2, eps;
+};
+
+__device__ __forceinline__ uint32_t cluster_address(uint32_t local, int rank) {
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(local), "r"(rank));
+    return out;
+}
+__device__ __forceinline__ float4 dsmem_load4(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ void flag_release(int* flag, int value) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(flag), "r"(value) : "memory");
+}
+__device__ __forceinline__ int flag_acquire(const int* flag) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+    return v;
+}
+
+// Writes a slot's value into this CTA's copy of the network.
+__device__ __forceinline__ void set_slot(TrainSmem& s, int slot, float w) {
+    if (slot < kHidden * kHidden) {
+        const int in = slot >> 6, o = slot & 63;
+        const __nv_bfloat16 b = __float2bfloat16_rn(w);
+        s.w2f[tc::kmajor(o, in, kHidden)] = b;
+        s.w2b[tc::kmajor(in, o, kHidden)] = b;
+        return;
+    }
+    const int p = param_of_slot(slot);
+    if (p < 0) return;
+    if (p < kPB1) reinterpret_cast<float*>(&s.l1[(p - kPW1) / 3])[(p - kPW1) % 3] = w;
+    else if (p < kPW2) s.l1[p - kPB1].w = w;
+    else if (p < kPW3) s.b2[p - kPB2] = w;
+    else if (p < kPB3) s.w3[p - kPW3] = w;
+    else s.b3 = w;
+}
+
+__global__ void __launch_bounds__(kThreadsTrain, 1) mlp_train_cluster_kernel(ClusterTrainArgs a) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ unsigned char smem_raw[];
+    TrainSmem& s = *reinterpret_cast<TrainSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    train_setup(s);
+    const int t = threadIdx.x;
+    const int rank = int(cluster.block_rank());
+    const int clusters = int(gridDim.x) / kClusterCtas, me = int(blockIdx.x) / kClusterCtas;
+    for (int slot = t; slot < kStride; slot += kThreadsTrain) {
+        const int p = param_of_slot(slot);
+        if (p >= 0) set_slot(s, slot, a.params[p]);
+    }
+    // The four slots this thread owns: value and Adam moments in registers.
+    const int s0 = rank * kSliceSlots + 4 * t;
+    const bool owner = 4 * t < kSliceSlots && s0 < kStride;
+    float master[4], mom1[4], mom2[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int p = owner ? param_of_slot(s0 + c) : -1;
+        master[c] = p >= 0 ? a.params[p] : 0.f;
+        mom1[c] = p >= 0 ? a.m[p] : 0.f;
+        mom2[c] = p >= 0 ? a.v[p] : 0.f;
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const int per_epoch = (a.itm + a.batch - 1) / a.batch;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int step = 0; step < a.steps; ++step) {
+        const int first = (step % per_epoch) * a.batch;
+        const int count = min(a.batch, a.itm - first);
+        if (ok)
+            ok = grad_step<true>(s, nullptr, nullptr, a.samples, first, count, 1.0f / float(count), nullptr, 0, phase);
+        tc::fence_before_sync();
+        cluster.sync();
+        tc::fence_after_sync();
+        float* ex = a.exchange + size_t(step & 1) * clusters * kStride;
+        if (owner) {
+            const uint32_t local = tc::smem_u32(&s.acc[s0]);
+            float4 sum = dsmem_load4(cluster_address(local, 0));
+#pragma unroll
+            for (int q = 1; q < kClusterCtas; ++q) {
+                const float4 v = dsmem_load4(cluster_address(local, q));
+                sum.x += v.x;
+                sum.y += v.y;
+                sum.z += v.z;
+                sum.w += v.w;
+            }
+            *reinterpret_cast<float4*>(ex + size_t(me) * kStride + s0) = sum;
+        }
+        __syncthreads();
+        // Publish this slice, then wait for the other clusters' (lane c of warp 0 polls
+        // cluster c's flag, all at once).
+        if (t == 0) {
+            __threadfence();
+            flag_release(a.flags + me * kClusterCtas + rank, step);
+        }
+        bool arrived = true;
+        if (t < 32) {
+            __syncwarp();
+            if (t < clusters && t != me) {
+                const long long start = clock64();
+                while (flag_acquire(a.flags + t * kClusterCtas + rank) < step) {
+                    if (clock64() - start > 2000000000LL) {
+                        arrived = false;
+                        break;
+                    }
+                }
+            }
+        }
+        ok = !__syncthreads_or(!arrived) && ok;
+        const float tstep = float(a.first_step + step + 1);
+        const float bias1 = 1.0f - powf(a.beta1, tstep), bias2 = 1.0f - powf(a.beta2, tstep);
+        if (owner) {
+            // The 8 clusters' sums, loaded together, added in cluster order.
+            float4 part[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                part[c] = c < clusters ? __ldcg(reinterpret_cast<const float4*>(ex + size_t(c) * kStride + s0))
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 g = part[0];
+#pragma unroll
+            for (int c = 1; c < 8; ++c) {
+                if (c >= clusters) break;
+                g.x += part[c].x;
+                g.y += part[c].y;
+                g.z += part[c].z;
+                g.w += part[c].w;
+            }
+            const float gs[4] = {g.x, g.y, g.z, g.w};
+            float w[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                mom1[c] = a.beta1 * mom1[c] + (1.f - a.beta1) * gs[c];
+                mom2[c] = a.beta2 * mom2[c] + (1.f - a.beta2) * gs[c] * gs[c];
+                w[c] = master[c] - a.lr * (mom1[c] / bias1) / (sqrtf(mom2[c] / bias2) + a.eps);
+                master[c] = w[c];
+            }
+            *reinterpret_cast<float4*>(&s.pub[s0]) = make_float4(w[0], w[1], w[2], w[3]);
+        }
+        cluster.sync();
+        // Pull the updated network from the cluster's owners (all loads in flight first).
+        constexpr int kPulls = (kStride / 4 + kThreadsTrain - 1) / kThreadsTrain;
+        float4 pulled[kPulls];
+#pragma unroll
+        for (int u = 0; u < kPulls; ++u) {
+            const int slot = 4 * (t + kThreadsTrain * u);
+            pulled[u] = slot < kStride
+                            ? dsmem_load4(cluster_address(tc::smem_u32(&s.pub[slot]), slot / kSliceSlots))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kPulls; ++u) {
+            const int slot = 4 * (t + kThreadsTrain * u);
+            if (slot < kStride) {
+                set_slot(s, slot, pulled[u].x);
+                set_slot(s, slot + 1, pulled[u].y);
+                set_slot(s, slot + 2, pulled[u].z);
+                set_slot(s, slot + 3, pulled[u].w);
+            }
+        }
+        tc::fence_async_smem();
+        __syncthreads();
+    }
+    if (me == 0 && owner) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int p = param_of_slot(s0 + c);
+            if (p >= 0) {
+                a.params[p] = master[c];
+                a.m[p] = mom1[c];
+                a.v[p] = mom2[c];
+            }
+        }
+    }
+    if (t == 0 && !ok) atomicExch(a.error, 1);
+    // The last pulls read the owners' shared memory: no CTA leaves before they are done.
+    cluster.sync();
     train_release(s);
 }
 
@@ -1032,6 +1293,69 @@ struct Adam {
     int step = 0;
 };
 
+// The clustered trainer: whether `ctas` CTAs (a multiple of kClusterCtas) fit at once;
+// it stays off once a launch of it has been refused.
+bool cluster_trainer_off = false;
+
+bool cluster_trainer_fits(int ctas) {
+    static int max_clusters = -1;
+    if (max_clusters < 0) {
+        max_clusters = 0;
+        if (cudaFuncSetAttribute(mlp_train_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(kTrainSmemBytes)) == cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = kClusterCtas;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(kClusterCtas);
+            cfg.blockDim = dim3(kThreadsTrain);
+            cfg.dynamicSmemBytes = kTrainSmemBytes;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int n = 0;
+            if (cudaOccupancyMaxActiveClusters(&n, mlp_train_cluster_kernel, &cfg) == cudaSuccess) max_clusters = n;
+        }
+        cudaGetLastError();
+    }
+    return !cluster_trainer_off && ctas % kClusterCtas == 0 && ctas <= 64 && ctas / kClusterCtas <= max_clusters;
+}
+
+// CTAs of the clustered trainer for a batch: one per 128 samples, rounded up to whole
+// clusters.
+int cluster_trainer_ctas(int batch) {
+    return ((batch + kRows - 1) / kRows + kClusterCtas - 1) / kClusterCtas * kClusterCtas;
+}
+
+// Launches it (a cooperative launch of 8-CTA clusters: every CTA resident).  Resets the
+// exchange flags first.  A refused launch turns it off and returns the error cleared.
+cudaError_t launch_cluster_trainer(cudaStream_t st, int ctas, const ClusterTrainArgs& ca, bool& launched) {
+    launched = false;
+    if (cudaMemsetAsync(ca.flags, 0xFF, size_t(ctas) * sizeof(int), st) != cudaSuccess) return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeCooperative;
+    attr[1].val.cooperative = 1;
+    cfg.gridDim = dim3(unsigned(ctas));
+    cfg.blockDim = dim3(kThreadsTrain);
+    cfg.dynamicSmemBytes = kTrainSmemBytes;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+    if (cudaLaunchKernelEx(&cfg, mlp_train_cluster_kernel, ca) != cudaSuccess) {
+        cudaGetLastError();
+        cluster_trainer_off = true;
+        return cudaSuccess;
+    }
+    launched = true;
+    return cudaSuccess;
+}
+
 // One optimiser step on samples [first, first + count).
 cudaError_t train_step(cudaStream_t st, float* params, float* m, float* v, Adam& adam, const float4* samples, int first,
                        int count, float* partials, int* error) {
@@ -1073,7 +1397,8 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     // The path store; afterwards it holds the fresh paths' state (10 floats per path).
     const size_t store_bytes = std::max(n * d * (TWO ? 2 : 1), 10 * n) * sizeof(float);
     const size_t net_bytes = size_t(kParams) * sizeof(float);
-    const size_t misc_floats = (size_t(3) + d) * kStride + size_t(max_train_blocks) * kStride + 2 * kHidden * kHidden;
+    const size_t misc_floats = (size_t(3) + d) * kStride + size_t(max_train_blocks) * kStride + 2 * kHidden * kHidden +
+                               size_t(2) * 8 * kStride + 64;
     if (ctx->lsmc_store.ensure(store_bytes) || ctx->lsmc_cash.ensure(n * sizeof(float)) ||
         ctx->mlp_scratch.ensure(n * (sizeof(float4) + sizeof(int) + sizeof(float)) +
                                 size_t(pblocks) * (sizeof(BlockStats) + sizeof(int)) + d * sizeof(TargetNorm) + 256) ||
@@ -1107,6 +1432,9 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
     float* nets = v + kStride;
     float* partials = nets + d * kStride;
     __nv_bfloat16* w2_tiles = reinterpret_cast<__nv_bfloat16*>(partials + size_t(max_train_blocks) * kStride);
+    float* exchange = reinterpret_cast<float*>(w2_tiles + 2 * kHidden * kHidden);  // clustered trainer
+    int* flags = reinterpret_cast<int*>(exchange + size_t(2) * 8 * kStride);
+    const int cluster_ctas = cluster_trainer_ctas(batch);
     double* finals = static_cast<double*>(ctx->lsmc_misc.ptr);
     double* lower_partials = finals + 2 * fblocks;
     double* coefs = static_cast<double*>(ctx->lsmc_coef.ptr);
@@ -1197,7 +1525,16 @@ kgpu_status mlp_run(kgpu_context* ctx, const kgpu_model* model, double strike, d
             // as long; later dates start from the previous date's network.
             const int date_epochs = adam.step == 0 ? 4 * epochs : epochs;
             const int steps = date_epochs * ((itm + batch - 1) / batch);
-            if (cooperative) {
+            bool clustered = false;
+            if (cluster_trainer_fits(cluster_ctas)) {
+                ClusterTrainArgs ca{params, m, v, samples, exchange, flags, error, itm, batch, steps,
+                                    adam.step, adam.lr, adam.beta1, adam.beta2, adam.eps};
+                MLP_TRY(launch_cluster_trainer(st, cluster_ctas, ca, clustered));
+            }
+            if (clustered) {
+                adam.step += steps;
+                launches += 1;
+            } else if (cooperative) {
                 TrainArgs ta{params, w2_tiles, m, v, samples, partials, barrier, error, itm, batch, steps,
                              adam.step, adam.lr, adam.beta1, adam.beta2, adam.eps};
                 void* args[] = {&ta};
@@ -1337,9 +1674,10 @@ kgpu_status kgpu_lsmc_mlp(kgpu_context* ctx, const kgpu_model* model, double str
 }
 
 extern "C" kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const float* samples, int32_t count,
-                                      int32_t batch, int32_t steps, double learning_rate) {
+                                      int32_t batch, int32_t steps, double learning_rate, int32_t trainer) {
     using namespace kgpu;
-    if (!ctx || !params || !samples || count < 1 || batch < 1 || steps < 1 || !(learning_rate > 0.0))
+    if (!ctx || !params || !samples || count < 1 || batch < 1 || steps < 1 || !(learning_rate > 0.0) ||
+        (trainer != KGPU_TRAINER_CLUSTER && trainer != KGPU_TRAINER_GRID))
         return KGPU_INVALID_INPUT;
     if (batch > 64 * kRows) {
         ctx->error = "the training batch is at most 8192 samples";
@@ -1353,13 +1691,16 @@ extern "C" kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const fl
         return KGPU_DEVICE_ERROR;
     }
     const int blocks = (std::min(batch, count) + kRows - 1) / kRows;
-    if (!cooperative_fits(ctx->device, blocks)) {
+    const int cluster_ctas = cluster_trainer_ctas(std::min(batch, count));
+    if (trainer == KGPU_TRAINER_CLUSTER ? !cluster_trainer_fits(cluster_ctas) : !cooperative_fits(ctx->device, blocks)) {
         ctx->error = "the training kernel's CTAs do not fit the device at once";
         return KGPU_UNSUPPORTED_OPERATION;
     }
     // Parameters, Adam moments, gradient partials ([parameter][CTA]), W2 tiles, the
-    // samples, the error word and the grid barrier.
-    const size_t floats = size_t(3) * kStride + size_t(blocks) * kStride + 2 * kHidden * kHidden;
+    // clustered trainer's slice sums and flags, the samples, the error word and the grid
+    // barrier.
+    const size_t floats = size_t(3) * kStride + size_t(blocks) * kStride + 2 * kHidden * kHidden +
+                          size_t(2) * 8 * kStride + 64;
     const size_t bytes = floats * 4 + size_t(count) * 16 + 64;
     if (ctx->mlp_scratch.ensure(bytes)) return KGPU_DEVICE_ERROR;
     float* dparams = static_cast<float*>(ctx->mlp_scratch.ptr);
@@ -1367,7 +1708,9 @@ extern "C" kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const fl
     float* dv = dm + kStride;
     float* dpartials = dv + kStride;
     __nv_bfloat16* w2_tiles = reinterpret_cast<__nv_bfloat16*>(dpartials + size_t(blocks) * kStride);
-    float4* dsamples = reinterpret_cast<float4*>(w2_tiles + 2 * kHidden * kHidden);
+    float* exchange = reinterpret_cast<float*>(w2_tiles + 2 * kHidden * kHidden);
+    int* flags = reinterpret_cast<int*>(exchange + size_t(2) * 8 * kStride);
+    float4* dsamples = reinterpret_cast<float4*>(flags + 64);
     int* derror = reinterpret_cast<int*>(dsamples + count);
     GridBarrier* barrier = reinterpret_cast<GridBarrier*>(derror + 2);
     cudaStream_t st = ctx->stream;
@@ -1381,8 +1724,19 @@ extern "C" kgpu_status kgpu_mlp_train(kgpu_context* ctx, float* params, const fl
                  0, float(learning_rate), adam.beta1, adam.beta2, adam.eps};
     void* args[] = {&ta};
     int failed = 0;
-    if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel), dim3(blocks), dim3(kThreadsTrain),
-                                    args, kTrainSmemBytes, st) != cudaSuccess ||
+    bool clustered = false;
+    if (trainer == KGPU_TRAINER_CLUSTER) {
+        ClusterTrainArgs ca{dparams, dm, dv, dsamples, exchange, flags, derror, count, batch, steps,
+                            0, float(learning_rate), adam.beta1, adam.beta2, adam.eps};
+        if (launch_cluster_trainer(st, cluster_ctas, ca, clustered) != cudaSuccess) return KGPU_DEVICE_ERROR;
+        if (!clustered) {
+            ctx->error = "the device refused the clustered trainer's cooperative cluster launch";
+            return KGPU_UNSUPPORTED_OPERATION;
+        }
+    }
+    ctx->last_launches = 1;
+    if ((!clustered && cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(mlp_train_kernel), dim3(blocks),
+                                                   dim3(kThreadsTrain), args, kTrainSmemBytes, st) != cudaSuccess) ||
         cudaMemcpyAsync(params, dparams, size_t(kParams) * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(&failed, derror, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) {

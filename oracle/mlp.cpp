@@ -7,8 +7,10 @@
 // (row = output unit), b2[64], w3[64], b3.  The loss is mean((f(x) - y)^2) over the
 // batch.  With `bf16` set, the operands the GPU hands to its tensor cores are rounded
 // to bfloat16 (round to nearest even) exactly where the GPU rounds them: the first
-// hidden layer's activations, W2 and the second layer's pre-activation gradients; the
-// rest is evaluated in double.  With `bf16` clear the whole computation is in double.
+// hidden layer's activations, W2, the second layer's pre-activation gradients (in dW2,
+// db2 and dH1), the first layer's pre-activation gradients and the inputs (in dW1 and
+// db1), and the second layer's activations and the output gradient (in dW3); the rest
+// is evaluated in double.  With `bf16` clear the whole computation is in double.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -65,10 +67,10 @@ extern "C" double kor_mlp_gradients(const float* params, const float* samples, i
         grads[PB3] += dout;
         for (int o = 0; o < H; ++o) {
             const bool on = z2[o] > 0.0;
-            grads[PW3 + o] += dout * (on ? z2[o] : 0.0);
+            grads[PW3 + o] += round(dout) * round(on ? z2[o] : 0.0);
             const double g = on ? dout * params[PW3 + o] : 0.0;
-            grads[PB2 + o] += g;
             dz2[o] = round(g);
+            grads[PB2 + o] += dz2[o];
         }
         for (int o = 0; o < H; ++o)
             for (int i = 0; i < H; ++i) grads[PW2 + o * H + i] += dz2[o] * h1[i];
@@ -76,9 +78,10 @@ extern "C" double kor_mlp_gradients(const float* params, const float* samples, i
             if (!((mask1 >> i) & 1ull)) continue;
             double dh = 0.0;
             for (int o = 0; o < H; ++o) dh += dz2[o] * w2[o * H + i];
-            grads[PW1 + 3 * i] += dh * x[0];
-            grads[PW1 + 3 * i + 1] += dh * x[1];
-            grads[PW1 + 3 * i + 2] += dh * x[2];
+            dh = round(dh);
+            grads[PW1 + 3 * i] += dh * round(x[0]);
+            grads[PW1 + 3 * i + 1] += dh * round(x[1]);
+            grads[PW1 + 3 * i + 2] += dh * round(x[2]);
             grads[PB1 + i] += dh;
         }
     }

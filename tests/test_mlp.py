@@ -83,10 +83,12 @@ def test_oracle_adam_first_step_and_descent():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("count,batch,steps", [(1000, 1000, 1), (3000, 1024, 12)])
-def test_tensor_core_adam_matches_oracle(native, count, batch, steps):
-    """kgpu_mlp_train (the cooperative tensor-core trainer: gradients, partial sums and
-    Adam in one launch) against the oracle's float32 Adam on the oracle's gradients.  One
+@pytest.mark.parametrize("trainer", ["cluster", "grid"])
+@pytest.mark.parametrize("count,batch,steps", [(1000, 1000, 1), (3000, 1024, 12), (20000, 8192, 6)])
+def test_tensor_core_adam_matches_oracle(native, count, batch, steps, trainer):
+    """kgpu_mlp_train (both tensor-core trainers: the clustered one, with its on-chip
+    network and slice exchange, and the grid-barrier one) against the oracle's float32
+    Adam on the oracle's gradients.  One
     step moves each parameter by the learning rate against the gradient's sign, so the
     parameters agree to rounding wherever the gradient is not negligible; over twelve
     steps the ratio m / sqrt(v) amplifies the 1e-3 relative gradient differences only for
@@ -97,7 +99,7 @@ def test_tensor_core_adam_matches_oracle(native, count, batch, steps):
     got = p.copy()
     native.check(native.lib.kgpu_mlp_train(
         native.handle, got.ctypes.data_as(C.POINTER(C.c_float)), x.ctypes.data_as(C.POINTER(C.c_float)),
-        count, batch, steps, lr))
+        count, batch, steps, lr, abi.TRAINER_CLUSTER if trainer == "cluster" else abi.TRAINER_GRID))
     ref = loader.mlp_adam(p, x, batch, steps, lr)
     diff = np.abs(got - ref)
     assert np.max(diff) <= lr * steps, np.max(diff)
