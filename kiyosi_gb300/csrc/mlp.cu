@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(kThreadsTrain, 1) mlp_train_cluster_kernel(Clu
             flag_release(a.flags + me * kClusterCtas + rank, step);
         }
         bool arrived = true;
-        if (t < 32) {
+        if (t < 32 && ok) {
             __syncwarp();
             if (t < clusters && t != me) {
                 const long long start = clock64();
