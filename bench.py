@@ -401,6 +401,22 @@ def run_kernel_only(args):
     """Device-resident pricings of one arm only, for ncu captures of the kernels."""
     from kiyosi_gb300 import _native, abi
     native = _native.context(0)
+    if args.kernel_only == "mlp-train-grid":
+        # The grid-barrier trainer alone: 40 Adam steps of batch 8192 over 65,536
+        # synthetic samples per call.
+        rng = np.random.default_rng(5)
+        x = rng.normal(size=(65536, 4)).astype(np.float32)
+        x[:, 3] = np.abs(x[:, 3]) * 0.1
+        p0 = rng.uniform(-0.3, 0.3, abi.MLP_PARAMS).astype(np.float32)
+        fp = C.POINTER(C.c_float)
+        for _ in range(args.warmup + args.steps):
+            q = p0.copy()
+            t0 = time.perf_counter()
+            native.check(native.lib.kgpu_mlp_train(native.handle, q.ctypes.data_as(fp), x.ctypes.data_as(fp),
+                                                   len(x), 8192, 40, 1e-3, abi.TRAINER_GRID))
+        print(json.dumps({"arm": "mlp-train-grid", "steps_per_call": 40,
+                          "us_per_step_host": (time.perf_counter() - t0) / 40 * 1e6}))
+        return
     if args.kernel_only.startswith("lsmc"):
         from kiyosi_gb300 import workloads
         ctx = workloads.heston_context()
@@ -864,7 +880,8 @@ def main():
                     help="LSMC network: in-the-money samples trained on per date (0: all)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the kernel's default launch shape instead of the autotuner's")
-    ap.add_argument("--kernel-only", choices=["fp32", "fp32-lanes", "fp64", "lsmc-poly", "lsmc-mlp", "shared-grid"],
+    ap.add_argument("--kernel-only", choices=["fp32", "fp32-lanes", "fp64", "lsmc-poly", "lsmc-mlp", "shared-grid",
+                                              "mlp-train-grid"],
                     help="run only the device-resident pricing of one arm (for profilers)")
     ap.add_argument("--tile", type=int, default=0, help="persistent tile paths (0 = default)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")

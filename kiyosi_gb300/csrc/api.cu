@@ -368,12 +368,18 @@ bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 // Samples per persistent work item.  FP64 Sobol items are one reference block (they
 // share the block's high part in shared memory); FP32 Sobol items may be any divisor
 // of 256 (every lane reads its own block's row of the high table).
-int64_t persistent_tile(bool sobol, int requested, int precision) {
+int64_t persistent_tile(bool sobol, int requested, int precision, int64_t book_samples, int sm_count) {
     if (sobol) {
         if (precision == KGPU_PRECISION_FP64) return 256;
         return (requested > 0 && requested <= 256 && 256 % requested == 0) ? requested : 64;
     }
-    return requested > 0 ? requested : 1024;
+    if (requested > 0) return requested;
+    // 1024-path items, halved (down to one path per lane) while the book has fewer than
+    // 16 items per SM: in large items a small book would leave most SMs idle and every
+    // lane walking many paths in turn.
+    int64_t tile = 1024;
+    while (tile > 32 && book_samples < tile * 16 * int64_t(sm_count)) tile >>= 1;
+    return tile;
 }
 
 }  // namespace
@@ -737,8 +743,10 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
     // Work items grouped by contract, in contract order.  Sobol tiles are one reference
     // block (they share the block's high gray-code bits).
     std::vector<int4> items;
+    int64_t book_samples = 0;
+    for (int i = 0; i < n; ++i) book_samples += k.info[i].samples;
     for (int i = 0; i < n; ++i) {
-        int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision);
+        int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision, book_samples, ctx->sm_count);
         for (int64_t b = 0; b < k.info[i].samples; b += tile)
             items.push_back(make_int4(i, int(b), int(std::min<int64_t>(tile, k.info[i].samples - b)), k.info[i].dims));
     }
@@ -754,7 +762,7 @@ kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
         int q = 0;
         for (int i = 0; i < n; ++i) {
             first_item[i] = q;
-            const int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision);
+            const int64_t tile = persistent_tile(k.sobol, s.tile_paths, s.precision, book_samples, ctx->sm_count);
             q += int((k.info[i].samples + tile - 1) / tile);
         }
         first_item[n] = q;
