@@ -350,11 +350,11 @@ __device__ __forceinline__ bool phase_grid_sync(int* arrive, volatile int* gener
 
 // Runs paths of a list to completion, a CTA batch of kThreads paths at a time.  After
 // every interval the batch's live paths are compacted to the front of the CTA through
-// shared memory, so its warps stay full while the batch thins out.  Completing the
-// monitoring list (drain false), a path that knocks in moves to the knocked-in pool.
+// shared memory, so its warps stay full while the batch thins out.  A path that knocks
+// in moves to the knocked-in pool.
 template <class Real, bool SOBOL>
 __device__ void phase_complete(const PhaseArgs<Real, SOBOL>& a, const PhaseEntry<Real, SOBOL>* list, int64_t count,
-                               int first_phase, bool drain, PhaseEntry<Real, SOBOL>* pool, int* warp_live) {
+                               int first_phase, PhaseEntry<Real, SOBOL>* pool, int* warp_live) {
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned below = lanemask_lt();
@@ -396,16 +396,45 @@ __device__ void phase_complete(const PhaseArgs<Real, SOBOL>& a, const PhaseEntry
                 phase_count(a.executed, L.contract, executed, lane);
                 alive = L.valid && !finished;
                 ++phase;
-                if (!drain) {
-                    const bool to_pool = alive && !L.monitoring;
-                    phase_append(a.knocked, knocked_count, to_pool, phase_entry<Real, SOBOL>(L, phase, pn), lane,
-                                 below);
-                    alive = alive && !to_pool;
-                }
+                const bool to_pool = alive && !L.monitoring;
+                phase_append(a.knocked, knocked_count, to_pool, phase_entry<Real, SOBOL>(L, phase, pn), lane, below);
+                alive = alive && !to_pool;
             } else {
                 alive = false;
             }
         }
+    }
+}
+
+// Runs the knocked-in pool to completion.  A knocked-in path only draws its interval
+// ends, so the warp keeps its 32 paths to the end with no compaction: lanes whose path
+// finished idle while the others take their remaining intervals (at most the contract's
+// interval count).
+template <class Real, bool SOBOL>
+__device__ void phase_drain(const PhaseArgs<Real, SOBOL>& a, int64_t count) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = int64_t(gridDim.x) * kWarps;
+    for (int64_t ch = (int64_t(blockIdx.x) * kThreads + threadIdx.x) / 32; ch * 32 < count; ch += warps) {
+        const int64_t idx = ch * 32 + lane;
+        PhaseLane<Real> L;
+        PcgSource<Real> pn;
+        L.valid = idx < count;
+        L.sample = 0;
+        L.contract = 0;
+        L.monitoring = L.knocked_in = false;
+        L.lr = L.cash = Real(0);
+        int phase = 0;
+        if (L.valid) phase = phase_load<Real, SOBOL>(a, a.knocked, idx, L, pn);
+        bool alive = L.valid;
+        int executed = 0;
+        while (__any_sync(kFull, alive)) {
+            L.valid = alive;
+            const bool finished = phase_interval<Real, SOBOL>(a, phase, L, pn, executed);
+            alive = alive && !finished;
+            ++phase;
+        }
+        phase_count(a.executed, L.contract, executed, lane);
     }
 }
 
@@ -461,9 +490,9 @@ __global__ void __launch_bounds__(kThreads, 4) phased_kernel(PhaseArgs<Real, SOB
         count = *(volatile int*)(a.counts + phase);
     }
     phase_complete<Real, SOBOL>(a, phase == 0 ? nullptr : a.lists + size_t(phase % 2) * a.total, count, phase,
-                                false, pool, warp_live);
+                                pool, warp_live);
     if (!phase_grid_sync(arrive, generation, failed)) return;
-    phase_complete<Real, SOBOL>(a, a.knocked, *(volatile int*)knocked_count, 0, true, pool, warp_live);
+    phase_drain<Real, SOBOL>(a, *(volatile int*)knocked_count);
 }
 
 // The high part of every reference block, dimension-major: out[d * blocks + b] is the
