@@ -43,9 +43,9 @@ SEED = 42
 # per launch.  The kernel is neither HBM- nor tensor-bound; its roofline is the op model
 # of kiyosi_gb300/roofline_ops.json against the measured pipe rates, with the SM issue
 # rate (4 warp-instructions per cycle per SM) beside it.
-PHASED_WARP_INST = 146560264
+PHASED_WARP_INST = 140338724
 PHASED_POSITIONS = 41683020
-PHASED_DRAM_BYTES = 4308224
+PHASED_DRAM_BYTES = 4312576
 PHASED_CAPTURE_PATHS = 1 << 19
 
 
