@@ -21,6 +21,20 @@ def _sign(option_type: str) -> float:
     return 1.0 if option_type == CALL else -1.0
 
 
+_SHARED_TIMES: dict = {}
+
+
+def _shared_times(times: tuple) -> tuple:
+    """One tuple object per distinct monitoring schedule, so that the notes of a book that
+    share a schedule share the object (host planners key their caches on it)."""
+    shared = _SHARED_TIMES.get(times)
+    if shared is None:
+        if len(_SHARED_TIMES) >= 4096:
+            _SHARED_TIMES.clear()
+        shared = _SHARED_TIMES[times] = times
+    return shared
+
+
 def _times(values: Sequence[float], expiry: float, name: str, start: float = 0.0) -> List[float]:
     out = [float(v) for v in values]
     if any(not math.isfinite(v) for v in out):
@@ -217,6 +231,14 @@ class Observation:
     coupon_barrier_level: Optional[float] = None
     coupon_rate: float = 0.0
 
+    def __hash__(self):
+        # The field hash, computed once: planners key their caches on observations.
+        h = self.__dict__.get("_hash")
+        if h is None:
+            h = hash((self.time, self.knock_out_level, self.coupon_barrier_level, self.coupon_rate))
+            object.__setattr__(self, "_hash", h)
+        return h
+
 
 BARRIER_STATES = (None, "no_event", "knocked_in", "knocked_out")
 
@@ -271,8 +293,8 @@ class AutocallableNote:
         _times([o.time for o in obs], self.expiry, "observations", self.effective_time)
         if self.knock_in_times is not None:
             object.__setattr__(self, "knock_in_times",
-                               tuple(_times(self.knock_in_times, self.expiry, "knock_in_times",
-                                            self.effective_time)))
+                               _shared_times(tuple(_times(self.knock_in_times, self.expiry, "knock_in_times",
+                                                          self.effective_time))))
         if not self.initial_spot > 0.0:
             raise InvalidInputError("initial spot must be positive")
         if self.upper_strike == 0.0:

@@ -665,7 +665,9 @@ def _event_grid(ctx: PricingContext, event_times, knock_in_times, expiry, time_s
         flags[np.isin(np.array(times), np.array(knock_in_times))] |= abi.STEP_KNOCK_IN
     excursion = (float(np.cumsum(np.abs(steps["drift"]) + 20.0 * steps["diffusion"])[-1])
                  if bsm else 0.0)
-    out = (times, steps, flags, excursion)
+    grid = np.array(times)
+    grid.flags.writeable = False
+    out = (times, steps, flags, excursion, grid)
     if key is not None:
         if len(_EVENT_GRID_CACHE) >= 256:
             _EVENT_GRID_CACHE.clear()
@@ -861,16 +863,13 @@ def autocallable(note: AutocallableNote, ctx: PricingContext, allow_bridge: bool
         note.knock_in_times is None or (len(note.knock_in_times) > 0
                                         and note.knock_in_times[-1] == note.expiry))
     events = [o for o in note.observations if o.time > 0.0]
-    times, steps, ki_flags, excursion = _event_grid(ctx, tuple(o.time for o in events),
-                                                    note.knock_in_times if daily else None,
-                                                    note.expiry, time_steps)
-    grid = np.array(times)
+    times, steps, ki_flags, excursion, grid = _event_grid(ctx, tuple(o.time for o in events),
+                                                          note.knock_in_times if daily else None,
+                                                          note.expiry, time_steps)
     flags = ki_flags.copy()
-    ev = np.zeros(len(events), EVENT_DTYPE)
-    position = np.searchsorted(grid, [o.time for o in events])
-    for k, (o, i) in enumerate(zip(events, position)):
-        flags[i] |= abi.STEP_EVENT
-        ev[k] = cash_event(note, o, spot, rate, int(i))
+    position = np.searchsorted(grid, [o.time for o in events]).tolist()
+    flags[position] |= abi.STEP_EVENT
+    ev = np.array([cash_event(note, o, spot, rate, i) for o, i in zip(events, position)], EVENT_DTYPE)
     c = _new_contract(abi.PAYOFF_AUTOCALLABLE, ctx.spot)
     flag = 0
     if note.knock_in_level is not None:

@@ -99,22 +99,39 @@ def shared_lane(note: AutocallableNote, ctx: PricingContext, index: int) -> Opti
     if isinstance(template, plans.Known):
         return None
     contract = template.contract.copy()
-    times = [t for t in note.knock_in_times if t > 0.0]
-    monitored = set(times)
+    times, monitored = _future_monitoring(note.knock_in_times)
     events = [o for o in note.observations if o.time > 0.0]
     on_grid = bool(times) and all(o.time == note.expiry or o.time in monitored for o in events)
+    records = template.events.tolist()
+    cash = [(r[_EVENT_STEP], r) for r in records]
     if not on_grid:
         observe = template.flags & abi.STEP_KNOCK_IN
         if not observe.any():
             return None
-        return Lane(index, note, contract, template.steps, observe.astype(np.uint8),
-                    [(int(e["step"]), tuple(e.tolist())) for e in template.events], False, False)
+        return Lane(index, note, contract, template.steps, observe.astype(np.uint8), cash, False, False)
     maturity_on_grid = times[-1] == note.expiry
     # With every event on a monitoring date or expiry, the scalar schedule (event dates,
     # monitoring dates and expiry) is this grid, step for step.
     observe = (template.flags & abi.STEP_KNOCK_IN).astype(np.uint8)
-    cash = [(int(e["step"]), tuple(e.tolist())) for e in template.events]
     return Lane(index, note, contract, template.steps, observe, cash, True, maturity_on_grid)
+
+
+_EVENT_STEP = plans.EVENT_DTYPE.names.index("step")
+_MONITORING: dict = {}
+
+
+def _future_monitoring(knock_in_times):
+    """The monitoring dates after valuation and their set, per schedule object (notes of
+    a book share the object; see instruments._shared_times)."""
+    hit = _MONITORING.get(id(knock_in_times))
+    if hit is not None and hit[0] is knock_in_times:
+        return hit[1], hit[2]
+    times = [t for t in knock_in_times if t > 0.0]
+    monitored = set(times)
+    if len(_MONITORING) >= 4096:
+        _MONITORING.clear()
+    _MONITORING[id(knock_in_times)] = (knock_in_times, times, monitored)
+    return times, monitored
 
 
 def _grid_key(lane: Lane):
@@ -283,7 +300,8 @@ def coupon_families(lanes: Sequence[Lane]) -> GroupPlan:
             families.append([])
         families[by_key[key]].append(i)
     plan = GroupPlan(list(lanes), [True] * len(lanes))
-    coupon = lambda i: portfolio_coupon(lanes[i].note)  # noqa: E731
+    coupons = [portfolio_coupon(lane.note) for lane in lanes]
+    coupon = coupons.__getitem__
     for family in families:
         if len(family) < 3:
             continue
