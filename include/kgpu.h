@@ -60,11 +60,12 @@ enum { KGPU_PRECISION_FP64 = 0, KGPU_PRECISION_FP32 = 1 };
  * reference's 256-sample blocks as CUDA blocks, sequential scaled-Welford moments per
  * block merged in block order.  PERSISTENT: the whole book at once.  A book whose every
  * contract is a Brownian-bridged autocallable (KGPU_C_BRIDGE, BSM) runs phase-major in
- * FP32: one launch per bridge interval advances every path still monitoring knock-in by
- * one interval, the lanes of a warp on the same grid positions, survivors compacted into
- * the next interval's list; knocked-in paths are completed by one final launch.  Other
- * books (and FP64) run the lane-refill kernel: warps pull (contract, tile) work items
- * from a device queue and refill finished lanes with the next path of the tile.
+ * FP32, as one cooperative launch: each grid step advances every path still monitoring
+ * knock-in by one bridge interval, the lanes of a warp on the same grid positions, and
+ * the survivors go to the next step's list; once few paths remain, CTAs complete them,
+ * then the knocked-in paths (interval ends only).  Other books (and FP64) run the
+ * lane-refill kernel: warps pull (contract, tile) work items from a device queue and
+ * refill finished lanes with the next path of the tile.
  * LANE_REFILL: the lane-refill kernel for every book.  Both persistent kernels store each
  * path's payoff and sum the payoffs in a fixed order, so their estimates are identical
  * for a book both can run. */
