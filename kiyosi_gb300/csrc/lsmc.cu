@@ -191,7 +191,6 @@ __global__ void coef_table_kernel(const double* coefs, Real* table, int n) {
 template <class Real, bool TWO>
 __device__ __forceinline__ void lower_bound_body(const LsmcParams<Real>& p, uint64_t seed, const Real* table,
                                                  const int* have, double* partials) {
-    constexpr int T = TWO ? 10 : 3;
     const int dims = TWO ? p.dates * p.substeps * 2 : p.dates;
     const Real inv_k = Real(1) / p.strike;
     double s0 = 0.0, s1 = 0.0;

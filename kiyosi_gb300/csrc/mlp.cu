@@ -732,27 +732,6 @@ __global__ void __launch_bounds__(kThreadsTrain, 1) mlp_train_cluster_kernel(Clu
     train_release(s);
 }
 
-// The network on the CUDA cores with the training kernel's BF16 rounding of the
-// hidden layer's inputs; `P` holds a snapshot whose W2 is already rounded to BF16.
-__device__ __forceinline__ float mlp_eval(const float* P, float x0, float x1, float x2) {
-    float h1[kHidden];
-#pragma unroll
-    for (int j = 0; j < kHidden; ++j) {
-        const float z = fmaf(P[kPW1 + 3 * j], x0, fmaf(P[kPW1 + 3 * j + 1], x1, fmaf(P[kPW1 + 3 * j + 2], x2, P[kPB1 + j])));
-        h1[j] = bf16_round(z > 0.f ? z : 0.f);
-    }
-    float out = P[kPB3];
-#pragma unroll 1
-    for (int o = 0; o < kHidden; ++o) {
-        float z = 0.f;
-#pragma unroll
-        for (int i = 0; i < kHidden; ++i) z = fmaf(P[kPW2 + o * kHidden + i], h1[i], z);
-        z += P[kPB2 + o];
-        out = fmaf(z > 0.f ? z : 0.f, P[kPW3 + o], out);
-    }
-    return out;
-}
-
 // Target normalisation of one date: the network fits (y - mean) / scale.
 struct TargetNorm {
     double mean, scale;
