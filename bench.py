@@ -789,6 +789,13 @@ def run_lsmc(args):
     alone_eq = price(abi.BASIS_MLP_STANDALONE, 22, samples=131072)
     polys = [price(abi.BASIS_POLY3, k) for k in range(21, 27)]
     equal = min(polys, key=lambda r: abs(r["wall_ms"] - mlp_eq["wall_ms"]))
+    # Context for the fixed comparison above: other path and sample counts of the
+    # network, each beside the polynomial run whose wall time is closest.
+    sweep = []
+    for log2_paths, samples in ((21, 131072), (22, 262144), (23, 131072)):
+        r = price(abi.BASIS_MLP, log2_paths, samples=samples)
+        near = min(polys, key=lambda q: abs(q["wall_ms"] - r["wall_ms"]))
+        sweep.append({"poly3_plus_network": r, "poly3_nearest_wall": near})
     # The trainer alone: Adam steps of batch 8192 over 65,536 samples, one launch.
     rng = np.random.default_rng(5)
     tsamples = rng.normal(size=(65536, 4)).astype(np.float32)
@@ -824,6 +831,7 @@ def run_lsmc(args):
                     "batch": 8192, "network": "3-64-64-1",
                     "timing": "host clock around kgpu_mlp_train, 1008 minus 8 steps"},
         "poly3_by_paths": polys,
+        "network_sweep": sweep,
     }
     print(json.dumps(line), flush=True)
 
