@@ -401,6 +401,20 @@ def run_kernel_only(args):
     """Device-resident pricings of one arm only, for ncu captures of the kernels."""
     from kiyosi_gb300 import _native, abi
     native = _native.context(0)
+    if args.kernel_only == "lv-book":
+        # The local-volatility book of `--notes` notes, FP32 persistent.
+        _, ctx, packed, paths, sampling = _workload("lv-book", args.notes)
+        s = abi.Settings(path_count=paths[0], sampling=sampling, antithetic=0, precision=abi.PRECISION_FP32,
+                         schedule=abi.SCHEDULE_PERSISTENT, seed=7)
+        model = ctx.kgpu_model()
+        book = packed.struct()
+        out = (abi.Estimate * len(packed.contracts))()
+        for _ in range(args.warmup + args.steps):
+            native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(book), C.byref(s),
+                                                    out, None))
+        print(json.dumps({"arm": "lv-book", "notes": args.notes, "path_kernel_ms": native.last_path_kernel_ms,
+                          "executed_steps": sum(e.executed_steps for e in out)}))
+        return
     if args.kernel_only == "mlp-train-grid":
         # The grid-barrier trainer alone: 40 Adam steps of batch 8192 over 65,536
         # synthetic samples per call.
@@ -491,7 +505,7 @@ def _first(packed, n):
                         packed.intervals, packed.daily)
 
 
-def _workload(name):
+def _workload(name, notes=4096):
     """(description, context, packed book, per-contract paths, sampling) of a named
     benchmark configuration."""
     from kiyosi_gb300 import plans, workloads
@@ -509,7 +523,7 @@ def _workload(name):
                 "Euler steps", ctx, b.build(), [1 << 22], 0)
     if name == "lv-book":
         ctx = PricingContext(workloads.lv_surface(), 100.0)
-        notes, paths = workloads.lv_book(4096)
+        notes, paths = workloads.lv_book(notes)
         for n in notes:
             b.add(plans.autocallable(n, ctx))
         return ("book of 4096 snowball/phoenix notes under local volatility (50x20 surface), "
@@ -884,12 +898,13 @@ def main():
     ap.add_argument("--paths", type=int, default=PATHS,
                     help="path count (profiling runs use smaller cases)")
     ap.add_argument("--dates", type=int, default=50, help="LSMC exercise dates (profiling runs)")
+    ap.add_argument("--notes", type=int, default=4096, help="local-volatility book size (profiling runs)")
     ap.add_argument("--mlp-samples", type=int, default=0,
                     help="LSMC network: in-the-money samples trained on per date (0: all)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="use the kernel's default launch shape instead of the autotuner's")
     ap.add_argument("--kernel-only", choices=["fp32", "fp32-lanes", "fp64", "lsmc-poly", "lsmc-mlp", "shared-grid",
-                                              "mlp-train-grid"],
+                                              "mlp-train-grid", "lv-book"],
                     help="run only the device-resident pricing of one arm (for profilers)")
     ap.add_argument("--tile", type=int, default=0, help="persistent tile paths (0 = default)")
     ap.add_argument("--ctas-per-sm", type=int, default=0, help="persistent CTAs per SM (0 = max)")

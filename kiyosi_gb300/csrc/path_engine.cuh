@@ -271,18 +271,31 @@ __device__ __forceinline__ Real spot_at(Real initial, Real log_return) {
 template <class Real>
 __device__ __forceinline__ void lv_bracket(const Real* nodes, int n, Real value, int& left,
                                            Real& weight) {
-    // partition_point(node <= value) - 1, clamped to [0, n-2]
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (nodes[mid] <= value)
-            lo = mid + 1;
-        else
-            hi = mid;
+    // partition_point(node <= value) - 1, clamped to [0, n-2].  `left` on entry is the
+    // bracket of a previous value of the same path (or < 0): a path's spot moves little
+    // per step and its time only forward, so walking from there usually takes no step;
+    // the walk ends on the same bracket as the search.
+    int l = left;
+    if (l < 0) {
+        int lo = 0, hi = n;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (nodes[mid] <= value)
+                lo = mid + 1;
+            else
+                hi = mid;
+        }
+        l = lo - 1;
+        l = l < 0 ? 0 : (l > n - 2 ? n - 2 : l);
+    } else {
+        while (l > 0 && !(nodes[l] <= value)) --l;
+        while (l < n - 2 && nodes[l + 1] <= value) ++l;
     }
-    int l = lo - 1;
-    l = l < 0 ? 0 : (l > n - 2 ? n - 2 : l);
-    Real w = (value - nodes[l]) / (nodes[l + 1] - nodes[l]);
+    Real w;
+    if constexpr (sizeof(Real) == 4)
+        w = __fdividef(value - nodes[l], nodes[l + 1] - nodes[l]);
+    else
+        w = (value - nodes[l]) / (nodes[l + 1] - nodes[l]);
     weight = w < Real(0) ? Real(0) : (w > Real(1) ? Real(1) : w);
     left = l;
 }
@@ -293,11 +306,10 @@ __device__ __forceinline__ Real lv_interpolate(Real low, Real high, Real weight)
 }
 
 template <class Real>
-__device__ __forceinline__ Real lv_at(const DevModel<Real>& m, Real time, Real spot) {
+__device__ __forceinline__ Real lv_at(const DevModel<Real>& m, Real time, Real spot, int& row, int& col) {
     const Real* years = m.lv;
     const Real* spots = m.lv + m.nt;
     const Real* values = m.lv + m.nt + m.ns;
-    int row, col;
     Real tw, sw;
     lv_bracket(years, m.nt, time, row, tw);
     lv_bracket(spots, m.ns, spot, col, sw);
@@ -324,6 +336,7 @@ struct PathState {
     int end;       // grid step ending the current bridge interval (-1: not started)
     int fixings;
     int executed;  // grid steps simulated
+    int lv_row, lv_col;  // local volatility: the surface cell of the previous step (-1: none)
     bool knocked_in;
     bool monitoring;
     bool knocked_out;
@@ -343,6 +356,7 @@ __device__ __forceinline__ void path_init(PathState<Real>& s, const ContractT<Re
     s.end = -1;
     s.fixings = 0;
     s.executed = 0;
+    s.lv_row = s.lv_col = -1;
     s.knocked_in = (c.flags & KGPU_C_KNOCKED_IN) != 0;
     s.monitoring = !s.knocked_in && (c.flags & KGPU_C_HAS_KNOCK_IN);
     s.knocked_out = false;
@@ -375,7 +389,7 @@ __device__ __forceinline__ void model_step(const DevModel<Real>& m, const StepT<
         s.v += m.kappa * (m.theta - vp) * dt + m.xi * sv * zv;
     } else {
         Real spot = m.spot * xexp(s.lr);
-        Real sigma = lv_at(m, st.time, spot);
+        Real sigma = lv_at(m, st.time, spot, s.lv_row, s.lv_col);
         Real dt = st.drift, sq = st.diffusion;
         s.lr += (m.rate - m.dividend - Real(0.5) * sigma * sigma) * dt + sigma * sq * n.normal();
     }
