@@ -736,6 +736,36 @@ def run_shared_grid(args):
     print(json.dumps(line), flush=True)
 
 
+def lsmc_roofline(poly, us_per_step):
+    """The two bounds of the LSMC configuration against the measured peaks of
+    MEASURED_PEAKS.json: the polynomial pricing's path-store traffic over HBM (per path
+    and date an 8-byte state write and read plus an 8-byte cash read and write:
+    2^20 x 50 x 24 B = 1.26 GB) over its whole wall time, and the trainer's tensor work
+    (fwd + bwd of every layer, 3 x 2 x (3*64 + 64*64 + 64) = 26,112 FLOP per sample) per
+    Adam step of 8,192 samples over its time per step."""
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops_sustained", 1700.0)
+    source = "of measured" if peaks else "of fallback"
+    store_bytes = poly["paths"] * 50 * 24
+    store_gbs = store_bytes / (poly["wall_ms"] * 1e-3) / 1e9
+    train_tflops = 26112 * 8192 / (us_per_step * 1e-6) / 1e12
+    return {
+        "path_store": {"bound": "hbm", "achieved": store_gbs, "peak": hbm, "unit": "GB/s",
+                       "frac": store_gbs / hbm, "algorithmic_bytes": store_bytes, "peak_source": source,
+                       "note": "poly3 FP32 at 2^20 paths over the whole pricing: 150 dependent launches of "
+                               "per-date passes, latency-bound"},
+        "trainer": {"bound": "tensor", "achieved": train_tflops, "peak": bf16, "unit": "TFLOP/s",
+                    "frac": train_tflops / bf16, "peak_source": source + " (sustained)",
+                    "note": "one Adam step is a dependent chain of phases across SMs"},
+    }
+
+
 def run_lsmc(args):
     """American put under Heston, 50 exercise dates x 5 Euler substeps, judged by the
     Heston ADI price.  Two comparisons of the polynomial LSMC (the reference's method)
@@ -846,6 +876,7 @@ def run_lsmc(args):
                     "timing": "host clock around kgpu_mlp_train, 1008 minus 8 steps"},
         "poly3_by_paths": polys,
         "network_sweep": sweep,
+        "roofline": lsmc_roofline(poly, us_per_step[abi.TRAINER_CLUSTER]),
     }
     print(json.dumps(line), flush=True)
 
