@@ -618,6 +618,7 @@ def asian(option: AsianOption, ctx: PricingContext, step_count: Optional[int] = 
 
 
 _EVENT_GRID_CACHE: dict = {}
+_EVENT_GRID_BY_ID: dict = {}
 
 
 def refine_grid(times: List[float], time_steps: Optional[int]) -> List[float]:
@@ -651,10 +652,21 @@ def _event_grid(ctx: PricingContext, event_times, knock_in_times, expiry, time_s
     Notes of one schedule share the result."""
     model = ctx.model
     bsm = isinstance(model, BlackScholesMertonParameters)
+    # Notes of a book share their schedule objects: look the grid up by the schedule's
+    # identity first (no hashing of a long tuple), then by its contents.
+    fast = (type(model), model.rate, model.dividend, getattr(model, "volatility", None), event_times,
+            id(knock_in_times), expiry, time_steps) if bsm else None
+    if fast is not None:
+        hit = _EVENT_GRID_BY_ID.get(fast)
+        if hit is not None and hit[0] is knock_in_times:
+            return hit[1]
     key = (type(model), model.rate, model.dividend, getattr(model, "volatility", None), event_times,
            knock_in_times, expiry, time_steps) if bsm else None
     hit = _EVENT_GRID_CACHE.get(key) if key is not None else None
     if hit is not None:
+        if len(_EVENT_GRID_BY_ID) >= 256:
+            _EVENT_GRID_BY_ID.clear()
+        _EVENT_GRID_BY_ID[fast] = (knock_in_times, hit)
         return hit
     times = sorted(set(list(event_times) + (list(knock_in_times) if knock_in_times is not None else [])
                        + [expiry]))
