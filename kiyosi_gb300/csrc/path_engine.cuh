@@ -844,6 +844,11 @@ __device__ __forceinline__ PlanPtrs<Real> plan_of(const DevBook<Real>& b, const 
 }
 
 // Advances one path by one unit of work (a grid step, or a bridge interval end).
+template <class Real, int MODEL, class Source>
+__device__ __forceinline__ bool grid_step(const DevModel<Real>& m, const ContractT<Real>& c,
+                                          const PlanPtrs<Real>& p, PathState<Real>& s, Source& n,
+                                          Real& value);
+
 // Returns true when the path has finished; its payoff is then in `value`.
 // EXT: the extended payoff set (scheduled barriers, continuous averages) is compiled in.
 template <class Real, int MODEL, bool EXT = true, class Source>
@@ -851,6 +856,11 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
                                           const PlanPtrs<Real>& p, PathState<Real>& s, Source& n,
                                           Real& value) {
     const int payoff = c.payoff;
+    // The grid-stepping families first: they take a step per call, the others mostly one
+    // call per path.
+    if (payoff == KGPU_PAYOFF_VANILLA_PATH || payoff == KGPU_PAYOFF_ASIAN || payoff == KGPU_PAYOFF_ACCUMULATOR ||
+        (payoff == KGPU_PAYOFF_AUTOCALLABLE && !(c.flags & KGPU_C_BRIDGE)))
+        return grid_step<Real, MODEL>(m, c, p, s, n, value);
     if (payoff == KGPU_PAYOFF_AUTOCALLABLE && (c.flags & KGPU_C_BRIDGE)) {
         // bridge_payoffs::<1, true>: the interval end is drawn first, then daily bridge
         // steps until knock-in is decided, then the interval end.  Each call evaluates at
@@ -1011,6 +1021,16 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
         return finish();
     }
     // Grid-stepping families.
+    return grid_step<Real, MODEL>(m, c, p, s, n, value);
+}
+
+// One grid step of the grid-stepping families (vanilla path, Asian on fixings, forward
+// autocallable, accumulator): model step, then the family's per-step rule.
+template <class Real, int MODEL, class Source>
+__device__ __forceinline__ bool grid_step(const DevModel<Real>& m, const ContractT<Real>& c,
+                                          const PlanPtrs<Real>& p, PathState<Real>& s, Source& n,
+                                          Real& value) {
+    const int payoff = c.payoff;
     const int i = s.i;
     const StepT<Real> st = p.steps[i];
     model_step<Real, MODEL>(m, st, s, n);
