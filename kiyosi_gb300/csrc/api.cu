@@ -374,11 +374,12 @@ int64_t persistent_tile(bool sobol, int requested, int precision, int64_t book_s
         return (requested > 0 && requested <= 256 && 256 % requested == 0) ? requested : 64;
     }
     if (requested > 0) return requested;
-    // 1024-path items, halved (down to one path per lane) while the book has fewer than
-    // 16 items per SM: in large items a small book would leave most SMs idle and every
-    // lane walking many paths in turn.
-    int64_t tile = 1024;
-    while (tile > 32 && book_samples < tile * 16 * int64_t(sm_count)) tile >>= 1;
+    // 128-path items (four paths per lane), halved down to one path per lane while the
+    // book has fewer than 128 items per SM: the grid holds 32 warps per SM, and items
+    // several times that keep every warp busy to the end (measured: the 2^22-path Heston
+    // Asian book in 1024-path items left 16% of the warps without an item).
+    int64_t tile = 128;
+    while (tile > 32 && book_samples < tile * 128 * int64_t(sm_count)) tile >>= 1;
     return tile;
 }
 
