@@ -471,11 +471,12 @@ kgpu_status kgpu_lsmc_price_scenarios(kgpu_context* ctx, const kgpu_model* model
  * buffers).  Limits: BSM or Heston models, pseudo-random sampling, settings asking for
  * KGPU_PRECISION_FP64 and KGPU_SCHEDULE_PLAIN (others are KGPU_UNSUPPORTED_OPERATION),
  * at most 4,194,304 samples per call.  Its scratch is one fixed 1.7 MB array in device
- * memory that every GPU loading this library holds until process exit.  The call
- * synchronises `stream`, so it cannot be captured into a CUDA graph.  Every call
- * shares the array, so calls that overlap on the GPU -- on different streams or from
- * different threads -- race; serialise them.  Errors are reported through
- * kgpu_last_error_message(NULL). */
+ * memory that every GPU loading this library holds until process exit.  The first call
+ * on a device, with that device current, looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any stream capture.
+ * The call synchronises `stream` before it returns.  Every call shares the array, so
+ * calls that overlap on the GPU -- on different streams or from different threads --
+ * race; serialise them.  Errors are reported through kgpu_last_error_message(NULL). */
 kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book* device_book,
                                         int32_t contract, const kgpu_settings* settings,
                                         kgpu_estimate* out, void* stream);

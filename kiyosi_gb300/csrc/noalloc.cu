@@ -45,7 +45,9 @@ kgpu_status noalloc_fail(kgpu_status status, const char* message) {
     return status;
 }
 
-// Device address of the scratch on the current device, looked up once per device.
+// Device address of the scratch on the current device, looked up by the first call on
+// each device (with that device current) and kept; that first call belongs before any
+// stream capture.
 kgpu_status scratch_address(NoAllocScratch** out) {
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices)
