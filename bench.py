@@ -450,15 +450,12 @@ def run_kernel_only(args):
                           "regression_ms": out.regression_ms, "launches": native.last_launches}))
         return
     if args.kernel_only == "shared-grid":
-        # the shared-grid book's lanes on the path-major FP32 schedule
-        from kiyosi_gb300 import plans, portfolio, workloads
+        # the shared-grid book's lanes (native planner) on the path-major FP32 schedule
+        from kiyosi_gb300 import portfolio, workloads
         ctx = workloads.c2_context()
-        book_plan = portfolio.plan_book(workloads.shared_grid_book(), ctx, True)
-        lanes = [lane for g in book_plan.groups for lane in g.simulated_lanes()]
-        builder = plans.BookBuilder()
-        for p in portfolio.lane_plans(lanes, ctx.spot):
-            builder.add(p)
-        packed = builder.build()
+        shared = portfolio.SharedPlan(portfolio.note_tables(workloads.shared_grid_book()), ctx.kgpu_model())
+        packed = shared.group_packed(0)
+        lanes = packed.contracts
         s = abi.Settings(path_count=args.paths, sampling=abi.SAMPLING_PSEUDO_RANDOM, antithetic=0,
                          precision=abi.PRECISION_FP32, schedule=abi.SCHEDULE_SHARED_GRID, seed=42)
         for _ in range(args.warmup + args.steps):
@@ -646,14 +643,24 @@ def run_shared_grid(args):
     ctx = workloads.c2_context()
     notes = workloads.shared_grid_book()
     paths, seed = 1 << 16, 42
+    # The book's plan: the library's native planner (what the engine call runs), and the
+    # Python restatement beside it (the oracle's lanes below).
+    t0 = time.perf_counter()
+    tables = portfolio.note_tables(notes)
+    t1 = time.perf_counter()
+    shared = portfolio.SharedPlan(tables, ctx.kgpu_model())
+    packed = shared.group_packed(0)
+    plan_s = time.perf_counter() - t0
+    tables_s = t1 - t0
+    assert shared.group_count == 1 and (shared.note_group >= 0).all()
     t0 = time.perf_counter()
     book = portfolio.plan_book(notes, ctx, True)
     lanes = [lane for g in book.groups for lane in g.simulated_lanes()]
-    builder = plans.BookBuilder()
+    python_book = plans.BookBuilder()
     for p in portfolio.lane_plans(lanes, ctx.spot):
-        builder.add(p)
-    packed = builder.build()
-    plan_s = time.perf_counter() - t0
+        python_book.add(p)
+    python_packed = python_book.build()
+    python_plan_s = time.perf_counter() - t0
     assert len(book.groups) == 1 and not book.scalar
 
     def cfg(precision, schedule):
@@ -683,7 +690,9 @@ def run_shared_grid(args):
     worst_se = max(abs(a.price - b.price) / max(b.sample_error, 1e-300) for a, b in zip(est32, est64))
     # The whole engine call from host notes (planning, staging, launch, results).
     engine = MonteCarloAutocallableEngine(path_count=paths, seed=seed, precision="fp32")
+    t0 = time.perf_counter()
     engine.price_many_on_shared_grid(notes, ctx)
+    e2e_first = time.perf_counter() - t0
     e2e = []
     for _ in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
@@ -719,8 +728,11 @@ def run_shared_grid(args):
                                           + packed.contracts.nbytes + packed.intervals.nbytes
                                           + (packed.daily.nbytes if packed.daily is not None else 0)),
                 "d2h_bytes_per_step": int(len(lanes) * C.sizeof(abi.Estimate)),
-                "includes": "host planning of the book (Python), staging, launch, results"},
-        "host_planning_s": plan_s,
+                "includes": "the engine call from host notes: note tables (Python), native planning, "
+                            "staging, launch, interpolation, results",
+                "first_call_s": e2e_first},
+        "host_planning": {"native_s": plan_s, "note_tables_s": tables_s, "python_planner_s": python_plan_s,
+                          "step_records": {"native": int(len(packed.steps)), "python": int(len(python_packed.steps))}},
         "gpu_launches": launches, "clocks": clocks.summary(),
         "path_kernel_ms": statistics.median(path),
         "lane_equivalent_path_steps_per_s": lane_path_steps / (ms / 1e3),

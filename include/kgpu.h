@@ -481,6 +481,105 @@ kgpu_status kgpu_price_contract_noalloc(const kgpu_model* model, const kgpu_book
                                         int32_t contract, const kgpu_settings* settings,
                                         kgpu_estimate* out, void* stream);
 
+/* ---- Planning a book of notes on one shared daily grid (host code; no GPU) ----
+ *
+ * The host half of MonteCarloAutocallableEngine::price_many_on_shared_grid
+ * (crates/kiyosi/src/engines/monte_carlo/autocallable.rs:127-152, planned by
+ * autocallable/portfolio.rs): which notes join a shared daily grid (DailyGrids::prepare,
+ * portfolio.rs:74-185), their groups (same_daily_grid, 872-901), the coupon families whose
+ * interior members are interpolated (price_coupon_families, 570-667), and each group's
+ * interval plan (SharedEvents::new, 903-1047) with one bridged lane contract per
+ * simulated note.  Notes are given as flat terms; knock-in monitoring times and
+ * observations are ranges of two shared tables. */
+
+/* An autocallable note (AutocallableNote, crates/kiyosi/src/instruments/autocallable.rs).
+ * Times are year fractions after valuation. */
+enum {
+    KGPU_NOTE_KNOCK_IN = 1,       /* knock_in_level is set */
+    KGPU_NOTE_MONITORING = 2,     /* knock-in monitored on the listed times (else at expiry) */
+    KGPU_NOTE_FIXED_COUPON = 4    /* knocked-in redemption is fixed_knock_in_coupon (else the
+                                     capped downside) */
+};
+enum { KGPU_STATE_UNKNOWN = 0, KGPU_STATE_NO_EVENT = 1, KGPU_STATE_KNOCKED_IN = 2, KGPU_STATE_KNOCKED_OUT = 3 };
+
+typedef struct kgpu_note {
+    double initial_spot;
+    double expiry;
+    double knock_in_level;
+    double upper_strike;
+    double lower_strike;
+    double maturity_coupon_rate;
+    double period_coupon;
+    double fixed_knock_in_coupon;
+    double principal;
+    double rebate_rate;
+    double annual_rebate_rate;
+    double effective_time;
+    int32_t flags;               /* KGPU_NOTE_* */
+    int32_t barrier_state;       /* KGPU_STATE_*: history strictly before valuation */
+    int32_t observation_offset;  /* first kgpu_note_observation */
+    int32_t observation_count;
+    int32_t monitoring_offset;   /* first monitoring time (KGPU_NOTE_MONITORING) */
+    int32_t monitoring_count;
+} kgpu_note;
+
+enum { KGPU_OBSERVATION_KNOCK_OUT = 1, KGPU_OBSERVATION_COUPON_BARRIER = 2 };
+
+typedef struct kgpu_note_observation {
+    double time;
+    double knock_out_level;       /* KGPU_OBSERVATION_KNOCK_OUT */
+    double coupon_barrier_level;  /* KGPU_OBSERVATION_COUPON_BARRIER */
+    double coupon_rate;           /* annual coupon accrued on knock-out */
+    int32_t flags;                /* KGPU_OBSERVATION_* */
+    int32_t reserved;
+} kgpu_note_observation;
+
+typedef struct kgpu_shared_plan kgpu_shared_plan;
+
+/* What a shared plan holds.  Pointers stay valid until kgpu_shared_plan_destroy. */
+typedef struct kgpu_shared_plan_view {
+    int32_t note_count;
+    int32_t group_count;
+    int32_t lane_count;                 /* simulated lanes of all groups */
+    int32_t reserved;
+    const int32_t* note_group;          /* [note_count]: the note's group, or -1 when the
+                                           scalar engine quotes it */
+    const int32_t* group_first_lane;    /* [group_count + 1]: group g's lanes are
+                                           [group_first_lane[g], group_first_lane[g + 1]) */
+    const int32_t* lane_note;           /* [lane_count]: the book index of each lane */
+    const uint8_t* lane_fp32;           /* [lane_count]: the lane's plan is representable in
+                                           FP32 (every finite nonzero value within
+                                           [2^-100, 2^120]; the model is not checked) */
+    const kgpu_book* group_books;       /* [group_count]: one book per group, its contracts
+                                           the group's lanes in order, ready for
+                                           kgpu_price_book with KGPU_SCHEDULE_SHARED_GRID */
+    const int32_t* group_status;        /* [group_count]: KGPU_OK, or why the group's interval
+                                           plan failed (raised when the group is priced) */
+    const char* const* group_message;   /* [group_count]: the failure's message, or "" */
+} kgpu_shared_plan_view;
+
+/* Plans `note_count` notes under a BSM `model` (other models quote every note with the
+ * scalar engine).  `simulate` (may be NULL) forces notes to be simulated although their
+ * coupon family would interpolate them (the members whose interpolation cancelled).  A
+ * note that fails the reference's checks (missing history, a non-finite plan) or that
+ * needs no sampling is left to the scalar engine (note_group -1), whose planner reports
+ * it.  KGPU_INVALID_INPUT for ranges outside the tables. */
+kgpu_status kgpu_shared_plan_create(const kgpu_model* model, const kgpu_note* notes, int32_t note_count,
+                                    const kgpu_note_observation* observations, int32_t observation_total,
+                                    const double* monitoring, int32_t monitoring_total, const uint8_t* simulate,
+                                    kgpu_shared_plan** out);
+
+kgpu_status kgpu_shared_plan_get(const kgpu_shared_plan* plan, kgpu_shared_plan_view* out);
+
+/* Fills the prices of the coupon families' interpolated members, linear in the coupon
+ * between the family's lowest- and highest-coupon members (portfolio.rs:570-667).
+ * note_prices[note_count] holds every simulated lane's price on entry.  retry[i] = 1
+ * marks a member whose interpolation cancels (|price| < 1e-12 x the magnitude of its two
+ * terms, or not finite), which the reference then simulates; its price is left as is. */
+kgpu_status kgpu_shared_plan_interpolate(const kgpu_shared_plan* plan, double* note_prices, uint8_t* retry);
+
+void kgpu_shared_plan_destroy(kgpu_shared_plan* plan);
+
 /* Loss and parameter gradients of the LSMC continuation network on one batch, computed
  * by the tensor-core training kernel that the MLP basis of kgpu_lsmc_price runs (no
  * counterpart in the reference: exposed so the kernels' gradients can be checked).

@@ -163,6 +163,38 @@ class LsmcResult(C.Structure):
                 ("regression_ms", _D)]
 
 
+NOTE_KNOCK_IN = 1
+NOTE_MONITORING = 2
+NOTE_FIXED_COUPON = 4
+STATE_UNKNOWN = 0
+STATE_NO_EVENT = 1
+STATE_KNOCKED_IN = 2
+STATE_KNOCKED_OUT = 3
+OBSERVATION_KNOCK_OUT = 1
+OBSERVATION_COUPON_BARRIER = 2
+
+
+class Note(C.Structure):
+    _fields_ = [("initial_spot", _D), ("expiry", _D), ("knock_in_level", _D), ("upper_strike", _D),
+                ("lower_strike", _D), ("maturity_coupon_rate", _D), ("period_coupon", _D),
+                ("fixed_knock_in_coupon", _D), ("principal", _D), ("rebate_rate", _D),
+                ("annual_rebate_rate", _D), ("effective_time", _D), ("flags", _I),
+                ("barrier_state", _I), ("observation_offset", _I), ("observation_count", _I),
+                ("monitoring_offset", _I), ("monitoring_count", _I)]
+
+
+class NoteObservation(C.Structure):
+    _fields_ = [("time", _D), ("knock_out_level", _D), ("coupon_barrier_level", _D),
+                ("coupon_rate", _D), ("flags", _I), ("reserved", _I)]
+
+
+class SharedPlanView(C.Structure):
+    _fields_ = [("note_count", _I), ("group_count", _I), ("lane_count", _I), ("reserved", _I),
+                ("note_group", _P(_I)), ("group_first_lane", _P(_I)), ("lane_note", _P(_I)),
+                ("lane_fp32", _P(C.c_uint8)), ("group_books", _P(Book)),
+                ("group_status", _P(_I)), ("group_message", _P(C.c_char_p))]
+
+
 STRUCT_SIZES = {
     "kgpu_settings": C.sizeof(Settings),
     "kgpu_model": C.sizeof(Model),
@@ -175,6 +207,9 @@ STRUCT_SIZES = {
     "kgpu_estimate": C.sizeof(Estimate),
     "kgpu_lsmc_settings": C.sizeof(LsmcSettings),
     "kgpu_lsmc_result": C.sizeof(LsmcResult),
+    "kgpu_note": C.sizeof(Note),
+    "kgpu_note_observation": C.sizeof(NoteObservation),
+    "kgpu_shared_plan_view": C.sizeof(SharedPlanView),
 }
 
 # Every entry point include/kgpu.h declares.
@@ -185,6 +220,8 @@ EXPORTED_SYMBOLS = (
     "kgpu_context_last_path_kernel_ms",
     "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count", "kgpu_pipe_rates",
     "kgpu_price_contract_noalloc", "kgpu_mlp_gradients", "kgpu_mlp_train", "kgpu_lsmc_price_scenarios",
+    "kgpu_shared_plan_create", "kgpu_shared_plan_get", "kgpu_shared_plan_interpolate",
+    "kgpu_shared_plan_destroy",
 )
 MLP_PARAMS = 4481
 
@@ -238,4 +275,13 @@ def declare(lib):
     lib.kgpu_mlp_train.restype = _I
     lib.kgpu_pipe_rates.argtypes = [V, C.POINTER(_D), _I]
     lib.kgpu_pipe_rates.restype = _I
+    lib.kgpu_shared_plan_create.argtypes = [_P(Model), _P(Note), _I, _P(NoteObservation), _I, _P(_D), _I,
+                                            _P(C.c_uint8), _P(V)]
+    lib.kgpu_shared_plan_create.restype = _I
+    lib.kgpu_shared_plan_get.argtypes = [V, _P(SharedPlanView)]
+    lib.kgpu_shared_plan_get.restype = _I
+    lib.kgpu_shared_plan_interpolate.argtypes = [V, _P(_D), _P(C.c_uint8)]
+    lib.kgpu_shared_plan_interpolate.restype = _I
+    lib.kgpu_shared_plan_destroy.argtypes = [V]
+    lib.kgpu_shared_plan_destroy.restype = None
     return lib

@@ -1,7 +1,9 @@
 """Builds libkiyosi_gpu.so in-tree with nvcc for sm_103a (GB300).
 
 Translation units compile in parallel; kernels_fp64.cu is compiled with --fmad=false so
-the FP64 kernels round every product and sum separately, as the Rust reference does.
+the FP64 kernels round every product and sum separately, as the Rust reference does, and
+the host planner (planner.cpp) with floating-point contraction off for the same reason
+(an Arm host compiler would otherwise fuse its products and sums).
 Usage: python -m kiyosi_gb300.build [--force]
 """
 import concurrent.futures as cf
@@ -25,6 +27,7 @@ UNITS = {
     "mlp.cu": [],
     "noalloc.cu": [],
     "pipes.cu": [],
+    "planner.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["device_rng.cuh", "path_engine.cuh", "kernels.cuh", "kernels_impl.cuh", "launch.h",
            "api_internal.h", "joe_kuo_6_21201.inc", "shared_grid.cuh", "lsmc_common.cuh", "tcgen05.cuh", "phased.cuh"]
@@ -43,7 +46,7 @@ def _newest(paths):
 
 def _compile(unit: str, flags, verbose: bool) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    obj = os.path.join(BUILD, os.path.splitext(unit)[0] + ".o")
     deps = [src, os.path.join(HERE, "..", "include", "kgpu.h")] + [
         os.path.join(CSRC, h) for h in HEADERS]
     if os.path.exists(obj) and os.path.getmtime(obj) >= _newest(deps) and not verbose:

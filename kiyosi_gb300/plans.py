@@ -57,8 +57,7 @@ def fp32_representable(plan, ctx: PricingContext) -> bool:
     last = list(CONTRACT_DTYPE.names).index("greek_log_weight")
     if not _fp32_ok([c[n] for n in CONTRACT_DTYPE.names[first:last + 1]]):
         return False
-    m = ctx.kgpu_model()
-    if not _fp32_ok([m.spot, m.rate, m.dividend, m.volatility, m.v0, m.kappa, m.theta, m.xi, m.rho]):
+    if not fp32_model_ok(ctx):
         return False
     st = plan.steps
     if not (_fp32_ok(st["drift"]) and _fp32_ok(st["diffusion"]) and _fp32_ok(st["discount"])):
@@ -72,6 +71,12 @@ def fp32_representable(plan, ctx: PricingContext) -> bool:
         if plan.daily is not None and not (_fp32_ok(plan.daily["weight"]) and _fp32_ok(plan.daily["width"])):
             return False
     return True
+
+
+def fp32_model_ok(ctx: PricingContext) -> bool:
+    """The model half of fp32_representable."""
+    m = ctx.kgpu_model()
+    return _fp32_ok([m.spot, m.rate, m.dividend, m.volatility, m.v0, m.kappa, m.theta, m.xi, m.rho])
 
 
 @dataclass

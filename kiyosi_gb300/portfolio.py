@@ -38,9 +38,12 @@ in a knock-out or knock-in level. They save work on the CPU. Here every strip me
 lane of the same launch. `threshold_strips` still describes them, for the oracle's
 restatement of the strip sums.
 """
+import ctypes as C
 import math
+import operator
 from dataclasses import dataclass, field, fields, replace
 from fractions import Fraction
+from itertools import chain, repeat
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -197,7 +200,12 @@ def interval_plan(lanes: Sequence[Lane], spot: float):
             weights = []
             for i in range(step - 1, first - 1, -1):
                 nxt = _fma(width[i], width[i], variance)
-                weights.append((i, (width[i] * width[i]) / nxt, width[i] * math.sqrt(variance / nxt)))
+                if nxt == 0.0:
+                    # 0 / 0 under a vanishing volatility: NaN weights refuse the bridge,
+                    # as the reference's floating-point division does
+                    weights.append((i, math.nan, math.nan))
+                else:
+                    weights.append((i, (width[i] * width[i]) / nxt, width[i] * math.sqrt(variance / nxt)))
                 total += drift[i]
                 variance = nxt
             diffusion = math.sqrt(variance)
@@ -455,11 +463,20 @@ def plan_book(notes: Sequence[AutocallableNote], ctx: PricingContext, shared_gri
 
 
 def price_many(engine, notes: Sequence[AutocallableNote], ctx: PricingContext,
-               shared_grid: bool) -> List[float]:
+               shared_grid: bool, planner: str = "native") -> List[float]:
     """Quotes of `notes` in input order.  Scalar quotes share one launch; each group's
     lanes go to the engine's path-major schedule when it has one (one path per sample
     settles every lane, kgpu's KGPU_SCHEDULE_SHARED_GRID), else into the same launch as
-    per-lane contracts (identical estimates, each lane re-walking the path)."""
+    per-lane contracts (identical estimates, each lane re-walking the path).
+
+    With a shared grid under BSM the book is planned by the library's native planner
+    (kgpu_shared_plan_create, `SharedPlan`); `planner="python"` plans it with this
+    module's restatement instead (same lanes, same prices)."""
+    if planner not in ("native", "python"):
+        raise InvalidInputError("planner must be 'native' or 'python'")
+    if (shared_grid and planner == "native" and isinstance(ctx.model, BlackScholesMertonParameters)
+            and getattr(engine, "_run_shared_book", None) is not None):
+        return _price_many_planned(engine, notes, ctx)
     book = plan_book(notes, ctx, shared_grid)
     prices: Dict[int, float] = {}
     pending = list(range(len(book.groups)))
@@ -495,3 +512,200 @@ def price_many(engine, notes: Sequence[AutocallableNote], ctx: PricingContext,
         pending = retry
         first = False
     return [prices[i] for i in range(len(notes))]
+
+
+# ---- the native planner (kgpu_shared_plan_* in include/kgpu.h) ----
+
+NOTE_DTYPE = np.dtype(abi.Note)
+NOTE_OBSERVATION_DTYPE = np.dtype(abi.NoteObservation)
+_STATE_CODES = {None: abi.STATE_UNKNOWN, "no_event": abi.STATE_NO_EVENT,
+                "knocked_in": abi.STATE_KNOCKED_IN, "knocked_out": abi.STATE_KNOCKED_OUT}
+_NOTE_TERMS = operator.attrgetter(
+    "initial_spot", "expiry", "knock_in_level", "upper_strike", "lower_strike",
+    "maturity_coupon_rate", "period_coupon", "fixed_knock_in_coupon", "principal", "rebate_rate",
+    "annual_rebate_rate", "effective_time", "barrier_state", "observations", "knock_in_times")
+
+
+@dataclass
+class NoteTables:
+    """A book of notes as kgpu_shared_plan_create's flat tables."""
+    notes: np.ndarray         # NOTE_DTYPE
+    observations: np.ndarray  # NOTE_OBSERVATION_DTYPE
+    monitoring: np.ndarray    # float64: every distinct monitoring schedule once
+
+
+def note_tables(notes: Sequence[AutocallableNote]) -> NoteTables:
+    """Flattens the notes' terms; notes sharing a monitoring schedule object share its
+    range of the monitoring table.  Observations are read column by column."""
+    rows = []
+    schedules: Dict[int, Tuple[int, int]] = {}
+    monitoring = []
+    total = 0
+    first_observation = 0
+    for note in notes:
+        (spot0, expiry, ki, upper, lower, maturity_coupon, period_coupon, fixed, principal,
+         rebate, annual_rebate, effective, state, obs, times) = _NOTE_TERMS(note)
+        flags = 0
+        if ki is None:
+            ki = 0.0
+        else:
+            flags |= abi.NOTE_KNOCK_IN
+        if fixed is None:
+            fixed = 0.0
+        else:
+            flags |= abi.NOTE_FIXED_COUPON
+        first = count = 0
+        if times is not None:
+            flags |= abi.NOTE_MONITORING
+            hit = schedules.get(id(times))
+            if hit is None:
+                hit = schedules[id(times)] = (total, len(times))
+                monitoring.append(times)
+                total += len(times)
+            first, count = hit
+        rows.append((spot0, expiry, ki, upper, lower, maturity_coupon, period_coupon, fixed,
+                     principal, rebate, annual_rebate, effective, flags, _STATE_CODES[state],
+                     first_observation, len(obs), first, count))
+        first_observation += len(obs)
+    table = np.array(rows, NOTE_DTYPE) if rows else np.zeros(0, NOTE_DTYPE)
+    every = list(chain.from_iterable(map(operator.attrgetter("observations"), notes)))
+    k = len(every)
+    obs_table = np.zeros(k, NOTE_OBSERVATION_DTYPE)
+    if k:
+        knock_out = list(map(operator.attrgetter("knock_out_level"), every))
+        barrier = list(map(operator.attrgetter("coupon_barrier_level"), every))
+        has_knock_out = np.fromiter(map(operator.is_not, knock_out, repeat(None)), bool, k)
+        has_barrier = np.fromiter(map(operator.is_not, barrier, repeat(None)), bool, k)
+        obs_table["time"] = np.fromiter(map(operator.attrgetter("time"), every), np.float64, k)
+        obs_table["coupon_rate"] = np.fromiter(map(operator.attrgetter("coupon_rate"), every), np.float64, k)
+        # None reads as NaN here and is zeroed; a given level keeps its value
+        obs_table["knock_out_level"] = np.where(has_knock_out, np.array(knock_out, np.float64), 0.0)
+        obs_table["coupon_barrier_level"] = np.where(has_barrier, np.array(barrier, np.float64), 0.0)
+        obs_table["flags"] = (has_knock_out * abi.OBSERVATION_KNOCK_OUT
+                              + has_barrier * abi.OBSERVATION_COUPON_BARRIER)
+    mon = (np.concatenate([np.asarray(t, np.float64) for t in monitoring]) if monitoring
+           else np.zeros(0, np.float64))
+    return NoteTables(table, obs_table, mon)
+
+
+class SharedPlan:
+    """The native plan of a book on shared daily grids (kgpu_shared_plan_create): which
+    notes are lanes of which group, each group's packed lane contracts, and the coupon
+    families' interpolation.  Holds the library's plan until closed."""
+
+    def __init__(self, tables: NoteTables, model: abi.Model, simulate: Optional[np.ndarray] = None):
+        from . import _native
+        from .errors import raise_for_status
+        self.lib = lib = _native.library()
+        self.tables = tables
+        P = C.POINTER
+        mask = None
+        if simulate is not None:
+            self._simulate = np.ascontiguousarray(simulate, np.uint8)
+            mask = self._simulate.ctypes.data_as(P(C.c_uint8))
+        handle = C.c_void_p()
+        status = lib.kgpu_shared_plan_create(
+            C.byref(model), tables.notes.ctypes.data_as(P(abi.Note)), len(tables.notes),
+            tables.observations.ctypes.data_as(P(abi.NoteObservation)), len(tables.observations),
+            tables.monitoring.ctypes.data_as(P(C.c_double)), len(tables.monitoring), mask,
+            C.byref(handle))
+        if status != 0:
+            raise_for_status(status, lib.kgpu_last_error_message(None).decode())
+        self.handle = handle
+        view = abi.SharedPlanView()
+        lib.kgpu_shared_plan_get(handle, C.byref(view))
+        self.view = view
+        n, g, k = view.note_count, view.group_count, view.lane_count
+        self.note_group = np.ctypeslib.as_array(view.note_group, (n,)).copy() if n else np.zeros(0, np.int32)
+        self.group_first_lane = np.ctypeslib.as_array(view.group_first_lane, (g + 1,)).copy()
+        self.lane_note = np.ctypeslib.as_array(view.lane_note, (k,)).copy() if k else np.zeros(0, np.int32)
+        self.lane_fp32 = (np.ctypeslib.as_array(view.lane_fp32, (k,)).astype(bool) if k
+                          else np.zeros(0, bool))
+        self.group_count = g
+
+    def group_lanes(self, g: int) -> np.ndarray:
+        """Book indices of group g's simulated lanes, in contract order."""
+        return self.lane_note[self.group_first_lane[g]:self.group_first_lane[g + 1]]
+
+    def group_fp32(self, g: int) -> np.ndarray:
+        return self.lane_fp32[self.group_first_lane[g]:self.group_first_lane[g + 1]]
+
+    def group_book(self, g: int) -> abi.Book:
+        """Group g's kgpu_book (the library's arrays); raises the group's planning failure."""
+        from .errors import raise_for_status
+        status = self.view.group_status[g]
+        if status != 0:
+            raise_for_status(status, self.view.group_message[g].decode())
+        return self.view.group_books[g]
+
+    def group_packed(self, g: int) -> plans.PackedBook:
+        """A numpy copy of group g's book (for the oracle and for device-resident runs)."""
+        b = self.group_book(g)
+
+        def take(ptr, ctype, dtype, n):
+            if n == 0 or not ptr:
+                return np.zeros(0, dtype)
+            raw = (ctype * n).from_address(C.cast(ptr, C.c_void_p).value)
+            return np.frombuffer(raw, dtype).copy()
+        steps = int(b.step_total)
+        return plans.PackedBook(take(b.contracts, abi.Contract, plans.CONTRACT_DTYPE, b.contract_count),
+                                take(b.steps, abi.Step, plans.STEP_DTYPE, steps),
+                                take(b.step_flags, C.c_uint8, np.uint8, steps),
+                                take(b.events, abi.Event, plans.EVENT_DTYPE, b.event_total),
+                                take(b.intervals, abi.BridgeInterval, plans.INTERVAL_DTYPE, b.interval_total),
+                                take(b.bridge_daily, abi.BridgeDaily, plans.DAILY_DTYPE, steps))
+
+    def interpolate(self, prices: np.ndarray) -> np.ndarray:
+        """Fills the interpolated members of `prices` (float64, one per note, every
+        simulated lane's price set); returns the mask of members to simulate instead."""
+        retry = np.zeros(len(prices), np.uint8)
+        self.lib.kgpu_shared_plan_interpolate(
+            self.handle, prices.ctypes.data_as(C.POINTER(C.c_double)),
+            retry.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return retry.astype(bool)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.kgpu_shared_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _price_many_planned(engine, notes: Sequence[AutocallableNote], ctx: PricingContext) -> List[float]:
+    """price_many on a shared daily grid with the native planner.  The scalar quotes are
+    planned first (their errors raise in book order, as plan_book's do), then every group
+    runs on the path-major schedule, then the scalar quotes' launch, then the families'
+    interpolation; members whose interpolation cancels are simulated after all."""
+    if len(notes) > MAX_CONTRACTS:
+        raise InvalidInputError("contract batch exceeds 1,048,576 instruments")
+    tables = note_tables(notes)
+    model = ctx.kgpu_model()
+    plan = SharedPlan(tables, model)
+    prices = np.full(len(notes), np.nan)
+    scalar = np.flatnonzero(plan.note_group < 0)
+    batch = [plans.autocallable(notes[i], ctx) for i in scalar]
+    pending = range(plan.group_count)
+    simulate = None
+    try:
+        while True:
+            for g in pending:
+                estimates = engine._run_shared_book(ctx, plan.group_book(g), plan.group_fp32(g))
+                prices[plan.group_lanes(g)] = [e.price for e in estimates]
+            if batch:
+                for i, e in zip(scalar, engine._run(ctx, batch)):
+                    prices[i] = e.price
+                batch = []
+            retry = plan.interpolate(prices)
+            if not retry.any():
+                return prices.tolist()
+            simulate = retry if simulate is None else (simulate | retry)
+            plan.close()
+            plan = SharedPlan(tables, model, simulate)
+            pending = sorted(set(plan.note_group[retry].tolist()))
+    finally:
+        plan.close()

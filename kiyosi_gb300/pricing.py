@@ -132,6 +132,43 @@ class _MonteCarloEngine:
         path per sample settles every lane)."""
         return self._run(ctx, lane_plans, schedule=abi.SCHEDULE_SHARED_GRID)
 
+    def _run_shared_book(self, ctx: PricingContext, book: abi.Book, lane_fp32):
+        """Prices the lanes of one shared daily grid from a packed group book (the native
+        planner's, portfolio.SharedPlan) with the path-major schedule.  As in _run, FP32
+        lanes whose plan FP32 cannot carry are priced by the FP64 kernels in a second
+        launch."""
+        seed = _resolve_seed(self.seed)
+        settings = self._settings(seed)
+        settings.schedule = abi.SCHEDULE_SHARED_GRID
+        n = book.contract_count
+        parts = [(settings, list(range(n)))]
+        if settings.precision == abi.PRECISION_FP32:
+            model_ok = plans.fp32_model_ok(ctx)
+            wide = [j for j in range(n) if not (model_ok and lane_fp32[j])]
+            if wide:
+                fp64 = abi.Settings.from_buffer_copy(settings)
+                fp64.precision = abi.PRECISION_FP64
+                narrow = sorted(set(range(n)) - set(wide))
+                parts = [(settings, narrow), (fp64, wide)]
+        native = context(self.device)
+        model = ctx.kgpu_model()
+        results = [None] * n
+        for part_settings, members in parts:
+            if not members:
+                continue
+            sub = book
+            if len(members) != n:
+                chosen = (abi.Contract * len(members))(*[book.contracts[j] for j in members])
+                sub = abi.Book.from_buffer_copy(book)
+                sub.contract_count = len(members)
+                sub.contracts = C.cast(chosen, C.POINTER(abi.Contract))
+            out = (abi.Estimate * len(members))()
+            native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(sub),
+                                                    C.byref(part_settings), out, None))
+            for k, j in enumerate(members):
+                results[j] = MonteCarloEstimate.from_native(out[k])
+        return results
+
     def _run(self, ctx: PricingContext, contract_plans, path_counts=None, cancel=None, schedule=None):
         """Prices plans (Known or ContractPlan) through kgpu_price_book."""
         seed = _resolve_seed(self.seed)
