@@ -368,6 +368,10 @@ const char* kgpu_last_error_message(const kgpu_context* ctx);
  * entries.  `cancel_flag` (may be NULL) is polled between launches and by persistent
  * kernels once per work item through host-mapped memory; a nonzero value ends the call
  * with KGPU_INTERRUPTED and no partial result (cancellation.rs:33-100).
+ * The persistent schedules run their launch sequence (plan compilation, path kernel,
+ * fixed-order reduction) as a CUDA graph once two consecutive calls on the context share
+ * their model, settings, contract table and book arrays; the book's contents are read at
+ * every launch, so a caller may change them between calls (see kgpu_context_last_graph).
  * Replaces PricingEngine::price_with_statistics of the MC engines and
  * MonteCarloAutocallableEngine::price_many (autocallable.rs:119-125). */
 kgpu_status kgpu_price_book(kgpu_context* ctx, const kgpu_model* model, const kgpu_book* book,
@@ -613,6 +617,12 @@ int32_t kgpu_context_last_launches(const kgpu_context* ctx);
 /* Device time of the last pricing call's path kernels alone (the plain or persistent
  * kernel launches, without plan compilation and reductions), summed over launches. */
 double kgpu_context_last_path_kernel_ms(const kgpu_context* ctx);
+/* How the last kgpu_price_book call ran its launch sequence (no counterpart in the
+ * reference): 0 launched directly, 1 captured into a CUDA graph and launched, 2 replayed
+ * that graph.  The persistent schedules capture on the second of two consecutive calls
+ * with the same model, settings, contract table and book arrays, and replay while the
+ * calls keep them; any other call on the context drops the graph. */
+int32_t kgpu_context_last_graph(const kgpu_context* ctx);
 
 /* Throughput of the device's pipes, measured on `ctx`'s device (no counterpart in the
  * reference: the denominators of the benchmark's op-model roofline).  rates[0..4], in

@@ -59,6 +59,11 @@ class Context:
     def last_launches(self) -> int:
         return self.lib.kgpu_context_last_launches(self.handle)
 
+    @property
+    def last_graph(self) -> int:
+        """0: the last book call launched directly; 1: captured its sequence; 2: replayed it."""
+        return self.lib.kgpu_context_last_graph(self.handle)
+
     def close(self):
         if self.handle:
             self.lib.kgpu_context_destroy(self.handle)

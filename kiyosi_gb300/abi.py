@@ -221,7 +221,7 @@ EXPORTED_SYMBOLS = (
     "kgpu_context_last_launches", "kgpu_abi_version", "kgpu_device_count", "kgpu_pipe_rates",
     "kgpu_price_contract_noalloc", "kgpu_mlp_gradients", "kgpu_mlp_train", "kgpu_lsmc_price_scenarios",
     "kgpu_shared_plan_create", "kgpu_shared_plan_get", "kgpu_shared_plan_interpolate",
-    "kgpu_shared_plan_destroy",
+    "kgpu_shared_plan_destroy", "kgpu_context_last_graph",
 )
 MLP_PARAMS = 4481
 
@@ -261,6 +261,8 @@ def declare(lib):
     lib.kgpu_context_last_path_kernel_ms.restype = C.c_double
     lib.kgpu_context_last_launches.argtypes = [V]
     lib.kgpu_context_last_launches.restype = _I
+    lib.kgpu_context_last_graph.argtypes = [V]
+    lib.kgpu_context_last_graph.restype = _I
     lib.kgpu_price_contract_noalloc.argtypes = [_P(Model), _P(Book), _I, _P(Settings),
                                                 _P(Estimate), V]
     lib.kgpu_price_contract_noalloc.restype = _I

@@ -142,8 +142,13 @@ static kgpu_status fail(kgpu_context* ctx, kgpu_status status, const char* fmt, 
             return fail(ctx, KGPU_DEVICE_ERROR, "%s: %s", #expr, cudaGetErrorString(_e));    \
     } while (0)
 
+static std::atomic<uint64_t> g_alloc_generation{0};
+
+uint64_t kgpu::alloc_generation() { return g_alloc_generation.load(); }
+
 kgpu_status DeviceBuffer::ensure(size_t n) {
     if (n <= bytes) return KGPU_OK;
+    g_alloc_generation.fetch_add(1);
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     bytes = 0;
@@ -157,6 +162,7 @@ kgpu_status DeviceBuffer::ensure(size_t n) {
 }
 
 void DeviceBuffer::release() {
+    if (ptr) g_alloc_generation.fetch_add(1);
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     bytes = 0;
@@ -164,6 +170,9 @@ void DeviceBuffer::release() {
 
 static kgpu_status upload(kgpu_context* ctx, DeviceBuffer& buf, const void* src, size_t bytes) {
     if (bytes == 0) return KGPU_OK;
+    // A capture pass follows a direct call with the same key, which staged exactly these
+    // bytes in the same buffer: nothing to copy (and a pageable copy cannot be captured).
+    if (ctx->capturing) return buf.bytes >= bytes ? KGPU_OK : KGPU_DEVICE_ERROR;
     if (buf.ensure(bytes) != KGPU_OK)
         return fail(ctx, KGPU_DEVICE_ERROR, "cudaMalloc of %zu bytes failed", bytes);
     CUDA_TRY(ctx, cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -225,6 +234,7 @@ void kgpu_context_destroy(kgpu_context* ctx) {
         cudaEventDestroy(e.second);
     }
     if (ctx->lsmc_exec) cudaGraphExecDestroy(ctx->lsmc_exec);
+    if (ctx->book_exec) cudaGraphExecDestroy(ctx->book_exec);
     for (cudaEvent_t e : ctx->lsmc_events)
         if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
@@ -238,6 +248,7 @@ const char* kgpu_last_error_message(const kgpu_context* ctx) {
 double kgpu_context_last_kernel_ms(const kgpu_context* ctx) { return ctx ? ctx->last_kernel_ms : 0.0; }
 double kgpu_context_last_path_kernel_ms(const kgpu_context* ctx) { return ctx ? ctx->last_path_kernel_ms : 0.0; }
 int32_t kgpu_context_last_launches(const kgpu_context* ctx) { return ctx ? ctx->last_launches : 0; }
+int32_t kgpu_context_last_graph(const kgpu_context* ctx) { return ctx ? ctx->last_graph : 0; }
 
 }  // extern "C"
 
@@ -258,11 +269,15 @@ cudaError_t path_kernel_begin(kgpu_context* ctx) {
         }
         ctx->path_events.push_back(e);
     }
-    return cudaEventRecord(ctx->path_events[ctx->path_events_used].first, ctx->stream);
+    // Inside a capture the record must be an external node of the graph, so that every
+    // replay records the event; outside one the flag is refused.
+    return cudaEventRecordWithFlags(ctx->path_events[ctx->path_events_used].first, ctx->stream,
+                                    ctx->capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
 }
 
 cudaError_t path_kernel_end(kgpu_context* ctx) {
-    return cudaEventRecord(ctx->path_events[ctx->path_events_used++].second, ctx->stream);
+    return cudaEventRecordWithFlags(ctx->path_events[ctx->path_events_used++].second, ctx->stream,
+                                    ctx->capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
 }
 
 // Sum of the recorded path-kernel times; call after the stream has been synchronised.
@@ -664,30 +679,49 @@ kgpu_status stage_values(Call& k, int* chunk_count) {
 
 // Sums the per-path values in a fixed order, reads the sums, the simulated positions and
 // the cancellation state back, and forms the estimates.
+// Ends a capture pass: instantiates the recorded launch sequence and launches it (none of
+// it has run yet).  On failure the call is repeated without capture (run_book).
+kgpu_status end_book_capture(kgpu_context* ctx) {
+    cudaGraph_t graph = nullptr;
+    ctx->capturing = false;
+    const bool recorded = cudaStreamEndCapture(ctx->stream, &graph) == cudaSuccess && graph;
+    cudaGraphExec_t exec = nullptr;
+    if (recorded && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+    if (graph) cudaGraphDestroy(graph);
+    if (exec && cudaGraphLaunch(exec, ctx->stream) != cudaSuccess) {
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
+    }
+    if (!exec) {
+        cudaGetLastError();
+        ctx->capture_failed = true;
+        return fail(ctx, KGPU_DEVICE_ERROR, "the launch sequence could not be captured");
+    }
+    ctx->book_exec = exec;
+    return KGPU_OK;
+}
+
+// Reads back a persistent or phase-major call's per-contract sums and counters, its
+// cancellation word and, for the phase-major kernel, its grid-barrier failure word
+// (phase_counts[failed_slot]), and turns the sums into estimates.
 template <class Real>
-kgpu_status finish_values(Call& k, int chunk_count, int& launches) {
+kgpu_status collect_values(Call& k, int failed_slot) {
     kgpu_context* ctx = k.ctx;
     const kgpu_settings& s = k.s;
     const int n = k.raw.contract_count;
-    reduce_values_kernel<Real><<<chunk_count, 256, 0, ctx->stream>>>(
-        static_cast<const Real*>(ctx->values.ptr), static_cast<const int4*>(ctx->chunks.ptr),
-        static_cast<const int64_t*>(ctx->value_offset.ptr), static_cast<TilePartial*>(ctx->tiles.ptr));
-    CUDA_TRY(ctx, cudaGetLastError());
-    reduce_tiles_kernel<<<n, 256, 0, ctx->stream>>>(static_cast<const TilePartial*>(ctx->tiles.ptr),
-                                                     static_cast<const int*>(ctx->first_item.ptr),
-                                                     static_cast<TilePartial*>(ctx->tile_out.ptr));
-    CUDA_TRY(ctx, cudaGetLastError());
-    launches += 2;
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev_stop, ctx->stream));
     std::vector<TilePartial> sums(n);
     std::vector<unsigned long long> executed(n);
-    int aborted = 0;
+    int aborted = 0, failed = 0;
     CUDA_TRY(ctx, cudaMemcpyAsync(sums.data(), ctx->tile_out.ptr, sizeof(TilePartial) * n, cudaMemcpyDeviceToHost,
                                   ctx->stream));
     CUDA_TRY(ctx, cudaMemcpyAsync(executed.data(), ctx->executed.ptr, sizeof(unsigned long long) * n,
                                   cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_TRY(ctx, cudaMemcpyAsync(&aborted, static_cast<int*>(ctx->queue.ptr) + 1, sizeof(int),
                                   cudaMemcpyDeviceToHost, ctx->stream));
+    if (failed_slot >= 0)
+        CUDA_TRY(ctx, cudaMemcpyAsync(&failed, static_cast<int*>(ctx->phase_counts.ptr) + failed_slot, sizeof(int),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     if (aborted) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
     for (int i = 0; i < n; ++i) {
@@ -701,7 +735,30 @@ kgpu_status finish_values(Call& k, int chunk_count, int& launches) {
             return fail(ctx, KGPU_COMPUTATION_FAILURE,
                         "Monte Carlo produced a non-finite parameter, path or result (contract %d)", i);
     }
+    if (failed) return fail(ctx, KGPU_DEVICE_ERROR, "the phase-major kernel's grid barrier timed out");
     return KGPU_OK;
+}
+
+// Reduces the per-path values in a fixed order, ends a capture pass, then collects.
+template <class Real>
+kgpu_status finish_values(Call& k, int chunk_count, int& launches, int failed_slot = -1) {
+    kgpu_context* ctx = k.ctx;
+    const int n = k.raw.contract_count;
+    reduce_values_kernel<Real><<<chunk_count, 256, 0, ctx->stream>>>(
+        static_cast<const Real*>(ctx->values.ptr), static_cast<const int4*>(ctx->chunks.ptr),
+        static_cast<const int64_t*>(ctx->value_offset.ptr), static_cast<TilePartial*>(ctx->tiles.ptr));
+    CUDA_TRY(ctx, cudaGetLastError());
+    reduce_tiles_kernel<<<n, 256, 0, ctx->stream>>>(static_cast<const TilePartial*>(ctx->tiles.ptr),
+                                                     static_cast<const int*>(ctx->first_item.ptr),
+                                                     static_cast<TilePartial*>(ctx->tile_out.ptr));
+    CUDA_TRY(ctx, cudaGetLastError());
+    launches += 2;
+    ctx->book_failed_slot = failed_slot;
+    if (ctx->capturing) {
+        kgpu_status st = end_book_capture(ctx);
+        if (st != KGPU_OK) return st;
+    }
+    return collect_values<Real>(k, failed_slot);
 }
 
 template <class Real>
@@ -933,15 +990,9 @@ kgpu_status run_phased_impl(Call& k, DevBook<Real> db, int& launches) {
     CUDA_TRY(ctx, path_kernel_begin(ctx));
     CUDA_TRY(ctx, launch_phased_fp32(grid, ctx->stream, a));
     launches += 1;
-    int failed = 0;
-    CUDA_TRY(ctx, cudaMemcpyAsync(&failed, static_cast<int*>(ctx->phase_counts.ptr) + phases + 4, sizeof(int),
-                                  cudaMemcpyDeviceToHost, ctx->stream));
     CUDA_TRY(ctx, path_kernel_end(ctx));
-    kgpu_status done = finish_values<Real>(k, chunk_count, launches);
-    // `failed` arrived with finish_values' synchronisation.
-    if (done == KGPU_OK && failed)
-        return fail(ctx, KGPU_DEVICE_ERROR, "the phase-major kernel's grid barrier timed out");
-    return done;
+    // phase_counts[phases + 4] is the grid barrier's failure word, read with the sums
+    return finish_values<Real>(k, chunk_count, launches, phases + 4);
 }
 
 template <class Real>
@@ -1096,6 +1147,70 @@ kgpu_status run_shared(Call& k, const DevBook<Real>& db, const SharedPlan& plan,
     return KGPU_OK;
 }
 
+// Key of a persistent call's launch sequence: everything its launches and its staged
+// metadata derive from -- the model's scalars, the settings, the book's device arrays and
+// sizes, the host contract table, whether a cancellation word is watched, the cached
+// Sobol sequence and the device buffers' addresses (through their reallocation count).
+std::vector<unsigned char> book_call_key(const Call& k) {
+    std::vector<unsigned char> key;
+    auto put = [&key](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), b, b + n);
+    };
+    kgpu_model m = *k.model;
+    m.lv_times = m.lv_spots = m.lv_values = nullptr;
+    put(&m, sizeof(m));
+    put(&k.s, sizeof(k.s));
+    const RawBook& r = k.raw;
+    const void* ptrs[] = {r.contracts, r.steps, r.flags, r.events, r.intervals, r.daily, k.lv_dev};
+    put(ptrs, sizeof(ptrs));
+    const int64_t sizes[] = {r.contract_count,
+                             r.step_total,
+                             r.event_total,
+                             r.interval_total,
+                             k.lv_values,
+                             k.cancel ? 1 : 0,
+                             k.ctx->sobol_dims,
+                             int64_t(k.ctx->sobol_seed),
+                             k.ctx->sobol_high_t_blocks,
+                             int64_t(kgpu::alloc_generation())};
+    put(sizes, sizeof(sizes));
+    put(k.book->contracts, sizeof(kgpu_contract) * size_t(r.contract_count));
+    return key;
+}
+
+// A call whose key equals the captured sequence's: launch the graph and collect.
+template <class Real>
+kgpu_status replay_book(Call& k) {
+    kgpu_context* ctx = k.ctx;
+    ctx->last_path_kernel_ms = 0.0;
+    if (k.cancel && *k.cancel) return fail(ctx, KGPU_INTERRUPTED, "cancelled");
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    kgpu_status st;
+    {
+        CancelWatcher watcher(k.cancel, ctx->cancel_host);
+        CUDA_TRY(ctx, cudaGraphLaunch(ctx->book_exec, ctx->stream));
+        ctx->path_events_used = ctx->book_path_events;
+        st = collect_values<Real>(k, ctx->book_failed_slot);
+    }
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop) == cudaSuccess) ctx->last_kernel_ms = ms;
+    if (st == KGPU_OK) ctx->last_path_kernel_ms = path_kernel_ms(ctx);
+    cudaGetLastError();
+    ctx->last_launches = ctx->book_launches;
+    return st;
+}
+
+template <class Real>
+kgpu_status run_direct(Call& k, const SharedPlan& shared, bool capture);
+
+// Prices a staged book.  The persistent schedules' launch sequence runs as a CUDA graph:
+// the first call with a key runs directly and stages the sequence's metadata on the
+// device; an identical second call captures the sequence (its uploads would copy the same
+// bytes into the same buffers, so they are skipped) and launches the graph; later
+// identical calls replay it.  Any other call on the context drops the graph.  Lane-refill
+// Sobol books of several dimension counts (one launch per count, synchronised in between)
+// run directly.
 template <class Real>
 kgpu_status run_book(Call& k) {
     kgpu_context* ctx = k.ctx;
@@ -1104,9 +1219,66 @@ kgpu_status run_book(Call& k) {
         kgpu_status planned = plan_shared(k, &shared);
         if (planned) return planned;
     }
+    bool graphable = k.s.schedule == KGPU_SCHEDULE_PERSISTENT || k.s.schedule == KGPU_SCHEDULE_LANE_REFILL;
+    if (graphable && k.sobol && !(k.s.schedule == KGPU_SCHEDULE_PERSISTENT && phased_eligible(k)))
+        for (const ContractInfo& ci : k.info) graphable = graphable && ci.dims == k.info[0].dims;
+    std::vector<unsigned char> key;
+    if (graphable) key = book_call_key(k);
+    ctx->last_graph = 0;
+    if (graphable && ctx->book_exec && ctx->book_key == key) {
+        ctx->last_graph = 2;
+        return replay_book<Real>(k);
+    }
+    if (ctx->book_exec) cudaGraphExecDestroy(ctx->book_exec);
+    ctx->book_exec = nullptr;
+    ctx->book_key.clear();
+    const bool capture = graphable && ctx->last_book_key == key;
+    ctx->last_book_key = key;
+    ctx->capture_failed = false;
+    kgpu_status st = run_direct<Real>(k, shared, capture);
+    if (capture && (ctx->capturing || ctx->capture_failed)) {
+        // The sequence could not be captured (an error inside the pass, or a refused
+        // capture): nothing of it ran.  Repeat the call directly.
+        if (ctx->capturing) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(ctx->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            ctx->capturing = false;
+        }
+        cudaGetLastError();
+        ctx->error.clear();
+        ctx->capture_failed = false;
+        ctx->last_book_key.clear();
+        if (ctx->book_exec) cudaGraphExecDestroy(ctx->book_exec);
+        ctx->book_exec = nullptr;
+        st = run_direct<Real>(k, shared, false);
+    } else if (capture && ctx->book_exec) {
+        if (st == KGPU_OK) {
+            ctx->book_key = key;
+            ctx->book_launches = ctx->last_launches;
+            ctx->book_path_events = ctx->path_events_used;
+            ctx->last_graph = 1;
+        } else {
+            cudaGraphExecDestroy(ctx->book_exec);
+            ctx->book_exec = nullptr;
+        }
+    }
+    return st;
+}
+
+template <class Real>
+kgpu_status run_direct(Call& k, const SharedPlan& shared, bool capture) {
+    kgpu_context* ctx = k.ctx;
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
     ctx->path_events_used = 0;
     ctx->last_path_kernel_ms = 0.0;
+    if (capture) {
+        if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
+            ctx->capturing = true;
+        else
+            ctx->capture_failed = true;  // run_book repeats the call directly
+        if (!ctx->capturing) return KGPU_DEVICE_ERROR;
+    }
     DevBook<Real> db;
     kgpu_status st = compile_book<Real>(k, &db);
     if (st) return st;

@@ -25,6 +25,10 @@ void build_sobol(int dims, uint64_t seed, std::vector<uint64_t>& directions,
 // Records the calling thread's last error message (kgpu_last_error_message(NULL)).
 void set_thread_error(const char* message);
 
+// Reallocations of any DeviceBuffer so far: a captured launch sequence bakes in buffer
+// addresses, so it is replayed only while this count is unchanged.
+uint64_t alloc_generation();
+
 struct BlockPartial;
 // MonteCarloEstimate of one contract from its block-merged scaled moments.
 void estimate_from_moments(const kgpu_contract& c, const kgpu_settings& s, int64_t paths,
@@ -67,6 +71,18 @@ struct kgpu_context {
     cudaGraphExec_t lsmc_exec = nullptr;
     std::vector<unsigned char> lsmc_key;
     cudaEvent_t lsmc_events[4] = {nullptr, nullptr, nullptr, nullptr};
+    // The persistent schedules' launch sequence as a CUDA graph: captured on the second
+    // of two consecutive calls with one key (the first one staged the sequence's metadata
+    // on the device) and replayed while the calls keep that key.
+    cudaGraphExec_t book_exec = nullptr;
+    std::vector<unsigned char> book_key;       // key of book_exec
+    std::vector<unsigned char> last_book_key;  // key of the previous direct call
+    bool capturing = false;                    // a capture pass is recording
+    bool capture_failed = false;               // the capture pass could not be completed
+    int book_launches = 0;                     // launches the graph holds
+    size_t book_path_events = 0;               // path-kernel event pairs it records
+    int book_failed_slot = -1;                 // phase_counts word of a grid-barrier timeout
+    int last_graph = 0;                        // the last call: 0 direct, 1 captured, 2 replayed
     // cancellation word mirrored into host-mapped memory for persistent kernels
     volatile int* cancel_host = nullptr;
     int* cancel_dev = nullptr;
