@@ -251,6 +251,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         device_call(s32)
     kernel_ms, path_ms, launches = [], [], 0
+    graph_modes = []
     est32 = None
     with Clocks(ranks.device) as clocks:
         ranks.barrier()
@@ -260,6 +261,7 @@ def run_ours(args):
             kernel_ms.append(ms)
             path_ms.append(pk)
             launches += nl
+            graph_modes.append(native.last_graph)
         ranks.barrier()
     clock = clocks.summary()
     total_ms = ranks.max(sum(kernel_ms))
@@ -332,6 +334,10 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": "path-steps/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
+        "launch_sequence": {"cuda_graph_replays": graph_modes.count(2), "captures": graph_modes.count(1),
+                            "direct": graph_modes.count(0),
+                            "note": "timed calls: the persistent schedule's sequence (plan compile, path "
+                                    "kernel, fixed-order reduction) replayed as one CUDA graph"},
         "clocks": clock,
         "roofline": roofline,
         "executed_path_steps_per_s": executed * args.steps / (total_ms / 1e3) * ranks.world,
