@@ -7,9 +7,11 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -316,29 +318,66 @@ bool fp32_value(double v) {
 
 // Whether FP32 kernels can carry contract c of a host book (every double field of the
 // contract, its steps, events, bridge records and the model).
-bool fp32_representable(const kgpu_model* m, const kgpu_book* b, const kgpu_contract& c) {
+// Checks of a host book over ranges of its step, flag, bridge-weight and interval arrays,
+// each computed once per distinct range: contracts that share a segment (the lanes of a
+// shared daily grid) share the result.
+struct RangeChecks {
+    const kgpu_book* b;
+    std::map<std::tuple<int64_t, int, bool>, bool> steps_fp32;
+    std::map<std::pair<int, int>, bool> intervals_fp32;
+    std::map<std::pair<int64_t, int>, int> event_steps;
+
+    bool steps_ok(const kgpu_contract& c) {
+        const bool bridged = b->bridge_daily && (c.flags & KGPU_C_BRIDGE);
+        const auto key = std::make_tuple(c.step_offset, c.step_count, bridged);
+        auto hit = steps_fp32.find(key);
+        if (hit != steps_fp32.end()) return hit->second;
+        bool ok = true;
+        for (int64_t q = c.step_offset; ok && q < c.step_offset + c.step_count; ++q) {
+            const kgpu_step& st = b->steps[q];
+            ok = fp32_value(st.drift) && fp32_value(st.diffusion) && fp32_value(st.discount) &&
+                 (!bridged || (fp32_value(b->bridge_daily[q].weight) && fp32_value(b->bridge_daily[q].width)));
+        }
+        steps_fp32.emplace(key, ok);
+        return ok;
+    }
+    bool intervals_ok(const kgpu_contract& c) {
+        const auto key = std::make_pair(c.bridge_offset, c.bridge_count);
+        auto hit = intervals_fp32.find(key);
+        if (hit != intervals_fp32.end()) return hit->second;
+        bool ok = true;
+        for (int q = c.bridge_offset; ok && q < c.bridge_offset + c.bridge_count; ++q)
+            ok = fp32_value(b->intervals[q].drift) && fp32_value(b->intervals[q].diffusion);
+        intervals_fp32.emplace(key, ok);
+        return ok;
+    }
+    // Steps flagged KGPU_STEP_EVENT in the contract's range.
+    int events(const kgpu_contract& c) {
+        const auto key = std::make_pair(c.step_offset, c.step_count);
+        auto hit = event_steps.find(key);
+        if (hit != event_steps.end()) return hit->second;
+        int n = 0;
+        for (int q = 0; q < c.step_count; ++q) n += (b->step_flags[c.step_offset + q] & KGPU_STEP_EVENT) != 0;
+        event_steps.emplace(key, n);
+        return n;
+    }
+};
+
+bool fp32_representable(const kgpu_model* m, const kgpu_book* b, const kgpu_contract& c, RangeChecks& ranges) {
     const double* first = &c.strike;
     const double* last = &c.greek_log_weight;
     for (const double* v = first; v <= last; ++v)
         if (!fp32_value(*v)) return false;
     for (double v : {m->spot, m->rate, m->dividend, m->volatility, m->v0, m->kappa, m->theta, m->xi, m->rho})
         if (!fp32_value(v)) return false;
-    for (int64_t q = c.step_offset; q < c.step_offset + c.step_count; ++q) {
-        const kgpu_step& st = b->steps[q];
-        if (!fp32_value(st.drift) || !fp32_value(st.diffusion) || !fp32_value(st.discount)) return false;
-        if (b->bridge_daily && (c.flags & KGPU_C_BRIDGE) &&
-            (!fp32_value(b->bridge_daily[q].weight) || !fp32_value(b->bridge_daily[q].width)))
-            return false;
-    }
+    if (!ranges.steps_ok(c)) return false;
     for (int q = c.event_offset; q < c.event_offset + c.event_count; ++q) {
         const kgpu_event& e = b->events[q];
         if (!fp32_value(e.knock_out) || !fp32_value(e.coupon_barrier)) return false;
         for (double v : e.payment)
             if (!fp32_value(v)) return false;
     }
-    if (c.flags & KGPU_C_BRIDGE)
-        for (int q = c.bridge_offset; q < c.bridge_offset + c.bridge_count; ++q)
-            if (!fp32_value(b->intervals[q].drift) || !fp32_value(b->intervals[q].diffusion)) return false;
+    if ((c.flags & KGPU_C_BRIDGE) && !ranges.intervals_ok(c)) return false;
     return true;
 }
 
@@ -1025,6 +1064,7 @@ kgpu_status plan_shared(Call& k, SharedPlan* plan) {
     for (int q = 0; q < bc.bridge_count; ++q) ends[b.intervals[bc.bridge_offset + q].end] = 1;
     std::vector<int16_t> slot(steps, -1);
     int slots = 0;
+    std::map<std::tuple<int64_t, int, int, int>, bool> prefixes;
     auto take = [&](int step) {
         if (step < 0 || step >= steps || !ends[step]) return false;
         if (slot[step] < 0) slot[step] = int16_t(slots++);
@@ -1036,15 +1076,26 @@ kgpu_status plan_shared(Call& k, SharedPlan* plan) {
             return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "lane %d: shared-grid lanes are bridged autocallables", i);
         if (k.info[i].dims != k.info[base].dims || k.info[i].paths != k.info[base].paths)
             return fail(ctx, KGPU_INVALID_INPUT, "lane %d: lanes share their sampling dimensions and path count", i);
-        bool prefix = c.bridge_count <= bc.bridge_count &&
-                      std::memcmp(b.steps + c.step_offset, b.steps + bc.step_offset,
-                                  sizeof(kgpu_step) * size_t(c.step_count)) == 0 &&
-                      std::memcmp(b.bridge_daily + c.step_offset, b.bridge_daily + bc.step_offset,
-                                  sizeof(kgpu_bridge_daily) * size_t(c.step_count)) == 0 &&
+        // Lanes that share a segment (or the base's own arrays) are compared once.
+        const auto seg = std::make_tuple(c.step_offset, c.step_count, c.bridge_offset, c.bridge_count);
+        auto known = prefixes.find(seg);
+        bool prefix;
+        if (known != prefixes.end()) {
+            prefix = known->second;
+        } else {
+            const bool same_steps = c.step_offset == bc.step_offset;
+            prefix = c.bridge_count <= bc.bridge_count &&
+                     (same_steps || (std::memcmp(b.steps + c.step_offset, b.steps + bc.step_offset,
+                                                 sizeof(kgpu_step) * size_t(c.step_count)) == 0 &&
+                                     std::memcmp(b.bridge_daily + c.step_offset, b.bridge_daily + bc.step_offset,
+                                                 sizeof(kgpu_bridge_daily) * size_t(c.step_count)) == 0)) &&
+                     (c.bridge_offset == bc.bridge_offset ||
                       std::memcmp(b.intervals + c.bridge_offset, b.intervals + bc.bridge_offset,
-                                  sizeof(kgpu_bridge_interval) * size_t(c.bridge_count)) == 0;
-        for (int q = 0; prefix && q < c.step_count; ++q)
-            prefix = ((b.step_flags[c.step_offset + q] ^ b.step_flags[bc.step_offset + q]) & KGPU_STEP_KNOCK_IN) == 0;
+                                  sizeof(kgpu_bridge_interval) * size_t(c.bridge_count)) == 0);
+            for (int q = 0; prefix && !same_steps && q < c.step_count; ++q)
+                prefix = ((b.step_flags[c.step_offset + q] ^ b.step_flags[bc.step_offset + q]) & KGPU_STEP_KNOCK_IN) == 0;
+            prefixes.emplace(seg, prefix);
+        }
         if (!prefix) return fail(ctx, KGPU_INVALID_INPUT, "lane %d: the grid is not a prefix of the longest lane's", i);
         for (int e = 0; e < c.event_count; ++e)
             if (!take(b.events[c.event_offset + e].step))
@@ -1337,6 +1388,7 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
         return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "the shared-grid schedule takes host books under BSM");
     // Validate contracts (MonteCarloSettings::validate, monte_carlo.rs:197-220).
     k.info.resize(n);
+    RangeChecks ranges{book, {}, {}, {}};
     for (int i = 0; i < n; ++i) {
         const kgpu_contract& c = book->contracts[i];
         int64_t paths = c.path_count > 0 ? c.path_count : s.path_count;
@@ -1386,13 +1438,12 @@ static kgpu_status price_book_impl(kgpu_context* ctx, const kgpu_model* model, c
         }
         if (!device_resident && c.payoff == KGPU_PAYOFF_AUTOCALLABLE) {
             // Every event step must be backed by an event record.
-            int events = 0;
-            for (int q = 0; q < c.step_count; ++q) events += (book->step_flags[c.step_offset + q] & KGPU_STEP_EVENT) != 0;
+            const int events = ranges.events(c);
             if (events != c.event_count)
                 return fail(ctx, KGPU_INVALID_INPUT, "contract %d: %d event steps but %d events", i, events,
                             c.event_count);
         }
-        if (s.precision == KGPU_PRECISION_FP32 && !device_resident && !fp32_representable(model, book, c))
+        if (s.precision == KGPU_PRECISION_FP32 && !device_resident && !fp32_representable(model, book, c, ranges))
             return fail(ctx, KGPU_UNSUPPORTED_OPERATION,
                         "contract %d: FP32 cannot carry this plan (a nonzero value below 2^-100 or above "
                         "2^120 in magnitude); price it in FP64",

@@ -41,9 +41,9 @@ restatement of the strip sums.
 import ctypes as C
 import math
 import operator
+import struct
 from dataclasses import dataclass, field, fields, replace
 from fractions import Fraction
-from itertools import chain, repeat
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -534,15 +534,19 @@ class NoteTables:
     monitoring: np.ndarray    # float64: every distinct monitoring schedule once
 
 
-def note_tables(notes: Sequence[AutocallableNote]) -> NoteTables:
-    """Flattens the notes' terms; notes sharing a monitoring schedule object share its
-    range of the monitoring table.  Observations are read column by column."""
-    rows = []
-    schedules: Dict[int, Tuple[int, int]] = {}
-    monitoring = []
-    total = 0
-    first_observation = 0
-    for note in notes:
+# kgpu_note: 12 doubles, then 6 int32; kgpu_note_observation: 4 doubles, then 2 int32
+# (little-endian, no padding; test_abi checks both sizes against the header).
+_NOTE_ROW = struct.Struct("<12d6i")
+_OBSERVATION_ROW = struct.Struct("<4d2i")
+
+
+def _note_encoding(note: AutocallableNote):
+    """The note's flat terms (the bytes of a kgpu_note without its table ranges) and the
+    bytes of its observation rows (None levels flagged absent).  Notes are frozen, so the
+    encoding is computed once per note object and kept on it, as Observation keeps its
+    hash."""
+    encoding = note.__dict__.get("_kgpu_encoding")
+    if encoding is None:
         (spot0, expiry, ki, upper, lower, maturity_coupon, period_coupon, fixed, principal,
          rebate, annual_rebate, effective, state, obs, times) = _NOTE_TERMS(note)
         flags = 0
@@ -554,38 +558,53 @@ def note_tables(notes: Sequence[AutocallableNote]) -> NoteTables:
             fixed = 0.0
         else:
             flags |= abi.NOTE_FIXED_COUPON
-        first = count = 0
         if times is not None:
             flags |= abi.NOTE_MONITORING
-            hit = schedules.get(id(times))
-            if hit is None:
-                hit = schedules[id(times)] = (total, len(times))
-                monitoring.append(times)
-                total += len(times)
-            first, count = hit
-        rows.append((spot0, expiry, ki, upper, lower, maturity_coupon, period_coupon, fixed,
-                     principal, rebate, annual_rebate, effective, flags, _STATE_CODES[state],
-                     first_observation, len(obs), first, count))
-        first_observation += len(obs)
-    table = np.array(rows, NOTE_DTYPE) if rows else np.zeros(0, NOTE_DTYPE)
-    every = list(chain.from_iterable(map(operator.attrgetter("observations"), notes)))
-    k = len(every)
-    obs_table = np.zeros(k, NOTE_OBSERVATION_DTYPE)
-    if k:
-        knock_out = list(map(operator.attrgetter("knock_out_level"), every))
-        barrier = list(map(operator.attrgetter("coupon_barrier_level"), every))
-        has_knock_out = np.fromiter(map(operator.is_not, knock_out, repeat(None)), bool, k)
-        has_barrier = np.fromiter(map(operator.is_not, barrier, repeat(None)), bool, k)
-        obs_table["time"] = np.fromiter(map(operator.attrgetter("time"), every), np.float64, k)
-        obs_table["coupon_rate"] = np.fromiter(map(operator.attrgetter("coupon_rate"), every), np.float64, k)
-        # None reads as NaN here and is zeroed; a given level keeps its value
-        obs_table["knock_out_level"] = np.where(has_knock_out, np.array(knock_out, np.float64), 0.0)
-        obs_table["coupon_barrier_level"] = np.where(has_barrier, np.array(barrier, np.float64), 0.0)
-        obs_table["flags"] = (has_knock_out * abi.OBSERVATION_KNOCK_OUT
-                              + has_barrier * abi.OBSERVATION_COUPON_BARRIER)
+        row = _NOTE_ROW.pack(spot0, expiry, ki, upper, lower, maturity_coupon, period_coupon, fixed,
+                             principal, rebate, annual_rebate, effective, flags, _STATE_CODES[state],
+                             0, len(obs), 0, 0)
+        pack = _OBSERVATION_ROW.pack
+        rows = []
+        for o in obs:
+            ko, cb = o.knock_out_level, o.coupon_barrier_level
+            rows.append(pack(o.time, 0.0 if ko is None else ko, 0.0 if cb is None else cb, o.coupon_rate,
+                             (0 if ko is None else abi.OBSERVATION_KNOCK_OUT)
+                             | (0 if cb is None else abi.OBSERVATION_COUPON_BARRIER), 0))
+        encoding = (row, b"".join(rows))
+        object.__setattr__(note, "_kgpu_encoding", encoding)
+    return encoding
+
+
+def note_tables(notes: Sequence[AutocallableNote]) -> NoteTables:
+    """Flattens the notes' terms into kgpu_shared_plan_create's tables: the notes'
+    encodings stacked, their observation ranges, and each distinct monitoring schedule
+    once (notes sharing a schedule object share its range)."""
+    if not notes:
+        return NoteTables(np.zeros(0, NOTE_DTYPE), np.zeros(0, NOTE_OBSERVATION_DTYPE), np.zeros(0, np.float64))
+    encodings = [_note_encoding(n) for n in notes]
+    table = np.frombuffer(b"".join([e[0] for e in encodings]), NOTE_DTYPE).copy()
+    observations = np.frombuffer(b"".join([e[1] for e in encodings]), NOTE_OBSERVATION_DTYPE).copy()
+    counts = table["observation_count"]
+    table["observation_offset"] = np.cumsum(counts) - counts
+    schedules: Dict[int, Tuple[int, int]] = {}
+    monitoring = []
+    total = 0
+    first = np.zeros(len(notes), np.int32)
+    count = np.zeros(len(notes), np.int32)
+    for i, times in enumerate(map(operator.attrgetter("knock_in_times"), notes)):
+        if times is None:
+            continue
+        hit = schedules.get(id(times))
+        if hit is None:
+            hit = schedules[id(times)] = (total, len(times))
+            monitoring.append(times)
+            total += len(times)
+        first[i], count[i] = hit
+    table["monitoring_offset"] = first
+    table["monitoring_count"] = count
     mon = (np.concatenate([np.asarray(t, np.float64) for t in monitoring]) if monitoring
            else np.zeros(0, np.float64))
-    return NoteTables(table, obs_table, mon)
+    return NoteTables(table, observations, mon)
 
 
 class SharedPlan:
@@ -694,8 +713,7 @@ def _price_many_planned(engine, notes: Sequence[AutocallableNote], ctx: PricingC
     try:
         while True:
             for g in pending:
-                estimates = engine._run_shared_book(ctx, plan.group_book(g), plan.group_fp32(g))
-                prices[plan.group_lanes(g)] = [e.price for e in estimates]
+                prices[plan.group_lanes(g)] = engine._run_shared_book(ctx, plan.group_book(g), plan.group_fp32(g))
             if batch:
                 for i, e in zip(scalar, engine._run(ctx, batch)):
                     prices[i] = e.price

@@ -12,6 +12,8 @@ import os
 from dataclasses import dataclass, replace
 from typing import Optional, Sequence, Tuple
 
+import numpy as np
+
 from . import abi, plans
 from ._native import context
 from .errors import InvalidInputError, UnsupportedOperationError
@@ -134,9 +136,9 @@ class _MonteCarloEngine:
 
     def _run_shared_book(self, ctx: PricingContext, book: abi.Book, lane_fp32):
         """Prices the lanes of one shared daily grid from a packed group book (the native
-        planner's, portfolio.SharedPlan) with the path-major schedule.  As in _run, FP32
-        lanes whose plan FP32 cannot carry are priced by the FP64 kernels in a second
-        launch."""
+        planner's, portfolio.SharedPlan) with the path-major schedule; returns the lanes'
+        prices (float64, contract order).  As in _run, FP32 lanes whose plan FP32 cannot
+        carry are priced by the FP64 kernels in a second launch."""
         seed = _resolve_seed(self.seed)
         settings = self._settings(seed)
         settings.schedule = abi.SCHEDULE_SHARED_GRID
@@ -152,7 +154,7 @@ class _MonteCarloEngine:
                 parts = [(settings, narrow), (fp64, wide)]
         native = context(self.device)
         model = ctx.kgpu_model()
-        results = [None] * n
+        prices = np.zeros(n, np.float64)
         for part_settings, members in parts:
             if not members:
                 continue
@@ -165,9 +167,8 @@ class _MonteCarloEngine:
             out = (abi.Estimate * len(members))()
             native.check(native.lib.kgpu_price_book(native.handle, C.byref(model), C.byref(sub),
                                                     C.byref(part_settings), out, None))
-            for k, j in enumerate(members):
-                results[j] = MonteCarloEstimate.from_native(out[k])
-        return results
+            prices[members] = np.frombuffer(out, np.dtype(abi.Estimate))["price"]
+        return prices
 
     def _run(self, ctx: PricingContext, contract_plans, path_counts=None, cancel=None, schedule=None):
         """Prices plans (Known or ContractPlan) through kgpu_price_book."""

@@ -245,6 +245,9 @@ class OracleEngine:
         return self._estimates(context, pack(lane_plans))
 
     def _run_shared_book(self, context, book, lane_fp32):
+        return np.array([e.price for e in self._shared_estimates(context, book)])
+
+    def _shared_estimates(self, context, book):
         n = book.contract_count
         b = plans.PackedBook(_array(book.contracts, abi.Contract, plans.CONTRACT_DTYPE, n).copy(),
                              _array(book.steps, abi.Step, plans.STEP_DTYPE, book.step_total).copy(),
