@@ -955,6 +955,7 @@ kgpu_status kgpu_shared_plan_get(const kgpu_shared_plan* plan, kgpu_shared_plan_
 kgpu_status kgpu_shared_plan_interpolate(const kgpu_shared_plan* plan, double* note_prices, uint8_t* retry) {
     if (!plan || (plan->note_count > 0 && (!note_prices || !retry)))
         return fail(KGPU_INVALID_INPUT, "plan, note_prices and retry must not be null");
+    if (plan->note_count == 0) return KGPU_OK;
     std::memset(retry, 0, size_t(plan->note_count));
     for (const kgpu_shared_plan::Strip& strip : plan->strips) {
         const double lower = note_prices[strip.low];

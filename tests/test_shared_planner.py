@@ -306,3 +306,11 @@ def test_gpu_engine_prices_equal_through_both_planners(precision):
         python = portfolio.price_many(engine, notes, context, True, planner="python")
         assert native == python
         assert native == engine.price_many_on_shared_grid(notes, context)
+
+
+def test_empty_book():
+    plan = portfolio.SharedPlan(portfolio.note_tables([]), ctx().kgpu_model())
+    assert plan.group_count == 0 and len(plan.note_group) == 0
+    assert not plan.interpolate(np.zeros(0)).any()
+    plan.close()
+    assert portfolio.price_many(OracleEngine(), [], ctx(), True) == []
