@@ -800,8 +800,59 @@ kgpu_status finish_values(Call& k, int chunk_count, int& launches, int failed_sl
     return collect_values<Real>(k, failed_slot);
 }
 
+// Books the segmented kernel takes: FP32 on the persistent schedule (the lane-refill
+// schedule asked for by name keeps its kernel), BSM, pseudo-random, every contract a
+// vanilla path reporting its payoff.
+bool segmented_eligible(const Call& k) {
+    if (k.s.precision != KGPU_PRECISION_FP32 || k.s.schedule != KGPU_SCHEDULE_PERSISTENT ||
+        k.model->kind != KGPU_MODEL_BSM || k.sobol || k.s.antithetic)
+        return false;
+    for (int i = 0; i < k.book->contract_count; ++i) {
+        const kgpu_contract& c = k.book->contracts[i];
+        if (c.payoff != KGPU_PAYOFF_VANILLA_PATH || (c.flags & (KGPU_C_OUTPUT_DELTA | KGPU_C_OUTPUT_GAMMA)))
+            return false;
+    }
+    return true;
+}
+
+// A vanilla-path book on the segmented kernel: per-path payoffs, then the same fixed-order
+// reduction as the persistent kernels.
+kgpu_status run_segmented(Call& k, const DevBook<float>& db, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const int n = k.raw.contract_count;
+    kgpu_status st;
+    int chunk_count = 0;
+    if ((st = stage_values<float>(k, &chunk_count))) return st;
+    std::vector<int> dims(n);
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        dims[i] = k.info[i].dims;
+        total += k.info[i].samples;
+    }
+    if ((st = upload(ctx, ctx->phase_dims, dims.data(), dims.size() * sizeof(int)))) return st;
+    SegmentArgs a;
+    a.book = db;
+    a.contract_count = n;
+    a.total = total;
+    a.value_offset = static_cast<const int64_t*>(ctx->value_offset.ptr);
+    a.dims = static_cast<const int*>(ctx->phase_dims.ptr);
+    a.seed = k.s.seed;
+    a.values = static_cast<float*>(ctx->values.ptr);
+    a.executed = static_cast<unsigned long long*>(ctx->executed.ptr);
+    a.cancel = k.cancel ? ctx->cancel_dev : nullptr;
+    a.aborted = static_cast<int*>(ctx->queue.ptr) + 1;
+    CancelWatcher watcher(k.cancel, ctx->cancel_host);
+    CUDA_TRY(ctx, path_kernel_begin(ctx));
+    CUDA_TRY(ctx, launch_segmented_fp32(total, ctx->stream, a));
+    CUDA_TRY(ctx, path_kernel_end(ctx));
+    launches += 1;
+    return finish_values<float>(k, chunk_count, launches);
+}
+
 template <class Real>
 kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
+    if constexpr (std::is_same<Real, float>::value)
+        if (segmented_eligible(k)) return run_segmented(k, db, launches);
     const bool ext = extended_payoffs(*k.book);
     kgpu_context* ctx = k.ctx;
     const kgpu_settings& s = k.s;

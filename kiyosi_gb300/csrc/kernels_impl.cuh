@@ -2,6 +2,7 @@
 // are defined by the including translation unit.
 #include "launch.h"
 #include "phased.cuh"
+#include "segmented.cuh"
 #include "shared_grid.cuh"
 
 namespace kgpu {
@@ -146,6 +147,14 @@ int phased_occupancy_fp32(bool sobol) {
     const cudaError_t e = sobol ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phased_kernel<float, true>, kThreads, 0)
                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phased_kernel<float, false>, kThreads, 0);
     return e == cudaSuccess && n > 0 ? n : 1;
+}
+
+cudaError_t launch_segmented_fp32(int64_t total, cudaStream_t s, const SegmentArgs& a) {
+    if (total <= 0) return cudaSuccess;
+    const int64_t threads = total * kSegments;
+    segmented_vanilla_kernel<kSegments>
+        <<<unsigned((threads + kSegmentThreads - 1) / kSegmentThreads), kSegmentThreads, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s) {

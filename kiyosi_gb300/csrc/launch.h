@@ -4,6 +4,7 @@
 
 #include "kernels.cuh"
 #include "phased.cuh"
+#include "segmented.cuh"
 #include "shared_grid.cuh"
 
 namespace kgpu {
@@ -50,6 +51,9 @@ cudaError_t launch_compile_arrays_fp32(const RawBook& b, StepT<float>* steps, Ev
 cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, true>& a);
 cudaError_t launch_phased_fp32(int blocks, cudaStream_t s, const PhaseArgs<float, false>& a);
 int phased_occupancy_fp32(bool sobol);
+
+// Books of BSM vanilla-path contracts, FP32, pseudo-random: kSegments lanes per path.
+cudaError_t launch_segmented_fp32(int64_t total, cudaStream_t s, const SegmentArgs& a);
 cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s);
 
 // The lanes of one shared daily grid, path-major, and the merge of their CTA sums.
