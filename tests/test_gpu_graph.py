@@ -139,3 +139,39 @@ def test_cancelled_replay(native):
     again = gpu_price(native, ctx, packed, s, cancel=flag)
     assert native.last_graph == 2
     _same(again, runs[0])
+
+
+def test_other_entry_points_in_between(native):
+    """A Sobol sequence of another seed and size built in between (kgpu_sobol_points
+    rebuilds the context's cached tables) is not read by a replay: the next call runs
+    directly and its estimate is unchanged."""
+    ctx = c2_context()
+    packed = pack([plans.autocallable(snowball_c2(), ctx)])
+    s = settings(1 << 18, 42, sobol=True, precision="fp32", schedule="persistent")
+    runs, modes = _calls(native, ctx, packed, s)
+    _captured_then_replayed(modes)
+    bits = np.zeros(64, np.uint64)
+    native.check(native.lib.kgpu_sobol_points(native.handle, 7, 33, 5, 0, 64,
+                                              bits.ctypes.data_as(C.POINTER(C.c_uint64)), None, 0))
+    after = gpu_price(native, ctx, packed, s)
+    assert native.last_graph == 0
+    _same(after, runs[0])
+
+
+def test_host_book_contents_change_under_one_contract_table(native):
+    """A host book whose step records change while its contract table stays: every call
+    uploads the book, and the replayed sequence prices the new records."""
+    ctx = c2_context()
+    packed = pack([plans.autocallable(snowball_c2(), ctx)])
+    s = settings(1 << 16, 42, sobol=True, precision="fp32", schedule="persistent")
+    runs, modes = _calls(native, ctx, packed, s, 4)
+    _captured_then_replayed(modes)
+    changed = plans.PackedBook(packed.contracts, packed.steps.copy(), packed.flags, packed.events.copy(),
+                               packed.intervals, packed.daily)
+    changed.events["payment"] *= 0.5
+    replayed = gpu_price(native, ctx, changed, s)
+    assert native.last_graph == 2 and replayed[0].price < runs[0][0].price
+    gpu_price(native, ctx, pack([plans.autocallable(snowball_c2(steps=252, years=1.0, months=12), ctx)]), s)
+    direct = gpu_price(native, ctx, changed, s)
+    assert native.last_graph == 0
+    _same(replayed, direct)
