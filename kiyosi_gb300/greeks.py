@@ -16,8 +16,15 @@ normals. Here every scenario's plan goes into one book, and one `kgpu_price_book
 prices them all. Each contract is sampled with the same seed and block streams, so the
 scenarios share their random numbers exactly as the reference's do.
 
-Time Greeks (theta, charm, color) need kiyosi's timestamp and calendar stencils, which
-this package's year-fraction contexts do not model. They report `unsupported`.
+Time Greeks (theta, charm, color; risk/numerical.rs:213-275, 594-630) move the valuation
+instant: with flat rates and year-fraction times, pricing at valuation + t is pricing the
+instrument with every time moved by -t.  The stencil is the reference's on whole
+microseconds of Actual/365 Fixed time: one day (or the requested shift), capped at an
+eighth of the remaining life and by the contract's start, halved until no observation
+the instrument's rule names lies inside it.  Theta is the price's difference across the
+stencil, charm and color those of the spot stencils' delta and gamma.  European options,
+autocallable notes and accumulators have the rule; other instruments report
+`unsupported`.
 """
 import math
 from dataclasses import dataclass, field, replace
@@ -33,13 +40,19 @@ VOLATILITY_GREEKS = ("vega", "volga", "vanna", "zomma")
 TIME_GREEKS = ("theta", "charm", "color")
 
 
+# Microseconds per Actual/365 Fixed year (time/date.rs:255-257).
+YEAR_MICROS = 365 * 86_400 * 1_000_000
+
+
 @dataclass(frozen=True)
 class NumericalShiftSettings:
-    """NumericalShiftSettings (risk/analytics.rs:382-421): absolute bumps; None picks
-    the automatic spot and volatility bumps."""
+    """NumericalShiftSettings (risk/analytics.rs:382-464): absolute bumps; None picks
+    the automatic spot, volatility and time bumps.  `time_shift` is in Actual/365 Fixed
+    years and must be a whole number of microseconds (one day by default)."""
     spot_shift: Optional[float] = None
     volatility_shift: Optional[float] = None
     rate_shift: float = 1e-4
+    time_shift: Optional[float] = None
 
     def validate(self):
         for name in ("spot_shift", "volatility_shift"):
@@ -48,6 +61,16 @@ class NumericalShiftSettings:
                 raise InvalidInputError(f"{name} must be positive and finite")
         if not (math.isfinite(self.rate_shift) and self.rate_shift > 0.0):
             raise InvalidInputError("rate_shift must be positive and finite")
+        self.time_shift_micros()
+
+    def time_shift_micros(self) -> int:
+        """NumericalShiftSettings::time_shift_micros (risk/analytics.rs:453-463)."""
+        if self.time_shift is None:
+            return 86_400 * 1_000_000
+        micros = self.time_shift * YEAR_MICROS if math.isfinite(self.time_shift) else math.nan
+        if not (micros >= 1.0 and abs(micros - round(micros)) <= 1e-6 * max(1.0, micros)):
+            raise InvalidInputError("time_shift must be positive with whole-microsecond precision")
+        return int(round(micros))
 
     def spot_shift_at(self, spot: float) -> float:
         return self.spot_shift if self.spot_shift is not None else min(0.01, 0.01 * spot)
@@ -87,13 +110,109 @@ def symmetric_shift(value: float, requested: float) -> float:
     return 0.0
 
 
-# A scenario is the BSM market (spot, volatility, rate, dividend).
-Scenario = Tuple[float, float, float, float]
+# A scenario is the BSM market (spot, volatility, rate, dividend), plus, for the time
+# stencils, the valuation shift in years (a fifth entry; absent means no shift).
+Scenario = Tuple[float, ...]
 
 
 def scenario_context(key: Scenario) -> PricingContext:
-    spot, vol, rate, dividend = key
+    spot, vol, rate, dividend = key[:4]
     return PricingContext(BlackScholesMertonParameters(rate, dividend, vol), spot)
+
+
+def _at(spot, vol, rate, dividend, shift: float) -> Scenario:
+    """The scenario valued `shift` years later (the plain market when shift is 0)."""
+    return (spot, vol, rate, dividend) if shift == 0.0 else (spot, vol, rate, dividend, shift)
+
+
+# ---- time stencils (risk/numerical.rs:213-275) ----
+
+@dataclass(frozen=True)
+class TimeRule:
+    """How an instrument moves in time: the start of its life (OptionContract::
+    valuation_start; None for none), the instrument valued `t` years later, and whether a
+    stencil [before, after] (years) keeps its history regime (time_stencil_available)."""
+    start: Optional[float]
+    valued_at: Callable[[float], object]
+    available: Callable[[float, float], bool]
+
+
+def _inside(times, before: float, after: float) -> bool:
+    return any(before <= t <= after for t in times)
+
+
+def time_rule(option) -> Optional[TimeRule]:
+    """The TimeRule of the instruments whose engines take numerical Greeks."""
+    from .instruments import Accumulator, AutocallableNote, EuropeanOption
+    if type(option) is EuropeanOption:
+        # vanilla.rs:181-200: no valuation start, every stencil available
+        return TimeRule(None, lambda t: replace(option, expiry=option.expiry - t), lambda b, a: True)
+    if isinstance(option, AutocallableNote):
+        def shifted(t):
+            times = None if option.knock_in_times is None else [x - t for x in option.knock_in_times]
+            return replace(option, expiry=option.expiry - t, effective_time=option.effective_time - t,
+                           observations=tuple(replace(o, time=o.time - t) for o in option.observations),
+                           knock_in_times=times)
+
+        def available(before, after):
+            # AutocallableNote::time_stencil_available (instruments/autocallable.rs:1556-1582)
+            from . import plans
+            from .errors import KiyosiError
+            try:
+                plans.autocallable_prior(shifted(before))
+            except KiyosiError:
+                return False
+            if option.barrier_state == "knocked_out":
+                return True
+            if _inside([o.time for o in option.observations], before, after):
+                return False
+            if (option.daily_knock_in and option.barrier_state != "knocked_in"
+                    and option.knock_in_affects_payoff()
+                    and _inside(option.knock_in_times, max(before, option.effective_time),
+                                min(after, option.expiry))):
+                return False
+            return True
+        return TimeRule(option.effective_time, shifted, available)
+    if isinstance(option, Accumulator):
+        # Accumulator::time_stencil_available (instruments/accumulator.rs:664-680).  This
+        # package's accumulators list only dates after valuation and carry their history
+        # as a quantity, so the valuation is the start of their life.
+        def available(before, after):
+            if option.knock_out_settled:
+                return True
+            return not (_inside(option.accumulation_times, before, after)
+                        or _inside(option.knock_out_times, before, after))
+        return TimeRule(0.0, lambda t: replace(
+            option, expiry=option.expiry - t, accumulation_times=[x - t for x in option.accumulation_times],
+            knock_out_times=[x - t for x in option.knock_out_times]), available)
+    return None
+
+
+def time_stencil(rule: TimeRule, expiry: float, shifts: NumericalShiftSettings) -> Optional[Tuple[int, int]]:
+    """time_stencil (risk/numerical.rs:213-275) under flat curves: (before, after) in
+    microseconds from valuation, or None.  The widths to the start of the contract's life
+    and to expiry are whole microseconds (floored)."""
+    before_width = math.inf if rule.start is None else math.floor(-rule.start * YEAR_MICROS)
+    after_width = math.floor(expiry * YEAR_MICROS)
+    radius = shifts.time_shift_micros()
+    shift = min(radius, max(0, before_width + after_width))
+    if shifts.time_shift is None:
+        # Near expiry the price is far from linear in time: keep the stencil away from it.
+        shift = min(shift, max(after_width // 8, 1))
+    if before_width > 0 and after_width > 0:
+        shift = min(shift, before_width, after_width)
+    shift = int(shift)
+
+    def legs(width):
+        return -int(min(width, before_width)), int(min(width, after_width))
+
+    def available(b, a):
+        return rule.available(b / YEAR_MICROS, a / YEAR_MICROS)
+    before, after = legs(shift)
+    while shifts.time_shift is None and shift > 1 and not available(before, after):
+        shift //= 2
+        before, after = legs(shift)
+    return (before, after) if before != after and available(before, after) else None
 
 
 def _check_request(request: Iterable[str]) -> Tuple[str, ...]:
@@ -106,10 +225,13 @@ def _check_request(request: Iterable[str]) -> Tuple[str, ...]:
 
 def _stencils(ctx: PricingContext, expiry: float, request, shifts: NumericalShiftSettings,
               discontinuity: Callable[[float], bool], price: Callable[[Scenario], float],
-              p0: float) -> PricingResult:
+              p0: float, stencil: Optional[Tuple[int, int]] = None,
+              time_supported: bool = False) -> PricingResult:
     """complete_greeks_with_pair without native spot Greeks (risk/numerical.rs:331-702)
     and expiry_greeks (33-132).  `price` maps a scenario to its price; with a recording
-    `price` this enumerates the scenarios the stencils need."""
+    `price` this enumerates the scenarios the stencils need.  `stencil` is the time
+    stencil in microseconds (None: unavailable); `time_supported` whether the instrument
+    has time Greeks at all."""
     model = ctx.model
     spot, vol, rate, dividend = ctx.spot, model.volatility, model.rate, model.dividend
     result = PricingResult(p0)
@@ -140,7 +262,8 @@ def _stencils(ctx: PricingContext, expiry: float, request, shifts: NumericalShif
                     put("speed", ((up2 - up) - (up - down) + (down - down2)) / h / h / two_h)
         for g in request:
             if g not in result.greeks:
-                result.status[g] = "unsupported" if g in TIME_GREEKS else "stencil_unavailable"
+                result.status[g] = ("unsupported" if g in TIME_GREEKS and not time_supported
+                                    else "stencil_unavailable")
         return result
 
     h = symmetric_shift(spot, shifts.spot_shift_at(spot))
@@ -193,11 +316,35 @@ def _stencils(ctx: PricingContext, expiry: float, request, shifts: NumericalShif
         if q > 0.0 and math.isfinite(2.0 * q):
             put("dividend_rho", (price((spot, vol, rate, dividend + q))
                                  - price((spot, vol, rate, dividend + -q))) / (2.0 * q))
+    if time_supported and stencil is not None and (want("theta") or want("charm") or want("color")):
+        # risk/numerical.rs:594-630: prices at both ends of the stencil (the base price at
+        # an end on valuation), then the spot stencils' delta and gamma at both ends.
+        before, after = stencil[0] / YEAR_MICROS, stencil[1] / YEAR_MICROS
+        years = (stencil[1] - stencil[0]) / YEAR_MICROS
+
+        def at(shift, s=spot):
+            return p0 if shift == 0.0 and s == spot else price(_at(s, vol, rate, dividend, shift))
+        prices = None
+        if want("theta"):
+            prices = (at(after), at(before))
+            put("theta", (prices[0] - prices[1]) / years)
+        if spot_ok and (want("charm") or want("color")):
+            if want("color"):
+                first, last = (prices[1], prices[0]) if prices is not None else (at(before), at(after))
+            else:
+                first, last = p0, p0
+
+            def derivatives(shift, center):
+                up, down = at(shift, spot + h), at(shift, spot - h)
+                return (up - down) / h / 2.0, ((up - center) - (center - down)) / h / h
+            low, high = derivatives(before, first), derivatives(after, last)
+            put("charm", (high[0] - low[0]) / years)
+            put("color", (high[1] - low[1]) / years)
     spot_undefined = discontinuity(0.0)
     for g in request:
         if g in result.greeks:
             continue
-        if g in TIME_GREEKS:
+        if g in TIME_GREEKS and not time_supported:
             result.status[g] = "unsupported"
         elif (g in SPOT_GREEKS and spot_undefined) or (g in VOLATILITY_GREEKS and vol == 0.0):
             result.status[g] = "undefined"
@@ -240,23 +387,47 @@ def numerical_greeks(engine, option, ctx: PricingContext, request: Iterable[str]
     pinned = engine.with_resolved_seed()
     base: Scenario = (ctx.spot, ctx.model.volatility, ctx.model.rate, ctx.model.dividend)
     needed: List[Scenario] = [base]
+    rule = time_rule(option)
+    stencil = None
+    if rule is not None and option.expiry > 0.0 and any(g in request for g in TIME_GREEKS):
+        stencil = time_stencil(rule, option.expiry, shifts)
 
     def record(key: Scenario) -> float:
         if key not in needed:
             needed.append(key)
         return 0.0
 
-    _stencils(ctx, option.expiry, request, shifts, discontinuity, record, 0.0)
-    prices = pinned._scenario_prices(option, [scenario_context(k) for k in needed])
+    _stencils(ctx, option.expiry, request, shifts, discontinuity, record, 0.0, stencil, rule is not None)
+    prices = _scenario_prices(pinned, option, rule, needed)
     table = dict(zip(needed, prices))
     result = _stencils(ctx, option.expiry, request, shifts, discontinuity, table.__getitem__,
-                       table[base])
+                       table[base], stencil, rule is not None)
     for g, value in result.greeks.items():
         if not math.isfinite(value):
             from .errors import ComputationFailureError
             raise ComputationFailureError(f"non-finite {g}")
     result.seed = pinned.seed
     return result
+
+
+def _scenario_prices(pinned, option, rule: Optional[TimeRule], keys: List[Scenario]) -> List[float]:
+    """Prices the scenarios on the pinned seed: the instrument valued at each scenario's
+    shift, in one book when the engine prices (contract, context) pairs
+    (`_scenario_prices_of`), else one call per shift."""
+    def instrument(key):
+        return option if len(key) == 4 else rule.valued_at(key[4])
+    pairs_call = getattr(pinned, "_scenario_prices_of", None)
+    if pairs_call is not None:
+        return pairs_call([(instrument(k), scenario_context(k)) for k in keys])
+    out: List[Optional[float]] = [None] * len(keys)
+    groups: Dict[float, List[int]] = {}
+    for i, k in enumerate(keys):
+        groups.setdefault(0.0 if len(k) == 4 else k[4], []).append(i)
+    for shift, members in groups.items():
+        prices = pinned._scenario_prices(instrument(keys[members[0]]), [scenario_context(keys[i]) for i in members])
+        for i, p in zip(members, prices):
+            out[i] = p
+    return out
 
 
 def barrier_discontinuity(option, ctx: PricingContext, radius: float) -> bool:

@@ -248,10 +248,16 @@ class _MonteCarloEngine:
         """Prices `contract` in each context with this engine's seed.  Engines with a
         per-contract plan price every context in one book (one launch, shared random
         numbers); the others price them one by one."""
+        return self._scenario_prices_of([(contract, c) for c in contexts])
+
+    def _scenario_prices_of(self, pairs):
+        """Prices (contract, context) pairs with this engine's seed, in one book when the
+        engine has per-contract plans (the time stencils' scenarios are the contract
+        valued at shifted instants)."""
         plan = getattr(self, "_plan", None)
         if plan is None:
-            return [self.price(contract, c) for c in contexts]
-        return [e.price for e in self._run(contexts[0], [plan(contract, c) for c in contexts])]
+            return [self.price(contract, c) for contract, c in pairs]
+        return [e.price for e in self._run(pairs[0][1], [plan(contract, c) for contract, c in pairs])]
 
 
 class MonteCarloVanillaEngine(_MonteCarloEngine):

@@ -99,9 +99,14 @@ def test_batched_scenarios_equal_scalar_bumped_prices():
     assert r.get("volga") == ((vu - p0) - (p0 - vd)) / v / v
     dr = greeks.symmetric_shift(0.05, 1e-4)
     assert r.get("rho") == (price(100.0, 0.2, 0.05 + dr, 0.02) - price(100.0, 0.2, 0.05 - dr, 0.02)) / (2 * dr)
-    assert r.status["theta"] == "unsupported"
+    # theta: the option valued one day later and one day earlier (a European option has
+    # no start of life, so the stencil is central: one day, capped at an eighth of life)
+    day = 86_400_000_000 / greeks.YEAR_MICROS
+    later = engine.price(EuropeanOption("call", 105.0, 1.0 - day), ctx)
+    earlier = engine.price(EuropeanOption("call", 105.0, 1.0 - -day), ctx)
+    assert r.get("theta") == (later - earlier) / (2 * 86_400_000_000 / greeks.YEAR_MICROS)
     with pytest.raises(GreekUnavailableError):
-        r.require("theta")
+        r.require("charm")
 
 
 def test_european_monte_carlo_greeks_near_closed_forms():
@@ -154,3 +159,129 @@ def test_engine_greeks_equal_scalar_bumped_prices(native):
     bumped = lambda s: PricingContext(note_ctx.model, s)  # noqa: E731
     assert g.price == auto.price(note, note_ctx)
     assert g.get("delta") == (auto.price(note, bumped(spot + h)) - auto.price(note, bumped(spot - h))) / h / 2.0
+
+
+def _bs_time_greeks(sign, s, k, t, r, q, v):
+    """Closed-form theta (d price / d valuation time), charm (d delta / d valuation time)."""
+    sq = v * math.sqrt(t)
+    d1 = (math.log(s / k) + (r - q + 0.5 * v * v) * t) / sq
+    d2 = d1 - sq
+    theta = (-s * math.exp(-q * t) * _npdf(d1) * v / (2.0 * math.sqrt(t))
+             - sign * r * k * math.exp(-r * t) * _ncdf(sign * d2)
+             + sign * q * s * math.exp(-q * t) * _ncdf(sign * d1))
+    charm = (sign * q * math.exp(-q * t) * _ncdf(sign * d1)
+             - math.exp(-q * t) * _npdf(d1) * (2.0 * (r - q) * t - d2 * sq) / (2.0 * t * sq))
+    return theta, charm
+
+
+def test_european_time_greeks_near_closed_forms():
+    ctx = _ctx()
+    for sign, kind in ((1.0, "call"), (-1.0, "put")):
+        option = EuropeanOption(kind, 100.0, 1.0)
+        engine = OracleEngine(plans.european, 1 << 16, 3)
+        r = greeks.numerical_greeks(engine, option, ctx, ("theta", "charm", "color"))
+        theta, charm = _bs_time_greeks(sign, 100.0, 100.0, 1.0, 0.05, 0.02, 0.2)
+        assert abs(r.get("theta") - theta) < 0.03 * abs(theta) + 0.02, (kind, r.get("theta"), theta)
+        assert abs(r.get("charm") - charm) < 0.25 * abs(charm) + 0.02, (kind, r.get("charm"), charm)
+        assert math.isfinite(r.get("color"))
+
+
+def _note(effective=0.0, state=None, daily=True, first=21):
+    from kiyosi_gb300.instruments import AutocallableNote, Observation
+    dt = 1.0 / 252.0
+    times = [effective + dt * (i + 1) for i in range(252)]
+    past = [t for t in (effective + dt * k for k in range(0, 400)) if t < 0.0]
+    obs = [Observation(times[first * (m + 1) - 1], knock_out_level=103.0, coupon_rate=0.1) for m in range(12)]
+    return AutocallableNote(initial_spot=100.0, expiry=times[-1], observations=obs, knock_in_level=80.0,
+                            knock_in_times=(past + [t for t in times if t >= 0.0]) if daily else None,
+                            upper_strike=100.0, maturity_coupon_rate=0.1, effective_time=effective,
+                            barrier_state=state)
+
+
+def test_time_stencils():
+    s = greeks.NumericalShiftSettings()
+    day = 86_400_000_000
+    # a European option: central, one day
+    rule = greeks.time_rule(EuropeanOption("call", 100.0, 1.0))
+    assert greeks.time_stencil(rule, 1.0, s) == (-day, day)
+    # an eighth of the remaining life near expiry
+    assert greeks.time_stencil(rule, 2.0 / 365.0, s) == (-day // 4, day // 4)
+    # a note valued at its start: forward only; the first monitoring date is 1/252 year
+    # away, beyond one day
+    note = _note()
+    assert greeks.time_stencil(greeks.time_rule(note), note.expiry, s) == (0, day)
+    # a seasoned note between two monitoring dates: central, halved until the window
+    # clears them
+    seasoned = _note(effective=-0.5 / 252.0, state="no_event")
+    before, after = greeks.time_stencil(greeks.time_rule(seasoned), seasoned.expiry, s)
+    assert before == -after and 0 < after < 0.5 * greeks.YEAR_MICROS / 252.0
+    assert not any(before / greeks.YEAR_MICROS <= t <= after / greeks.YEAR_MICROS
+                   for t in seasoned.knock_in_times)
+    # knock-in no longer matters once knocked in: monitoring dates do not block, and the
+    # start of the note's life caps the stencil
+    knocked = _note(effective=-0.5 / 252.0, state="knocked_in")
+    width = math.floor(0.5 / 252.0 * greeks.YEAR_MICROS)
+    assert greeks.time_stencil(greeks.time_rule(knocked), knocked.expiry, s) == (-width, width)
+    # an explicit shift is not shortened for observations: none for a note seasoned ten
+    # days whose window then holds monitoring dates
+    explicit = greeks.NumericalShiftSettings(time_shift=2.0 / 252.0)
+    older = _note(effective=-10.5 / 252.0, state="no_event")
+    assert greeks.time_stencil(greeks.time_rule(older), older.expiry, explicit) is None
+    assert greeks.time_stencil(greeks.time_rule(older), older.expiry, s) is not None
+    with pytest.raises(InvalidInputError):
+        greeks.NumericalShiftSettings(time_shift=0.3e-13).validate()
+
+
+def test_autocallable_theta_is_the_shifted_prices_difference():
+    ctx = c2_context()
+    note = _note()
+    engine = OracleEngine(plans.autocallable, 1 << 13, 9)
+    r = greeks.numerical_greeks(engine, note, ctx, ("theta", "delta", "charm"))
+    rule = greeks.time_rule(note)
+    before, after = greeks.time_stencil(rule, note.expiry, greeks.NumericalShiftSettings())
+    assert before == 0
+    later = engine.price(rule.valued_at(after / greeks.YEAR_MICROS), ctx)
+    assert r.get("theta") == (later - r.price) / ((after - before) / greeks.YEAR_MICROS)
+    assert math.isfinite(r.get("charm"))
+
+
+def test_observation_at_valuation_blocks_the_time_stencil():
+    from kiyosi_gb300.instruments import AutocallableNote, Observation
+    note = AutocallableNote(initial_spot=100.0, expiry=1.0, observations=[Observation(0.0, 110.0, None, 0.1),
+                                                                         Observation(1.0, 103.0, None, 0.1)],
+                            knock_in_level=80.0, upper_strike=100.0, maturity_coupon_rate=0.1,
+                            barrier_state="no_event")
+    assert greeks.time_stencil(greeks.time_rule(note), 1.0, greeks.NumericalShiftSettings()) is None
+    engine = OracleEngine(plans.autocallable, 1 << 10, 9)
+    r = greeks.numerical_greeks(engine, note, c2_context(), ("theta", "delta"))
+    assert r.status["theta"] == "stencil_unavailable" and "delta" in r.greeks
+
+
+@pytest.mark.gpu
+def test_engine_time_greeks_on_the_gpu(native):
+    """The engines' theta, charm and color on the GB300: the same stencils as the oracle
+    engine's (FP64 to 1e-9), one book for every scenario, and theta near the closed form."""
+    from kiyosi_gb300.pricing import MonteCarloAutocallableEngine, MonteCarloVanillaEngine
+    ctx = _ctx()
+    option = EuropeanOption("call", 100.0, 1.0)
+    engine = MonteCarloVanillaEngine(path_count=1 << 16, seed=3)
+    r = engine.price_with_greeks(option, ctx, ("theta", "charm", "color", "delta"))
+    ref = greeks.numerical_greeks(OracleEngine(plans.european, 1 << 16, 3), option, ctx,
+                                  ("theta", "charm", "color", "delta"))
+    for g in ("theta", "charm", "color", "delta"):
+        assert abs(r.get(g) - ref.get(g)) <= 1e-9 * max(1.0, abs(ref.get(g))), (g, r.get(g), ref.get(g))
+    theta, charm = _bs_time_greeks(1.0, 100.0, 100.0, 1.0, 0.05, 0.02, 0.2)
+    assert abs(r.get("theta") - theta) < 0.03 * abs(theta)
+    # a note valued at its start (forward stencil), FP64 and FP32
+    note_ctx = c2_context()
+    note = _note()
+    ref = greeks.numerical_greeks(OracleEngine(plans.autocallable, 1 << 13, 9), note, note_ctx, ("theta", "delta"))
+    auto = MonteCarloAutocallableEngine(path_count=1 << 13, seed=9)
+    got = auto.price_with_greeks(note, note_ctx, ("theta", "delta"))
+    assert abs(got.get("theta") - ref.get("theta")) <= 1e-8 * max(1.0, abs(ref.get("theta")))
+    fast = MonteCarloAutocallableEngine(path_count=1 << 13, seed=9, precision="fp32").price_with_greeks(
+        note, note_ctx, ("theta",))
+    # FP32 paths on the same normals: a path whose knock-out flips moves theta by about
+    # a payment / paths / one day
+    assert abs(fast.get("theta") - ref.get("theta")) < 0.2 * abs(ref.get("theta")) + 0.3, (
+        fast.get("theta"), ref.get("theta"))
