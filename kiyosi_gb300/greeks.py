@@ -22,9 +22,9 @@ instrument with every time moved by -t.  The stencil is the reference's on whole
 microseconds of Actual/365 Fixed time: one day (or the requested shift), capped at an
 eighth of the remaining life and by the contract's start, halved until no observation
 the instrument's rule names lies inside it.  Theta is the price's difference across the
-stencil, charm and color those of the spot stencils' delta and gamma.  European options,
-autocallable notes and accumulators have the rule; other instruments report
-`unsupported`.
+stencil, charm and color those of the spot stencils' delta and gamma.  European and
+American options, autocallable notes and accumulators have the rule; other instruments
+report `unsupported`.
 """
 import math
 from dataclasses import dataclass, field, replace
@@ -143,9 +143,9 @@ def _inside(times, before: float, after: float) -> bool:
 
 def time_rule(option) -> Optional[TimeRule]:
     """The TimeRule of the instruments whose engines take numerical Greeks."""
-    from .instruments import Accumulator, AutocallableNote, EuropeanOption
-    if type(option) is EuropeanOption:
-        # vanilla.rs:181-200: no valuation start, every stencil available
+    from .instruments import Accumulator, AmericanOption, AutocallableNote, EuropeanOption
+    if type(option) in (EuropeanOption, AmericanOption):
+        # vanilla.rs:181-200, 375-377: no valuation start, every stencil available
         return TimeRule(None, lambda t: replace(option, expiry=option.expiry - t), lambda b, a: True)
     if isinstance(option, AutocallableNote):
         def shifted(t):

@@ -138,7 +138,8 @@ def american_greeks(engine, option, ctx, request, shifts=None):
     batched LSMC scenario calls (greek_prices / american_spots, american.rs:820-946).
     For a call, rho and dividend rho whose rate stencil crosses the no-early-exercise
     boundary use the exercise-grid estimator on both sides (american.rs:1606-1656).
-    Time Greeks report `unsupported`, as for the other engines."""
+    Theta, charm and color price the option valued at the time stencil's ends (its
+    expiry moved; greeks.time_stencil), each instant's scenarios in one batched call."""
     from . import greeks as G
     from .errors import ComputationFailureError, UnsupportedOperationError
     from .pricing import _resolve_seed
@@ -150,24 +151,37 @@ def american_greeks(engine, option, ctx, request, shifts=None):
         raise UnsupportedOperationError("numerical Greeks need Black-Scholes-Merton parameters")
     if option.expiry > 0.0 and shifts.spot_shift is None:
         shifts = G.NumericalShiftSettings(AMERICAN_SPOT_SHIFT * ctx.spot, shifts.volatility_shift,
-                                          shifts.rate_shift)
+                                          shifts.rate_shift, shifts.time_shift)
     seed = _resolve_seed(engine.seed)
     discontinuity = G.vanilla_discontinuity(option, ctx)
     base = (ctx.spot, model.volatility, model.rate, model.dividend)
     needed = [base]
+    rule = G.time_rule(option)
+    stencil = None
+    if option.expiry > 0.0 and any(g in request for g in G.TIME_GREEKS):
+        stencil = G.time_stencil(rule, option.expiry, shifts)
 
     def record(key):
         if key not in needed:
             needed.append(key)
         return 0.0
 
-    G._stencils(ctx, option.expiry, request, shifts, discontinuity, record, 0.0)
-    if option.expiry == 0.0:
-        prices = [max(option.sign * (k[0] - option.strike), 0.0) for k in needed]
-    else:
-        prices = price_american_scenarios(engine, option, [G.scenario_context(k) for k in needed], seed)
+    G._stencils(ctx, option.expiry, request, shifts, discontinuity, record, 0.0, stencil, True)
+    prices = [None] * len(needed)
+    instants = {}
+    for i, k in enumerate(needed):
+        instants.setdefault(0.0 if len(k) == 4 else k[4], []).append(i)
+    for shift, members in instants.items():
+        valued = option if shift == 0.0 else rule.valued_at(shift)
+        if valued.expiry == 0.0:
+            values = [max(valued.sign * (needed[i][0] - valued.strike), 0.0) for i in members]
+        else:
+            values = price_american_scenarios(engine, valued, [G.scenario_context(needed[i]) for i in members], seed)
+        for i, v in zip(members, values):
+            prices[i] = v
     table = dict(zip(needed, prices))
-    result = G._stencils(ctx, option.expiry, request, shifts, discontinuity, table.__getitem__, table[base])
+    result = G._stencils(ctx, option.expiry, request, shifts, discontinuity, table.__getitem__, table[base],
+                         stencil, True)
     if option.expiry > 0.0 and option.sign > 0.0:
         spot, vol, rate, dividend = base
         for greek, value, can_switch in (("rho", rate, dividend <= 0.0), ("dividend_rho", dividend, rate >= 0.0)):

@@ -1,6 +1,6 @@
 """CPU: the American Greeks' host logic (lsmc.american_greeks) with the GPU pricer
 replaced by a smooth function of the scenario, so the stencils, the 8%-of-spot default
-bump, the time-Greek statuses and the call's rate-shortcut boundary are checked without a
+bump, the time stencil and the call's rate-shortcut boundary are checked without a
 device (american.rs:555-557, 1487-1687)."""
 import math
 
@@ -14,10 +14,10 @@ from kiyosi_gb300.market import BlackScholesMertonParameters, HestonParameters, 
 from kiyosi_gb300.pricing import MonteCarloVanillaEngine
 
 
-def _value(ctx):
+def _value(ctx, expiry=1.0):
     m = ctx.model
     return (0.1 * ctx.spot ** 2 / 100.0 + 3.0 * m.volatility ** 2 - 7.0 * m.rate + 2.0 * m.dividend
-            + 0.5 * ctx.spot * m.volatility)
+            + 0.5 * ctx.spot * m.volatility + 4.0 * expiry + 0.01 * ctx.spot * expiry)
 
 
 @pytest.fixture
@@ -26,7 +26,7 @@ def calls(monkeypatch):
 
     def fake(engine, option, contexts, seed, shortcut=True):
         seen.append((len(contexts), shortcut, seed))
-        return [_value(c) for c in contexts]
+        return [_value(c, option.expiry) for c in contexts]
     monkeypatch.setattr(lsmc, "price_american_scenarios", fake)
     return seen
 
@@ -35,7 +35,7 @@ def test_put_greeks_follow_the_stencils(calls):
     engine = MonteCarloVanillaEngine(path_count=1024, step_count=10, seed=5)
     ctx = PricingContext(BlackScholesMertonParameters(0.05, 0.02, 0.2), 100.0)
     res = engine.price_with_greeks(AmericanOption("put", 100.0, 1.0), ctx,
-                                   ["delta", "gamma", "vega", "rho", "dividend_rho", "theta"])
+                                   ["delta", "gamma", "vega", "rho", "dividend_rho", "theta", "charm"])
     h = symmetric_shift(100.0, 8.0)  # 8% of spot
     v = symmetric_shift(0.2, 1e-4)
 
@@ -48,9 +48,12 @@ def test_put_greeks_follow_the_stencils(calls):
     assert res.greeks["vega"] == (at(vol=0.2 + v) - at(vol=0.2 - v)) / (2.0 * v)
     assert math.isclose(res.greeks["rho"], -7.0, rel_tol=1e-6)
     assert math.isclose(res.greeks["dividend_rho"], 2.0, rel_tol=1e-6)
-    assert res.status["theta"] == "unsupported"
-    # Every scenario in one batch, on the engine's seed.
-    assert len(calls) == 1 and calls[0][1] and calls[0][2] == 5
+    # The stencil is one day each way (no valuation start); the fake's time terms give
+    # theta -(4 + 0.01 S) and charm -0.01.
+    assert math.isclose(res.greeks["theta"], -5.0, rel_tol=1e-9)
+    assert math.isclose(res.greeks["charm"], -0.01, rel_tol=1e-6)
+    # One batch per instant (valuation, a day later, a day earlier), on the engine's seed.
+    assert len(calls) == 3 and all(c[1] and c[2] == 5 for c in calls)
 
 
 def test_call_rho_crossing_the_no_early_exercise_boundary(calls):

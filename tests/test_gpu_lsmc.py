@@ -151,7 +151,14 @@ def test_american_greeks_equal_scalar_bumped_prices():
     # A put's delta lies in [-1, 0], its gamma and vega are positive, its rho negative.
     assert -1.0 < res.greeks["delta"] < 0.0 and res.greeks["gamma"] > 0.0
     assert res.greeks["vega"] > 0.0 and res.greeks["rho"] < 0.0
-    assert res.status["theta"] == "unsupported"
+    # theta: the option valued a day later and a day earlier (its expiry moved), each
+    # priced on the pinned seed; a put loses value with time
+    from kiyosi_gb300.greeks import YEAR_MICROS
+    day = 86_400_000_000 / YEAR_MICROS
+    later = engine.price(AmericanOption("put", 100.0, 1.0 - day), ctx)
+    earlier = engine.price(AmericanOption("put", 100.0, 1.0 - -day), ctx)
+    assert res.greeks["theta"] == (later - earlier) / (2 * 86_400_000_000 / YEAR_MICROS)
+    assert res.greeks["theta"] < 0.0
 
 
 def test_call_without_early_exercise_is_the_european_price():
