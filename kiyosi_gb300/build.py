@@ -30,7 +30,7 @@ UNITS = {
     "planner.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["device_rng.cuh", "path_engine.cuh", "kernels.cuh", "kernels_impl.cuh", "launch.h",
-           "api_internal.h", "joe_kuo_6_21201.inc", "shared_grid.cuh", "lsmc_common.cuh", "tcgen05.cuh", "phased.cuh", "segmented.cuh"]
+           "api_internal.h", "joe_kuo_6_21201.inc", "shared_grid.cuh", "lsmc_common.cuh", "tcgen05.cuh", "phased.cuh", "segmented.cuh", "straight.cuh"]
 
 
 def nvcc() -> str:

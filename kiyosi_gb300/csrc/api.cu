@@ -849,10 +849,65 @@ kgpu_status run_segmented(Call& k, const DevBook<float>& db, int& launches) {
     return finish_values<float>(k, chunk_count, launches);
 }
 
+// Books the straight kernel takes: FP32 on the persistent schedule, pseudo-random, every
+// contract a path that takes every grid step (an Asian on fixings or a vanilla path)
+// reporting its payoff, under any model.
+bool straight_eligible(const Call& k) {
+    if (k.s.precision != KGPU_PRECISION_FP32 || k.s.schedule != KGPU_SCHEDULE_PERSISTENT || k.sobol ||
+        k.s.antithetic)
+        return false;
+    for (int i = 0; i < k.book->contract_count; ++i) {
+        const kgpu_contract& c = k.book->contracts[i];
+        if ((c.payoff != KGPU_PAYOFF_ASIAN && c.payoff != KGPU_PAYOFF_VANILLA_PATH) ||
+            (c.flags & (KGPU_C_OUTPUT_DELTA | KGPU_C_OUTPUT_GAMMA)))
+            return false;
+    }
+    return true;
+}
+
+// Such a book on the straight kernel: per-path payoffs, then the same fixed-order
+// reduction as the persistent kernels.
+kgpu_status run_straight(Call& k, const DevBook<float>& db, int& launches) {
+    kgpu_context* ctx = k.ctx;
+    const int n = k.raw.contract_count;
+    kgpu_status st;
+    int chunk_count = 0;
+    if ((st = stage_values<float>(k, &chunk_count))) return st;
+    std::vector<int> dims(n);
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        dims[i] = k.info[i].dims;
+        total += k.info[i].samples;
+    }
+    if ((st = upload(ctx, ctx->phase_dims, dims.data(), dims.size() * sizeof(int)))) return st;
+    StraightArgs a;
+    a.book = db;
+    a.contract_count = n;
+    a.total = total;
+    a.value_offset = static_cast<const int64_t*>(ctx->value_offset.ptr);
+    a.dims = static_cast<const int*>(ctx->phase_dims.ptr);
+    a.seed = k.s.seed;
+    a.values = static_cast<float*>(ctx->values.ptr);
+    a.executed = static_cast<unsigned long long*>(ctx->executed.ptr);
+    a.cancel = k.cancel ? ctx->cancel_dev : nullptr;
+    a.aborted = static_cast<int*>(ctx->queue.ptr) + 1;
+    const size_t smem = size_t(k.lv_values) * sizeof(float) + 16;
+    if (smem > 227 * 1024)
+        return fail(ctx, KGPU_UNSUPPORTED_OPERATION, "the local-volatility surface exceeds shared memory");
+    CancelWatcher watcher(k.cancel, ctx->cancel_host);
+    CUDA_TRY(ctx, path_kernel_begin(ctx));
+    CUDA_TRY(ctx, launch_straight_fp32(k.model->kind, total, smem, ctx->stream, a, *k.model, k.lv_dev));
+    CUDA_TRY(ctx, path_kernel_end(ctx));
+    launches += 1;
+    return finish_values<float>(k, chunk_count, launches);
+}
+
 template <class Real>
 kgpu_status run_persistent(Call& k, DevBook<Real> db, int& launches) {
-    if constexpr (std::is_same<Real, float>::value)
+    if constexpr (std::is_same<Real, float>::value) {
         if (segmented_eligible(k)) return run_segmented(k, db, launches);
+        if (straight_eligible(k)) return run_straight(k, db, launches);
+    }
     const bool ext = extended_payoffs(*k.book);
     kgpu_context* ctx = k.ctx;
     const kgpu_settings& s = k.s;

@@ -4,6 +4,7 @@
 #include "phased.cuh"
 #include "segmented.cuh"
 #include "shared_grid.cuh"
+#include "straight.cuh"
 
 namespace kgpu {
 
@@ -155,6 +156,26 @@ cudaError_t launch_segmented_fp32(int64_t total, cudaStream_t s, const SegmentAr
     segmented_vanilla_kernel<kSegments>
         <<<unsigned((threads + kSegmentThreads - 1) / kSegmentThreads), kSegmentThreads, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+template <int MODEL>
+static cudaError_t straight_one(int64_t total, size_t smem, cudaStream_t s, const StraightArgs& a,
+                                const kgpu_model& m, const double* lv) {
+    auto k = straight_path_kernel<MODEL>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    k<<<unsigned((total + kStraightThreads - 1) / kStraightThreads), kStraightThreads, smem, s>>>(a, m, lv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_straight_fp32(int model, int64_t total, size_t smem, cudaStream_t s, const StraightArgs& a,
+                                 const kgpu_model& m, const double* lv) {
+    if (total <= 0) return cudaSuccess;
+    switch (model) {
+        case KGPU_MODEL_BSM: return straight_one<KGPU_MODEL_BSM>(total, smem, s, a, m, lv);
+        case KGPU_MODEL_HESTON: return straight_one<KGPU_MODEL_HESTON>(total, smem, s, a, m, lv);
+        default: return straight_one<KGPU_MODEL_LOCAL_VOL>(total, smem, s, a, m, lv);
+    }
 }
 
 cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s) {

@@ -5,6 +5,7 @@
 #include "kernels.cuh"
 #include "phased.cuh"
 #include "segmented.cuh"
+#include "straight.cuh"
 #include "shared_grid.cuh"
 
 namespace kgpu {
@@ -54,6 +55,11 @@ int phased_occupancy_fp32(bool sobol);
 
 // Books of BSM vanilla-path contracts, FP32, pseudo-random: kSegments lanes per path.
 cudaError_t launch_segmented_fp32(int64_t total, cudaStream_t s, const SegmentArgs& a);
+
+// Books of paths that take every grid step (Asians on fixings, vanilla paths), FP32,
+// pseudo-random: one thread per path.  `smem`: the local-volatility surface.
+cudaError_t launch_straight_fp32(int model, int64_t total, size_t smem, cudaStream_t s, const StraightArgs& a,
+                                 const kgpu_model& m, const double* lv);
 cudaError_t launch_sobol_high_t(const SobolTables& t, int blocks, uint32_t* out, cudaStream_t s);
 
 // The lanes of one shared daily grid, path-major, and the merge of their CTA sums.
