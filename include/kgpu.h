@@ -63,12 +63,15 @@ enum { KGPU_PRECISION_FP64 = 0, KGPU_PRECISION_FP32 = 1 };
  * FP32, as one cooperative launch: each grid step advances every path still monitoring
  * knock-in by one bridge interval, the lanes of a warp on the same grid positions, and
  * the survivors go to the next step's list; once few paths remain, CTAs complete them,
- * then the knocked-in paths (interval ends only).  Other books (and FP64) run the
- * lane-refill kernel: warps pull (contract, tile) work items from a device queue and
- * refill finished lanes with the next path of the tile.
- * LANE_REFILL: the lane-refill kernel for every book.  Both persistent kernels store each
- * path's payoff and sum the payoffs in a fixed order, so their estimates are identical
- * for a book both can run. */
+ * then the knocked-in paths (interval ends only).  In FP32 under PCG32, a book of BSM
+ * vanilla paths runs eight lanes per path (the path's steps in segments, the segment sums
+ * added in a fixed order: prices within 1e-5 relative), and any other book of Asians and
+ * vanilla paths one thread per path.  Other books (and FP64) run the lane-refill kernel:
+ * warps pull (contract, tile) work items from a device queue and refill finished lanes
+ * with the next path of the tile.
+ * LANE_REFILL: the lane-refill kernel for every book.  The persistent kernels store each
+ * path's payoff and sum the payoffs in a fixed order, so the phase-major and lane-refill
+ * estimates are identical for a book both can run. */
 /* KGPU_SCHEDULE_SHARED_GRID: the book's contracts are the lanes of one shared daily grid
  * (bridged autocallables whose steps, bridge intervals and bridge weights are prefixes of
  * the longest lane's, with equal sampling dimensions and path counts).  One thread per
