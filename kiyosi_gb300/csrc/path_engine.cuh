@@ -1024,6 +1024,25 @@ __device__ __forceinline__ bool path_step(const DevModel<Real>& m, const Contrac
     return grid_step<Real, MODEL>(m, c, p, s, n, value);
 }
 
+// The per-step rule of an Asian on its fixings (the spot added at each fixing step) and of
+// a vanilla path (none).
+template <class Real>
+__device__ __forceinline__ void fixing_rule(const ContractT<Real>& c, uint8_t fl, PathState<Real>& s) {
+    if (c.payoff == KGPU_PAYOFF_ASIAN && (fl & KGPU_STEP_FIXING)) {
+        s.acc += spot_at(c.spot, s.lr);
+        s.fixings += 1;
+    }
+}
+
+// Their payoff after the last step: the call or put on the fixings' average (Asian) or on
+// the terminal spot (vanilla path), discounted.
+template <class Real>
+__device__ __forceinline__ Real fixing_value(const ContractT<Real>& c, const PathState<Real>& s) {
+    Real underlying = c.payoff == KGPU_PAYOFF_ASIAN ? s.acc / Real(s.fixings) : spot_at(c.spot, s.lr);
+    Real x = c.sign * (underlying - c.strike);
+    return (x > Real(0) ? x : Real(0)) * c.final_discount;
+}
+
 // One grid step of the grid-stepping families (vanilla path, Asian on fixings, forward
 // autocallable, accumulator): model step, then the family's per-step rule.
 template <class Real, int MODEL, class Source>
@@ -1074,14 +1093,9 @@ __device__ __forceinline__ bool grid_step(const DevModel<Real>& m, const Contrac
         value = s.acc * unit(s.lr) * c.final_discount;
         return true;
     }
-    if (payoff == KGPU_PAYOFF_ASIAN && (fl & KGPU_STEP_FIXING)) {
-        s.acc += spot_at(c.spot, s.lr);
-        s.fixings += 1;
-    }
+    fixing_rule(c, fl, s);
     if (!last) return false;
-    Real underlying = payoff == KGPU_PAYOFF_ASIAN ? s.acc / Real(s.fixings) : spot_at(c.spot, s.lr);
-    Real x = c.sign * (underlying - c.strike);
-    value = (x > Real(0) ? x : Real(0)) * c.final_discount;
+    value = fixing_value(c, s);
     return true;
 }
 

@@ -5,11 +5,11 @@
 // The lane-refill kernel exists for books whose paths end at different steps (knock-outs,
 // bridge skips): a warp pulls work items from a queue and refills finished lanes, and
 // every unit of work goes through the payoff dispatch.  A path that never ends early
-// needs none of that.  Here a thread walks one sample with the lane-refill kernel's own
-// grid_step on the same normals (path_samples over the model's transitions,
-// engines/monte_carlo.rs:1498-1676), so each path's payoff is that kernel's; only the
-// queue, the refills and the per-unit dispatch are gone.  The Heston Asian book (2^22
-// paths x 252 steps) is such a book.
+// needs none of that.  Here a thread walks one sample through the model step and the
+// fixing rule of the lane-refill kernel's grid_step, on the same normals (path_samples
+// over the model's transitions, engines/monte_carlo.rs:1498-1676), so each path's payoff
+// is that kernel's; only the queue, the refills, the per-unit dispatch and the step's
+// bookkeeping are gone.  The Heston Asian book (2^22 paths x 252 steps) is such a book.
 #pragma once
 #include "kernels.cuh"
 
@@ -64,12 +64,26 @@ __global__ void __launch_bounds__(kStraightThreads, 4)
         path_init(s, c, m.v0);
         PcgSource<float> n;
         n.start(a.seed, uint64_t(sample), a.dims[contract]);
-        float value = 0.f;
-        bool finished = false;
-        for (int guard = c.step_count + 1; !finished && guard > 0; --guard)
-            finished = grid_step<float, MODEL>(m, c, p, s, n, value);
-        a.values[a.value_offset[contract] + sample] = finished ? value : xnan(0.f);
-        steps_done = s.executed;
+        // grid_step's model step and fixing rule, step by step to the last; a plan without
+        // steps gives NaN there (no step ends the path) and here.
+        const int steps = c.step_count;
+        if (MODEL == KGPU_MODEL_HESTON && !n.has_spare) {
+            // A Heston step takes both normals of one Box-Muller draw, so a path that
+            // starts on a fresh draw starts every step on one: stating it lets the
+            // compiler drop the spare's branches.
+            for (int i = 0; i < steps; ++i) {
+                n.has_spare = false;
+                model_step<float, MODEL>(m, p.steps[i], s, n);
+                fixing_rule(c, p.flags[i], s);
+            }
+        } else {
+            for (int i = 0; i < steps; ++i) {
+                model_step<float, MODEL>(m, p.steps[i], s, n);
+                fixing_rule(c, p.flags[i], s);
+            }
+        }
+        a.values[a.value_offset[contract] + sample] = steps > 0 ? fixing_value(c, s) : xnan(0.f);
+        steps_done = steps;
     }
     // Simulated steps per contract, one atomic per warp when the warp's samples share one.
     const int head = __shfl_sync(kFull, contract, 0);
