@@ -123,10 +123,19 @@ __device__ __forceinline__ float unit52f(uint64_t k) {
     return fmaf(hi, 0x1p-32f, fmaf(lo, 0x1p-52f, 0x1p-53f));
 }
 
+// FP32 square root on the SFU (PTX sqrt.approx.f32, one MUFU operation; sqrt(+0) = +0):
+// IEEE sqrtf adds a Newton correction and a special-case branch to it, about eight more
+// instructions for a last-bit difference that FP32 paths do not need.
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ void box_muller(uint64_t b1, uint64_t b2, float* cosine, float* sine) {
     float u1 = unit52f(b1);
     float u2 = unit52f(b2);
-    float radius = sqrtf(-2.0f * __logf(u1));
+    float radius = sqrt_approx(-2.0f * __logf(u1));
     // u2 - rint(u2) for u2 in [0, 1] (rint(0.5) = 0) as a compare and select; the
     // result is the same float for every u2 in that range.
     float turns = u2 > 0.5f ? u2 - 1.0f : u2;

@@ -1153,7 +1153,7 @@ __global__ void __launch_bounds__(256) mlp_fresh_advance_kernel(LsmcParams<float
                 for (int j = 0; j < p.substeps; ++j) {
                     const float z1 = n.normal(), z2 = n.normal();
                     const float vp = v > 0.f ? v : 0.f;
-                    const float sv = sqrtf(vp) * p.sqrt_h;
+                    const float sv = xsqrt(vp) * p.sqrt_h;
                     x += (p.rate - p.dividend - 0.5f * vp) * p.h + sv * z1;
                     v += p.kappa * (p.theta - vp) * p.h + p.xi * sv * (p.rho * z1 + p.rho_bar * z2);
                 }

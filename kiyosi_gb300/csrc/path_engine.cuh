@@ -255,7 +255,7 @@ __device__ __forceinline__ float xlog1p(float x) { return log1pf(x); }
 __device__ __forceinline__ double xsin(double x) { return sin(x); }
 __device__ __forceinline__ float xsin(float x) { return sinf(x); }
 __device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
-__device__ __forceinline__ float xsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ float xsqrt(float x) { return sqrt_approx(x); }
 __device__ __forceinline__ double xinf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
 __device__ __forceinline__ float xinf(float) { return __int_as_float(0x7f800000); }
 __device__ __forceinline__ double xnan(double) { return __longlong_as_double(0x7ff8000000000000LL); }
