@@ -118,7 +118,8 @@ struct DevModel {
 // ------------------------------------------------------------------------------------
 // Normal sources.
 // ------------------------------------------------------------------------------------
-template <class Real>
+// EXACT_RADIUS: the FP32 Box-Muller radius by IEEE sqrtf instead of the SFU root.
+template <class Real, bool EXACT_RADIUS = false>
 struct PcgSource {
     Pcg g;
     Real spare;
@@ -127,7 +128,7 @@ struct PcgSource {
     __device__ __forceinline__ void draw(Real& c, Real& s) {
         uint64_t b1 = pcg_bits52(g);
         uint64_t b2 = pcg_bits52(g);
-        box_muller(b1, b2, &c, &s);
+        box_muller(b1, b2, &c, &s, EXACT_RADIUS);
     }
     // Positions the stream at the first normal of `sample` (dims normals per sample).
     __device__ __forceinline__ void start(uint64_t seed, uint64_t sample, int dims) {

@@ -114,12 +114,12 @@ __global__ void __launch_bounds__(kSharedThreads) shared_grid_kernel(SharedArgs<
                 walk(neg, lr_neg, mn_neg);
             }
         } else {
-            PcgSource<Real> n;
+            PcgSource<Real, true> n;
             n.start(a.seed, uint64_t(sample), a.dims);
             walk(n, lr, mn);
             if (paired) {
                 n.start(a.seed, uint64_t(sample), a.dims);
-                Negated<PcgSource<Real>, Real> neg{n};
+                Negated<PcgSource<Real, true>, Real> neg{n};
                 walk(neg, lr_neg, mn_neg);
             }
         }
